@@ -1,0 +1,145 @@
+/* phylo_gpu.h -- C ABI of the GB300 (sm_103a) tree-scoring library.
+ *
+ * This is the boundary that phylocaml's OCaml externals would bind in place
+ * of its CPU stubs: plain pointers and sizes, status codes, no OCaml or
+ * torch types.  Each entry point names the reference interface it replaces
+ * (paths inside the phylocaml tree).
+ *
+ * Conventions
+ *   - Every call returns pgpu_status; PGPU_OK is 0.  On failure the context
+ *     keeps a message readable with pgpu_last_error().  An OCaml stub turns
+ *     a non-zero status into `failwith msg`, as lib/mlmodel.c does for LAPACK
+ *     failures (lib/mlmodel.c:110-120).
+ *   - "Host" entry points take caller-owned host buffers, copy them to the
+ *     device, run, copy results back and return when the results are in the
+ *     caller's buffers (synchronous, like the reference's externals).
+ *   - "_dev" entry points take device pointers and are asynchronous on the
+ *     context's stream (pgpu_set_stream); call pgpu_synchronize() before
+ *     reading results.
+ *   - A context owns its device memory and stream.  Calls on different
+ *     contexts may run concurrently from different threads; calls on one
+ *     context must not overlap.
+ *
+ * Tree layout (pgpu_tree)
+ *   A rooted binary tree with n_tips leaves.  Tips have ids 0..n_tips-1.
+ *   Internal node k (0 <= k < n_tips-1) has id n_tips+k; its children
+ *   left[k] and right[k] must have ids smaller than n_tips+k (a postorder,
+ *   as produced by Tree.post_order_edges, lib/tree.ml:171-187).  The root is
+ *   id 2*n_tips-2.  brlen[id] is the length of the branch above node id
+ *   (2*n_tips-2 entries; the root has none); Fitch ignores it.
+ */
+#ifndef PHYLO_GPU_H
+#define PHYLO_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int pgpu_status;
+
+enum {
+  PGPU_OK = 0,
+  PGPU_ERR_ARG = 1,            /* bad size, pointer, layout or tree        */
+  PGPU_ERR_CUDA = 2,           /* CUDA runtime error                        */
+  PGPU_ERR_OOM = 3,            /* device allocation failed                  */
+  PGPU_ERR_NAN = 4,            /* NaN/Inf in a model matrix (mlModel.ml:557-568) */
+  PGPU_ERR_NONREVERSIBLE = 5,  /* Q is not reversible w.r.t. pi             */
+  PGPU_ERR_EIGEN = 6,          /* eigendecomposition did not converge       */
+  PGPU_ERR_OVERFLOW = 7,       /* a count does not fit its output type      */
+  PGPU_ERR_TIMEOUT = 8,        /* a bounded device wait gave up             */
+  PGPU_ERR_UNSUPPORTED = 9,    /* device or configuration not supported     */
+  PGPU_ERR_LIMIT = 10          /* size above a documented maximum           */
+};
+
+typedef struct pgpu_ctx pgpu_ctx;
+
+typedef struct {
+  int32_t n_tips;
+  const int32_t *left;   /* [n_tips-1] */
+  const int32_t *right;  /* [n_tips-1] */
+  const double *brlen;   /* [2*n_tips-2] or NULL */
+} pgpu_tree;
+
+/* ---- context ------------------------------------------------------------
+ * No reference counterpart: phylocaml's externals run on the caller's
+ * thread with no device state.  The context carries what a custom block's
+ * finalizer would own (lib/bitvector/bv.c:183-189). */
+pgpu_status pgpu_create(pgpu_ctx **out, int device);
+void pgpu_destroy(pgpu_ctx *ctx);
+const char *pgpu_last_error(const pgpu_ctx *ctx);
+pgpu_status pgpu_set_stream(pgpu_ctx *ctx, void *cuda_stream);
+pgpu_status pgpu_synchronize(pgpu_ctx *ctx);
+/* Number of kernels this library launched on ctx since creation. */
+uint64_t pgpu_kernel_launches(const pgpu_ctx *ctx);
+/* Library version as 10000*major + 100*minor + patch. */
+int pgpu_version(void);
+
+/* Host-only: the stack-machine evaluation order the kernels use for `tree`
+ * (no device work, ctx may be NULL).  ops_out receives 3*(n_tips-1) ints,
+ * (internal index k, first child id, second child id) per step in
+ * evaluation order; *max_depth the largest number of intermediate node
+ * results alive at once.  No reference counterpart: phylocaml recurses
+ * (lib/tree.ml:171-187). */
+pgpu_status pgpu_tree_schedule(pgpu_ctx *ctx, const pgpu_tree *tree, int32_t *ops_out,
+                               int32_t *max_depth);
+
+/* ---- Fitch parsimony -----------------------------------------------------
+ * State sets are packed lanes of lane_bits bits (4, 8, 16 or 32) in uint32
+ * words, site s in lane s % (32/lane_bits) of word s / (32/lane_bits),
+ * lowest lane in the lowest bits.  lane_bits 8 with one state bit per
+ * alphabet code is the reference's BV8 layout (lib/bitvector/bv.h:29-34);
+ * lane_bits 4 packs the four nucleotides (A=1, C=2, G=4, T=8,
+ * lib/alphabet.ml:301-307) eight sites to a word.  Lanes past the last site
+ * are ignored on input and written as zero. */
+
+/* Bitvector.BVn.fitch_median_2 (lib/bitvector.mli:94; bv_CAML_fitch_median2,
+ * lib/bitvector/bv.c:463-480, and bv_fitch, bv.c:148-160).  out[i] = a&b,
+ * or a|b where a&b is empty; *union_count = number of such sites. */
+pgpu_status pgpu_fitch_median2(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b,
+                               uint32_t *out, size_t n_sites, int lane_bits,
+                               uint64_t *union_count);
+
+/* NonAdditive_c.median_2 (lib/nonAdditive_c.ml:19-35): the same median with
+ * the cost sum_i weights[i] * [a_i & b_i == 0], weights taken per site (the
+ * left operand's weights in the reference).  Integer weights make the
+ * float sum of the reference exact. */
+pgpu_status pgpu_fitch_median2_weighted(pgpu_ctx *ctx, const uint32_t *a,
+                                        const uint32_t *b, const uint32_t *weights,
+                                        uint32_t *out, size_t n_sites, int lane_bits,
+                                        uint64_t *cost);
+
+/* Bitvector.BVn.distance (lib/bitvector.mli:90; bv_distance, bv.c:46-55). */
+pgpu_status pgpu_fitch_distance(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b,
+                                size_t n_sites, int lane_bits, uint64_t *distance);
+
+/* The whole Fitch postorder: Node.Make1D.median_2 (lib/node.ml:183-198)
+ * applied at every internal node of Tree.post_order_edges
+ * (lib/tree.ml:171-187), node cost summed as in lib/node.ml:191.
+ *   tips       [n_tips][n_words] packed state sets, n_words = ceil(n_sites*lane_bits/32)
+ *   weights    [n_sites] per-site weights, or NULL for 1
+ *   node_sets  [n_tips-1][n_words] out: state set of internal node k in row k
+ *   site_cost  [n_sites] out (or NULL): number of internal nodes at which
+ *              site s took the union
+ *   total      out: sum_s weights[s] * site_cost[s] (a per-site count is at
+ *              most n_tips-1, so it always fits uint32; the total is exact
+ *              while it stays below 2^64) */
+pgpu_status pgpu_fitch_tree(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
+                            const uint32_t *weights, size_t n_sites, int lane_bits,
+                            uint32_t *node_sets, uint32_t *site_cost, uint64_t *total);
+
+/* Device-pointer form of pgpu_fitch_tree, asynchronous on the context's
+ * stream.  Rows are ld_words apart (ld_words % 4 == 0, every pointer 16-byte
+ * aligned); tree arrays are host pointers.  *total_dev is overwritten. */
+pgpu_status pgpu_fitch_tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree,
+                                const uint32_t *tips_dev, size_t ld_words,
+                                const uint32_t *weights_dev, size_t n_sites,
+                                int lane_bits, uint32_t *node_sets_dev,
+                                uint32_t *site_cost_dev, uint64_t *total_dev);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PHYLO_GPU_H */

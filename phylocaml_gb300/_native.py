@@ -1,0 +1,203 @@
+"""ctypes binding of libphylo_gpu.so (the C ABI declared in include/phylo_gpu.h).
+
+This is the only route from Python to the GPU kernels.  There is no CPU
+fallback: if the shared object is missing or no sm_100-family device is
+present, calls raise ``NativeError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libphylo_gpu.so"
+
+PGPU_OK = 0
+STATUS_NAMES = {
+    0: "PGPU_OK", 1: "PGPU_ERR_ARG", 2: "PGPU_ERR_CUDA", 3: "PGPU_ERR_OOM",
+    4: "PGPU_ERR_NAN", 5: "PGPU_ERR_NONREVERSIBLE", 6: "PGPU_ERR_EIGEN",
+    7: "PGPU_ERR_OVERFLOW", 8: "PGPU_ERR_TIMEOUT", 9: "PGPU_ERR_UNSUPPORTED",
+    10: "PGPU_ERR_LIMIT",
+}
+
+
+class NativeError(RuntimeError):
+    """A C-ABI call failed (status != PGPU_OK), or the library is missing.
+
+    Mirrors the reference's ``failwith`` on LAPACK errors (lib/mlmodel.c:110-120):
+    the message is the library's own.
+    """
+
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class PgpuTree(C.Structure):
+    _fields_ = [
+        ("n_tips", C.c_int32),
+        ("left", C.POINTER(C.c_int32)),
+        ("right", C.POINTER(C.c_int32)),
+        ("brlen", C.POINTER(C.c_double)),
+    ]
+
+
+class PgpuModel(C.Structure):
+    _fields_ = [
+        ("n_states", C.c_int32),
+        ("n_rates", C.c_int32),
+        ("Q", C.POINTER(C.c_double)),
+        ("pi", C.POINTER(C.c_double)),
+        ("rates", C.POINTER(C.c_double)),
+        ("probs", C.POINTER(C.c_double)),
+    ]
+
+
+_P = C.c_void_p
+_SZ = C.c_size_t
+_I = C.c_int
+_U64P = C.POINTER(C.c_uint64)
+_DP = C.POINTER(C.c_double)
+
+# name -> (restype, argtypes); the complete list of exported entry points
+SIGNATURES: dict[str, tuple] = {
+    "pgpu_create": (_I, [C.POINTER(_P), _I]),
+    "pgpu_destroy": (None, [_P]),
+    "pgpu_last_error": (C.c_char_p, [_P]),
+    "pgpu_set_stream": (_I, [_P, _P]),
+    "pgpu_synchronize": (_I, [_P]),
+    "pgpu_kernel_launches": (C.c_uint64, [_P]),
+    "pgpu_version": (_I, []),
+    "pgpu_tree_schedule": (_I, [_P, C.POINTER(PgpuTree), _P, C.POINTER(C.c_int32)]),
+    "pgpu_fitch_median2": (_I, [_P, _P, _P, _P, _SZ, _I, _U64P]),
+    "pgpu_fitch_median2_weighted": (_I, [_P, _P, _P, _P, _P, _SZ, _I, _U64P]),
+    "pgpu_fitch_distance": (_I, [_P, _P, _P, _SZ, _I, _U64P]),
+    "pgpu_fitch_tree": (_I, [_P, C.POINTER(PgpuTree), _P, _P, _SZ, _I, _P, _P, _U64P]),
+    "pgpu_fitch_tree_dev": (_I, [_P, C.POINTER(PgpuTree), _P, _SZ, _P, _SZ, _I, _P, _P, _P]),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load() -> C.CDLL:
+    """Loads libphylo_gpu.so and declares every signature; raises if absent."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not LIB_PATH.exists():
+            raise NativeError(9, f"{LIB_PATH} is missing; build it with phylocaml_gb300.build.build()")
+        lib = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def ptr(a) -> int | None:
+    """Address of a numpy array's data, a torch tensor's data, or None."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    if isinstance(a, int):
+        return a
+    raise TypeError(f"cannot take the address of {type(a)}")
+
+
+def make_tree(left: np.ndarray, right: np.ndarray, brlen: np.ndarray | None = None):
+    """Builds a PgpuTree; returns (struct, keepalive) -- keep both alive."""
+    left = np.ascontiguousarray(left, dtype=np.int32)
+    right = np.ascontiguousarray(right, dtype=np.int32)
+    keep = [left, right]
+    t = PgpuTree()
+    t.n_tips = len(left) + 1
+    t.left = left.ctypes.data_as(C.POINTER(C.c_int32))
+    t.right = right.ctypes.data_as(C.POINTER(C.c_int32))
+    if brlen is not None:
+        brlen = np.ascontiguousarray(brlen, dtype=np.float64)
+        keep.append(brlen)
+        t.brlen = brlen.ctypes.data_as(C.POINTER(C.c_double))
+    return t, keep
+
+
+class Context:
+    """Owns one pgpu_ctx (device memory and a stream) on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = _P()
+        st = self.lib.pgpu_create(C.byref(h), device)
+        if st != PGPU_OK:
+            raise NativeError(st, f"pgpu_create(device={device}) failed "
+                                  "(needs an sm_100-family GPU and the CUDA runtime)")
+        self.h = h
+        self.device = device
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.pgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def check(self, st: int, what: str) -> None:
+        if st != PGPU_OK:
+            msg = self.lib.pgpu_last_error(self.h)
+            raise NativeError(st, f"{what}: {msg.decode() if msg else ''}")
+
+    def call(self, name: str, *args) -> None:
+        self.check(getattr(self.lib, name)(self.h, *args), name)
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.pgpu_kernel_launches(self.h))
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        self.call("pgpu_set_stream", stream_handle)
+
+    def synchronize(self) -> None:
+        self.call("pgpu_synchronize")
+
+
+_default: Context | None = None
+
+
+def default_context() -> Context:
+    """A process-wide context on device 0, created on first use."""
+    global _default
+    with _lock:
+        if _default is None:
+            _default = Context(0)
+        return _default
+
+
+def tree_schedule(left: np.ndarray, right: np.ndarray):
+    """Host-only schedule query: (ops [n_int, 3] int32, max stack depth)."""
+    lib = load()
+    t, keep = make_tree(left, right)
+    ops = np.empty((len(keep[0]), 3), dtype=np.int32)
+    depth = C.c_int32(0)
+    st = lib.pgpu_tree_schedule(None, C.byref(t), ops.ctypes.data, C.byref(depth))
+    if st != PGPU_OK:
+        raise NativeError(st, "pgpu_tree_schedule: invalid tree")
+    return ops, int(depth.value)

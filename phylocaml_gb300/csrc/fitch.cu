@@ -1,0 +1,467 @@
+// Fitch parsimony on packed state-set lanes.
+//
+// Reference semantics: bv_fitch (lib/bitvector/bv.c:148-160) and
+// NonAdditive_c.median_2 (lib/nonAdditive_c.ml:19-35): per site
+//   m = a & b;  if m == 0 { m = a | b; cost += w }.
+//
+// Lanes of LB bits (4, 8, 16, 32) are processed a whole 32-bit word at a
+// time with no per-site branch.  With H the lane-MSB mask,
+//   nz = (((m & ~H) + ~H) | m) & H      MSB set in every non-empty lane
+//   e  = nz ^ H                          MSB set in every empty lane
+//   fill = e | (e - (e >> (LB-1)))       all bits of every empty lane
+//   med  = m | ((a | b) & fill)
+// and e >> (LB-1) holds a 1 in the lowest bit of each empty lane, which is
+// added to LB-bit lane counters in one integer add (flushed to 32-bit
+// per-site counters before a lane counter can wrap).
+//
+// The tree kernel (fitch_tree_kernel) gives each CTA a tile of W words
+// (W*32/LB sites) and walks the whole postorder for it:
+//   warp 0, lane 0   producer: streams the tip rows of the tile, in the order
+//                    the schedule reads them, into a STAGES-deep shared ring
+//                    with 1-D bulk copies (cp.async.bulk) on mbarriers;
+//   warps 1..W/32    consumers: one word per thread; children that are
+//                    internal nodes come from a per-thread stack in shared
+//                    memory, tips from the ring; every median is written
+//                    once to its output row with a streaming store.
+// HBM traffic is therefore the compulsory minimum: each tip row read once,
+// each internal row written once, plus weights and per-site counts.
+#include <algorithm>
+
+#include "pgpu_internal.cuh"
+
+namespace {
+
+template <int LB>
+struct Lanes {
+  static constexpr uint32_t H =
+      LB == 4 ? 0x88888888u : LB == 8 ? 0x80808080u : LB == 16 ? 0x80008000u : 0x80000000u;
+  static constexpr int PER = 32 / LB;
+  // increments a LB-bit counter can take before it may wrap
+  static constexpr uint32_t FLUSH = LB >= 32 ? 0xffffffffu : ((1u << (LB >= 32 ? 0 : LB)) - 1u);
+};
+
+template <int LB>
+__device__ __forceinline__ uint32_t fitch_word(uint32_t a, uint32_t b, uint32_t &e_lsb) {
+  constexpr uint32_t H = Lanes<LB>::H;
+  const uint32_t m = a & b;
+  const uint32_t nz = (((m & ~H) + ~H) | m) & H;
+  const uint32_t e = nz ^ H;
+  const uint32_t fill = e | (e - (e >> (LB - 1)));
+  e_lsb = e >> (LB - 1);
+  return m | ((a | b) & fill);
+}
+
+// mask of the valid lanes of word w (all lanes except in the last word)
+template <int LB>
+__host__ __device__ __forceinline__ uint32_t valid_lanes(size_t w, size_t n_sites) {
+  constexpr int PER = Lanes<LB>::PER;
+  const size_t first = w * PER;
+  if (first + PER <= n_sites) return 0xffffffffu;
+  if (first >= n_sites) return 0u;
+  const int rem = int(n_sites - first);
+  return (1u << (rem * LB)) - 1u;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sums v over the block and adds it to *dst (one atomic per block).
+__device__ __forceinline__ void block_add_u64(unsigned long long v, unsigned long long *dst,
+                                              unsigned long long *red) {
+  v = warp_sum_u64(v);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned long long s = lane < nw ? red[lane] : 0ull;
+    s = warp_sum_u64(s);
+    if (lane == 0 && s) atomicAdd(dst, s);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// per-node kernels (fitch_median_2 / distance)
+// ---------------------------------------------------------------------------
+
+template <int LB, bool WEIGHTED, bool WRITE>
+__global__ void __launch_bounds__(256) fitch_pair_kernel(const uint32_t *__restrict__ a,
+                                                         const uint32_t *__restrict__ b,
+                                                         const uint32_t *__restrict__ weights,
+                                                         uint32_t *__restrict__ out,
+                                                         size_t n_words, size_t n_sites,
+                                                         unsigned long long *count) {
+  __shared__ unsigned long long red[8];
+  constexpr int PER = Lanes<LB>::PER;
+  unsigned long long acc = 0;
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < n_words;
+       w += (size_t)gridDim.x * blockDim.x) {
+    uint32_t e;
+    const uint32_t valid = valid_lanes<LB>(w, n_sites);
+    const uint32_t med = fitch_word<LB>(__ldg(a + w), __ldg(b + w), e) & valid;
+    e &= valid;
+    if (WRITE) out[w] = med;
+    if (WEIGHTED) {
+#pragma unroll
+      for (int l = 0; l < PER; ++l)
+        if ((e >> (l * LB)) & 1u) acc += __ldg(weights + w * PER + l);
+    } else {
+      acc += __popc(e);
+    }
+  }
+  block_add_u64(acc, count, red);
+}
+
+// ---------------------------------------------------------------------------
+// tree kernel
+// ---------------------------------------------------------------------------
+
+struct FitchTreeArgs {
+  const uint32_t *tips;       // [n_tips][ld]
+  const uint32_t *weights;    // [n_sites] or null
+  uint32_t *node_sets;        // [n_int][ld]
+  uint32_t *site_cost;        // [n_sites] or null
+  unsigned long long *total;  // accumulated
+  const int4 *ops;            // [n_int] SchedOp
+  const int32_t *tip_seq;     // [n_tips]
+  int *flag;
+  size_t ld, n_words, n_sites;
+  int32_t n_tips, n_ops;
+  int W, stages, depth;
+};
+
+template <int LB>
+__global__ void __launch_bounds__(544) fitch_tree_kernel(const FitchTreeArgs p) {
+  constexpr int PER = Lanes<LB>::PER;
+  constexpr uint32_t FLUSH = Lanes<LB>::FLUSH;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ unsigned long long red[32];
+  const int W = p.W, S = p.stages;
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem);
+  uint64_t *empty = full + S;
+  uint32_t *ring = reinterpret_cast<uint32_t *>(smem + 16 * S);  // [S][W]
+  uint32_t *stk = ring + (size_t)S * W;                           // [depth][W]
+  const size_t tile0 = (size_t)blockIdx.x * W;
+  const int tid = threadIdx.x;
+  const int n_consumer_warps = W / 32;
+
+  if (tid == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], n_consumer_warps);
+    }
+    fence_mbarrier_init();
+  }
+  __syncthreads();
+
+  if (tid < 32) {
+    // ---------------- producer ----------------
+    if (tid == 0) {
+      const size_t span = min((size_t)W, p.ld - tile0);
+      const uint32_t bytes = (uint32_t)(span * sizeof(uint32_t));
+      int issued = 0;
+      bool ok = true;
+      for (int j = 0; j < p.n_tips && ok; ++j) {
+        const int slot = j % S, round = j / S;
+        if (round > 0) ok = mbar_wait_bounded(&empty[slot], (round - 1) & 1, p.flag);
+        if (!ok) break;
+        const int32_t tip = __ldg(p.tip_seq + j);
+        mbar_arrive_expect_tx(&full[slot], bytes);
+        bulk_g2s(ring + (size_t)slot * W, p.tips + (size_t)tip * p.ld + tile0, bytes, &full[slot]);
+        issued = j + 1;
+      }
+      // every issued copy must land before this CTA may exit
+      for (int j = max(0, issued - S); j < issued; ++j)
+        (void)mbar_wait_bounded(&full[j % S], (j / S) & 1, p.flag);
+    }
+    return;
+  }
+
+  // ---------------- consumers ----------------
+  const int c = tid - 32;
+  const int lane = tid & 31;
+  const size_t word = tile0 + c;
+  const bool active = word < p.n_words;
+  const uint32_t valid = active ? valid_lanes<LB>(word, p.n_sites) : 0u;
+  const uint32_t valid_lsb = valid & (Lanes<LB>::H >> (LB - 1));
+  uint32_t cnt = 0;                 // LB-bit lane counters
+  uint32_t acc[PER];                // per-site counters
+#pragma unroll
+  for (int l = 0; l < PER; ++l) acc[l] = 0;
+  uint32_t since = 0;
+  int sp = 0;
+  int taken = 0;
+  bool ok = true;
+
+  auto take = [&](uint32_t &v) {
+    const int slot = taken % S;
+    // every lane waits and the verdict is made warp-uniform before any
+    // warp-synchronous step, so a timeout cannot split the warp
+    const bool got = __all_sync(0xffffffffu, mbar_wait_bounded(&full[slot], (taken / S) & 1, p.flag));
+    if (!got) {
+      ok = false;
+      return;
+    }
+    v = ring[(size_t)slot * W + c];
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[slot]);
+    ++taken;
+  };
+
+  for (int i = 0; i < p.n_ops && ok; ++i) {
+    const int4 op = __ldg(p.ops + i);
+    uint32_t x = 0, y = 0;
+    if (op.z >= p.n_tips) y = stk[(size_t)(--sp) * W + c];
+    if (op.y >= p.n_tips) x = stk[(size_t)(--sp) * W + c];
+    if (op.y < p.n_tips) take(x);
+    if (op.z < p.n_tips && ok) take(y);
+    if (!ok) break;
+    uint32_t e;
+    const uint32_t med = fitch_word<LB>(x, y, e) & valid;
+    stk[(size_t)(sp++) * W + c] = med;
+    if (active) __stcs(p.node_sets + (size_t)op.x * p.ld + word, med);
+    cnt += e & valid_lsb;
+    if (LB < 32 && ++since == FLUSH) {
+#pragma unroll
+      for (int l = 0; l < PER; ++l) acc[l] += (cnt >> (l * LB)) & (FLUSH);
+      cnt = 0;
+      since = 0;
+    }
+  }
+  if (LB < 32) {
+#pragma unroll
+    for (int l = 0; l < PER; ++l) acc[l] += (cnt >> (l * LB)) & (FLUSH);
+  } else {
+    acc[0] += cnt;
+  }
+
+  unsigned long long wsum = 0;
+  if (active && ok) {
+    const size_t s0 = word * PER;
+#pragma unroll
+    for (int l = 0; l < PER; ++l) {
+      const size_t s = s0 + l;
+      if (s < p.n_sites) {
+        if (p.site_cost) p.site_cost[s] = acc[l];
+        const uint32_t w = p.weights ? __ldg(p.weights + s) : 1u;
+        wsum += (unsigned long long)w * acc[l];
+      }
+    }
+  }
+  // block reduction over the consumer warps only
+  wsum = warp_sum_u64(wsum);
+  const int cw = c >> 5;
+  if (lane == 0) red[cw] = wsum;
+  asm volatile("bar.sync 1, %0;" ::"r"(W) : "memory");
+  if (cw == 0) {
+    unsigned long long s = lane < n_consumer_warps ? red[lane] : 0ull;
+    s = warp_sum_u64(s);
+    if (lane == 0 && s) atomicAdd(p.total, s);
+  }
+}
+
+template <int LB>
+pgpu_status launch_pair(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b, const uint32_t *w,
+                        uint32_t *out, size_t n_words, size_t n_sites,
+                        unsigned long long *count, int mode) {
+  const int threads = 256;
+  size_t blocks = (n_words + threads - 1) / threads;
+  blocks = std::min<size_t>(std::max<size_t>(blocks, 1), (size_t)ctx->num_sms * 8);
+  if (mode == 0)
+    fitch_pair_kernel<LB, false, true><<<(unsigned)blocks, threads, 0, ctx->stream>>>(
+        a, b, w, out, n_words, n_sites, count);
+  else if (mode == 1)
+    fitch_pair_kernel<LB, true, true><<<(unsigned)blocks, threads, 0, ctx->stream>>>(
+        a, b, w, out, n_words, n_sites, count);
+  else
+    fitch_pair_kernel<LB, false, false><<<(unsigned)blocks, threads, 0, ctx->stream>>>(
+        a, b, w, out, n_words, n_sites, count);
+  return pgpu_after_launch(ctx, "fitch_pair_kernel");
+}
+
+bool lane_bits_ok(int lb) { return lb == 4 || lb == 8 || lb == 16 || lb == 32; }
+
+size_t words_for(size_t n_sites, int lb) { return (n_sites * (size_t)lb + 31) / 32; }
+
+// mode 0: median + count, 1: median + weighted cost, 2: distance only
+pgpu_status pair_host(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b, const uint32_t *w,
+                      uint32_t *out, size_t n_sites, int lb, uint64_t *result, int mode) {
+  if (!ctx) return PGPU_ERR_ARG;
+  if (!lane_bits_ok(lb)) return pgpu_set_err(ctx, PGPU_ERR_ARG, "lane_bits must be 4, 8, 16 or 32");
+  if (!a || !b || !result || (mode != 2 && !out) || (mode == 1 && !w))
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "fitch: null buffer");
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  const size_t n_words = words_for(n_sites, lb);
+  void *da, *db, *dout, *dw = nullptr, *dc;
+  PGPU_TRY(pgpu_buf(ctx, BUF_A, n_words * 4, &da));
+  PGPU_TRY(pgpu_buf(ctx, BUF_B, n_words * 4, &db));
+  PGPU_TRY(pgpu_buf(ctx, BUF_OUT, n_words * 4, &dout));
+  PGPU_TRY(pgpu_buf(ctx, BUF_SCALAR, 64, &dc));
+  if (mode == 1) PGPU_TRY(pgpu_buf(ctx, BUF_WEIGHTS, n_sites * 4, &dw));
+  cudaStream_t s = ctx->stream;
+  PGPU_CUDA(ctx, cudaMemcpyAsync(da, a, n_words * 4, cudaMemcpyHostToDevice, s));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(db, b, n_words * 4, cudaMemcpyHostToDevice, s));
+  if (mode == 1) PGPU_CUDA(ctx, cudaMemcpyAsync(dw, w, n_sites * 4, cudaMemcpyHostToDevice, s));
+  PGPU_CUDA(ctx, cudaMemsetAsync(dc, 0, 8, s));
+  if (n_words) {
+    auto *cnt = reinterpret_cast<unsigned long long *>(dc);
+    const uint32_t *pa = (const uint32_t *)da, *pb = (const uint32_t *)db,
+                   *pw = (const uint32_t *)dw;
+    uint32_t *po = (uint32_t *)dout;
+    switch (lb) {
+      case 4: PGPU_TRY(launch_pair<4>(ctx, pa, pb, pw, po, n_words, n_sites, cnt, mode)); break;
+      case 8: PGPU_TRY(launch_pair<8>(ctx, pa, pb, pw, po, n_words, n_sites, cnt, mode)); break;
+      case 16: PGPU_TRY(launch_pair<16>(ctx, pa, pb, pw, po, n_words, n_sites, cnt, mode)); break;
+      default: PGPU_TRY(launch_pair<32>(ctx, pa, pb, pw, po, n_words, n_sites, cnt, mode)); break;
+    }
+  }
+  if (mode != 2) PGPU_CUDA(ctx, cudaMemcpyAsync(out, dout, n_words * 4, cudaMemcpyDeviceToHost, s));
+  uint64_t *hc = reinterpret_cast<uint64_t *>(ctx->h_pinned);
+  PGPU_CUDA(ctx, cudaMemcpyAsync(hc, dc, 8, cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  *result = *hc;
+  return PGPU_OK;
+}
+
+template <int LB>
+pgpu_status launch_tree(pgpu_ctx *ctx, FitchTreeArgs &args, size_t n_tiles) {
+  const size_t smem = 16 * (size_t)args.stages + 4 * (size_t)(args.stages + args.depth) * args.W;
+  PGPU_CUDA(ctx, cudaFuncSetAttribute(fitch_tree_kernel<LB>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)std::max<size_t>(smem, 48 * 1024)));
+  fitch_tree_kernel<LB><<<(unsigned)n_tiles, 32 + args.W, smem, ctx->stream>>>(args);
+  return pgpu_after_launch(ctx, "fitch_tree_kernel");
+}
+
+pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips, size_t ld,
+                     const uint32_t *weights, size_t n_sites, int lb, uint32_t *node_sets,
+                     uint32_t *site_cost, uint64_t *total) {
+  if (!lane_bits_ok(lb)) return pgpu_set_err(ctx, PGPU_ERR_ARG, "lane_bits must be 4, 8, 16 or 32");
+  const size_t n_words = words_for(n_sites, lb);
+  if (!tips || !node_sets || !total) return pgpu_set_err(ctx, PGPU_ERR_ARG, "fitch_tree: null buffer");
+  if (ld % 4 != 0 || ld < n_words)
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "fitch_tree: ld_words (%zu) must be a multiple of 4 and >= %zu",
+                        ld, n_words);
+  if (((uintptr_t)tips | (uintptr_t)node_sets) & 15)
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "fitch_tree: tip and node rows must be 16-byte aligned");
+  const TreeSchedule *sch;
+  const int4 *dops;
+  const int32_t *dseq;
+  PGPU_TRY(pgpu_schedule_device(ctx, tree, &sch, &dops, &dseq));
+  const int32_t n = tree->n_tips;
+  cudaStream_t s = ctx->stream;
+  PGPU_CUDA(ctx, cudaMemsetAsync(total, 0, sizeof(uint64_t), s));
+  if (n_words == 0) return PGPU_OK;
+
+  // tile width: about two tiles per SM, 32..512 words, and shared memory for
+  // the ring and the stack within 100 KB so two CTAs fit on an SM
+  const size_t target_tiles = (size_t)std::max(ctx->num_sms, 1) * 2;
+  size_t W = (n_words + target_tiles - 1) / target_tiles;
+  W = std::min<size_t>(std::max<size_t>((W + 31) / 32 * 32, 64), 512);
+  int stages = 16;
+  const int depth = sch->max_depth;
+  while (W > 32 && 16 * stages + 4 * (size_t)(stages + depth) * W > 100 * 1024) W -= 32;
+  if (16 * stages + 4 * (size_t)(stages + depth) * W > ctx->smem_optin)
+    return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: tree needs a stack of %d rows; too deep",
+                        depth);
+  FitchTreeArgs args;
+  args.tips = tips;
+  args.weights = weights;
+  args.node_sets = node_sets;
+  args.site_cost = site_cost;
+  args.total = reinterpret_cast<unsigned long long *>(total);
+  args.ops = dops;
+  args.tip_seq = dseq;
+  args.flag = ctx->d_flag;
+  args.ld = ld;
+  args.n_words = n_words;
+  args.n_sites = n_sites;
+  args.n_tips = n;
+  args.n_ops = (int32_t)sch->ops.size();
+  args.W = (int)W;
+  args.stages = stages;
+  args.depth = depth;
+  const size_t n_tiles = (n_words + W - 1) / W;
+  switch (lb) {
+    case 4: return launch_tree<4>(ctx, args, n_tiles);
+    case 8: return launch_tree<8>(ctx, args, n_tiles);
+    case 16: return launch_tree<16>(ctx, args, n_tiles);
+    default: return launch_tree<32>(ctx, args, n_tiles);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+pgpu_status pgpu_fitch_median2(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b, uint32_t *out,
+                               size_t n_sites, int lane_bits, uint64_t *union_count) {
+  return pair_host(ctx, a, b, nullptr, out, n_sites, lane_bits, union_count, 0);
+}
+
+pgpu_status pgpu_fitch_median2_weighted(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b,
+                                        const uint32_t *weights, uint32_t *out, size_t n_sites,
+                                        int lane_bits, uint64_t *cost) {
+  return pair_host(ctx, a, b, weights, out, n_sites, lane_bits, cost, 1);
+}
+
+pgpu_status pgpu_fitch_distance(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b,
+                                size_t n_sites, int lane_bits, uint64_t *distance) {
+  return pair_host(ctx, a, b, nullptr, nullptr, n_sites, lane_bits, distance, 2);
+}
+
+pgpu_status pgpu_fitch_tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips_dev,
+                                size_t ld_words, const uint32_t *weights_dev, size_t n_sites,
+                                int lane_bits, uint32_t *node_sets_dev, uint32_t *site_cost_dev,
+                                uint64_t *total_dev) {
+  if (!ctx) return PGPU_ERR_ARG;
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  return tree_dev(ctx, tree, tips_dev, ld_words, weights_dev, n_sites, lane_bits, node_sets_dev,
+                  site_cost_dev, total_dev);
+}
+
+pgpu_status pgpu_fitch_tree(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
+                            const uint32_t *weights, size_t n_sites, int lane_bits,
+                            uint32_t *node_sets, uint32_t *site_cost, uint64_t *total) {
+  if (!ctx) return PGPU_ERR_ARG;
+  if (!tree || !tips || !node_sets || !total)
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "fitch_tree: null argument");
+  if (!lane_bits_ok(lane_bits))
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "lane_bits must be 4, 8, 16 or 32");
+  if (tree->n_tips < 2) return pgpu_set_err(ctx, PGPU_ERR_ARG, "tree: need at least 2 tips");
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  const size_t n_words = words_for(n_sites, lane_bits);
+  const size_t ld = (n_words + 3) / 4 * 4;
+  const size_t n = (size_t)tree->n_tips, n_int = n - 1;
+  void *dt, *dn, *dw = nullptr, *dsc = nullptr, *dtot;
+  PGPU_TRY(pgpu_buf(ctx, BUF_TIPS, n * ld * 4, &dt));
+  PGPU_TRY(pgpu_buf(ctx, BUF_OUT, n_int * ld * 4, &dn));
+  PGPU_TRY(pgpu_buf(ctx, BUF_SCALAR, 64, &dtot));
+  if (weights) PGPU_TRY(pgpu_buf(ctx, BUF_WEIGHTS, n_sites * 4, &dw));
+  if (site_cost) PGPU_TRY(pgpu_buf(ctx, BUF_SITECOST, n_sites * 4, &dsc));
+  cudaStream_t s = ctx->stream;
+  if (n_words) {
+    PGPU_CUDA(ctx, cudaMemcpy2DAsync(dt, ld * 4, tips, n_words * 4, n_words * 4, n,
+                                     cudaMemcpyHostToDevice, s));
+    if (weights)
+      PGPU_CUDA(ctx, cudaMemcpyAsync(dw, weights, n_sites * 4, cudaMemcpyHostToDevice, s));
+  }
+  PGPU_TRY(tree_dev(ctx, tree, (const uint32_t *)dt, ld, (const uint32_t *)dw, n_sites, lane_bits,
+                    (uint32_t *)dn, (uint32_t *)dsc, (uint64_t *)dtot));
+  if (n_words) {
+    PGPU_CUDA(ctx, cudaMemcpy2DAsync(node_sets, n_words * 4, dn, ld * 4, n_words * 4, n_int,
+                                     cudaMemcpyDeviceToHost, s));
+    if (site_cost)
+      PGPU_CUDA(ctx, cudaMemcpyAsync(site_cost, dsc, n_sites * 4, cudaMemcpyDeviceToHost, s));
+  }
+  uint64_t *ht = reinterpret_cast<uint64_t *>(ctx->h_pinned);
+  PGPU_CUDA(ctx, cudaMemcpyAsync(ht, dtot, 8, cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  PGPU_TRY(pgpu_check_flag(ctx, "fitch_tree"));
+  *total = *ht;
+  return PGPU_OK;
+}
+
+}  // extern "C"

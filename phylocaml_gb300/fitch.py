@@ -1,0 +1,86 @@
+"""Fitch parsimony through the C ABI (GPU kernels in csrc/fitch.cu).
+
+``fitch_tree`` scores a whole tree in one call: it is what
+Tree.post_order_edges (lib/tree.ml:171-187) with Node.Make1D.median_2
+(lib/node.ml:183-198) and NodeData.median_2 = NonAdditive_c.median_2
+(lib/nonAdditive_c.ml:19-35) compute, node by node, in the reference.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native
+from .synth import pack_lanes, unpack_lanes
+from .tree import RootedTree
+
+
+def n_words(n_sites: int, lane_bits: int) -> int:
+    return (n_sites * lane_bits + 31) // 32
+
+
+def _check_lanes(lane_bits: int) -> None:
+    if lane_bits not in (4, 8, 16, 32):
+        raise ValueError("lane_bits must be 4, 8, 16 or 32")
+
+
+@dataclass
+class FitchResult:
+    node_sets: np.ndarray   # uint32 [n_tips-1, n_words] packed state sets, row k = node n_tips+k
+    site_cost: np.ndarray   # uint32 [n_sites]
+    total: int              # sum_s w_s * site_cost[s]
+    lane_bits: int
+    n_sites: int
+
+    def states(self) -> np.ndarray:
+        """Unpacked state sets [n_tips-1, n_sites]."""
+        return unpack_lanes(self.node_sets, self.n_sites, self.lane_bits)
+
+
+def fitch_tree(tree: RootedTree, tip_words: np.ndarray, n_sites: int, lane_bits: int = 4,
+               weights: np.ndarray | None = None, ctx: _native.Context | None = None,
+               site_cost: bool = True) -> FitchResult:
+    """Fitch postorder over packed tip state sets [n_tips, n_words] (uint32)."""
+    _check_lanes(lane_bits)
+    ctx = ctx or _native.default_context()
+    tip_words = np.ascontiguousarray(tip_words, dtype=np.uint32)
+    nw = n_words(n_sites, lane_bits)
+    if tip_words.shape != (tree.n_tips, nw):
+        raise ValueError(f"tip_words must be [{tree.n_tips}, {nw}], got {tip_words.shape}")
+    w = None
+    if weights is not None:
+        w = np.ascontiguousarray(weights, dtype=np.uint32)
+        if w.shape != (n_sites,):
+            raise ValueError("weights must have one entry per site")
+    node_sets = np.empty((tree.n_internal, nw), dtype=np.uint32)
+    sc = np.empty(n_sites, dtype=np.uint32) if site_cost else None
+    total = C.c_uint64(0)
+    t, keep = _native.make_tree(tree.left, tree.right)
+    ctx.call("pgpu_fitch_tree", C.byref(t), _native.ptr(tip_words), _native.ptr(w), n_sites,
+             lane_bits, _native.ptr(node_sets), _native.ptr(sc), C.byref(total))
+    del keep
+    return FitchResult(node_sets, sc if sc is not None else np.empty(0, np.uint32),
+                       int(total.value), lane_bits, n_sites)
+
+
+def fitch_tree_states(tree: RootedTree, tip_states: np.ndarray, lane_bits: int = 4,
+                      weights: np.ndarray | None = None,
+                      ctx: _native.Context | None = None) -> FitchResult:
+    """Same as fitch_tree for unpacked masks [n_tips, n_sites]."""
+    n_sites = tip_states.shape[1]
+    return fitch_tree(tree, pack_lanes(tip_states, lane_bits), n_sites, lane_bits, weights, ctx)
+
+
+def fitch_tree_dev(tree: RootedTree, tips_dev, ld_words: int, n_sites: int, lane_bits: int,
+                   weights_dev, node_sets_dev, site_cost_dev, total_dev,
+                   ctx: _native.Context | None = None, keep: list | None = None) -> None:
+    """Asynchronous device-pointer form (torch tensors or raw addresses)."""
+    ctx = ctx or _native.default_context()
+    t, k = _native.make_tree(tree.left, tree.right)
+    ctx.call("pgpu_fitch_tree_dev", C.byref(t), _native.ptr(tips_dev), ld_words,
+             _native.ptr(weights_dev), n_sites, lane_bits, _native.ptr(node_sets_dev),
+             _native.ptr(site_cost_dev), _native.ptr(total_dev))
+    if keep is not None:
+        keep.append(k)

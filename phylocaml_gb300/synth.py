@@ -1,0 +1,114 @@
+"""Seeded synthetic alignments for the scoring workloads.
+
+No public dataset is involved: every workload is generated here from a seed,
+with the shapes and distributions of the reference workloads (Yule trees,
+GTR+Gamma4 DNA, ambiguity codes, integer pattern weights).
+
+DNA states use phylocaml's bit-flag codes (lib/alphabet.ml:301-307):
+A=1, C=2, G=4, T=8; an IUPAC ambiguity code is the OR of its bases
+(lib/alphabet.ml:309-326) and a gap or missing cell is 0xF in the 4-bit
+layout (all four bases possible).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import tree as _tree
+
+A, C, G, T = 1, 2, 4, 8
+GAP4 = 0xF
+# two- and three-base IUPAC codes (M R W S Y K V H D B) as bit masks
+AMBIGUOUS = np.array([A | C, A | G, A | T, G | C, T | C, G | T,
+                      G | T | C, G | T | A, C | T | A, G | C | A], dtype=np.uint8)
+
+
+def pack_lanes(states: np.ndarray, lane_bits: int) -> np.ndarray:
+    """Packs [rows, n_sites] masks (each < 2**lane_bits) into uint32 words,
+    site s in lane s % (32/lane_bits) of word s // (32/lane_bits)."""
+    states = np.atleast_2d(states)
+    rows, n = states.shape
+    per = 32 // lane_bits
+    n_words = (n * lane_bits + 31) // 32
+    if lane_bits in (4, 8) and states.dtype == np.uint8:
+        # byte-level packing, little-endian words
+        nb = n_words * 4
+        out = np.zeros((rows, nb), dtype=np.uint8)
+        if lane_bits == 8:
+            out[:, :n] = states
+        else:
+            out[:, : n // 2] = states[:, 0 : n - (n % 2) : 2] | (states[:, 1:n:2] << 4)
+            if n % 2:
+                out[:, n // 2] = states[:, n - 1]
+        return out.view("<u4").astype(np.uint32, copy=False)
+    padded = np.zeros((rows, n_words * per), dtype=np.uint32)
+    padded[:, :n] = states
+    padded = padded.reshape(rows, n_words, per)
+    shifts = (np.arange(per, dtype=np.uint32) * lane_bits).astype(np.uint32)
+    return np.bitwise_or.reduce(padded << shifts, axis=2).astype(np.uint32)
+
+
+def unpack_lanes(words: np.ndarray, n_sites: int, lane_bits: int) -> np.ndarray:
+    words = np.atleast_2d(words).astype(np.uint32)
+    per = 32 // lane_bits
+    mask = np.uint32(0xFFFFFFFF if lane_bits == 32 else (1 << lane_bits) - 1)
+    shifts = (np.arange(per, dtype=np.uint32) * lane_bits).astype(np.uint32)
+    lanes = (words[:, :, None] >> shifts) & mask
+    return lanes.reshape(words.shape[0], -1)[:, :n_sites]
+
+
+def jc_states(tr: _tree.RootedTree, n_sites: int, rng: np.random.Generator,
+              n_states: int = 4) -> np.ndarray:
+    """Tip states (0..n_states-1) under a Jukes-Cantor-like process: along a
+    branch of length t each site is redrawn uniformly with probability
+    1 - exp(-t * n/(n-1)).  Returns [n_tips, n_sites] uint8."""
+    n = tr.n_tips
+    tips = np.empty((n, n_sites), dtype=np.uint8)
+    live = {tr.n_nodes - 1: rng.integers(0, n_states, n_sites, dtype=np.uint8)}
+    for v in tr.depth_first_order():
+        k = v - n
+        parent = live.pop(v)
+        for c in (int(tr.left[k]), int(tr.right[k])):
+            p = 1.0 - np.exp(-tr.brlen[c] * n_states / (n_states - 1))
+            row = tips[c] if c < n else np.empty(n_sites, dtype=np.uint8)
+            row[:] = parent
+            m = int(rng.binomial(n_sites, p))
+            if m:
+                idx = rng.integers(0, n_sites, m)
+                row[idx] = rng.integers(0, n_states, m, dtype=np.uint8)
+            if c >= n:
+                live[c] = row
+    return tips
+
+
+def inject_ambiguity(masks: np.ndarray, frac: float, rng: np.random.Generator,
+                     gap_share: float = 0.5) -> np.ndarray:
+    """Replaces, in place, a fraction of cells by IUPAC ambiguity codes or
+    gaps (0xF); returns the array."""
+    m = int(round(frac * masks.size))
+    if m:
+        idx = rng.integers(0, masks.size, m)
+        codes = AMBIGUOUS[rng.integers(0, len(AMBIGUOUS), m)]
+        gap = rng.random(m) < gap_share
+        codes[gap] = GAP4
+        masks.reshape(-1)[idx] = codes
+    return masks
+
+
+def fitch_workload(n_tips: int, n_sites: int, seed: int, ambiguity: float = 0.03,
+                   mean_brlen: float = 0.1, max_weight: int = 8):
+    """Tree, tip masks [n_tips, n_sites] (uint8 4-bit DNA codes) and pattern
+    weights uniform in 1..max_weight."""
+    rng = np.random.default_rng(seed)
+    tr = _tree.yule(n_tips, rng, mean_brlen)
+    masks = jc_states(tr, n_sites, rng)
+    np.left_shift(np.uint8(1), masks, out=masks)
+    masks = inject_ambiguity(masks, ambiguity, rng)
+    weights = rng.integers(1, max_weight + 1, n_sites, dtype=np.uint32)
+    return tr, masks, weights
+
+
+def compress_patterns(columns: np.ndarray):
+    """Collapses identical site columns: [n_tips, n_sites] -> (patterns
+    [n_tips, n_pat], weights [n_pat] float64 counts, site -> pattern index)."""
+    uniq, inverse, counts = np.unique(columns.T, axis=0, return_inverse=True, return_counts=True)
+    return np.ascontiguousarray(uniq.T), counts.astype(np.float64), inverse.reshape(-1)
