@@ -176,7 +176,9 @@ def bench_fitch(args, rank, world, local):
     units = tr.n_internal * n_sites
 
     ctx = _native.Context(local)
-    stream = torch.cuda.current_stream(dev)
+    # an explicit stream: the legacy default stream has handle 0, which the
+    # C ABI reads as "use the context's own stream"
+    stream = torch.cuda.Stream(dev)
     ctx.set_stream(stream.cuda_stream)
     tips = torch.zeros((tr.n_tips, ld), dtype=torch.int32, device=dev)
     tips[:, :nw] = torch.from_numpy(words.view(np.int32)).to(dev)
@@ -184,6 +186,8 @@ def bench_fitch(args, rank, world, local):
     out = torch.empty((tr.n_internal, ld), dtype=torch.int32, device=dev)
     sc = torch.empty(n_sites, dtype=torch.int32, device=dev)
     tot = torch.zeros(1, dtype=torch.int64, device=dev)
+
+    torch.cuda.synchronize(dev)
 
     def step():
         fitch.fitch_tree_dev(tr, tips, ld, n_sites, 4, wd, out, sc, tot, ctx=ctx)

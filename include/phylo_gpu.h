@@ -70,6 +70,9 @@ typedef struct {
 pgpu_status pgpu_create(pgpu_ctx **out, int device);
 void pgpu_destroy(pgpu_ctx *ctx);
 const char *pgpu_last_error(const pgpu_ctx *ctx);
+/* Runs the context's work on cuda_stream (a cudaStream_t).  NULL gives the
+ * context its own non-blocking stream back; the legacy default stream
+ * (handle 0) therefore cannot be selected -- pass an explicit stream. */
 pgpu_status pgpu_set_stream(pgpu_ctx *ctx, void *cuda_stream);
 pgpu_status pgpu_synchronize(pgpu_ctx *ctx);
 /* Number of kernels this library launched on ctx since creation. */

@@ -55,6 +55,12 @@ pgpu_status pgpu_check_flag(pgpu_ctx *ctx, const char *what) {
       return pgpu_set_err(ctx, PGPU_ERR_TIMEOUT, "%s: a device wait gave up", what);
     if (flag & PGPU_FLAG_BADCODE)
       return pgpu_set_err(ctx, PGPU_ERR_ARG, "%s: a tip code is outside the code table", what);
+    if (flag & PGPU_FLAG_NAN)
+      return pgpu_set_err(ctx, PGPU_ERR_NAN, "%s: NaN or Inf in Q or pi (or pi <= 0)", what);
+    if (flag & PGPU_FLAG_NONREV)
+      return pgpu_set_err(ctx, PGPU_ERR_NONREVERSIBLE, "%s: Q is not reversible w.r.t. pi", what);
+    if (flag & PGPU_FLAG_EIGEN)
+      return pgpu_set_err(ctx, PGPU_ERR_EIGEN, "%s: eigendecomposition did not converge", what);
     return pgpu_set_err(ctx, PGPU_ERR_CUDA, "%s: device error flag %d", what, flag);
   }
   return PGPU_OK;

@@ -109,6 +109,15 @@ pgpu_status pgpu_schedule_device(pgpu_ctx *ctx, const pgpu_tree *tree, const Tre
 
 #define PGPU_FLAG_TIMEOUT 1
 #define PGPU_FLAG_BADCODE 2
+#define PGPU_FLAG_NAN 4
+#define PGPU_FLAG_NONREV 8
+#define PGPU_FLAG_EIGEN 16
+
+// error-word bit of a model status (PGPU_ERR_NAN / _NONREVERSIBLE / _EIGEN)
+__host__ __device__ inline int pgpu_model_flag(int st) {
+  return st == PGPU_ERR_NAN ? PGPU_FLAG_NAN
+                            : st == PGPU_ERR_NONREVERSIBLE ? PGPU_FLAG_NONREV : PGPU_FLAG_EIGEN;
+}
 #define PGPU_WAIT_NS 2000000000ull   // 2 s budget for any single device wait
 
 #ifdef __CUDACC__

@@ -1,0 +1,345 @@
+// FP64 transition matrices on the GPU: eigendecomposition of a reversible
+// rate matrix and P(t) = U exp(D t) U^-1.
+//
+// Reference: MlModel.diagonalize (lib/mlModel.ml:554-583) calls LAPACK
+// dsyev/dgeev + dgetrf/dgetri through lib/mlmodel.c:163-262, and
+// MlModel.compose (lib/mlModel.ml:585-587) builds P with two dgemm calls
+// (compose_gtr, lib/mlmodel.c:325-342): P = exp(Q t) read row-major,
+// P[i][j] = Pr(j | i, t); t == -1 returns Q itself and t < 1e-10 the
+// identity (EPSILON, lib/mlmodel.h:17).
+//
+// Here a reversible Q (pi_i Q_ij = pi_j Q_ji) is symmetrised,
+// B = Pi^1/2 Q Pi^-1/2, and B = V diag(lambda) V^T is found with the cyclic
+// two-sided Jacobi method in round-robin order (all n/2 disjoint rotations of
+// a step applied at once), one CTA per matrix, everything in FP64 shared
+// memory.  Then U = Pi^-1/2 V and U^-1 = V^T Pi^1/2, so Q = U diag(lambda) U^-1
+// and P(t) = U diag(exp(lambda t)) U^-1.  Jacobi needs no LAPACK and gives
+// orthogonal V to working precision.
+#include <cmath>
+
+#include "pgpu_internal.cuh"
+#include "pmatrix.cuh"
+
+namespace {
+
+constexpr int MAXS = 64;
+constexpr int LDA = MAXS + 1;   // padded rows against bank conflicts
+
+struct EigArgs {
+  const double *Q;    // [n_models][S][S]
+  const double *pi;   // [n_models][S]
+  double *U;          // [n_models][S][S]
+  double *lam;        // [n_models][S]
+  double *Ui;         // [n_models][S][S]
+  int *status;        // [n_models]: 0 ok, PGPU_ERR_* otherwise
+  int S;
+  int max_sweeps;
+};
+
+__global__ void __launch_bounds__(256) jacobi_eig_kernel(const EigArgs p) {
+  extern __shared__ __align__(16) double sm[];
+  const int S = p.S, N = S + (S & 1);
+  double *A = sm;                     // [N][LDA]
+  double *V = A + (size_t)N * LDA;    // [N][LDA]
+  double *cs = V + (size_t)N * LDA;   // [N/2][2]
+  int *pr = reinterpret_cast<int *>(cs + N);  // [N/2][2]
+  int *order = pr + N;                        // [N]
+  __shared__ double red[8];
+  __shared__ int bad;
+  const int m = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  const double *Q = p.Q + (size_t)m * S * S;
+  const double *pi = p.pi + (size_t)m * S;
+  if (tid == 0) bad = 0;
+  __syncthreads();
+
+  // B = Pi^1/2 Q Pi^-1/2, checked for NaN/Inf and for reversibility
+  for (int e = tid; e < N * N; e += nt) {
+    const int i = e / N, j = e % N;
+    double v = 0.0, vt = 0.0;
+    if (i < S && j < S) {
+      const double qi = Q[i * S + j], qt = Q[j * S + i];
+      const double pi_i = pi[i], pi_j = pi[j];
+      if (!isfinite(qi) || !isfinite(pi_i) || !(pi_i > 0.0)) atomicOr(&bad, 1);
+      v = sqrt(pi_i) * qi / sqrt(pi_j);
+      vt = sqrt(pi_j) * qt / sqrt(pi_i);
+      if (fabs(v - vt) > 1e-10 * (fabs(v) + fabs(vt)) + 1e-300 && fabs(v - vt) > 1e-12)
+        atomicOr(&bad, 2);
+    }
+    A[i * LDA + j] = 0.5 * (v + vt);
+    V[i * LDA + j] = (i == j) ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  if (bad) {
+    if (tid == 0) p.status[m] = (bad & 1) ? PGPU_ERR_NAN : PGPU_ERR_NONREVERSIBLE;
+    return;
+  }
+  if (tid < N) order[tid] = tid;
+  __syncthreads();
+
+  int sweep = 0;
+  bool converged = false;
+  for (; sweep < p.max_sweeps; ++sweep) {
+    // off-diagonal and total squared norms
+    double off = 0.0, fro = 0.0;
+    for (int e = tid; e < N * N; e += nt) {
+      const int i = e / N, j = e % N;
+      const double a = A[i * LDA + j];
+      fro += a * a;
+      if (i != j) off += a * a;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      off += __shfl_xor_sync(0xffffffffu, off, o);
+      fro += __shfl_xor_sync(0xffffffffu, fro, o);
+    }
+    if ((tid & 31) == 0) red[tid >> 5] = off;
+    __syncthreads();
+    double off_t = 0.0;
+    for (int w = 0; w < (nt >> 5); ++w) off_t += red[w];
+    __syncthreads();
+    if ((tid & 31) == 0) red[tid >> 5] = fro;
+    __syncthreads();
+    double fro_t = 0.0;
+    for (int w = 0; w < (nt >> 5); ++w) fro_t += red[w];
+    __syncthreads();
+    if (off_t <= 1e-34 * fro_t) {
+      converged = true;
+      break;
+    }
+    for (int step = 0; step < N - 1; ++step) {
+      // rotation parameters of the N/2 disjoint pairs of this step
+      if (tid < N / 2) {
+        int a = order[tid], b = order[N - 1 - tid];
+        if (a > b) {
+          const int t = a;
+          a = b;
+          b = t;
+        }
+        const double apq = A[a * LDA + b];
+        double c = 1.0, s = 0.0;
+        if (fabs(apq) > 1e-300) {
+          const double th = (A[b * LDA + b] - A[a * LDA + a]) / (2.0 * apq);
+          double t;
+          if (th == 0.0) t = 1.0;
+          else if (fabs(th) > 1e150) t = 0.5 / th;
+          else t = copysign(1.0, th) / (fabs(th) + sqrt(th * th + 1.0));
+          c = 1.0 / sqrt(t * t + 1.0);
+          s = t * c;
+        }
+        pr[2 * tid] = a;
+        pr[2 * tid + 1] = b;
+        cs[2 * tid] = c;
+        cs[2 * tid + 1] = s;
+      }
+      __syncthreads();
+      // rows p, q of every pair
+      for (int e = tid; e < (N / 2) * N; e += nt) {
+        const int k = e / N, j = e % N;
+        const int a = pr[2 * k], b = pr[2 * k + 1];
+        const double c = cs[2 * k], s = cs[2 * k + 1];
+        const double xa = A[a * LDA + j], xb = A[b * LDA + j];
+        A[a * LDA + j] = c * xa - s * xb;
+        A[b * LDA + j] = s * xa + c * xb;
+      }
+      __syncthreads();
+      // columns p, q of every pair, and of V
+      for (int e = tid; e < (N / 2) * N; e += nt) {
+        const int k = e / N, i = e % N;
+        const int a = pr[2 * k], b = pr[2 * k + 1];
+        const double c = cs[2 * k], s = cs[2 * k + 1];
+        const double xa = A[i * LDA + a], xb = A[i * LDA + b];
+        A[i * LDA + a] = c * xa - s * xb;
+        A[i * LDA + b] = s * xa + c * xb;
+        const double va = V[i * LDA + a], vb = V[i * LDA + b];
+        V[i * LDA + a] = c * va - s * vb;
+        V[i * LDA + b] = s * va + c * vb;
+      }
+      __syncthreads();
+      if (tid < N / 2) {
+        const int a = pr[2 * tid], b = pr[2 * tid + 1];
+        A[a * LDA + b] = 0.0;
+        A[b * LDA + a] = 0.0;
+      }
+      // next round-robin arrangement: position 0 fixed, the rest rotate
+      if (tid == 0) {
+        const int last = order[N - 1];
+        for (int i = N - 1; i > 1; --i) order[i] = order[i - 1];
+        order[1] = last;
+      }
+      __syncthreads();
+    }
+  }
+  // outputs: lambda, U = Pi^-1/2 V, Ui = V^T Pi^1/2
+  for (int e = tid; e < S * S; e += nt) {
+    const int i = e / S, j = e % S;
+    p.U[(size_t)m * S * S + e] = V[i * LDA + j] / sqrt(pi[i]);
+    p.Ui[(size_t)m * S * S + e] = V[j * LDA + i] * sqrt(pi[j]);
+  }
+  for (int i = tid; i < S; i += nt) p.lam[(size_t)m * S + i] = A[i * LDA + i];
+  if (tid == 0) p.status[m] = converged ? 0 : PGPU_ERR_EIGEN;
+}
+
+// P[b][r] = U diag(exp(lambda * rate_r * t_b)) Ui for every branch b and
+// rate r of one model.  One CTA per branch.  Writes FP64 and, if P32 is
+// given, an FP32 copy.  t == -1 (compose only) gives Q; t < 1e-10 gives I.
+struct ComposeArgs {
+  const double *U, *lam, *Ui;   // one model
+  const double *t;              // [n_br]
+  const double *rates;          // [R] or null (rate 1)
+  double *P;                    // [n_br][R][S][S] or null
+  float *P32;                   // [n_br][R][S][S] or null
+  int S, R;
+  int n_br;
+  int allow_q;                  // t == -1 returns Q (the reference's compose)
+  const int *status;            // eigendecomposition status or null
+  int *flag;
+};
+
+__global__ void __launch_bounds__(256) compose_kernel(const ComposeArgs p) {
+  extern __shared__ __align__(16) double sm[];
+  const int S = p.S, R = p.R, SS = S * S;
+  double *U = sm, *Ui = U + SS, *e = Ui + SS;   // e: [R][S]
+  const int b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  if (p.status && *p.status) {
+    if (b == 0 && tid == 0) atomicOr(p.flag, pgpu_model_flag(*p.status));
+    return;
+  }
+  for (int i = tid; i < SS; i += nt) {
+    U[i] = p.U[i];
+    Ui[i] = p.Ui[i];
+  }
+  const double t = p.t[b];
+  const bool q_mode = p.allow_q && t == -1.0;
+  const bool ident = !q_mode && !(t >= 1e-10);
+  for (int i = tid; i < R * S; i += nt) {
+    const int r = i / S, k = i % S;
+    const double rate = p.rates ? p.rates[r] : 1.0;
+    e[i] = q_mode ? p.lam[k] * rate : exp(p.lam[k] * rate * t);
+  }
+  __syncthreads();
+  for (int o = tid; o < R * SS; o += nt) {
+    const int r = o / SS, i = (o % SS) / S, j = o % S;
+    double v;
+    if (ident) {
+      v = (i == j) ? 1.0 : 0.0;
+    } else {
+      v = 0.0;
+      for (int k = 0; k < S; ++k) v = fma(U[i * S + k] * e[r * S + k], Ui[k * S + j], v);
+    }
+    const size_t off = ((size_t)b * R + r) * SS + (size_t)i * S + j;
+    if (p.P) p.P[off] = v;
+    if (p.P32) p.P32[off] = (float)v;
+  }
+}
+
+size_t eig_smem(int S) {
+  const int N = S + (S & 1);
+  return sizeof(double) * (2 * (size_t)N * LDA + N) + sizeof(int) * 2 * (size_t)N;
+}
+
+}  // namespace
+
+pgpu_status pgpu_launch_eig(pgpu_ctx *ctx, const double *Q_dev, const double *pi_dev, int S,
+                            int n_models, double *U_dev, double *lam_dev, double *Ui_dev,
+                            int *status_dev) {
+  if (S < 1 || S > MAXS)
+    return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "model: %d states; at most %d are supported", S, MAXS);
+  EigArgs a{Q_dev, pi_dev, U_dev, lam_dev, Ui_dev, status_dev, S, 40};
+  const size_t smem = eig_smem(S);
+  PGPU_CUDA(ctx, cudaFuncSetAttribute(jacobi_eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+  jacobi_eig_kernel<<<n_models, S <= 8 ? 64 : 256, smem, ctx->stream>>>(a);
+  return pgpu_after_launch(ctx, "jacobi_eig_kernel");
+}
+
+pgpu_status pgpu_launch_compose(pgpu_ctx *ctx, const double *U_dev, const double *lam_dev,
+                                const double *Ui_dev, int S, const double *t_dev, int n_br,
+                                const double *rates_dev, int R, double *P_dev, float *P32_dev,
+                                bool allow_q, const int *status_dev) {
+  if (n_br <= 0) return PGPU_OK;
+  ComposeArgs a{U_dev, lam_dev, Ui_dev, t_dev,       rates_dev,  P_dev,       P32_dev,
+                S,     R,       n_br,   allow_q ? 1 : 0, status_dev, ctx->d_flag};
+  const size_t smem = sizeof(double) * (2 * (size_t)S * S + (size_t)R * S);
+  PGPU_CUDA(ctx, cudaFuncSetAttribute(compose_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)std::max<size_t>(smem, 1024)));
+  const int threads = R * S * S <= 64 ? 64 : (R * S * S <= 128 ? 128 : 256);
+  compose_kernel<<<n_br, threads, smem, ctx->stream>>>(a);
+  return pgpu_after_launch(ctx, "compose_kernel");
+}
+
+// ---------------------------------------------------------------------------
+// C ABI (host buffers)
+// ---------------------------------------------------------------------------
+
+static pgpu_status status_to_err(pgpu_ctx *ctx, int st) {
+  switch (st) {
+    case 0: return PGPU_OK;
+    case PGPU_ERR_NAN: return pgpu_set_err(ctx, st, "model: NaN or Inf in Q or pi (or pi <= 0)");
+    case PGPU_ERR_NONREVERSIBLE:
+      return pgpu_set_err(ctx, st, "model: Q is not reversible with respect to pi");
+    case PGPU_ERR_EIGEN:
+      return pgpu_set_err(ctx, st, "model: Jacobi eigendecomposition did not converge");
+    default: return pgpu_set_err(ctx, PGPU_ERR_CUDA, "model: status %d", st);
+  }
+}
+
+extern "C" {
+
+pgpu_status pgpu_model_diagonalize(pgpu_ctx *ctx, const double *Q, const double *pi, int S,
+                                   double *U, double *lambda, double *Ui) {
+  if (!ctx) return PGPU_ERR_ARG;
+  if (!Q || !pi || !U || !lambda || !Ui) return pgpu_set_err(ctx, PGPU_ERR_ARG, "model: null buffer");
+  if (S < 1 || S > MAXS) return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "model: 1..%d states", MAXS);
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  const size_t SS = (size_t)S * S;
+  void *dq, *dpi, *du, *dl, *dui, *dst;
+  PGPU_TRY(pgpu_buf(ctx, BUF_A, SS * 8, &dq));
+  PGPU_TRY(pgpu_buf(ctx, BUF_B, S * 8, &dpi));
+  PGPU_TRY(pgpu_buf(ctx, BUF_C, SS * 8, &du));
+  PGPU_TRY(pgpu_buf(ctx, BUF_D, S * 8, &dl));
+  PGPU_TRY(pgpu_buf(ctx, BUF_E, SS * 8, &dui));
+  PGPU_TRY(pgpu_buf(ctx, BUF_SCALAR, 64, &dst));
+  cudaStream_t s = ctx->stream;
+  PGPU_CUDA(ctx, cudaMemcpyAsync(dq, Q, SS * 8, cudaMemcpyHostToDevice, s));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(dpi, pi, S * 8, cudaMemcpyHostToDevice, s));
+  PGPU_TRY(pgpu_launch_eig(ctx, (double *)dq, (double *)dpi, S, 1, (double *)du, (double *)dl,
+                           (double *)dui, (int *)dst));
+  int *hst = reinterpret_cast<int *>(ctx->h_pinned);
+  PGPU_CUDA(ctx, cudaMemcpyAsync(hst, dst, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(U, du, SS * 8, cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(lambda, dl, S * 8, cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(Ui, dui, SS * 8, cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  return status_to_err(ctx, *hst);
+}
+
+pgpu_status pgpu_model_compose(pgpu_ctx *ctx, const double *U, const double *lambda,
+                               const double *Ui, int S, const double *t, size_t n_t,
+                               double *P_out) {
+  if (!ctx) return PGPU_ERR_ARG;
+  if (!U || !lambda || !Ui || !P_out || (n_t && !t))
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "compose: null buffer");
+  if (S < 1 || S > MAXS) return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "compose: 1..%d states", MAXS);
+  if (n_t == 0) return PGPU_OK;
+  if (n_t > 0x7fffffff) return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "compose: too many branch lengths");
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  const size_t SS = (size_t)S * S;
+  void *du, *dl, *dui, *dt, *dp;
+  PGPU_TRY(pgpu_buf(ctx, BUF_C, SS * 8, &du));
+  PGPU_TRY(pgpu_buf(ctx, BUF_D, S * 8, &dl));
+  PGPU_TRY(pgpu_buf(ctx, BUF_E, SS * 8, &dui));
+  PGPU_TRY(pgpu_buf(ctx, BUF_F, n_t * 8, &dt));
+  PGPU_TRY(pgpu_buf(ctx, BUF_G, n_t * SS * 8, &dp));
+  cudaStream_t s = ctx->stream;
+  PGPU_CUDA(ctx, cudaMemcpyAsync(du, U, SS * 8, cudaMemcpyHostToDevice, s));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(dl, lambda, S * 8, cudaMemcpyHostToDevice, s));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(dui, Ui, SS * 8, cudaMemcpyHostToDevice, s));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(dt, t, n_t * 8, cudaMemcpyHostToDevice, s));
+  PGPU_TRY(pgpu_launch_compose(ctx, (double *)du, (double *)dl, (double *)dui, S, (double *)dt,
+                               (int)n_t, nullptr, 1, (double *)dp, nullptr, true));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(P_out, dp, n_t * SS * 8, cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  return PGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,19 @@
+// Launchers shared by the likelihood translation units (pmatrix.cu).
+#pragma once
+#include "pgpu_internal.cuh"
+
+// Eigendecomposition of n_models reversible S x S rate matrices (device
+// buffers).  status_dev[m] receives 0 or a PGPU_ERR_* code per model.
+pgpu_status pgpu_launch_eig(pgpu_ctx *ctx, const double *Q_dev, const double *pi_dev, int S,
+                            int n_models, double *U_dev, double *lam_dev, double *Ui_dev,
+                            int *status_dev);
+
+// P[b][r] = U diag(exp(lambda * rates[r] * t[b])) Ui for n_br branch lengths
+// of one model; FP64 into P_dev and/or FP32 into P32_dev (either may be
+// null).  With allow_q, t == -1 yields Q (MlModel.compose's special case).
+// If status_dev is given and non-zero the matrices are not built and the
+// context's error word records the model failure.
+pgpu_status pgpu_launch_compose(pgpu_ctx *ctx, const double *U_dev, const double *lam_dev,
+                                const double *Ui_dev, int S, const double *t_dev, int n_br,
+                                const double *rates_dev, int R, double *P_dev, float *P32_dev,
+                                bool allow_q, const int *status_dev = nullptr);

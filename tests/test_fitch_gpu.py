@@ -140,7 +140,9 @@ def test_tree_device_api_matches_host_api(ctx):
     sc = torch.zeros(50_001, dtype=torch.int32, device=dev)
     wd = torch.from_numpy(w.view(np.int32)).to(dev)
     tot = torch.zeros(1, dtype=torch.int64, device=dev)
-    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.synchronize(dev)
+    ctx.set_stream(stream.cuda_stream)
     try:
         fitch.fitch_tree_dev(tr, tips, ld, 50_001, 4, wd, out, sc, tot, ctx=ctx)
         ctx.synchronize()
