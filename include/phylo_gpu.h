@@ -142,6 +142,68 @@ pgpu_status pgpu_fitch_tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree,
                                 int lane_bits, uint32_t *node_sets_dev,
                                 uint32_t *site_cost_dev, uint64_t *total_dev);
 
+/* ---- substitution models and transition matrices (FP64 on the GPU) ----
+ * Q is row-major, rows sum to zero, and reversible with respect to pi
+ * (pi_i Q_ij = pi_j Q_ji) -- the models MlModel.create builds
+ * (lib/mlModel.ml:664-746: JC69 ... GTR).  Non-reversible matrices are
+ * rejected with PGPU_ERR_NONREVERSIBLE. */
+typedef struct {
+  int32_t n_states;      /* S */
+  int32_t n_rates;       /* R, rate classes (DiscreteGamma/Custom, mlModel.mli:11-19) */
+  const double *Q;       /* [S][S] */
+  const double *pi;      /* [S] stationary frequencies (priors) */
+  const double *rates;   /* [R] rate multipliers */
+  const double *probs;   /* [R] class probabilities */
+} pgpu_model;
+
+/* Partial likelihood of each tip code: row c is the vector a tip with code
+ * c contributes (1 for every state the code allows; all ones for a gap
+ * treated as missing). */
+typedef struct {
+  int32_t n_codes;       /* 1..256 */
+  const double *table;   /* [n_codes][S] */
+} pgpu_tip_codes;
+
+/* MlModel.diagonalize (lib/mlModel.ml:554-583; likelihood_CAML_diagonalize_gtr
+ * and _sym, lib/mlmodel.c:200-271): Q = U diag(lambda) Ui, row-major, on
+ * the GPU in FP64 (Jacobi on Pi^1/2 Q Pi^-1/2).  S <= 64. */
+pgpu_status pgpu_model_diagonalize(pgpu_ctx *ctx, const double *Q, const double *pi, int S,
+                                   double *U, double *lambda, double *Ui);
+
+/* MlModel.compose for n_t branch lengths (lib/mlModel.ml:585-587;
+ * compose_gtr, lib/mlmodel.c:325-342): P_out[k] = U diag(exp(lambda t[k])) Ui,
+ * row-major, P[i][j] = Pr(j | i, t).  t == -1 returns Q, t < 1e-10 the
+ * identity, as the reference does. */
+pgpu_status pgpu_model_compose(pgpu_ctx *ctx, const double *U, const double *lambda,
+                               const double *Ui, int S, const double *t, size_t n_t,
+                               double *P_out);
+
+/* ---- Felsenstein pruning -------------------------------------------------
+ * The tree log-likelihood that Likelihood_c.median_2 / root_cost would
+ * compute (lib/likelihood_c.ml:15-21, stubs in the reference) for
+ * n_pat weighted site patterns:
+ *   tip_codes  [n_tips][n_pat] codes into codes->table
+ *   weights    [n_pat] pattern weights, or NULL for 1
+ *   precision  32: FP32 conditional likelihoods; 64: the FP64 form.  P
+ *              matrices are always built in FP64 on the GPU; the log-
+ *              likelihood is always summed in FP64 with compensation.
+ *   lnl        out: sum_s weights[s] * site_lnl[s]
+ *   site_lnl   [n_pat] out (or NULL)
+ * tree->brlen is required.  This entry point takes S = 4 (DNA); 20- and
+ * 61-state models go through the batched tensor-core path. */
+pgpu_status pgpu_prune_lnl(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *model,
+                           const pgpu_tip_codes *codes, const uint8_t *tip_codes,
+                           const double *weights, size_t n_pat, int precision, double *lnl,
+                           double *site_lnl);
+
+/* Device-pointer form, asynchronous on the context's stream: tip rows
+ * ld_pat bytes apart (ld_pat % 16 == 0, 16-byte aligned), *lnl_dev a
+ * device double.  tree, model and codes stay host structures. */
+pgpu_status pgpu_prune_lnl_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *model,
+                               const pgpu_tip_codes *codes, const uint8_t *tip_codes_dev,
+                               size_t ld_pat, const double *weights_dev, size_t n_pat,
+                               int precision, double *lnl_dev, double *site_lnl_dev);
+
 #ifdef __cplusplus
 }
 #endif

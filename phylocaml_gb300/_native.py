@@ -55,6 +55,13 @@ class PgpuModel(C.Structure):
     ]
 
 
+class PgpuTipCodes(C.Structure):
+    _fields_ = [
+        ("n_codes", C.c_int32),
+        ("table", C.POINTER(C.c_double)),
+    ]
+
+
 _P = C.c_void_p
 _SZ = C.c_size_t
 _I = C.c_int
@@ -76,6 +83,12 @@ SIGNATURES: dict[str, tuple] = {
     "pgpu_fitch_distance": (_I, [_P, _P, _P, _SZ, _I, _U64P]),
     "pgpu_fitch_tree": (_I, [_P, C.POINTER(PgpuTree), _P, _P, _SZ, _I, _P, _P, _U64P]),
     "pgpu_fitch_tree_dev": (_I, [_P, C.POINTER(PgpuTree), _P, _SZ, _P, _SZ, _I, _P, _P, _P]),
+    "pgpu_model_diagonalize": (_I, [_P, _P, _P, _I, _P, _P, _P]),
+    "pgpu_model_compose": (_I, [_P, _P, _P, _P, _I, _P, _SZ, _P]),
+    "pgpu_prune_lnl": (_I, [_P, C.POINTER(PgpuTree), C.POINTER(PgpuModel),
+                            C.POINTER(PgpuTipCodes), _P, _P, _SZ, _I, _DP, _P]),
+    "pgpu_prune_lnl_dev": (_I, [_P, C.POINTER(PgpuTree), C.POINTER(PgpuModel),
+                                C.POINTER(PgpuTipCodes), _P, _SZ, _P, _SZ, _I, _P, _P]),
 }
 
 _lib = None

@@ -116,6 +116,11 @@ void pgpu_destroy(pgpu_ctx *ctx) {
   for (int i = 0; i < BUF_COUNT; ++i)
     if (ctx->buf[i]) cudaFree(ctx->buf[i]);
   if (ctx->d_flag) cudaFree(ctx->d_flag);
+  for (int k = 0; k < 2; ++k) {
+    if (ctx->stage_h[k]) cudaFreeHost(ctx->stage_h[k]);
+    if (ctx->stage_d[k]) cudaFree(ctx->stage_d[k]);
+    if (ctx->stage_ev[k]) cudaEventDestroy(ctx->stage_ev[k]);
+  }
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   (void)cudaGetLastError();

@@ -129,26 +129,41 @@ struct FitchTreeArgs {
   int *flag;
   size_t ld, n_words, n_sites;
   int32_t n_tips, n_ops;
-  int W, stages, depth;
+  int W, depth;               // W words per tile (4 per consumer thread)
 };
 
+constexpr int FT_STAGES = 16;   // ring depth (power of two)
+
 template <int LB>
-__global__ void __launch_bounds__(544) fitch_tree_kernel(const FitchTreeArgs p) {
+__device__ __forceinline__ uint4 fitch_quad(const uint4 a, const uint4 b, const uint4 valid,
+                                            uint4 &e) {
+  uint4 m;
+  m.x = fitch_word<LB>(a.x, b.x, e.x) & valid.x;
+  m.y = fitch_word<LB>(a.y, b.y, e.y) & valid.y;
+  m.z = fitch_word<LB>(a.z, b.z, e.z) & valid.z;
+  m.w = fitch_word<LB>(a.w, b.w, e.w) & valid.w;
+  return m;
+}
+
+template <int LB>
+__global__ void __launch_bounds__(160) fitch_tree_kernel(const FitchTreeArgs p) {
   constexpr int PER = Lanes<LB>::PER;
   constexpr uint32_t FLUSH = Lanes<LB>::FLUSH;
+  constexpr uint32_t LSB = Lanes<LB>::H >> (LB - 1);
+  constexpr int ST = FT_STAGES;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ unsigned long long red[32];
-  const int W = p.W, S = p.stages;
+  const int W = p.W, Q = W / 4;   // Q consumer threads, one uint4 each
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);
-  uint64_t *empty = full + S;
-  uint32_t *ring = reinterpret_cast<uint32_t *>(smem + 16 * S);  // [S][W]
-  uint32_t *stk = ring + (size_t)S * W;                           // [depth][W]
+  uint64_t *empty = full + ST;
+  uint4 *ring = reinterpret_cast<uint4 *>(smem + 16 * ST);   // [ST][Q]
+  uint4 *stk = ring + (size_t)ST * Q;                         // [depth][Q]
   const size_t tile0 = (size_t)blockIdx.x * W;
   const int tid = threadIdx.x;
-  const int n_consumer_warps = W / 32;
+  const int n_consumer_warps = Q / 32;
 
   if (tid == 0) {
-    for (int s = 0; s < S; ++s) {
+    for (int s = 0; s < ST; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], n_consumer_warps);
     }
@@ -162,49 +177,62 @@ __global__ void __launch_bounds__(544) fitch_tree_kernel(const FitchTreeArgs p) 
       const size_t span = min((size_t)W, p.ld - tile0);
       const uint32_t bytes = (uint32_t)(span * sizeof(uint32_t));
       int issued = 0;
-      bool ok = true;
-      for (int j = 0; j < p.n_tips && ok; ++j) {
-        const int slot = j % S, round = j / S;
-        if (round > 0) ok = mbar_wait_bounded(&empty[slot], (round - 1) & 1, p.flag);
-        if (!ok) break;
+      for (int j = 0; j < p.n_tips; ++j) {
+        const int slot = j & (ST - 1), round = j / ST;
+        if (round > 0 && !mbar_wait_bounded(&empty[slot], (round - 1) & 1, p.flag)) break;
         const int32_t tip = __ldg(p.tip_seq + j);
         mbar_arrive_expect_tx(&full[slot], bytes);
-        bulk_g2s(ring + (size_t)slot * W, p.tips + (size_t)tip * p.ld + tile0, bytes, &full[slot]);
+        bulk_g2s(ring + (size_t)slot * Q, p.tips + (size_t)tip * p.ld + tile0, bytes, &full[slot]);
         issued = j + 1;
       }
       // every issued copy must land before this CTA may exit
-      for (int j = max(0, issued - S); j < issued; ++j)
-        (void)mbar_wait_bounded(&full[j % S], (j / S) & 1, p.flag);
+      for (int j = max(0, issued - ST); j < issued; ++j)
+        (void)mbar_wait_bounded(&full[j & (ST - 1)], (j / ST) & 1, p.flag);
     }
     return;
   }
 
-  // ---------------- consumers ----------------
+  // ---------------- consumers: words 4c .. 4c+3 of the tile ----------------
   const int c = tid - 32;
   const int lane = tid & 31;
-  const size_t word = tile0 + c;
-  const bool active = word < p.n_words;
-  const uint32_t valid = active ? valid_lanes<LB>(word, p.n_sites) : 0u;
-  const uint32_t valid_lsb = valid & (Lanes<LB>::H >> (LB - 1));
-  uint32_t cnt = 0;                 // LB-bit lane counters
-  uint32_t acc[PER];                // per-site counters
+  const size_t word0 = tile0 + 4 * (size_t)c;
+  const bool active = word0 < p.ld;           // the quad lies inside the row
+  uint4 valid;
+  valid.x = valid_lanes<LB>(word0 + 0, p.n_sites);
+  valid.y = valid_lanes<LB>(word0 + 1, p.n_sites);
+  valid.z = valid_lanes<LB>(word0 + 2, p.n_sites);
+  valid.w = valid_lanes<LB>(word0 + 3, p.n_sites);
+  uint4 cnt = make_uint4(0, 0, 0, 0);   // LB-bit lane counters
+  uint32_t acc[4][PER];                  // per-site counters
 #pragma unroll
-  for (int l = 0; l < PER; ++l) acc[l] = 0;
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int l = 0; l < PER; ++l) acc[q][l] = 0;
   uint32_t since = 0;
-  int sp = 0;
-  int taken = 0;
+  int sp = 0, taken = 0;
   bool ok = true;
 
-  auto take = [&](uint32_t &v) {
-    const int slot = taken % S;
+  auto flush = [&]() {
+#pragma unroll
+    for (int l = 0; l < PER; ++l) {
+      acc[0][l] += (cnt.x >> (l * LB)) & FLUSH;
+      acc[1][l] += (cnt.y >> (l * LB)) & FLUSH;
+      acc[2][l] += (cnt.z >> (l * LB)) & FLUSH;
+      acc[3][l] += (cnt.w >> (l * LB)) & FLUSH;
+    }
+    cnt = make_uint4(0, 0, 0, 0);
+  };
+  auto take = [&](uint4 &v) {
+    const int slot = taken & (ST - 1);
     // every lane waits and the verdict is made warp-uniform before any
     // warp-synchronous step, so a timeout cannot split the warp
-    const bool got = __all_sync(0xffffffffu, mbar_wait_bounded(&full[slot], (taken / S) & 1, p.flag));
+    const bool got =
+        __all_sync(0xffffffffu, mbar_wait_bounded(&full[slot], (taken / ST) & 1, p.flag));
     if (!got) {
       ok = false;
       return;
     }
-    v = ring[(size_t)slot * W + c];
+    v = ring[(size_t)slot * Q + c];
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[slot]);
     ++taken;
@@ -212,41 +240,47 @@ __global__ void __launch_bounds__(544) fitch_tree_kernel(const FitchTreeArgs p) 
 
   for (int i = 0; i < p.n_ops && ok; ++i) {
     const int4 op = __ldg(p.ops + i);
-    uint32_t x = 0, y = 0;
-    if (op.z >= p.n_tips) y = stk[(size_t)(--sp) * W + c];
-    if (op.y >= p.n_tips) x = stk[(size_t)(--sp) * W + c];
+    uint4 x = make_uint4(0, 0, 0, 0), y = make_uint4(0, 0, 0, 0);
+    if (op.z >= p.n_tips) y = stk[(size_t)(--sp) * Q + c];
+    if (op.y >= p.n_tips) x = stk[(size_t)(--sp) * Q + c];
     if (op.y < p.n_tips) take(x);
     if (op.z < p.n_tips && ok) take(y);
     if (!ok) break;
-    uint32_t e;
-    const uint32_t med = fitch_word<LB>(x, y, e) & valid;
-    stk[(size_t)(sp++) * W + c] = med;
-    if (active) __stcs(p.node_sets + (size_t)op.x * p.ld + word, med);
-    cnt += e & valid_lsb;
+    uint4 e;
+    const uint4 med = fitch_quad<LB>(x, y, valid, e);
+    stk[(size_t)(sp++) * Q + c] = med;
+    if (active) __stcs(reinterpret_cast<uint4 *>(p.node_sets + (size_t)op.x * p.ld + word0), med);
+    cnt.x += e.x & valid.x & LSB;
+    cnt.y += e.y & valid.y & LSB;
+    cnt.z += e.z & valid.z & LSB;
+    cnt.w += e.w & valid.w & LSB;
     if (LB < 32 && ++since == FLUSH) {
-#pragma unroll
-      for (int l = 0; l < PER; ++l) acc[l] += (cnt >> (l * LB)) & (FLUSH);
-      cnt = 0;
+      flush();
       since = 0;
     }
   }
   if (LB < 32) {
-#pragma unroll
-    for (int l = 0; l < PER; ++l) acc[l] += (cnt >> (l * LB)) & (FLUSH);
+    flush();
   } else {
-    acc[0] += cnt;
+    acc[0][0] += cnt.x;
+    acc[1][0] += cnt.y;
+    acc[2][0] += cnt.z;
+    acc[3][0] += cnt.w;
   }
 
   unsigned long long wsum = 0;
-  if (active && ok) {
-    const size_t s0 = word * PER;
+  if (ok) {
 #pragma unroll
-    for (int l = 0; l < PER; ++l) {
-      const size_t s = s0 + l;
-      if (s < p.n_sites) {
-        if (p.site_cost) p.site_cost[s] = acc[l];
-        const uint32_t w = p.weights ? __ldg(p.weights + s) : 1u;
-        wsum += (unsigned long long)w * acc[l];
+    for (int q = 0; q < 4; ++q) {
+      const size_t s0 = (word0 + q) * PER;
+#pragma unroll
+      for (int l = 0; l < PER; ++l) {
+        const size_t s = s0 + l;
+        if (s < p.n_sites) {
+          if (p.site_cost) p.site_cost[s] = acc[q][l];
+          const uint32_t w = p.weights ? __ldg(p.weights + s) : 1u;
+          wsum += (unsigned long long)w * acc[q][l];
+        }
       }
     }
   }
@@ -254,7 +288,7 @@ __global__ void __launch_bounds__(544) fitch_tree_kernel(const FitchTreeArgs p) 
   wsum = warp_sum_u64(wsum);
   const int cw = c >> 5;
   if (lane == 0) red[cw] = wsum;
-  asm volatile("bar.sync 1, %0;" ::"r"(W) : "memory");
+  asm volatile("bar.sync 1, %0;" ::"r"(Q) : "memory");
   if (cw == 0) {
     unsigned long long s = lane < n_consumer_warps ? red[lane] : 0ull;
     s = warp_sum_u64(s);
@@ -327,11 +361,11 @@ pgpu_status pair_host(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b, const
 
 template <int LB>
 pgpu_status launch_tree(pgpu_ctx *ctx, FitchTreeArgs &args, size_t n_tiles) {
-  const size_t smem = 16 * (size_t)args.stages + 4 * (size_t)(args.stages + args.depth) * args.W;
+  const size_t smem = 16 * (size_t)FT_STAGES + 4 * (size_t)(FT_STAGES + args.depth) * args.W;
   PGPU_CUDA(ctx, cudaFuncSetAttribute(fitch_tree_kernel<LB>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)std::max<size_t>(smem, 48 * 1024)));
-  fitch_tree_kernel<LB><<<(unsigned)n_tiles, 32 + args.W, smem, ctx->stream>>>(args);
+  fitch_tree_kernel<LB><<<(unsigned)n_tiles, 32 + args.W / 4, smem, ctx->stream>>>(args);
   return pgpu_after_launch(ctx, "fitch_tree_kernel");
 }
 
@@ -355,15 +389,22 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
   PGPU_CUDA(ctx, cudaMemsetAsync(total, 0, sizeof(uint64_t), s));
   if (n_words == 0) return PGPU_OK;
 
-  // tile width: about two tiles per SM, 32..512 words, and shared memory for
-  // the ring and the stack within 100 KB so two CTAs fit on an SM
-  const size_t target_tiles = (size_t)std::max(ctx->num_sms, 1) * 2;
-  size_t W = (n_words + target_tiles - 1) / target_tiles;
-  W = std::min<size_t>(std::max<size_t>((W + 31) / 32 * 32, 64), 512);
-  int stages = 16;
+  // tile width W = 128 * cw words (cw consumer warps of 32 threads x 4 words):
+  // the one that minimises the words the busiest SM handles, given that
+  // every SM takes ceil(tiles / SMs) tiles; ties go to the wider tile
   const int depth = sch->max_depth;
-  while (W > 32 && 16 * stages + 4 * (size_t)(stages + depth) * W > 100 * 1024) W -= 32;
-  if (16 * stages + 4 * (size_t)(stages + depth) * W > ctx->smem_optin)
+  const size_t sms = (size_t)std::max(ctx->num_sms, 1);
+  size_t W = 128, best = ~size_t(0);
+  for (size_t cw = 1; cw <= 4; ++cw) {
+    const size_t w = 128 * cw, tiles = (n_words + w - 1) / w;
+    const size_t cost = (tiles + sms - 1) / sms * w;
+    if (cost <= best) {
+      best = cost;
+      W = w;
+    }
+  }
+  const size_t smem = 16 * (size_t)FT_STAGES + 4 * (size_t)(FT_STAGES + depth) * W;
+  if (smem > ctx->smem_optin)
     return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: tree needs a stack of %d rows; too deep",
                         depth);
   FitchTreeArgs args;
@@ -381,7 +422,6 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
   args.n_tips = n;
   args.n_ops = (int32_t)sch->ops.size();
   args.W = (int)W;
-  args.stages = stages;
   args.depth = depth;
   const size_t n_tiles = (n_words + W - 1) / W;
   switch (lb) {

@@ -65,6 +65,12 @@ struct pgpu_ctx {
   bool sched_valid = false;
   std::vector<int32_t> sched_left, sched_right;
   TreeSchedule sched;
+  // double-buffered pinned staging of small per-call parameters
+  void *stage_h[2] = {};
+  void *stage_d[2] = {};
+  size_t stage_cap[2] = {};
+  cudaEvent_t stage_ev[2] = {};
+  int stage_next = 0, stage_cur = 0;
 };
 
 pgpu_status pgpu_set_err(pgpu_ctx *ctx, pgpu_status st, const char *fmt, ...);
@@ -92,6 +98,12 @@ pgpu_status pgpu_buf(pgpu_ctx *ctx, int slot, size_t bytes, void **out);
 pgpu_status pgpu_after_launch(pgpu_ctx *ctx, const char *what);
 // Reads and clears the device error word after a synchronize.
 pgpu_status pgpu_check_flag(pgpu_ctx *ctx, const char *what);
+// Pinned host block and its device twin for `bytes` of small parameters;
+// fill *host, then pgpu_stage_commit copies it on the context's stream.
+// Two blocks alternate, so the host only waits for the copy issued two
+// calls earlier.
+pgpu_status pgpu_stage(pgpu_ctx *ctx, size_t bytes, void **host, void **dev);
+pgpu_status pgpu_stage_commit(pgpu_ctx *ctx, size_t bytes);
 
 // ---------------------------------------------------------------------------
 // tree schedule (schedule.cpp)

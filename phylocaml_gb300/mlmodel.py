@@ -1,0 +1,266 @@
+"""MlModel for the GPU (lib/mlModel.ml, lib/mlModel.mli).
+
+The specification types and ``create`` follow the reference: the rate matrix
+Q of each substitution model is assembled on the host in FP64 exactly as
+lib/mlModel.ml does (off-diagonal rates times the target frequency, diagonal
+the negative row sum, then mean rate normalised to 1, m_meanrate
+lib/mlModel.ml:204-213), and the eigendecomposition (``diagonalize``) and
+``compose`` run on the GPU in FP64 through the C ABI.
+
+Supported: JC69, F81, K2P, F84, HKY85, TN93, GTR and Const (a given matrix,
+m_file lib/mlModel.ml:473-488) with gaps as missing data; site variation
+Constant, DiscreteGamma(k, alpha) and DiscreteCustom.  DiscreteGamma uses the
+means of k equal-probability categories (Yang 1994), which is what
+lib/mlModel.mli:12-13 documents and test/mlModelTest.ml:44-60 checks (mean
+rate 1); the reference's own gamma_rates (lib/mlModel.ml:93-99) takes
+quantiles at i/k instead and gives a first rate of 0 -- ``gamma_rates_quantile``
+reproduces that for comparison.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native
+
+MINIMUM = 1e-13          # lib/mlModel.ml:8
+EPSILON_FLOAT = 2.220446049250313e-16
+
+
+class Error(ValueError):
+    """MlModel.Error (lib/mlModel.ml:3)."""
+
+
+@dataclass
+class Spec:
+    """MlModel.s (lib/mlModel.ml:38-44) for a gap-as-missing alphabet."""
+    substitution: tuple                 # ("JC69",) ("F81",) ("K2P", b) ("F84", k) ("HKY85", k)
+                                        # ("TN93", (a, b)) ("GTR", co) ("Const", matrix)
+    site_variation: tuple = ("Constant",)   # ("DiscreteGamma", k, alpha) | ("DiscreteCustom", [(r, p)])
+    base_priors: object = "Equal"           # "Equal" | ("Empirical", freqs)
+    alphabet_size: int = 4
+
+
+@dataclass
+class Model:
+    """MlModel.t (lib/mlModel.ml:53-63) with the eigen system from the GPU."""
+    spec: Spec
+    priors: np.ndarray
+    rates: np.ndarray
+    probs: np.ndarray
+    q: np.ndarray
+    u: np.ndarray
+    lam: np.ndarray
+    ui: np.ndarray
+    _keep: list = field(default_factory=list, repr=False)
+
+    @property
+    def n_states(self) -> int:
+        return self.q.shape[0]
+
+    def to_pgpu(self):
+        """(pgpu_model struct, keepalive list)."""
+        q = np.ascontiguousarray(self.q, np.float64)
+        pi = np.ascontiguousarray(self.priors, np.float64)
+        r = np.ascontiguousarray(self.rates, np.float64)
+        p = np.ascontiguousarray(self.probs, np.float64)
+        m = _native.PgpuModel()
+        m.n_states = q.shape[0]
+        m.n_rates = len(r)
+        dp = C.POINTER(C.c_double)
+        m.Q, m.pi, m.rates, m.probs = (a.ctypes.data_as(dp) for a in (q, pi, r, p))
+        return m, [q, pi, r, p]
+
+
+# ---- rate matrices (host FP64, as lib/mlModel.ml assembles them) ----------
+
+def m_meanrate(srm: np.ndarray, pi: np.ndarray) -> np.ndarray:
+    mr = float(np.sum(-np.diag(srm) * pi))
+    return srm / mr
+
+
+def _fill_diag(srm: np.ndarray) -> np.ndarray:
+    np.fill_diagonal(srm, 0.0)
+    np.fill_diagonal(srm, -srm.sum(axis=1))
+    return srm
+
+
+def m_jc69(a: int) -> np.ndarray:
+    srm = np.ones((a, a))
+    np.fill_diagonal(srm, -(a - 1.0))
+    return m_meanrate(srm, np.full(a, 1.0 / a))
+
+
+def m_k2p(beta: float, a: int) -> np.ndarray:
+    if a != 4:
+        raise Error("Alphabet does not support this model")
+    beta = max(beta, MINIMUM)
+    srm = np.full((a, a), beta)
+    srm[1, 3] = srm[3, 1] = srm[2, 0] = srm[0, 2] = 1.0
+    np.fill_diagonal(srm, -1.0 - 2.0 * beta)
+    return m_meanrate(srm, np.full(a, 1.0 / a))
+
+
+def m_tn93(pi: np.ndarray, alpha: float, beta: float, a: int) -> np.ndarray:
+    if a != 4:
+        raise Error("Alphabet size does not support this model")
+    srm = np.ones((a, a))
+    srm[0, 2] = srm[2, 0] = alpha
+    srm[1, 3] = srm[3, 1] = beta
+    srm = srm * pi[None, :]
+    return m_meanrate(_fill_diag(srm), pi)
+
+
+def m_f81(pi: np.ndarray, a: int) -> np.ndarray:
+    srm = np.tile(pi, (a, 1)).astype(np.float64)
+    return m_meanrate(_fill_diag(srm), pi)
+
+
+def m_hky85(pi: np.ndarray, kappa: float, a: int) -> np.ndarray:
+    return m_tn93(pi, kappa, kappa, a)
+
+
+def m_f84(pi: np.ndarray, kappa: float, a: int) -> np.ndarray:
+    y = pi[1] + pi[3]
+    r = pi[0] + pi[2]
+    return m_tn93(pi, 1.0 + kappa / r, 1.0 + kappa / y, a)
+
+
+def m_gtr(pi: np.ndarray, co, a: int) -> np.ndarray:
+    co = np.asarray(co, np.float64)
+    want = ((a + 1) * (a - 2)) // 2
+    if len(co) != want:
+        raise Error(f"Length of GTR parameters (I) is incorrect for the alphabet. "
+                    f"They should be {want}, but are {len(co)}.")
+    full = np.append(co, 1.0)            # the last exchangeability is fixed to 1
+    iu = np.triu_indices(a, 1)
+    srm = np.zeros((a, a))
+    srm[iu] = full * pi[iu[1]]
+    srm[(iu[1], iu[0])] = full * pi[iu[0]]
+    return m_meanrate(_fill_diag(srm), pi)
+
+
+def m_file(pi: np.ndarray, f_rr, a: int) -> np.ndarray:
+    f = np.asarray(f_rr, np.float64)
+    if f.shape != (a, a):
+        raise Error("Const matrix does not match the alphabet")
+    return m_meanrate(_fill_diag(f.copy()), pi)
+
+
+# ---- site rate classes ------------------------------------------------------
+
+def gamma_rates(alpha: float, k: int) -> np.ndarray:
+    """Mean rate of each of k equal-probability categories of Gamma(alpha,
+    rate alpha) (Yang 1994); the rates average to 1."""
+    from scipy.special import gammainc, gammaincinv
+    if k == 1:
+        return np.ones(1)
+    cuts = np.append(gammaincinv(alpha, np.arange(1, k) / k) / alpha, np.inf)
+    upper = np.append(gammainc(alpha + 1.0, alpha * cuts[:-1]), 1.0)
+    lower = np.concatenate([[0.0], upper[:-1]])
+    return k * (upper - lower)
+
+
+def gamma_rates_quantile(alpha: float, k: int) -> np.ndarray:
+    """The reference's gamma_rates (lib/mlModel.ml:93-99): the quantile at
+    p = i/k of Gamma(shape alpha, scale alpha); rate 0 first."""
+    from scipy.special import gammaincinv
+    p = np.arange(k) / k
+    return gammaincinv(alpha, p) * alpha
+
+
+def _priors(spec: Spec) -> np.ndarray:
+    a = spec.alphabet_size
+    if spec.base_priors == "Equal":
+        return np.full(a, 1.0 / a)
+    kind, p = spec.base_priors
+    p = np.maximum(np.asarray(p, np.float64), MINIMUM)
+    s = p.sum()
+    if abs(s - 1.0) >= EPSILON_FLOAT:       # `=.` (lib/internal.ml:12)
+        p = p / s
+    if len(p) != a:
+        raise Error(f"Priors (length {len(p)}) don't match alphabet (length {a})")
+    return p
+
+
+def _site_classes(spec: Spec):
+    sv = spec.site_variation
+    if sv[0] == "Constant":
+        return np.ones(1), np.ones(1)
+    if sv[0] == "DiscreteGamma":
+        k, alpha = sv[1], sv[2]
+        return gamma_rates(alpha, k), np.full(k, 1.0 / k)
+    if sv[0] == "DiscreteCustom":
+        arr = np.asarray(sv[1], np.float64)
+        return arr[:, 0].copy(), arr[:, 1].copy()
+    raise Error(f"site variation {sv[0]} is not supported")
+
+
+def substitution_matrix(spec: Spec, priors: np.ndarray) -> tuple[np.ndarray, bool]:
+    """(Q, sym) as MlModel.create chooses them (lib/mlModel.ml:723-741)."""
+    a = spec.alphabet_size
+    s = spec.substitution
+    name = s[0]
+    if name == "JC69":
+        return m_jc69(a), True
+    if name == "K2P":
+        return m_k2p(s[1], a), True
+    if name == "F81":
+        return m_f81(priors, a), False
+    if name == "F84":
+        return m_f84(priors, s[1], a), False
+    if name == "HKY85":
+        return m_hky85(priors, s[1], a), False
+    if name == "TN93":
+        return m_tn93(priors, s[1][0], s[1][1], a), False
+    if name == "GTR":
+        co = s[1] if len(s) > 1 and len(s[1]) else np.ones(((a - 2) * (a + 1)) // 2)
+        return m_gtr(priors, co, a), False
+    if name == "Const":
+        return m_file(priors, s[1], a), False
+    raise Error(f"substitution model {name} is not supported")
+
+
+def diagonalize(q: np.ndarray, pi: np.ndarray, ctx: _native.Context | None = None):
+    """GPU FP64 eigen system: (U, lambda, Ui) with Q = U diag(lambda) Ui."""
+    if np.isnan(q).any():
+        # MlModel.diagonalize asserts the matrix holds no NaN (lib/mlModel.ml:557-568)
+        raise Error("rate matrix contains NaN")
+    ctx = ctx or _native.default_context()
+    S = q.shape[0]
+    q = np.ascontiguousarray(q, np.float64)
+    pi = np.ascontiguousarray(pi, np.float64)
+    U = np.empty((S, S))
+    lam = np.empty(S)
+    Ui = np.empty((S, S))
+    ctx.call("pgpu_model_diagonalize", q.ctypes.data, pi.ctypes.data, S, U.ctypes.data,
+             lam.ctypes.data, Ui.ctypes.data)
+    return U, lam, Ui
+
+
+def create(spec: Spec, ctx: _native.Context | None = None) -> Model:
+    """MlModel.create (lib/mlModel.ml:664-746)."""
+    priors = _priors(spec)
+    rates, probs = _site_classes(spec)
+    q, sym = substitution_matrix(spec, priors)
+    # JC69 and K2P are symmetric (the reference diagonalises them with dsyev,
+    # lib/mlmodel.c:163-197): their stationary distribution is uniform
+    # whatever the priors field holds
+    eq = np.full(spec.alphabet_size, 1.0 / spec.alphabet_size) if sym else priors
+    U, lam, Ui = diagonalize(q, eq, ctx)
+    return Model(spec, priors, rates, probs, q, U, lam, Ui)
+
+
+def compose(model: Model, t, ctx: _native.Context | None = None) -> np.ndarray:
+    """MlModel.compose (lib/mlModel.ml:585-587): P = exp(Q t), or Q for
+    t == -1, I for t < 1e-10.  ``t`` may be a scalar or an array of lengths
+    (then [n, S, S] is returned)."""
+    ctx = ctx or _native.default_context()
+    ts = np.atleast_1d(np.asarray(t, np.float64))
+    S = model.n_states
+    out = np.empty((len(ts), S, S))
+    ctx.call("pgpu_model_compose", model.u.ctypes.data, model.lam.ctypes.data,
+             model.ui.ctypes.data, S, ts.ctypes.data, len(ts), out.ctypes.data)
+    return out[0] if np.ndim(t) == 0 else out

@@ -112,3 +112,92 @@ def compress_patterns(columns: np.ndarray):
     [n_tips, n_pat], weights [n_pat] float64 counts, site -> pattern index)."""
     uniq, inverse, counts = np.unique(columns.T, axis=0, return_inverse=True, return_counts=True)
     return np.ascontiguousarray(uniq.T), counts.astype(np.float64), inverse.reshape(-1)
+
+
+# ---- GTR + Gamma DNA ---------------------------------------------------------
+
+def random_gtr_spec(rng: np.random.Generator, alpha: float = 0.5, k: int = 4):
+    """GTR with exchangeabilities ~ U(0.5, 2) (the last fixed to 1, the
+    reference's parameterisation, lib/mlModel.ml:396-400), base frequencies ~
+    Dirichlet(5,5,5,5), and k discrete Gamma(alpha) rate classes."""
+    from .mlmodel import Spec
+    co = rng.uniform(0.5, 2.0, 5)
+    pi = rng.dirichlet([5.0, 5.0, 5.0, 5.0])
+    return Spec(("GTR", co), ("DiscreteGamma", k, alpha), ("Empirical", pi), 4)
+
+
+def host_model(spec):
+    """Q, pi, rates, probs of a spec, assembled on the host (no GPU)."""
+    from . import mlmodel as M
+    pi = M._priors(spec)
+    q, sym = M.substitution_matrix(spec, pi)
+    rates, probs = M._site_classes(spec)
+    return q, pi, rates, probs
+
+
+def _expm_rev(q: np.ndarray, pi: np.ndarray, ts: np.ndarray) -> np.ndarray:
+    """exp(Q t) for a reversible Q via its symmetrised eigen system (numpy, data
+    generation only)."""
+    s = np.sqrt(pi)
+    b = s[:, None] * q / s[None, :]
+    lam, v = np.linalg.eigh((b + b.T) / 2)
+    u = v / s[:, None]
+    ui = v.T * s[None, :]
+    e = np.exp(lam[None, :] * ts[:, None])
+    return np.einsum("ik,tk,kj->tij", u, e, ui)
+
+
+def simulate_sites(tr: _tree.RootedTree, q: np.ndarray, pi: np.ndarray, rates: np.ndarray,
+                   probs: np.ndarray, n_sites: int, rng: np.random.Generator) -> np.ndarray:
+    """Tip states [n_tips, n_sites] (uint8 state index) simulated down the tree
+    under the rate matrix q with discrete rate classes."""
+    S, R = q.shape[0], len(rates)
+    n = tr.n_tips
+    cls = rng.choice(R, size=n_sites, p=probs).astype(np.int32)
+    tips = np.empty((n, n_sites), dtype=np.uint8)
+    root = tr.n_nodes - 1
+    cum_pi = np.cumsum(pi)
+    live = {root: np.minimum(np.searchsorted(cum_pi, rng.random(n_sites)), S - 1).astype(np.uint8)}
+    for v in tr.depth_first_order():
+        k = v - n
+        parent = live.pop(v)
+        key = cls * S + parent                                   # (rate class, parent state)
+        for c in (int(tr.left[k]), int(tr.right[k])):
+            P = _expm_rev(q, pi, rates * tr.brlen[c])           # [R, S, S]
+            cum = np.cumsum(np.clip(P, 0.0, None), axis=2)
+            cum = (cum / cum[:, :, -1:]).reshape(R * S, S).astype(np.float32)
+            u = rng.random(n_sites, dtype=np.float32)
+            child = np.zeros(n_sites, dtype=np.uint8)
+            for j in range(S - 1):
+                child += u > np.take(cum[:, j], key)
+            if c < n:
+                tips[c] = child
+            else:
+                live[c] = child
+    return tips
+
+
+def dna_code_table() -> np.ndarray:
+    """[16, 4] tip partials of the 4-bit DNA codes: bit j set -> state j
+    possible; code 0 (no state) is read as missing (all ones)."""
+    m = np.arange(16)[:, None]
+    t = ((m >> np.arange(4)[None, :]) & 1).astype(np.float64)
+    t[0] = 1.0
+    return t
+
+
+def prune_workload(n_tips: int, n_sites: int, seed: int, mean_brlen: float = 0.1,
+                   ambiguity: float = 0.0, alpha: float = 0.5):
+    """Yule tree, random GTR+Gamma4 model, simulated DNA compressed to
+    weighted patterns.  Returns (tree, spec, codes [n_tips, n_pat] uint8
+    4-bit masks, weights [n_pat] float64)."""
+    rng = np.random.default_rng(seed)
+    tr = _tree.yule(n_tips, rng, mean_brlen)
+    spec = random_gtr_spec(rng, alpha)
+    q, pi, rates, probs = host_model(spec)
+    states = simulate_sites(tr, q, pi, rates, probs, n_sites, rng)
+    masks = (np.uint8(1) << states).astype(np.uint8)
+    if ambiguity > 0:
+        inject_ambiguity(masks, ambiguity, rng)
+    pats, w, _ = compress_patterns(masks)
+    return tr, spec, pats, w

@@ -1,0 +1,193 @@
+"""GPU: FP64 model build and Felsenstein pruning through the C ABI, against
+the LAPACK-based model oracle and the FP64 pruning oracle."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from oracle import mlmodel_oracle as O
+from phylocaml_gb300 import mlmodel as M, synth, tree as T
+
+pytestmark = pytest.mark.gpu
+
+# FP64 on the GPU against the FP64 oracle: the two differ only by the
+# eigensolver (Jacobi vs LAPACK dgeev, ~1e-15 per P entry) and summation order.
+FP64_REL = 1e-9
+# the FP32 form's bound on |lnL_fp32 - lnL_fp64| per tree
+FP32_ABS = 1e-3
+
+
+def reversible_q(rng, S):
+    pi = rng.dirichlet(np.ones(S))
+    ex = rng.lognormal(size=(S, S))
+    ex = (ex + ex.T) / 2
+    q = ex * pi[None, :]
+    np.fill_diagonal(q, 0.0)
+    np.fill_diagonal(q, -q.sum(axis=1))
+    return q / -(np.diag(q) * pi).sum(), pi
+
+
+SPECS = {
+    "JC69": M.Spec(("JC69",)), "K2P": M.Spec(("K2P", 0.3)),
+    "F81": M.Spec(("F81",), base_priors=("Empirical", [0.1, 0.2, 0.3, 0.4])),
+    "F84": M.Spec(("F84", 2.0), base_priors=("Empirical", [0.1, 0.2, 0.3, 0.4])),
+    "HKY85": M.Spec(("HKY85", 2.0), base_priors=("Empirical", [0.1, 0.2, 0.3, 0.4])),
+    "TN93": M.Spec(("TN93", (2.0, 3.0)), base_priors=("Empirical", [0.1, 0.2, 0.3, 0.4])),
+    "GTR": M.Spec(("GTR", [1.1, 0.7, 1.9, 0.6, 1.4]), ("DiscreteGamma", 4, 0.5),
+                  ("Empirical", [0.3, 0.2, 0.25, 0.25])),
+}
+
+
+@pytest.mark.parametrize("name", list(SPECS))
+def test_create_and_compose_match_lapack_oracle(ctx, name):
+    m = M.create(SPECS[name], ctx)
+    u, d, ui = O.diagonalize_gtr(m.q)
+    # mlModelTest.ml:5-7 lengths, plus -1 (returns Q) and a few ordinary ones
+    ts = np.array([np.finfo(float).tiny, 0.0, 1e-11, 0.05, 1.0, 100.0, -1.0])
+    P = M.compose(m, ts, ctx)
+    for t, p in zip(ts, P):
+        assert np.abs(p - O.compose_gtr(u, d, ui, float(t))).max() < 1e-12, t
+    assert np.allclose(M.compose(m, -1.0, ctx), m.q, atol=1e-13)
+    assert np.allclose(m.u @ np.diag(m.lam) @ m.ui, m.q, atol=1e-13)
+
+
+@pytest.mark.parametrize("S", [20, 61, 64])
+def test_large_state_spaces(ctx, S):
+    rng = np.random.default_rng(S)
+    q, pi = reversible_q(rng, S)
+    U, lam, Ui = M.diagonalize(q, pi, ctx)
+    assert np.abs(U @ np.diag(lam) @ Ui - q).max() < 1e-12
+    from scipy.linalg import expm
+    for t in (0.01, 0.5, 3.0):
+        p = M.compose(M.Model(None, pi, np.ones(1), np.ones(1), q, U, lam, Ui), t, ctx)
+        assert np.abs(p - expm(q * t)).max() < 1e-12
+
+
+def test_model_errors(ctx):
+    from phylocaml_gb300 import _native
+    q = M.m_gtr(np.full(4, 0.25), [1, 2, 3, 4, 5], 4)
+    pi = np.full(4, 0.25)
+    out = [np.empty((4, 4)), np.empty(4), np.empty((4, 4))]
+    bad = q.copy()
+    bad[0, 1] = np.nan
+    with pytest.raises(_native.NativeError) as e:
+        ctx.call("pgpu_model_diagonalize", bad.ctypes.data, pi.ctypes.data, 4,
+                 *[o.ctypes.data for o in out])
+    assert e.value.status == 4
+    nonrev = q.copy()
+    nonrev[0, 1] += 0.5
+    nonrev[0, 0] -= 0.5
+    with pytest.raises(_native.NativeError) as e:
+        ctx.call("pgpu_model_diagonalize", nonrev.ctypes.data, pi.ctypes.data, 4,
+                 *[o.ctypes.data for o in out])
+    assert e.value.status == 5
+    with pytest.raises(M.Error):
+        M.diagonalize(bad, pi, ctx)
+
+
+def oracle_lnl(orc, tr, model, codes, w, n_threads=1, site=False):
+    P = O.pmatrices(model.q, model.priors, model.rates, tr.brlen)
+    return orc.prune_lnl(tr.left, tr.right, P, model.priors, model.probs, codes,
+                         synth.dna_code_table(), w, n_threads=n_threads, site_lnl=site)
+
+
+def test_small_config_fp64_and_fp32(ctx, orc):
+    """16 taxa, 1,000 GTR+Gamma4 sites with 5% ambiguity, compressed to patterns."""
+    from phylocaml_gb300 import likelihood as Lk
+    tr, spec, pats, w = synth.prune_workload(16, 1000, seed=0, ambiguity=0.05)
+    m = M.create(spec, ctx)
+    exp, exp_site = oracle_lnl(orc, tr, m, pats, w, site=True)
+    g64, s64 = Lk.tree_lnl(tr, m, pats, synth.dna_code_table(), w, 64, ctx, site_lnl=True)
+    g32, s32 = Lk.tree_lnl(tr, m, pats, synth.dna_code_table(), w, 32, ctx, site_lnl=True)
+    assert abs(g64 - exp) <= FP64_REL * abs(exp)
+    assert np.abs(s64 - exp_site).max() <= 1e-10 * np.abs(exp_site).max()
+    assert abs(g32 - exp) <= FP32_ABS
+    assert np.abs(s32 - exp_site).max() < 1e-4
+    assert abs(Lk.root_cost(tr, m, pats, synth.dna_code_table(), w, 64, ctx) + g64) < 1e-9
+
+
+@pytest.mark.parametrize("shape", ["yule", "caterpillar", "balanced"])
+@pytest.mark.parametrize("rates", ["constant", "gamma4", "custom8"])
+def test_trees_and_rate_classes(ctx, orc, shape, rates):
+    from phylocaml_gb300 import likelihood as Lk
+    rng = np.random.default_rng(hash((shape, rates)) % 2**32)
+    tr = {"yule": lambda: T.yule(64, rng, 0.1), "caterpillar": lambda: T.caterpillar(150, 0.05),
+          "balanced": lambda: T.balanced(128, 0.08)}[shape]()
+    sv = {"constant": ("Constant",), "gamma4": ("DiscreteGamma", 4, 0.7),
+          "custom8": ("DiscreteCustom", [(r, 1 / 8) for r in np.linspace(0.2, 1.8, 8)])}[rates]
+    spec = M.Spec(("GTR", rng.uniform(0.5, 2, 5)), sv, ("Empirical", rng.dirichlet([5] * 4)))
+    m = M.create(spec, ctx)
+    q, pi, rr, pp = synth.host_model(spec)
+    states = synth.simulate_sites(tr, q, pi, rr, pp, 3001, rng)
+    codes = (np.uint8(1) << states).astype(np.uint8)
+    w = rng.integers(1, 5, 3001).astype(np.float64)
+    exp = oracle_lnl(orc, tr, m, codes, w)
+    g64 = Lk.tree_lnl(tr, m, codes, synth.dna_code_table(), w, 64, ctx)
+    g32 = Lk.tree_lnl(tr, m, codes, synth.dna_code_table(), w, 32, ctx)
+    assert abs(g64 - exp) <= FP64_REL * abs(exp)
+    assert abs(g32 - exp) <= FP32_ABS
+    g_unw = Lk.tree_lnl(tr, m, codes, synth.dna_code_table(), None, 64, ctx)
+    assert abs(g_unw - oracle_lnl(orc, tr, m, codes, None)) <= FP64_REL * abs(g_unw)
+
+
+def test_edge_cases(ctx):
+    from phylocaml_gb300 import likelihood as Lk, _native
+    tr = T.RootedTree(np.array([0], np.int32), np.array([1], np.int32), np.array([0.1, 0.2]))
+    m = M.create(SPECS["JC69"], ctx)
+    codes = np.array([[1, 2, 15], [1, 4, 0]], np.uint8)
+    lnl, site = Lk.tree_lnl(tr, m, codes, synth.dna_code_table(), None, 64, ctx, site_lnl=True)
+    P = O.pmatrices(m.q, m.priors, m.rates, tr.brlen)
+    # two tips: L = sum_i pi_i P_a[i, x] P_b[i, y]
+    exp0 = np.log(0.25 * np.sum(P[0, 0, :, 0] * P[1, 0, :, 0]))
+    assert abs(site[0] - exp0) < 1e-12
+    assert abs(site[2]) < 1e-12            # gap against missing: likelihood 1
+    assert Lk.tree_lnl(tr, m, np.zeros((2, 0), np.uint8), synth.dna_code_table(), None, 32, ctx) == 0.0
+    with pytest.raises(_native.NativeError):
+        Lk.tree_lnl(tr, m, np.array([[1], [20]], np.uint8), synth.dna_code_table(), None, 32, ctx)
+    with pytest.raises(_native.NativeError):
+        Lk.tree_lnl(tr, m, codes, synth.dna_code_table(), None, 16, ctx)
+    bad = T.RootedTree(tr.left, tr.right, np.array([0.1, -1.0]))
+    with pytest.raises(_native.NativeError):
+        Lk.tree_lnl(bad, m, codes, synth.dna_code_table(), None, 32, ctx)
+
+
+def test_device_api_matches_host_api(ctx):
+    import torch
+    from phylocaml_gb300 import likelihood as Lk
+    tr, spec, pats, w = synth.prune_workload(40, 20000, seed=3)
+    m = M.create(spec, ctx)
+    host = Lk.tree_lnl(tr, m, pats, synth.dna_code_table(), w, 32, ctx)
+    n_pat = pats.shape[1]
+    ld = (n_pat + 15) // 16 * 16
+    dev = torch.device("cuda:0")
+    tips = torch.zeros((tr.n_tips, ld), dtype=torch.uint8, device=dev)
+    tips[:, :n_pat] = torch.from_numpy(pats).to(dev)
+    wd = torch.from_numpy(w).to(dev)
+    out = torch.zeros(1, dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.synchronize(dev)
+    ctx.set_stream(stream.cuda_stream)
+    try:
+        Lk.tree_lnl_dev(tr, m, tips, ld, n_pat, synth.dna_code_table(), wd, out, 32, ctx=ctx)
+        ctx.synchronize()
+    finally:
+        ctx.set_stream(None)
+    assert float(out.item()) == host
+
+
+def test_full_size_precision_config(ctx, orc):
+    """512 taxa, 500,000 GTR+Gamma4 sites (BL ~ Exp(0.05)) compressed to
+    patterns: the FP32 form within 1e-3 of the FP64 oracle, the FP64 form
+    within FP64_REL."""
+    from phylocaml_gb300 import likelihood as Lk
+    tr, spec, pats, w = synth.prune_workload(512, 500_000, seed=2, mean_brlen=0.05)
+    m = M.create(spec, ctx)
+    exp = oracle_lnl(orc, tr, m, pats, w, n_threads=os.cpu_count() or 4)
+    g64 = Lk.tree_lnl(tr, m, pats, synth.dna_code_table(), w, 64, ctx)
+    g32 = Lk.tree_lnl(tr, m, pats, synth.dna_code_table(), w, 32, ctx)
+    print(f"lnL oracle {exp!r} fp64 {g64!r} (d {g64 - exp:.3e}) fp32 {g32!r} (d {g32 - exp:.3e})")
+    assert abs(g64 - exp) <= FP64_REL * abs(exp)
+    assert abs(g32 - exp) <= FP32_ABS
