@@ -142,6 +142,30 @@ pgpu_status pgpu_fitch_tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree,
                                 int lane_bits, uint32_t *node_sets_dev,
                                 uint32_t *site_cost_dev, uint64_t *total_dev);
 
+/* No counterpart in the reference (phylocaml allocates a result per call,
+ * lib/bitvector/bv.c:163-178).  pgpu_fitch_tree_dev for callers that may not
+ * allocate device memory: a program that keeps the GPU's memory in its own
+ * pool, a service that forbids cudaMalloc once it is serving (an allocation
+ * can synchronise the device), or work being recorded into a CUDA graph.  It
+ * takes no context and allocates nothing: its scratch (the tree's schedule
+ * and an error word) lives in one fixed device array in the library, about
+ * 320 KB, held on every GPU that loads the library until the process exits.
+ *   - trees of at most 16,384 tips; larger ones return PGPU_ERR_LIMIT;
+ *   - runs on cuda_stream (a cudaStream_t, or NULL for the legacy stream) of
+ *     the current device and returns after that stream has finished;
+ *     PGPU_ERR_TIMEOUT if a bounded device wait gave up;
+ *   - all calls share the array: calls whose GPU work overlaps (other
+ *     streams or host threads on the same device) race and must be
+ *     serialised by the caller;
+ *   - the first call on each device looks the array up with
+ *     cudaGetSymbolAddress; make it before any stream capture starts.
+ * Arguments as for pgpu_fitch_tree_dev. */
+pgpu_status pgpu_fitch_tree_noalloc(const pgpu_tree *tree, const uint32_t *tips_dev,
+                                    size_t ld_words, const uint32_t *weights_dev,
+                                    size_t n_sites, int lane_bits, uint32_t *node_sets_dev,
+                                    uint32_t *site_cost_dev, uint64_t *total_dev,
+                                    void *cuda_stream);
+
 /* ---- substitution models and transition matrices (FP64 on the GPU) ----
  * Q is row-major, rows sum to zero, and reversible with respect to pi
  * (pi_i Q_ij = pi_j Q_ji) -- the models MlModel.create builds

@@ -434,6 +434,88 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
 
 }  // namespace
 
+// Launches the tree kernel on device arrays the caller manages (schedule ops,
+// tip sequence, error word) on an explicit stream, without a context.  Used
+// by the entry point that allocates nothing (noalloc.cu).
+pgpu_status pgpu_fitch_tree_launch_raw(cudaStream_t stream, const int4 *ops, const int32_t *tip_seq,
+                                       int n_ops, int depth, int *flag, int32_t n_tips,
+                                       const uint32_t *tips, size_t ld, const uint32_t *weights,
+                                       size_t n_sites, int lb, uint32_t *node_sets,
+                                       uint32_t *site_cost, uint64_t *total) {
+  if (!lane_bits_ok(lb)) return PGPU_ERR_ARG;
+  const size_t n_words = words_for(n_sites, lb);
+  if (!tips || !node_sets || !total || ld % 4 != 0 || ld < n_words) return PGPU_ERR_ARG;
+  if (((uintptr_t)tips | (uintptr_t)node_sets) & 15) return PGPU_ERR_ARG;
+  int dev = 0, sms = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return PGPU_ERR_CUDA;
+  }
+  if (cudaMemsetAsync(total, 0, sizeof(uint64_t), stream) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return PGPU_ERR_CUDA;
+  }
+  if (n_words == 0) return PGPU_OK;
+  const size_t nsm = (size_t)std::max(sms, 1);
+  size_t W = 128, best = ~size_t(0);
+  for (size_t cw = 1; cw <= 4; ++cw) {
+    const size_t w = 128 * cw, tiles = (n_words + w - 1) / w;
+    const size_t cost = (tiles + nsm - 1) / nsm * w;
+    if (cost <= best) {
+      best = cost;
+      W = w;
+    }
+  }
+  const size_t smem = 16 * (size_t)FT_STAGES + 4 * (size_t)(FT_STAGES + depth) * W;
+  if (smem > (size_t)optin) return PGPU_ERR_LIMIT;
+  FitchTreeArgs a;
+  a.tips = tips;
+  a.weights = weights;
+  a.node_sets = node_sets;
+  a.site_cost = site_cost;
+  a.total = reinterpret_cast<unsigned long long *>(total);
+  a.ops = ops;
+  a.tip_seq = tip_seq;
+  a.flag = flag;
+  a.ld = ld;
+  a.n_words = n_words;
+  a.n_sites = n_sites;
+  a.n_tips = n_tips;
+  a.n_ops = n_ops;
+  a.W = (int)W;
+  a.depth = depth;
+  const size_t n_tiles = (n_words + W - 1) / W;
+  const int threads = 32 + (int)W / 4;
+  const int dyn = (int)std::max<size_t>(smem, 48 * 1024);
+  cudaError_t e = cudaSuccess;
+  switch (lb) {
+    case 4:
+      e = cudaFuncSetAttribute(fitch_tree_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+      if (e == cudaSuccess) fitch_tree_kernel<4><<<(unsigned)n_tiles, threads, smem, stream>>>(a);
+      break;
+    case 8:
+      e = cudaFuncSetAttribute(fitch_tree_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+      if (e == cudaSuccess) fitch_tree_kernel<8><<<(unsigned)n_tiles, threads, smem, stream>>>(a);
+      break;
+    case 16:
+      e = cudaFuncSetAttribute(fitch_tree_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+      if (e == cudaSuccess) fitch_tree_kernel<16><<<(unsigned)n_tiles, threads, smem, stream>>>(a);
+      break;
+    default:
+      e = cudaFuncSetAttribute(fitch_tree_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+      if (e == cudaSuccess) fitch_tree_kernel<32><<<(unsigned)n_tiles, threads, smem, stream>>>(a);
+      break;
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return PGPU_ERR_CUDA;
+  }
+  return PGPU_OK;
+}
+
 extern "C" {
 
 pgpu_status pgpu_fitch_median2(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b, uint32_t *out,
