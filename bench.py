@@ -2,21 +2,27 @@
 """Benchmark of the tree-scoring hot path on one GB300 (or N, one rank each).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload fitch]
+                    [--workload prune|fitch|all]
 
 Prints ONE JSON line.  Workloads (seeded synthetic data, no dataset):
 
+  prune   (headline) Felsenstein pruning, 512-taxon Yule tree (branch
+          lengths ~ Exp(0.05)), 500,000 DNA sites simulated under GTR+Gamma4
+          (exchangeabilities ~ U(0.5,2), frequencies ~ Dirichlet(5,5,5,5),
+          alpha 0.5), compressed to weighted patterns.  A step is one
+          pgpu_prune_lnl_dev call: FP64 eigendecomposition and P(t) build on
+          the GPU, the fused pruning kernel, the compensated lnL sum.
+          `value` is the throughput of the fastest FP32-unit form whose lnL is
+          within 1e-3 of the FP64 oracle; the FP64-on-GPU form is timed beside.
   fitch   Fitch parsimony, 1,024-taxon Yule tree, 1,000,000 DNA sites as
-          4-bit masks (8 sites per uint32), 3% ambiguity, weights 1..8.
-          A step is one pgpu_fitch_tree_dev call: the full postorder, all
-          1,023 internal state sets written, per-site costs and the total.
+          4-bit masks (8 per uint32), 3% ambiguity, weights 1..8.  A step is
+          one pgpu_fitch_tree_dev call.
 
-`value` is node-site updates per second (internal nodes x sites / time)
-with inputs resident in HBM; `e2e` is the same through the host-buffer C-ABI
-call (pgpu_fitch_tree) with the host<->device copies inside the timed region.
-Inputs (512 MB of tips) are larger than the 129 MB L2, so no flush is needed
-between steps.  `--impl reference` times the reference's CPU Fitch path
-(bv_fitch over the same postorder, one character per byte) on the host cores.
+`value` is node-site-pattern updates per second (internal nodes x patterns /
+time) with inputs resident in HBM; `e2e` is the same metric through the
+host-buffer C-ABI call with the host<->device copies inside the timed region.
+`--impl reference` times the reference's CPU path on the host cores: the
+restated FP64 pruning (phylocaml has no pruning code), or bv_fitch.
 """
 from __future__ import annotations
 
@@ -336,28 +342,242 @@ def bench_fitch_reference(args):
     }
 
 
+# ---------------------------------------------------------------------------
+# Felsenstein pruning, 512 taxa x 500,000 GTR+Gamma4 sites
+# ---------------------------------------------------------------------------
+
+PRUNE_TAXA, PRUNE_SITES, PRUNE_BL = 512, 500_000, 0.05
+PRUNE_GATE = 1e-3
+FORMS = {32: "fp32", 48: "fp32x2", 64: "fp64"}
+# FP32 lane instructions per node-pattern-rate of each form (counted from
+# csrc/prune.cu: two children x 4 rows, then the product and the rescale test)
+FP32_INSTR_PER_NODE_RATE = {32: 2 * 4 * 5 + 4 + 6, 48: 2 * 4 * 59 + 4 * 6 + 6}
+
+
+def prune_data(rank):
+    from phylocaml_gb300 import synth
+    return synth.prune_workload(PRUNE_TAXA, PRUNE_SITES, seed=2 + rank, mean_brlen=PRUNE_BL)
+
+
+def prune_oracle_lnl(tr, spec, pats, w, n_threads, limit=None):
+    """FP64 oracle lnL (and its wall time) over the first `limit` patterns."""
+    import oracle
+    from oracle import mlmodel_oracle as O
+    from phylocaml_gb300 import synth
+    q, pi, rates, probs = synth.host_model(spec)
+    P = O.pmatrices(q, pi, rates, tr.brlen)
+    sub = pats if limit is None else np.ascontiguousarray(pats[:, :limit])
+    ww = w if limit is None else np.ascontiguousarray(w[:limit])
+    t = time.perf_counter()
+    v = oracle.prune_lnl(tr.left, tr.right, P, pi, probs, sub, synth.dna_code_table(), ww,
+                         n_threads=n_threads)
+    return v, time.perf_counter() - t
+
+
+def bench_prune(args, rank, world, local):
+    import torch
+    from phylocaml_gb300 import _native, likelihood as Lk, mlmodel as M, synth
+
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    tr, spec, pats, w = prune_data(rank)
+    n_pat = pats.shape[1]
+    ld = (n_pat + 15) // 16 * 16
+    units = tr.n_internal * n_pat
+    R = 4
+    ctx = _native.Context(local)
+    model = M.create(spec, ctx)
+    table = synth.dna_code_table()
+    stream = torch.cuda.Stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    tips = torch.zeros((tr.n_tips, ld), dtype=torch.uint8, device=dev)
+    tips[:, :n_pat] = torch.from_numpy(pats).to(dev)
+    wd = torch.from_numpy(w).to(dev)
+    out = torch.zeros(1, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize(dev)
+    cores = os.cpu_count() or 1
+    exp, oracle_mt_s = prune_oracle_lnl(tr, spec, pats, w, cores) if rank == 0 else (None, None)
+
+    def step(prec):
+        Lk.tree_lnl_dev(tr, model, tips, ld, n_pat, table, wd, out, prec, ctx=ctx)
+
+    def timed(prec, k, sample_clocks=False):
+        for _ in range(args.warmup):
+            step(prec)
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+        l0 = ctx.launches
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(k)]
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for i in range(k):
+            ev[i][0].record(stream)
+            step(prec)
+            ev[i][1].record(stream)
+        t1.record(stream)
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+        el = t0.elapsed_time(t1)
+        if world > 1:
+            tt = torch.tensor([el], device=dev, dtype=torch.float64)
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            el = float(tt.item())
+        return el, statistics.mean(a.elapsed_time(b) for a, b in ev), ctx.launches - l0, \
+            float(out.item())
+
+    forms = {}
+    for prec in (32, 48):
+        clk = ClockSampler(local)
+        clk.start()
+        el, per, launches, lnl = timed(prec, args.steps)
+        forms[FORMS[prec]] = {"ms_per_step": el / args.steps, "value": world * units * args.steps /
+                              (el * 1e-3), "lnl": lnl, "launches": launches, "clocks": clk.stop(),
+                              "per_launch_ms": per}
+    k64 = max(3, min(args.steps, 10))
+    el, per, launches, lnl = timed(64, k64)
+    forms["fp64"] = {"ms_per_step": el / k64, "value": world * units * k64 / (el * 1e-3), "lnl": lnl,
+                     "launches": launches, "per_launch_ms": per}
+    for f in forms.values():
+        f["dlnl_vs_oracle"] = None if exp is None else f["lnl"] - exp
+        f["within_gate"] = None if exp is None else abs(f["lnl"] - exp) <= PRUNE_GATE
+
+    # headline: fastest FP32-unit form inside the gate
+    cand = [(FORMS[p], p) for p in (32, 48) if forms[FORMS[p]]["within_gate"]]
+    head_name, head_prec = min(cand, key=lambda x: forms[x[0]]["ms_per_step"]) if cand else ("fp32x2", 48)
+    head = forms[head_name]
+
+    # end to end through the host-buffer call (pinned host tips and weights)
+    ctx.set_stream(None)
+    pin_tips = torch.from_numpy(pats).pin_memory().numpy()
+    pin_w = torch.from_numpy(w).pin_memory().numpy()
+    Lk.tree_lnl(tr, model, pin_tips, table, pin_w, head_prec, ctx)
+    e2e_steps = max(3, min(args.steps, 20))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_lnl = Lk.tree_lnl(tr, model, pin_tips, table, pin_w, head_prec, ctx)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+
+    peaks, peak_src = load_peaks()
+    clocks = head["clocks"]
+    sm_mhz = clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    lane_peak = n_sm * 128 * sm_mhz * 1e6 / 1e12            # Tinst/s at the sampled clock
+    instr = FP32_INSTR_PER_NODE_RATE[head_prec] * R * units
+    achieved = instr / (head["per_launch_ms"] * 1e-3) / 1e12
+    rec = {
+        "metric": "node-site-pattern updates/s on 1 GB300, FP32 vs FP64 form at |dlnL|<=1e-3",
+        "value": head["value"], "unit": "node-site-pattern updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32x2" if head_prec == 48 else "f32", "data": "synthetic",
+        "config": {"workload": "prune: 512-taxon Yule tree (BL ~ Exp(0.05)), 500,000 GTR+Gamma4 "
+                               "DNA sites (alpha 0.5) compressed to weighted patterns",
+                   "n_tips": tr.n_tips, "n_patterns": n_pat, "n_rates": R, "form": head_name,
+                   "l2": "each step reads the 228 MB tip-code matrix (> L2) once; no flush"},
+        "forms": forms,
+        "fp64_form": {"value": forms["fp64"]["value"], "ms_per_step": forms["fp64"]["ms_per_step"],
+                      "speedup_of_headline": head["value"] / forms["fp64"]["value"]},
+        "dlnl": {"oracle_lnl": exp, "headline_vs_oracle": head["dlnl_vs_oracle"],
+                 "gate": PRUNE_GATE, "within_gate": head["within_gate"]},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": lane_peak, "unit": "Tinst/s",
+                     "frac": achieved / lane_peak,
+                     "peak_source": f"derived: {n_sm} SMs x 128 FP32 lanes x {sm_mhz:.0f} MHz "
+                                    "(sampled SM clock); HBM is not the bound (0.23 GB per step)",
+                     "kernel": f"prune_tree_kernel<{'Ff32' if head_prec == 48 else 'Fp32'},4>",
+                     "per_launch_ms": head["per_launch_ms"], "fp32_instr_per_step": instr,
+                     "traffic": profile_traffic("prune_tree_kernel_512x446k")},
+        "e2e": {"value": units / e2e_s, "unit": "node-site-pattern updates/s",
+                "h2d_bytes_per_step": int(pats.nbytes + w.nbytes), "d2h_bytes_per_step": 8,
+                "ms_per_step": e2e_s * 1e3, "lnl_matches_device": e2e_lnl == head["lnl"]},
+        "gpu_launches": int(head["launches"]),
+        "clocks": clocks,
+    }
+    if rank == 0:
+        # CPU baseline: the FP64 restatement (phylocaml has no pruning code),
+        # one core, on a bounded sample of the patterns
+        _, t_small = prune_oracle_lnl(tr, spec, pats, w, 1, limit=2000)
+        per_pat = t_small / 2000
+        lim = int(min(n_pat, max(2000, 10.0 / max(per_pat, 1e-9))))
+        _, t_cpu = prune_oracle_lnl(tr, spec, pats, w, 1, limit=lim)
+        rec["cpu_baseline"] = {"value": tr.n_internal * lim / t_cpu, "unit": "node-site-pattern updates/s",
+                               "cores": 1, "kind": "port",
+                               "sample": f"{tr.n_tips} taxa x {lim} of {n_pat} patterns, FP64 "
+                                         f"restatement (oracle/prune_oracle.c), {t_cpu:.1f} s",
+                               "all_cores": {"cores": cores, "value": units / oracle_mt_s}}
+    ctx.close()
+    return rec
+
+
+def bench_prune_reference(args):
+    """The FP64 pruning restatement on all host cores (phylocaml itself has
+    no pruning code: Likelihood_c.median_2 is a TODO)."""
+    tr, spec, pats, w = prune_data(0)
+    n_pat = pats.shape[1]
+    cores = os.cpu_count() or 1
+    _, t0 = prune_oracle_lnl(tr, spec, pats, w, cores, limit=min(n_pat, 20_000))
+    lim = int(min(n_pat, max(20_000, 20_000 * 5.0 / max(t0, 1e-9))))
+    for _ in range(args.warmup):
+        prune_oracle_lnl(tr, spec, pats, w, cores, limit=min(lim, 20_000))
+    times = [prune_oracle_lnl(tr, spec, pats, w, cores, limit=lim)[1] for _ in range(args.steps)]
+    total = sum(times)
+    value = tr.n_internal * lim * args.steps / total
+    return {
+        "metric": "node-site-pattern updates/s on 1 GB300, FP32 vs FP64 form at |dlnL|<=1e-3",
+        "value": value, "unit": "node-site-pattern updates/s", "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
+        "impl": "reference", "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "prune: 512-taxon Yule tree (BL ~ Exp(0.05)), 500,000 GTR+Gamma4 "
+                               "DNA sites (alpha 0.5) compressed to weighted patterns",
+                   "n_patterns": n_pat},
+        "cpu_baseline": {"value": value, "unit": "node-site-pattern updates/s", "cores": cores,
+                         "kind": "port",
+                         "sample": f"{tr.n_tips} taxa x {lim} of {n_pat} patterns per step, FP64 "
+                                   f"restatement over {cores} threads"},
+        "e2e": {"value": value, "unit": "node-site-pattern updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
-    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["fitch"], default="fitch")
+    ap.add_argument("--workload", choices=["prune", "fitch", "all"], default="all")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_info()
+    head = "fitch" if args.workload == "fitch" else "prune"
 
     if args.impl == "reference":
         if rank != 0:
             return
-        rec = bench_fitch_reference(args)
+        if args.steps is None:
+            args.steps = 3
+        rec = bench_fitch_reference(args) if head == "fitch" else bench_prune_reference(args)
         print(json.dumps(rec), flush=True)
         return
 
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
-    rec = bench_fitch(args, rank, world, local)
+    steps_given = args.steps
+    if head == "prune":
+        args.steps = steps_given if steps_given is not None else 30
+        rec = bench_prune(args, rank, world, local)
+        if args.workload == "all":
+            args.steps = steps_given if steps_given is not None else 2000
+            rec["fitch"] = bench_fitch(args, rank, world, local)
+    else:
+        args.steps = steps_given if steps_given is not None else 2000
+        rec = bench_fitch(args, rank, world, local)
     if rank == 0:
         print(json.dumps(rec), flush=True)
     if world > 1:

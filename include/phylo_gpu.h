@@ -208,9 +208,13 @@ pgpu_status pgpu_model_compose(pgpu_ctx *ctx, const double *U, const double *lam
  * n_pat weighted site patterns:
  *   tip_codes  [n_tips][n_pat] codes into codes->table
  *   weights    [n_pat] pattern weights, or NULL for 1
- *   precision  32: FP32 conditional likelihoods; 64: the FP64 form.  P
- *              matrices are always built in FP64 on the GPU; the log-
- *              likelihood is always summed in FP64 with compensation.
+ *   precision  32: FP32 conditional likelihoods (P - I rounded once to FP32);
+ *              48: FP32 pairs -- every value an unevaluated sum of two
+ *              floats, every sum and product error-free, about 48
+ *              significant bits, on the FP32 units;
+ *              64: the FP64 form.  P matrices are always built in FP64 on
+ *              the GPU; the log-likelihood is always summed in FP64 with
+ *              compensation.
  *   lnl        out: sum_s weights[s] * site_lnl[s]
  *   site_lnl   [n_pat] out (or NULL)
  * tree->brlen is required.  This entry point takes S = 4 (DNA); 20- and

@@ -132,7 +132,48 @@ struct FitchTreeArgs {
   int W, depth;               // W words per tile (4 per consumer thread)
 };
 
-constexpr int FT_STAGES = 16;   // ring depth (power of two)
+// Ring depth and tile width of one launch.  Deeper rings keep more tip rows
+// in flight per CTA; the depth is the largest of 64/32/16 whose shared
+// memory still lets every CTA of the launch be resident at once.
+struct FitchPlan {
+  size_t W = 128;        // words per tile
+  int stages = 16;       // ring depth
+  size_t smem = 0;       // dynamic shared memory per CTA
+  size_t tiles = 0;
+};
+
+inline size_t fitch_smem(int stages, int depth, size_t W) {
+  return 16 * (size_t)stages + 4 * (size_t)(stages + depth) * W;
+}
+
+// W = 128 * cw words (cw consumer warps of 32 threads x 4 words): the one
+// that minimises the words the busiest SM handles, given that every SM takes
+// ceil(tiles / SMs) tiles; ties go to the wider tile.
+inline FitchPlan fitch_plan(size_t n_words, int depth, int num_sms, size_t smem_optin) {
+  FitchPlan pl;
+  const size_t sms = (size_t)(num_sms > 0 ? num_sms : 1);
+  size_t best = ~size_t(0);
+  for (size_t cw = 1; cw <= 4; ++cw) {
+    const size_t w = 128 * cw, tiles = (n_words + w - 1) / w;
+    const size_t cost = (tiles + sms - 1) / sms * w;
+    if (cost <= best) {
+      best = cost;
+      pl.W = w;
+    }
+  }
+  pl.tiles = (n_words + pl.W - 1) / pl.W;
+  const size_t per_sm = std::max<size_t>((pl.tiles + sms - 1) / sms, 1);
+  const size_t budget = std::min<size_t>(200 * 1024 / per_sm, smem_optin);
+  pl.stages = 16;
+  for (int st : {64, 32}) {
+    if (fitch_smem(st, depth, pl.W) <= budget) {
+      pl.stages = st;
+      break;
+    }
+  }
+  pl.smem = fitch_smem(pl.stages, depth, pl.W);
+  return pl;
+}
 
 template <int LB>
 __device__ __forceinline__ uint4 fitch_quad(const uint4 a, const uint4 b, const uint4 valid,
@@ -145,12 +186,11 @@ __device__ __forceinline__ uint4 fitch_quad(const uint4 a, const uint4 b, const 
   return m;
 }
 
-template <int LB>
+template <int LB, int ST>
 __global__ void __launch_bounds__(160) fitch_tree_kernel(const FitchTreeArgs p) {
   constexpr int PER = Lanes<LB>::PER;
   constexpr uint32_t FLUSH = Lanes<LB>::FLUSH;
   constexpr uint32_t LSB = Lanes<LB>::H >> (LB - 1);
-  constexpr int ST = FT_STAGES;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ unsigned long long red[32];
   const int W = p.W, Q = W / 4;   // Q consumer threads, one uint4 each
@@ -238,18 +278,34 @@ __global__ void __launch_bounds__(160) fitch_tree_kernel(const FitchTreeArgs p) 
     ++taken;
   };
 
+  // the top of the stack stays in registers: most nodes are consumed by the
+  // very next step
+  uint4 top = make_uint4(0, 0, 0, 0);
+  bool top_valid = false;
+  auto pop = [&]() -> uint4 {
+    if (top_valid) {
+      top_valid = false;
+      return top;
+    }
+    return stk[(size_t)(--sp) * Q + c];
+  };
+  int4 op = p.n_ops > 0 ? __ldg(p.ops) : make_int4(0, 0, 0, 0);
   for (int i = 0; i < p.n_ops && ok; ++i) {
-    const int4 op = __ldg(p.ops + i);
+    // the next step's schedule entry is fetched while this one runs
+    const int4 next = i + 1 < p.n_ops ? __ldg(p.ops + i + 1) : op;
     uint4 x = make_uint4(0, 0, 0, 0), y = make_uint4(0, 0, 0, 0);
-    if (op.z >= p.n_tips) y = stk[(size_t)(--sp) * Q + c];
-    if (op.y >= p.n_tips) x = stk[(size_t)(--sp) * Q + c];
+    if (op.z >= p.n_tips) y = pop();
+    if (op.y >= p.n_tips) x = pop();
     if (op.y < p.n_tips) take(x);
     if (op.z < p.n_tips && ok) take(y);
     if (!ok) break;
     uint4 e;
     const uint4 med = fitch_quad<LB>(x, y, valid, e);
-    stk[(size_t)(sp++) * Q + c] = med;
+    if (top_valid) stk[(size_t)(sp++) * Q + c] = top;
+    top = med;
+    top_valid = true;
     if (active) __stcs(reinterpret_cast<uint4 *>(p.node_sets + (size_t)op.x * p.ld + word0), med);
+    op = next;
     cnt.x += e.x & valid.x & LSB;
     cnt.y += e.y & valid.y & LSB;
     cnt.z += e.z & valid.z & LSB;
@@ -359,14 +415,32 @@ pgpu_status pair_host(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b, const
   return PGPU_OK;
 }
 
+template <int LB, int ST>
+cudaError_t launch_tree_st(cudaStream_t stream, const FitchTreeArgs &args, const FitchPlan &pl) {
+  cudaError_t e = cudaFuncSetAttribute(fitch_tree_kernel<LB, ST>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)std::max<size_t>(pl.smem, 48 * 1024));
+  if (e != cudaSuccess) return e;
+  fitch_tree_kernel<LB, ST><<<(unsigned)pl.tiles, 32 + (int)pl.W / 4, pl.smem, stream>>>(args);
+  return cudaGetLastError();
+}
+
 template <int LB>
-pgpu_status launch_tree(pgpu_ctx *ctx, FitchTreeArgs &args, size_t n_tiles) {
-  const size_t smem = 16 * (size_t)FT_STAGES + 4 * (size_t)(FT_STAGES + args.depth) * args.W;
-  PGPU_CUDA(ctx, cudaFuncSetAttribute(fitch_tree_kernel<LB>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)std::max<size_t>(smem, 48 * 1024)));
-  fitch_tree_kernel<LB><<<(unsigned)n_tiles, 32 + args.W / 4, smem, ctx->stream>>>(args);
-  return pgpu_after_launch(ctx, "fitch_tree_kernel");
+cudaError_t launch_tree_lb(cudaStream_t stream, const FitchTreeArgs &args, const FitchPlan &pl) {
+  switch (pl.stages) {
+    case 64: return launch_tree_st<LB, 64>(stream, args, pl);
+    case 32: return launch_tree_st<LB, 32>(stream, args, pl);
+    default: return launch_tree_st<LB, 16>(stream, args, pl);
+  }
+}
+
+cudaError_t launch_tree(cudaStream_t stream, int lb, const FitchTreeArgs &args, const FitchPlan &pl) {
+  switch (lb) {
+    case 4: return launch_tree_lb<4>(stream, args, pl);
+    case 8: return launch_tree_lb<8>(stream, args, pl);
+    case 16: return launch_tree_lb<16>(stream, args, pl);
+    default: return launch_tree_lb<32>(stream, args, pl);
+  }
 }
 
 pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips, size_t ld,
@@ -389,22 +463,9 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
   PGPU_CUDA(ctx, cudaMemsetAsync(total, 0, sizeof(uint64_t), s));
   if (n_words == 0) return PGPU_OK;
 
-  // tile width W = 128 * cw words (cw consumer warps of 32 threads x 4 words):
-  // the one that minimises the words the busiest SM handles, given that
-  // every SM takes ceil(tiles / SMs) tiles; ties go to the wider tile
   const int depth = sch->max_depth;
-  const size_t sms = (size_t)std::max(ctx->num_sms, 1);
-  size_t W = 128, best = ~size_t(0);
-  for (size_t cw = 1; cw <= 4; ++cw) {
-    const size_t w = 128 * cw, tiles = (n_words + w - 1) / w;
-    const size_t cost = (tiles + sms - 1) / sms * w;
-    if (cost <= best) {
-      best = cost;
-      W = w;
-    }
-  }
-  const size_t smem = 16 * (size_t)FT_STAGES + 4 * (size_t)(FT_STAGES + depth) * W;
-  if (smem > ctx->smem_optin)
+  const FitchPlan pl = fitch_plan(n_words, depth, ctx->num_sms, ctx->smem_optin);
+  if (pl.smem > ctx->smem_optin)
     return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: tree needs a stack of %d rows; too deep",
                         depth);
   FitchTreeArgs args;
@@ -421,15 +482,16 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
   args.n_sites = n_sites;
   args.n_tips = n;
   args.n_ops = (int32_t)sch->ops.size();
-  args.W = (int)W;
+  args.W = (int)pl.W;
   args.depth = depth;
-  const size_t n_tiles = (n_words + W - 1) / W;
-  switch (lb) {
-    case 4: return launch_tree<4>(ctx, args, n_tiles);
-    case 8: return launch_tree<8>(ctx, args, n_tiles);
-    case 16: return launch_tree<16>(ctx, args, n_tiles);
-    default: return launch_tree<32>(ctx, args, n_tiles);
+  const cudaError_t e = launch_tree(ctx->stream, lb, args, pl);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return pgpu_set_err(ctx, PGPU_ERR_CUDA, "launch of fitch_tree_kernel failed: %s",
+                        cudaGetErrorString(e));
   }
+  ctx->launches++;
+  return PGPU_OK;
 }
 
 }  // namespace
@@ -458,18 +520,8 @@ pgpu_status pgpu_fitch_tree_launch_raw(cudaStream_t stream, const int4 *ops, con
     return PGPU_ERR_CUDA;
   }
   if (n_words == 0) return PGPU_OK;
-  const size_t nsm = (size_t)std::max(sms, 1);
-  size_t W = 128, best = ~size_t(0);
-  for (size_t cw = 1; cw <= 4; ++cw) {
-    const size_t w = 128 * cw, tiles = (n_words + w - 1) / w;
-    const size_t cost = (tiles + nsm - 1) / nsm * w;
-    if (cost <= best) {
-      best = cost;
-      W = w;
-    }
-  }
-  const size_t smem = 16 * (size_t)FT_STAGES + 4 * (size_t)(FT_STAGES + depth) * W;
-  if (smem > (size_t)optin) return PGPU_ERR_LIMIT;
+  const FitchPlan pl = fitch_plan(n_words, depth, sms, (size_t)optin);
+  if (pl.smem > (size_t)optin) return PGPU_ERR_LIMIT;
   FitchTreeArgs a;
   a.tips = tips;
   a.weights = weights;
@@ -484,30 +536,9 @@ pgpu_status pgpu_fitch_tree_launch_raw(cudaStream_t stream, const int4 *ops, con
   a.n_sites = n_sites;
   a.n_tips = n_tips;
   a.n_ops = n_ops;
-  a.W = (int)W;
+  a.W = (int)pl.W;
   a.depth = depth;
-  const size_t n_tiles = (n_words + W - 1) / W;
-  const int threads = 32 + (int)W / 4;
-  const int dyn = (int)std::max<size_t>(smem, 48 * 1024);
-  cudaError_t e = cudaSuccess;
-  switch (lb) {
-    case 4:
-      e = cudaFuncSetAttribute(fitch_tree_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
-      if (e == cudaSuccess) fitch_tree_kernel<4><<<(unsigned)n_tiles, threads, smem, stream>>>(a);
-      break;
-    case 8:
-      e = cudaFuncSetAttribute(fitch_tree_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
-      if (e == cudaSuccess) fitch_tree_kernel<8><<<(unsigned)n_tiles, threads, smem, stream>>>(a);
-      break;
-    case 16:
-      e = cudaFuncSetAttribute(fitch_tree_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
-      if (e == cudaSuccess) fitch_tree_kernel<16><<<(unsigned)n_tiles, threads, smem, stream>>>(a);
-      break;
-    default:
-      e = cudaFuncSetAttribute(fitch_tree_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
-      if (e == cudaSuccess) fitch_tree_kernel<32><<<(unsigned)n_tiles, threads, smem, stream>>>(a);
-      break;
-  }
+  cudaError_t e = launch_tree(stream, lb, a, pl);
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) {
     (void)cudaGetLastError();

@@ -29,6 +29,7 @@ enum {
   BUF_G,
   BUF_H,
   BUF_I,
+  BUF_J,
   BUF_COUNT
 };
 

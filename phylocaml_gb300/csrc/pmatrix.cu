@@ -15,6 +15,7 @@
 // memory.  Then U = Pi^-1/2 V and U^-1 = V^T Pi^1/2, so Q = U diag(lambda) U^-1
 // and P(t) = U diag(exp(lambda t)) U^-1.  Jacobi needs no LAPACK and gives
 // orthogonal V to working precision.
+#include <algorithm>
 #include <cmath>
 
 #include "pgpu_internal.cuh"
@@ -193,6 +194,7 @@ struct ComposeArgs {
   int allow_q;                  // t == -1 returns Q (the reference's compose)
   const int *status;            // eigendecomposition status or null
   int *flag;
+  int p32_mode;                 // P32Mode
 };
 
 __global__ void __launch_bounds__(256) compose_kernel(const ComposeArgs p) {
@@ -228,7 +230,68 @@ __global__ void __launch_bounds__(256) compose_kernel(const ComposeArgs p) {
     }
     const size_t off = ((size_t)b * R + r) * SS + (size_t)i * S + j;
     if (p.P) p.P[off] = v;
-    if (p.P32) p.P32[off] = (float)v;
+    if (p.P32) {
+      const double d = (p.p32_mode != P32_PLAIN && i == j) ? v - 1.0 : v;
+      if (p.p32_mode == P32_MINUS_I_PAIRS) {
+        const float hi = (float)d;
+        p.P32[2 * off] = hi;
+        p.P32[2 * off + 1] = (float)(d - (double)hi);
+      } else {
+        p.P32[off] = (float)d;
+      }
+    }
+  }
+}
+
+// Tip rows: tab[t][r][c][i] = sum_j P(t, r)[i][j] * code_tab[c][j] for every
+// tip t (the branch above it), rate r and tip code c, formed in FP64 from the
+// eigen system and stored as float, float pair (hi, lo) or double.  A tip
+// child then costs the pruning kernel one table read instead of a
+// matrix-vector product.
+struct TipTabArgs {
+  const double *U, *lam, *Ui;
+  const double *t;          // [n_tips] branch lengths above the tips
+  const double *rates;      // [R]
+  const double *code_tab;   // [n_codes][S]
+  void *out;
+  int S, R, n_codes, form;  // form: 0 float, 1 float pair, 2 double
+  const int *status;
+};
+
+__global__ void __launch_bounds__(128) tip_table_kernel(const TipTabArgs p) {
+  extern __shared__ __align__(16) double sm[];
+  const int S = p.S, SS = S * S;
+  double *P = sm;   // [S][S]
+  const int tip = blockIdx.x, r = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
+  if (p.status && *p.status) return;
+  const double tt = p.t[tip], rate = p.rates ? p.rates[r] : 1.0;
+  const bool ident = !(tt >= 1e-10);
+  for (int o = tid; o < SS; o += nt) {
+    const int i = o / S, j = o % S;
+    double v = 0.0;
+    if (ident) {
+      v = i == j ? 1.0 : 0.0;
+    } else {
+      for (int k = 0; k < S; ++k) v = fma(p.U[i * S + k] * exp(p.lam[k] * rate * tt), p.Ui[k * S + j], v);
+    }
+    P[o] = v;
+  }
+  __syncthreads();
+  const size_t base = ((size_t)tip * p.R + r) * p.n_codes * S;
+  for (int o = tid; o < p.n_codes * S; o += nt) {
+    const int c = o / S, i = o % S;
+    double v = 0.0;
+    for (int j = 0; j < S; ++j) v = fma(P[i * S + j], p.code_tab[c * S + j], v);
+    const size_t at = base + o;
+    if (p.form == 0) {
+      static_cast<float *>(p.out)[at] = (float)v;
+    } else if (p.form == 1) {
+      const float hi = (float)v;
+      static_cast<float *>(p.out)[2 * at] = hi;
+      static_cast<float *>(p.out)[2 * at + 1] = (float)(v - (double)hi);
+    } else {
+      static_cast<double *>(p.out)[at] = v;
+    }
   }
 }
 
@@ -255,16 +318,31 @@ pgpu_status pgpu_launch_eig(pgpu_ctx *ctx, const double *Q_dev, const double *pi
 pgpu_status pgpu_launch_compose(pgpu_ctx *ctx, const double *U_dev, const double *lam_dev,
                                 const double *Ui_dev, int S, const double *t_dev, int n_br,
                                 const double *rates_dev, int R, double *P_dev, float *P32_dev,
-                                bool allow_q, const int *status_dev) {
+                                bool allow_q, const int *status_dev, int p32_mode) {
   if (n_br <= 0) return PGPU_OK;
   ComposeArgs a{U_dev, lam_dev, Ui_dev, t_dev,       rates_dev,  P_dev,       P32_dev,
-                S,     R,       n_br,   allow_q ? 1 : 0, status_dev, ctx->d_flag};
+                S,     R,       n_br,   allow_q ? 1 : 0, status_dev, ctx->d_flag,
+                p32_mode};
   const size_t smem = sizeof(double) * (2 * (size_t)S * S + (size_t)R * S);
   PGPU_CUDA(ctx, cudaFuncSetAttribute(compose_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)std::max<size_t>(smem, 1024)));
   const int threads = R * S * S <= 64 ? 64 : (R * S * S <= 128 ? 128 : 256);
   compose_kernel<<<n_br, threads, smem, ctx->stream>>>(a);
   return pgpu_after_launch(ctx, "compose_kernel");
+}
+
+pgpu_status pgpu_launch_tip_table(pgpu_ctx *ctx, const double *U_dev, const double *lam_dev,
+                                  const double *Ui_dev, int S, const double *t_dev, int n_tips,
+                                  const double *rates_dev, int R, const double *code_tab_dev,
+                                  int n_codes, void *out_dev, int form, const int *status_dev) {
+  if (n_tips <= 0) return PGPU_OK;
+  TipTabArgs a{U_dev, lam_dev, Ui_dev, t_dev, rates_dev, code_tab_dev, out_dev, S, R, n_codes, form,
+               status_dev};
+  const size_t smem = sizeof(double) * (size_t)S * S;
+  PGPU_CUDA(ctx, cudaFuncSetAttribute(tip_table_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)std::max<size_t>(smem, 1024)));
+  tip_table_kernel<<<dim3(n_tips, R), 128, smem, ctx->stream>>>(a);
+  return pgpu_after_launch(ctx, "tip_table_kernel");
 }
 
 // ---------------------------------------------------------------------------

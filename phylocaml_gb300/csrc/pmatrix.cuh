@@ -12,8 +12,25 @@ pgpu_status pgpu_launch_eig(pgpu_ctx *ctx, const double *Q_dev, const double *pi
 // of one model; FP64 into P_dev and/or FP32 into P32_dev (either may be
 // null).  With allow_q, t == -1 yields Q (MlModel.compose's special case).
 // If status_dev is given and non-zero the matrices are not built and the
-// context's error word records the model failure.
+// context's error word records the model failure.  p32_mode selects the FP32
+// copy: P, P - I (formed in FP64 before rounding, which keeps the small
+// entries of short branches at full relative precision), or P - I as
+// (hi, lo) float pairs.
+enum P32Mode {
+  P32_PLAIN = 0,          // fl32(P)
+  P32_MINUS_I = 1,        // fl32(P - I)
+  P32_MINUS_I_PAIRS = 2   // (hi, lo) float pairs of P - I, two floats per entry
+};
 pgpu_status pgpu_launch_compose(pgpu_ctx *ctx, const double *U_dev, const double *lam_dev,
                                 const double *Ui_dev, int S, const double *t_dev, int n_br,
                                 const double *rates_dev, int R, double *P_dev, float *P32_dev,
-                                bool allow_q, const int *status_dev = nullptr);
+                                bool allow_q, const int *status_dev = nullptr,
+                                int p32_mode = P32_PLAIN);
+
+// Tip rows tab[t][r][c][i] = (P(t, r) code_tab[c])[i] for the n_tips branches
+// above the tips (t_dev holds their lengths), in FP64, stored as float
+// (form 0), (hi, lo) float pairs (form 1) or double (form 2).
+pgpu_status pgpu_launch_tip_table(pgpu_ctx *ctx, const double *U_dev, const double *lam_dev,
+                                  const double *Ui_dev, int S, const double *t_dev, int n_tips,
+                                  const double *rates_dev, int R, const double *code_tab_dev,
+                                  int n_codes, void *out_dev, int form, const int *status_dev);

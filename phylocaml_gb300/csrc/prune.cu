@@ -38,7 +38,8 @@ namespace {
 
 struct PruneArgs {
   const uint8_t *tip_codes;   // [n_tips][ld_pat]
-  const void *P;              // [2n-2][R][S][S] of T
+  const void *P;              // [2n-2][R][S][S] coefficients of the form (see below)
+  const void *tiptab;         // [n_tips][R][n_codes][S] tip rows P(t,r) code_tab[c] (form's values)
   const double *code_tab;     // [n_codes][S]
   const double *pi;           // [S]
   const double *probs;        // [R]
@@ -49,34 +50,7 @@ struct PruneArgs {
   const int32_t *tip_seq;
   int *flag;
   size_t ld_pat, n_pat;
-  int n_tips, n_ops, n_codes, R, NT, stages, depth;
-};
-
-template <typename T>
-struct ScaleTraits;
-template <>
-struct ScaleTraits<float> {
-  static constexpr float thresh = 0x1p-32f;
-  __device__ static float pow2(int k) {  // 2^k for -126 <= k <= 127
-    return __int_as_float((127 + k) << 23);
-  }
-  __device__ static int exponent(float x) {
-    int e;
-    (void)frexpf(x, &e);
-    return e;
-  }
-};
-template <>
-struct ScaleTraits<double> {
-  static constexpr double thresh = 0x1p-256;
-  __device__ static double pow2(int k) {  // 2^k for -1022 <= k <= 1023
-    return __longlong_as_double((long long)(1023 + k) << 52);
-  }
-  __device__ static int exponent(double x) {
-    int e;
-    (void)frexp(x, &e);
-    return e;
-  }
+  int n_tips, n_ops, n_codes, R, NP, depth;
 };
 
 __device__ __forceinline__ void two_sum(double a, double b, double &s, double &e) {
@@ -100,34 +74,203 @@ __device__ __forceinline__ void warp_csum(double &s, double &c) {
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
-template <typename T, int S, int RM>
-struct PruneLayout {
-  __host__ __device__ static size_t ring_off(int stages) { return 16 * (size_t)stages; }
-  __host__ __device__ static size_t tab_off(int stages, int NT) { return align16(ring_off(stages) + (size_t)stages * NT); }
-  __host__ __device__ static size_t stk_off(int stages, int NT, int n_codes) {
-    return align16(tab_off(stages, NT) + (size_t)n_codes * S * sizeof(T));
+constexpr int PR_STAGES = 8;      // ring depth in postorder steps (power of two)
+constexpr int PR_THREADS = 256;   // consumer threads per CTA
+
+// ---- the three arithmetic forms -------------------------------------------
+// Fp32  values float;  P buffer holds fl32(P - I);  y_i = x_i + sum_j D_ij x_j
+// Fp64  values double; P buffer holds P;            y_i = sum_j P_ij x_j
+// Ff32  values are unevaluated float pairs (hi + lo, about 48 significant
+//       bits); P buffer holds (hi, lo) pairs of P - I; every sum and product
+//       is an error-free float transformation, so the only roundings are of
+//       the order of 2^-48.  Sites that share subtree patterns share their
+//       rounding errors, which then add up linearly over the patterns; the
+//       pair form keeps that sum far below 1e-3 where plain FP32 cannot.
+
+struct ff {
+  float h, l;
+};
+
+__device__ __forceinline__ ff two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {   // |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return fast_two_sum(p, e);
+}
+
+// 2^k as a float for 0 <= k <= 127
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
+
+struct Fp32 {
+  using V = float;
+  using Coef = float;
+  static constexpr float thresh = 0x1p-32f;
+  __device__ static V zero() { return 0.0f; }
+  __device__ static float mag(V v) { return v; }
+  __device__ static double to_d(V v) { return (double)v; }
+  __device__ static V mul(V a, V b) { return a * b; }
+  __device__ static V scale(V v, int k) { return v * pow2f(k); }
+  __device__ static void load_tip(const void *tab, size_t at, V *y) {
+    const float4 v = reinterpret_cast<const float4 *>(tab)[at];
+    y[0] = v.x;
+    y[1] = v.y;
+    y[2] = v.z;
+    y[3] = v.w;
   }
-  __host__ __device__ static size_t bytes(int stages, int NT, int n_codes, int depth) {
-    return stk_off(stages, NT, n_codes) + (size_t)depth * RM * S * NT * sizeof(T);
+  // y[i] = x[i] + sum_j D[i][j] x[j]
+  __device__ static void rows(const Coef *D, const V *x, V *y) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float4 d = reinterpret_cast<const float4 *>(D)[i];
+      float s = d.x * x[0];
+      s = fmaf(d.y, x[1], s);
+      s = fmaf(d.z, x[2], s);
+      s = fmaf(d.w, x[3], s);
+      y[i] = x[i] + s;
+    }
   }
 };
 
-template <typename T, int S, int RM>
-__global__ void __launch_bounds__(160) prune_tree_kernel(const PruneArgs p) {
-  extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ double2 red[8];
-  using L = PruneLayout<T, S, RM>;
-  constexpr int RS = RM * S;
-  const int NT = p.NT, ST = p.stages, R = p.R;
-  uint64_t *full = reinterpret_cast<uint64_t *>(smem);
-  uint64_t *empty = full + ST;
-  uint8_t *ring = smem + L::ring_off(ST);                                  // [ST][NT]
-  T *tab = reinterpret_cast<T *>(smem + L::tab_off(ST, NT));               // [n_codes][S]
-  T *stk = reinterpret_cast<T *>(smem + L::stk_off(ST, NT, p.n_codes));    // [depth][RS][NT]
-  const size_t tile0 = (size_t)blockIdx.x * NT;
-  const int tid = threadIdx.x;
+struct Fp64 {
+  using V = double;
+  using Coef = double;
+  static constexpr double thresh = 0x1p-256;
+  __device__ static V zero() { return 0.0; }
+  __device__ static double mag(V v) { return v; }
+  __device__ static double to_d(V v) { return v; }
+  __device__ static V mul(V a, V b) { return a * b; }
+  __device__ static V scale(V v, int k) { return v * __longlong_as_double((long long)(1023 + k) << 52); }
+  __device__ static void load_tip(const void *tab, size_t at, V *y) {
+    const double2 a = reinterpret_cast<const double2 *>(tab)[2 * at];
+    const double2 b = reinterpret_cast<const double2 *>(tab)[2 * at + 1];
+    y[0] = a.x;
+    y[1] = a.y;
+    y[2] = b.x;
+    y[3] = b.y;
+  }
+  __device__ static void rows(const Coef *P, const V *x, V *y) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const double2 a = reinterpret_cast<const double2 *>(P)[2 * i];
+      const double2 b = reinterpret_cast<const double2 *>(P)[2 * i + 1];
+      double s = a.x * x[0];
+      s = fma(a.y, x[1], s);
+      s = fma(b.x, x[2], s);
+      s = fma(b.y, x[3], s);
+      y[i] = s;
+    }
+  }
+};
 
-  for (int i = tid; i < p.n_codes * S; i += blockDim.x) tab[i] = (T)p.code_tab[i];
+struct Ff32 {
+  using V = ff;
+  using Coef = float2;
+  static constexpr float thresh = 0x1p-32f;
+  __device__ static V zero() { return {0.0f, 0.0f}; }
+  __device__ static float mag(V v) { return v.h; }
+  __device__ static double to_d(V v) { return (double)v.h + (double)v.l; }
+  __device__ static V mul(V a, V b) { return ff_mul(a, b); }
+  __device__ static V scale(V v, int k) {
+    const float f = pow2f(k);
+    return {v.h * f, v.l * f};
+  }
+  __device__ static void load_tip(const void *tab, size_t at, V *y) {
+    const float4 a = reinterpret_cast<const float4 *>(tab)[2 * at];
+    const float4 b = reinterpret_cast<const float4 *>(tab)[2 * at + 1];
+    y[0] = {a.x, a.y};
+    y[1] = {a.z, a.w};
+    y[2] = {b.x, b.y};
+    y[3] = {b.z, b.w};
+  }
+  __device__ static void rows(const Coef *D, const V *x, V *y) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float4 d01 = reinterpret_cast<const float4 *>(D)[2 * i];
+      const float4 d23 = reinterpret_cast<const float4 *>(D)[2 * i + 1];
+      const float dh[4] = {d01.x, d01.z, d23.x, d23.z};
+      const float dl[4] = {d01.y, d01.w, d23.y, d23.w};
+      // c = sum_j D_ij x_j with the exact product errors and sum errors kept
+      float sh = 0.0f, sl = 0.0f;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float ph = __fmul_rn(dh[j], x[j].h);
+        float pe = __fmaf_rn(dh[j], x[j].h, -ph);
+        pe = __fmaf_rn(dh[j], x[j].l, pe);
+        pe = __fmaf_rn(dl[j], x[j].h, pe);
+        const ff t = two_sum(sh, ph);
+        sh = t.h;
+        sl = __fadd_rn(sl, __fadd_rn(t.l, pe));
+      }
+      // y = x + c
+      const ff t = two_sum(x[i].h, sh);
+      y[i] = fast_two_sum(t.h, __fadd_rn(t.l, __fadd_rn(x[i].l, sl)));
+    }
+  }
+};
+
+// Shared memory of one CTA: PR_STAGES per-op slots, then the CLV stack.
+// A slot holds everything one postorder step reads, staged by the producer:
+//   [0, NP)            tip codes of child a (if a is a tip)
+//   [NP, 2 NP)         tip codes of child b
+//   coef block a       R x 16 coefficients of the branch above a (internal a)
+//   coef block b
+//   tip block a        R x n_codes x 4 tip rows of the branch above a (tip a)
+//   tip block b
+template <typename Pol>
+struct PruneLayout {
+  using V = typename Pol::V;
+  using Coef = typename Pol::Coef;
+  __host__ __device__ static size_t coef_bytes(int R) { return (size_t)R * 16 * sizeof(Coef); }
+  __host__ __device__ static size_t tip_bytes(int R, int n_codes) {
+    return (size_t)R * n_codes * 4 * sizeof(V);
+  }
+  __host__ __device__ static size_t coef_off(int NP) { return 2 * (size_t)NP; }
+  __host__ __device__ static size_t tip_off(int NP, int R) { return coef_off(NP) + 2 * coef_bytes(R); }
+  __host__ __device__ static size_t slot_bytes(int NP, int R, int n_codes) {
+    return (tip_off(NP, R) + 2 * tip_bytes(R, n_codes) + 127) & ~size_t(127);
+  }
+  __host__ __device__ static size_t ring_off() { return 128; }
+  __host__ __device__ static size_t stk_off(int NP, int R, int n_codes) {
+    return ring_off() + (size_t)PR_STAGES * slot_bytes(NP, R, n_codes);
+  }
+  __host__ __device__ static size_t bytes(int NP, int R, int n_codes, int depth) {
+    return stk_off(NP, R, n_codes) + (size_t)depth * 4 * PR_THREADS * sizeof(V);
+  }
+};
+
+// One CTA: 32 producer threads + PR_THREADS consumers.  Consumer c works on
+// pattern c / RT of the tile and rate class c % RT (RT lanes per pattern,
+// R <= RT of them active).  Each thread holds the 4 state values of its rate
+// class; the RT lanes of a pattern agree on rescaling through shuffles.
+template <typename Pol, int RT>
+__global__ void __launch_bounds__(32 + PR_THREADS) prune_tree_kernel(const PruneArgs p) {
+  using V = typename Pol::V;
+  using Coef = typename Pol::Coef;
+  using L = PruneLayout<Pol>;
+  constexpr int ST = PR_STAGES, NT = PR_THREADS;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ double2 red[NT / 32];
+  const int NP = p.NP, R = p.R, NC = p.n_codes;
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem);     // [ST]
+  uint64_t *empty = full + ST;                              // [ST]
+  const size_t SB = L::slot_bytes(NP, R, NC);
+  unsigned char *ring = smem + L::ring_off();               // [ST][SB]
+  V *stk = reinterpret_cast<V *>(smem + L::stk_off(NP, R, NC));   // [depth][4][NT]
+  const size_t tile0 = (size_t)blockIdx.x * NP;
+  const int tid = threadIdx.x;
+  const size_t CB = L::coef_bytes(R), TB = L::tip_bytes(R, NC);
+
   if (tid == 0) {
     for (int s = 0; s < ST; ++s) {
       mbar_init(&full[s], 1);
@@ -138,145 +281,157 @@ __global__ void __launch_bounds__(160) prune_tree_kernel(const PruneArgs p) {
   __syncthreads();
 
   if (tid < 32) {
+    // producer: everything step i reads goes into slot i % ST
     if (tid == 0) {
-      const size_t span = min((size_t)NT, p.ld_pat - tile0);
-      const uint32_t bytes = (uint32_t)span;
+      const uint32_t code_bytes = (uint32_t)min((size_t)NP, p.ld_pat - tile0);
+      const unsigned char *Pg = static_cast<const unsigned char *>(p.P);
+      const unsigned char *Tg = static_cast<const unsigned char *>(p.tiptab);
       int issued = 0;
-      for (int j = 0; j < p.n_tips; ++j) {
-        const int slot = j % ST, round = j / ST;
+      for (int i = 0; i < p.n_ops; ++i) {
+        const int slot = i & (ST - 1), round = i / ST;
         if (round > 0 && !mbar_wait_bounded(&empty[slot], (round - 1) & 1, p.flag)) break;
-        const int32_t tip = __ldg(p.tip_seq + j);
-        mbar_arrive_expect_tx(&full[slot], bytes);
-        bulk_g2s(ring + (size_t)slot * NT, p.tip_codes + (size_t)tip * p.ld_pat + tile0, bytes,
-                 &full[slot]);
-        issued = j + 1;
+        const int4 op = __ldg(p.ops + i);
+        unsigned char *sl = ring + (size_t)slot * SB;
+        uint32_t tx = 0;
+        for (int h = 0; h < 2; ++h) {
+          const int ch = h == 0 ? op.y : op.z;
+          tx += ch < p.n_tips ? code_bytes + (uint32_t)TB : (uint32_t)CB;
+        }
+        mbar_arrive_expect_tx(&full[slot], tx);
+        for (int h = 0; h < 2; ++h) {
+          const int ch = h == 0 ? op.y : op.z;
+          if (ch < p.n_tips) {
+            bulk_g2s(sl + (size_t)h * NP, p.tip_codes + (size_t)ch * p.ld_pat + tile0, code_bytes,
+                     &full[slot]);
+            bulk_g2s(sl + L::tip_off(NP, R) + h * TB, Tg + (size_t)ch * TB, (uint32_t)TB, &full[slot]);
+          } else {
+            bulk_g2s(sl + L::coef_off(NP) + h * CB, Pg + (size_t)ch * CB, (uint32_t)CB, &full[slot]);
+          }
+        }
+        issued = i + 1;
       }
-      for (int j = max(0, issued - ST); j < issued; ++j)
-        (void)mbar_wait_bounded(&full[j % ST], (j / ST) & 1, p.flag);
+      for (int i = max(0, issued - ST); i < issued; ++i)
+        (void)mbar_wait_bounded(&full[i & (ST - 1)], (i / ST) & 1, p.flag);
     }
     return;
   }
 
   const int c = tid - 32, lane = tid & 31;
-  const size_t pat = tile0 + c;
+  const int pl = c / RT, r = c % RT;
+  const size_t pat = tile0 + pl;
   const bool active = pat < p.n_pat;
-  const T *P = reinterpret_cast<const T *>(p.P);
-  const size_t PB = (size_t)R * S * S;   // one branch's block
+  const bool rate_on = r < R;
 
-  T top[RS];
+  V top[4];
   bool top_valid = false;
-  int sp = 0, taken = 0, escale = 0;
+  int sp = 0, escale = 0;
   bool ok = true;
 
-  auto take = [&]() -> int {
-    const int slot = taken % ST;
-    const bool got =
-        __all_sync(0xffffffffu, mbar_wait_bounded(&full[slot], (taken / ST) & 1, p.flag));
-    if (!got) {
-      ok = false;
-      return 0;
-    }
-    int code = ring[(size_t)slot * NT + c];
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[slot]);
-    ++taken;
-    if (code >= p.n_codes) {
-      if (active) atomicOr(p.flag, PGPU_FLAG_BADCODE);
-      code = 0;
-    }
-    return code;
-  };
-  auto pop = [&](T *dst) {
+  auto pop = [&](V *dst) {
     if (top_valid) {
 #pragma unroll
-      for (int e = 0; e < RS; ++e) dst[e] = top[e];
+      for (int e = 0; e < 4; ++e) dst[e] = top[e];
       top_valid = false;
     } else {
       --sp;
 #pragma unroll
-      for (int e = 0; e < RS; ++e) dst[e] = stk[((size_t)sp * RS + e) * NT + c];
-    }
-  };
-  // acc = (or *=) P_child * x, x from registers or from the tip code table
-  auto apply = [&](int child, const T *x, int code, T *acc, bool first) {
-    const T *Pc = P + (size_t)child * PB;
-#pragma unroll
-    for (int r = 0; r < RM; ++r) {
-      if (r < R) {
-        T xv[S];
-#pragma unroll
-        for (int j = 0; j < S; ++j) xv[j] = code >= 0 ? tab[code * S + j] : x[r * S + j];
-#pragma unroll
-        for (int i = 0; i < S; ++i) {
-          const T *row = Pc + ((size_t)r * S + i) * S;
-          T s = 0;
-#pragma unroll
-          for (int j = 0; j < S; ++j) s = fma(__ldg(row + j), xv[j], s);
-          acc[r * S + i] = first ? s : acc[r * S + i] * s;
-        }
-      }
+      for (int e = 0; e < 4; ++e) dst[e] = stk[((size_t)sp * 4 + e) * NT + c];
     }
   };
 
   for (int i = 0; i < p.n_ops && ok; ++i) {
+    const int slot = i & (ST - 1);
     const int4 op = __ldg(p.ops + i);
     const int a = op.y, b = op.z;
-    T xa[RS], xb[RS];
+    V xa[4], xb[4];
     if (b >= p.n_tips) pop(xb);
     if (a >= p.n_tips) pop(xa);
-    int ca = -1, cb = -1;
-    if (a < p.n_tips) ca = take();
-    if (b < p.n_tips && ok) cb = take();
-    if (!ok) break;
-    T acc[RS];
-    apply(a, xa, ca, acc, true);
-    apply(b, xb, cb, acc, false);
-    // exact power-of-two rescaling
-    T mx = 0;
-#pragma unroll
-    for (int e = 0; e < RS; ++e)
-      if (e < R * S) mx = fmax(mx, acc[e]);
-    if (mx < ScaleTraits<T>::thresh && mx > (T)0) {
-      const int ex = ScaleTraits<T>::exponent(mx);
-      escale += ex;
-      const T f = ScaleTraits<T>::pow2(-ex);
-#pragma unroll
-      for (int e = 0; e < RS; ++e) acc[e] *= f;
+    const bool got =
+        __all_sync(0xffffffffu, mbar_wait_bounded(&full[slot], (i / ST) & 1, p.flag));
+    if (!got) {
+      ok = false;
+      break;
     }
-    // push
+    const unsigned char *sl = ring + (size_t)slot * SB;
+    V acc[4];
+    if (rate_on) {
+      V y[2][4];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int ch = h == 0 ? a : b;
+        if (ch < p.n_tips) {
+          int code = sl[h * NP + pl];
+          if (code >= NC) {
+            if (active && r == 0) atomicOr(p.flag, PGPU_FLAG_BADCODE);
+            code = 0;
+          }
+          Pol::load_tip(sl + L::tip_off(NP, R) + h * TB, (size_t)r * NC + code, y[h]);
+        } else {
+          Pol::rows(reinterpret_cast<const Coef *>(sl + L::coef_off(NP) + h * CB) + r * 16,
+                    h == 0 ? xa : xb, y[h]);
+        }
+      }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) acc[e] = Pol::mul(y[0][e], y[1][e]);
+    } else {
+#pragma unroll
+      for (int e = 0; e < 4; ++e) acc[e] = Pol::zero();
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[slot]);
+    // exact power-of-two rescaling, agreed by the RT lanes of the pattern;
+    // rare, so the group maximum is formed only when some lane needs it
+    auto mx = fmax(fmax(Pol::mag(acc[0]), Pol::mag(acc[1])), fmax(Pol::mag(acc[2]), Pol::mag(acc[3])));
+    if (__any_sync(0xffffffffu, mx < Pol::thresh && mx > 0)) {
+#pragma unroll
+      for (int o = 1; o < RT; o <<= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      if (mx < Pol::thresh && mx > 0) {
+        int ex;
+        (void)frexp((double)mx, &ex);
+        escale += ex;
+        // two steps when the largest entry is subnormal, so each factor
+        // stays a normal power of two
+        const int k1 = min(-ex, 120), k2 = -ex - k1;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[e] = Pol::scale(acc[e], k1);
+        if (k2 > 0) {
+#pragma unroll
+          for (int e = 0; e < 4; ++e) acc[e] = Pol::scale(acc[e], k2);
+        }
+      }
+    }
     if (top_valid) {
 #pragma unroll
-      for (int e = 0; e < RS; ++e) stk[((size_t)sp * RS + e) * NT + c] = top[e];
+      for (int e = 0; e < 4; ++e) stk[((size_t)sp * 4 + e) * NT + c] = top[e];
       ++sp;
     }
 #pragma unroll
-    for (int e = 0; e < RS; ++e) top[e] = acc[e];
+    for (int e = 0; e < 4; ++e) top[e] = acc[e];
     top_valid = true;
   }
 
-  // root likelihood, weighted log, compensated block sum
+  // root: sum over rate classes of probs[r] * sum_i pi_i x_i, in FP64
+  double part = 0.0;
+  if (ok && rate_on) {
+    double lr = 0.0;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) lr += p.pi[e] * Pol::to_d(top[e]);
+    part = p.probs[r] * lr;
+  }
+#pragma unroll
+  for (int o = 1; o < RT; o <<= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
   double s = 0.0, comp = 0.0;
-  if (ok && active) {
-    double Ls = 0.0;
-#pragma unroll
-    for (int r = 0; r < RM; ++r) {
-      if (r < R) {
-        double lr = 0.0;
-#pragma unroll
-        for (int i = 0; i < S; ++i) lr += p.pi[i] * (double)top[r * S + i];
-        Ls += p.probs[r] * lr;
-      }
-    }
-    const double lnl = log(Ls) + (double)escale * 0.69314718055994530942;
+  if (ok && active && r == 0) {
+    const double lnl = log(part) + (double)escale * 0.69314718055994530942;
     if (p.site_lnl) p.site_lnl[pat] = lnl;
     s = p.weights ? p.weights[pat] * lnl : lnl;
   }
   warp_csum(s, comp);
-  const int cw = c >> 5, ncw = NT / 32;
+  const int cw = c >> 5;
   if (lane == 0) red[cw] = make_double2(s, comp);
   asm volatile("bar.sync 1, %0;" ::"r"(NT) : "memory");
   if (cw == 0) {
-    double2 v = lane < ncw ? red[lane] : make_double2(0.0, 0.0);
+    double2 v = lane < NT / 32 ? red[lane] : make_double2(0.0, 0.0);
     double ss = v.x, cc = v.y;
     warp_csum(ss, cc);
     if (lane == 0) p.partials[blockIdx.x] = make_double2(ss, cc);
@@ -298,16 +453,29 @@ __global__ void __launch_bounds__(32) prune_finalize_kernel(const double2 *parti
   out[0] = s + c;
 }
 
-template <typename T, int S, int RM>
-pgpu_status launch_prune(pgpu_ctx *ctx, PruneArgs &a, size_t n_tiles) {
-  const size_t smem = PruneLayout<T, S, RM>::bytes(a.stages, a.NT, a.n_codes, a.depth);
-  if (smem > ctx->smem_optin)
-    return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "prune: %zu bytes of shared memory needed", smem);
-  PGPU_CUDA(ctx, cudaFuncSetAttribute(prune_tree_kernel<T, S, RM>,
+template <typename Pol, int RT>
+pgpu_status launch_prune_rt(pgpu_ctx *ctx, PruneArgs &a, size_t n_tiles, size_t smem) {
+  PGPU_CUDA(ctx, cudaFuncSetAttribute(prune_tree_kernel<Pol, RT>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)std::max<size_t>(smem, 48 * 1024)));
-  prune_tree_kernel<T, S, RM><<<(unsigned)n_tiles, 32 + a.NT, smem, ctx->stream>>>(a);
+  prune_tree_kernel<Pol, RT><<<(unsigned)n_tiles, 32 + PR_THREADS, smem, ctx->stream>>>(a);
   return pgpu_after_launch(ctx, "prune_tree_kernel");
+}
+
+template <typename Pol>
+pgpu_status launch_prune(pgpu_ctx *ctx, PruneArgs &a, int RT) {
+  a.NP = PR_THREADS / RT;
+  const size_t n_tiles = (a.n_pat + a.NP - 1) / a.NP;
+  const size_t smem = PruneLayout<Pol>::bytes(a.NP, a.R, a.n_codes, a.depth);
+  if (smem > ctx->smem_optin)
+    return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "prune: %zu bytes of shared memory needed (tree too deep)",
+                        smem);
+  switch (RT) {
+    case 1: return launch_prune_rt<Pol, 1>(ctx, a, n_tiles, smem);
+    case 2: return launch_prune_rt<Pol, 2>(ctx, a, n_tiles, smem);
+    case 4: return launch_prune_rt<Pol, 4>(ctx, a, n_tiles, smem);
+    default: return launch_prune_rt<Pol, 8>(ctx, a, n_tiles, smem);
+  }
 }
 
 }  // namespace
@@ -394,8 +562,8 @@ pgpu_status prune_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *m,
                       const double *weights, size_t n_pat, int precision, double *lnl_dev,
                       double *site_lnl_dev) {
   PGPU_TRY(check_model(ctx, m, codes));
-  if (precision != 32 && precision != 64)
-    return pgpu_set_err(ctx, PGPU_ERR_ARG, "prune: precision must be 32 or 64");
+  if (precision != 32 && precision != 48 && precision != 64)
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "prune: precision must be 32, 48 or 64");
   if (!tree || !tree->brlen) return pgpu_set_err(ctx, PGPU_ERR_ARG, "prune: tree->brlen is required");
   if (!tips || !lnl_dev) return pgpu_set_err(ctx, PGPU_ERR_ARG, "prune: null buffer");
   if (ld_pat % 16 != 0 || ld_pat < n_pat || ((uintptr_t)tips & 15))
@@ -424,10 +592,11 @@ pgpu_status prune_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *m,
   PGPU_TRY(pgpu_stage_commit(ctx, lay.bytes));
 
   // device scratch: eigen system, P matrices, per-CTA partial sums
-  const int NT = precision == 32 ? 128 : 64;
-  const size_t n_tiles = (n_pat + NT - 1) / NT;
+  const int RT = R <= 1 ? 1 : R <= 2 ? 2 : R <= 4 ? 4 : 8;
+  const size_t n_tiles = (n_pat + (PR_THREADS / RT) - 1) / (PR_THREADS / RT);
   const size_t SS = (size_t)S * S;
-  const size_t p_bytes = (size_t)n_br * R * SS * (precision == 32 ? 4 : 8);
+  const size_t coef = precision == 32 ? 4 : 8;   // float, double, or float pair
+  const size_t p_bytes = (size_t)n_br * R * SS * coef;
   void *deig, *dP, *dpart;
   PGPU_TRY(pgpu_buf(ctx, BUF_H, 2 * SS * 8 + S * 8 + 64, &deig));
   PGPU_TRY(pgpu_buf(ctx, BUF_I, p_bytes, &dP));
@@ -437,12 +606,22 @@ pgpu_status prune_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *m,
   PGPU_TRY(pgpu_launch_eig(ctx, rebase(d, lay.Q), rebase(d, lay.pi), S, 1, dU, dlam, dUi, dst));
   PGPU_TRY(pgpu_launch_compose(ctx, dU, dlam, dUi, S, rebase(d, lay.brlen), n_br,
                                rebase(d, lay.rates), R, precision == 64 ? (double *)dP : nullptr,
-                               precision == 32 ? (float *)dP : nullptr, false, dst));
+                               precision == 64 ? nullptr : (float *)dP, false, dst,
+                               precision == 32 ? P32_MINUS_I : precision == 48 ? P32_MINUS_I_PAIRS
+                                                                               : P32_PLAIN));
+  // tip rows in FP64, stored in the form's value type
+  const size_t tt_vals = (size_t)n * R * codes->n_codes * S;
+  void *dtt;
+  PGPU_TRY(pgpu_buf(ctx, BUF_J, tt_vals * (precision == 32 ? 4 : 8), &dtt));
+  PGPU_TRY(pgpu_launch_tip_table(ctx, dU, dlam, dUi, S, rebase(d, lay.brlen), n, rebase(d, lay.rates),
+                                 R, rebase(d, lay.tab), codes->n_codes, dtt,
+                                 precision == 32 ? 0 : precision == 48 ? 1 : 2, dst));
   if (n_pat == 0) {
     PGPU_CUDA(ctx, cudaMemsetAsync(lnl_dev, 0, sizeof(double), ctx->stream));
     return PGPU_OK;
   }
   PruneArgs a;
+  a.tiptab = dtt;
   a.tip_codes = tips;
   a.P = dP;
   a.code_tab = rebase(d, lay.tab);
@@ -460,16 +639,11 @@ pgpu_status prune_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *m,
   a.n_ops = (int)sch->ops.size();
   a.n_codes = codes->n_codes;
   a.R = R;
-  a.NT = NT;
-  a.stages = 32;
+  a.NP = 0;
   a.depth = std::max(sch->max_depth, 1);
-  if (precision == 32) {
-    if (R <= 4) PGPU_TRY((launch_prune<float, 4, 4>(ctx, a, n_tiles)));
-    else PGPU_TRY((launch_prune<float, 4, 8>(ctx, a, n_tiles)));
-  } else {
-    if (R <= 4) PGPU_TRY((launch_prune<double, 4, 4>(ctx, a, n_tiles)));
-    else PGPU_TRY((launch_prune<double, 4, 8>(ctx, a, n_tiles)));
-  }
+  if (precision == 32) PGPU_TRY(launch_prune<Fp32>(ctx, a, RT));
+  else if (precision == 48) PGPU_TRY(launch_prune<Ff32>(ctx, a, RT));
+  else PGPU_TRY(launch_prune<Fp64>(ctx, a, RT));
   prune_finalize_kernel<<<1, 32, 0, ctx->stream>>>((const double2 *)dpart, (int)n_tiles, lnl_dev);
   return pgpu_after_launch(ctx, "prune_finalize_kernel");
 }

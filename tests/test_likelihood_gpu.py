@@ -22,6 +22,11 @@ FP64_REL = 1e-9
 FP32_PER_NODE = 1e-7
 
 
+# FP32 pairs (precision 48): about 48 significant bits per value; the tree
+# error must stay within the 1e-3 gate whatever the pattern count.
+FP32X2_ABS = 1e-3
+
+
 def fp32_bound(n_internal, weights, n_pat):
     wsum = float(np.sum(weights)) if weights is not None else float(n_pat)
     return FP32_PER_NODE * n_internal * wsum
@@ -109,6 +114,9 @@ def test_small_config_fp64_and_fp32(ctx, orc):
     exp, exp_site = oracle_lnl(orc, tr, m, pats, w, site=True)
     g64, s64 = Lk.tree_lnl(tr, m, pats, synth.dna_code_table(), w, 64, ctx, site_lnl=True)
     g32, s32 = Lk.tree_lnl(tr, m, pats, synth.dna_code_table(), w, 32, ctx, site_lnl=True)
+    g48, s48 = Lk.tree_lnl(tr, m, pats, synth.dna_code_table(), w, 48, ctx, site_lnl=True)
+    assert abs(g48 - exp) <= FP32X2_ABS
+    assert np.abs(s48 - exp_site).max() <= 1e-9 * np.abs(exp_site).max()
     assert abs(g64 - exp) <= FP64_REL * abs(exp)
     assert np.abs(s64 - exp_site).max() <= 1e-10 * np.abs(exp_site).max()
     assert abs(g32 - exp) <= fp32_bound(tr.n_internal, w, pats.shape[1])
@@ -134,8 +142,10 @@ def test_trees_and_rate_classes(ctx, orc, shape, rates):
     exp = oracle_lnl(orc, tr, m, codes, w)
     g64 = Lk.tree_lnl(tr, m, codes, synth.dna_code_table(), w, 64, ctx)
     g32 = Lk.tree_lnl(tr, m, codes, synth.dna_code_table(), w, 32, ctx)
+    g48 = Lk.tree_lnl(tr, m, codes, synth.dna_code_table(), w, 48, ctx)
     assert abs(g64 - exp) <= FP64_REL * abs(exp)
     assert abs(g32 - exp) <= fp32_bound(tr.n_internal, w, codes.shape[1])
+    assert abs(g48 - exp) <= FP32X2_ABS
     g_unw = Lk.tree_lnl(tr, m, codes, synth.dna_code_table(), None, 64, ctx)
     assert abs(g_unw - oracle_lnl(orc, tr, m, codes, None)) <= FP64_REL * abs(g_unw)
 
@@ -188,13 +198,16 @@ def test_device_api_matches_host_api(ctx):
 def test_full_size_precision_config(ctx, orc):
     """512 taxa, 500,000 GTR+Gamma4 sites (BL ~ Exp(0.05)) compressed to
     patterns: the FP64 form within FP64_REL of the oracle, plain FP32 within
-    its per-node bound."""
+    its per-node bound, the FP32-pair form within the 1e-3 gate."""
     from phylocaml_gb300 import likelihood as Lk
     tr, spec, pats, w = synth.prune_workload(512, 500_000, seed=2, mean_brlen=0.05)
     m = M.create(spec, ctx)
     exp = oracle_lnl(orc, tr, m, pats, w, n_threads=os.cpu_count() or 4)
     g64 = Lk.tree_lnl(tr, m, pats, synth.dna_code_table(), w, 64, ctx)
     g32 = Lk.tree_lnl(tr, m, pats, synth.dna_code_table(), w, 32, ctx)
-    print(f"lnL oracle {exp!r} fp64 {g64!r} (d {g64 - exp:.3e}) fp32 {g32!r} (d {g32 - exp:.3e})")
+    g48 = Lk.tree_lnl(tr, m, pats, synth.dna_code_table(), w, 48, ctx)
+    print(f"lnL oracle {exp!r} fp64 {g64!r} (d {g64 - exp:.3e}) fp32 {g32!r} (d {g32 - exp:.3e}) "
+          f"fp32x2 {g48!r} (d {g48 - exp:.3e})")
     assert abs(g64 - exp) <= FP64_REL * abs(exp)
     assert abs(g32 - exp) <= fp32_bound(tr.n_internal, w, pats.shape[1])
+    assert abs(g48 - exp) <= FP32X2_ABS
