@@ -544,17 +544,170 @@ def bench_prune_reference(args):
     }
 
 
+# ---------------------------------------------------------------------------
+# batched protein / codon scoring, 2,048 variants x 128 taxa
+# ---------------------------------------------------------------------------
+
+BATCH_VARIANTS, BATCH_TAXA = 2048, 128
+BATCH_PAT = (5_000, 200_000)
+BATCH_SAMPLE = 1024
+
+
+def batch_data(rank, device, n_var=BATCH_VARIANTS):
+    """Seeded variants: even ids 20-state (LogNormal(0,1) exchangeabilities,
+    Dirichlet(1 x 20) frequencies, Gamma4 with alpha 0.5), odd ids 61-state
+    codon (kappa ~ U(1,4), omega ~ U(0.1,1)); Yule trees of 128 taxa,
+    branch lengths ~ Exp(0.1); pattern counts ~ U{5,000..200,000}; tip codes
+    drawn uniformly over the states and the missing code on the device."""
+    import torch
+    from phylocaml_gb300 import mlmodel as M, synth, tree as T
+    from phylocaml_gb300.batch import Variant
+    rng = np.random.default_rng(4000 + rank)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(4000 + rank)
+    out = []
+    g4 = M.gamma_rates(0.5, 4)
+    for k in range(n_var):
+        tr = T.yule(BATCH_TAXA, rng, 0.1)
+        if k % 2 == 0:
+            q, pi = synth.protein_model(rng)
+            rates, probs = g4, np.full(4, 0.25)
+        else:
+            q, pi = synth.codon_model(float(rng.uniform(1, 4)), float(rng.uniform(0.1, 1)))
+            rates, probs = np.ones(1), np.ones(1)
+        S = q.shape[0]
+        n_pat = int(rng.integers(BATCH_PAT[0], BATCH_PAT[1] + 1))
+        ld = Variant.ld_for(n_pat)
+        codes = torch.randint(0, S + 1, (BATCH_TAXA, ld), dtype=torch.uint8, device=device,
+                              generator=gen)
+        out.append(Variant(tr, q, pi, rates, probs, synth.state_code_table(S), codes, None, n_pat))
+    return out
+
+
+def bench_batch(args, rank, world, local):
+    import torch
+    from phylocaml_gb300 import _native
+    from phylocaml_gb300.batch import Batch
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    variants = batch_data(rank, dev)
+    ctx = _native.Context(local)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.synchronize(dev)
+    ctx.set_stream(stream.cuda_stream)
+    b = Batch(variants, ctx)
+    n_pat_total = b.patterns
+    units = sum((v.tree.n_internal) * v.n_pat for v in variants)
+    flops = 0.0   # unpadded tensor-core MACs x 2: internal children only
+    for v in variants:
+        S = v.q.shape[0]
+        internal_children = int(np.sum(v.tree.left >= v.tree.n_tips) + np.sum(v.tree.right >= v.tree.n_tips))
+        flops += 2.0 * S * S * internal_children * len(v.rates) * v.n_pat
+    lnl = torch.zeros(len(variants), dtype=torch.float64, device=dev)
+    site = torch.zeros(n_pat_total, dtype=torch.float64, device=dev)
+    for _ in range(args.warmup):
+        b.run_dev(lnl, site)
+    torch.cuda.synchronize(dev)
+    # the whole run (P setup, persistent tensor-core launch, sums) as a graph
+    graph = None
+    try:
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            b.run_dev(lnl, site)
+        graph = g
+    except Exception as e:   # capture unsupported: run the calls directly
+        graph = None
+        capture_error = str(e)[:200]
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    l0 = ctx.launches
+    clocks = ClockSampler(local)
+    clocks.start()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    k = args.steps
+    with torch.cuda.stream(stream):          # replay on the stream the events watch
+        t0.record(stream)
+        for _ in range(k):
+            if graph is not None:
+                graph.replay()
+            else:
+                b.run_dev(lnl, site)
+        t1.record(stream)
+    torch.cuda.synchronize(dev)
+    clk = clocks.stop()
+    # the same steps without the graph, for the launch-overhead comparison
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.run_dev(lnl, site)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ungraphed_ms = e0.elapsed_time(e1)
+    el = t0.elapsed_time(t1)
+    if world > 1:
+        tt = torch.tensor([el], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        el = float(tt.item())
+    launches = ctx.launches - l0 if graph is None else k * 4
+    # FP64 comparison on the first BATCH_SAMPLE patterns of every variant
+    f64 = b.run_fp64(BATCH_SAMPLE)
+    site_h = site.cpu().numpy()
+    tc_sample, off = [], 0
+    for v in variants:
+        tc_sample.append(float(site_h[off: off + min(v.n_pat, BATCH_SAMPLE)].sum()))
+        off += v.n_pat
+    tc_sample = np.array(tc_sample)
+    bad_tc = np.flatnonzero(~np.isfinite(tc_sample))
+    bad_64 = np.flatnonzero(~np.isfinite(f64))
+    ok = np.isfinite(tc_sample) & np.isfinite(f64)
+    err = np.abs(tc_sample - f64)[ok]
+    rel = err / np.abs(f64[ok])
+    n_nonfinite_sites = int(np.sum(~np.isfinite(site_h)))
+    peaks, peak_src = load_peaks()
+    tf32_peak = peaks["bf16_tflops"] / 2.0
+    per_s = el / k * 1e-3
+    rec = {
+        "metric": "node-site-pattern updates/s, 2,048 protein/codon variants in one persistent launch",
+        "value": world * units * k / (el * 1e-3), "unit": "node-site-pattern updates/s",
+        "ms_per_step": el / k, "steps": k, "dtype": "tf32 (fp32 accumulate)",
+        "config": {"workload": "batch: 2,048 variants x 128 taxa, patterns ~ U{5,000..200,000}; "
+                               "even: 20-state LogNormal/Dirichlet Q + Gamma4; odd: 61-state codon "
+                               "Q (kappa ~ U(1,4), omega ~ U(0.1,1))",
+                   "patterns": n_pat_total, "work_items": b.work_items,
+                   "graph_captured": graph is not None, "ungraphed_ms_per_step": ungraphed_ms},
+        "lnl_error_vs_fp64": {"sample_patterns_per_variant": BATCH_SAMPLE,
+                              "max_abs": float(err.max()), "median_abs": float(np.median(err)),
+                              "max_rel": float(rel.max()), "median_rel": float(np.median(rel)),
+                              "per_variant_abs_first8": [float(x) for x in err[:8]],
+                              "nonfinite_variants_tc": bad_tc[:16].tolist(),
+                              "nonfinite_variants_fp64": bad_64[:16].tolist(),
+                              "nonfinite_sites_tc": n_nonfinite_sites},
+        "roofline": {"bound": "tensor", "achieved": flops / per_s / 1e12, "peak": tf32_peak,
+                     "unit": "TFLOP/s", "frac": flops / per_s / 1e12 / tf32_peak,
+                     "peak_source": f"derived: TF32 dense = half the {peak_src} BF16 figure",
+                     "algorithmic_flops_per_step": flops, "kernel": "batch_tc_kernel"},
+        "gpu_launches": int(launches), "clocks": clk,
+    }
+    if graph is None:
+        rec["config"]["graph_capture_error"] = capture_error
+    b.close()
+    ctx.close()
+    return rec
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["prune", "fitch", "all"], default="all")
+    ap.add_argument("--workload", choices=["prune", "fitch", "batch", "all"], default="all")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_info()
-    head = "fitch" if args.workload == "fitch" else "prune"
+    head = args.workload if args.workload in ("fitch", "batch") else "prune"
 
     if args.impl == "reference":
         if rank != 0:
@@ -575,6 +728,11 @@ def main():
         if args.workload == "all":
             args.steps = steps_given if steps_given is not None else 2000
             rec["fitch"] = bench_fitch(args, rank, world, local)
+            args.steps = steps_given if steps_given is not None else 3
+            rec["batch"] = bench_batch(args, rank, world, local)
+    elif head == "batch":
+        args.steps = steps_given if steps_given is not None else 3
+        rec = bench_batch(args, rank, world, local)
     else:
         args.steps = steps_given if steps_given is not None else 2000
         rec = bench_fitch(args, rank, world, local)

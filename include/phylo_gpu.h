@@ -232,6 +232,48 @@ pgpu_status pgpu_prune_lnl_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_
                                size_t ld_pat, const double *weights_dev, size_t n_pat,
                                int precision, double *lnl_dev, double *site_lnl_dev);
 
+/* ---- batched scoring of many trees and models --------------------------
+ * One variant = one tree, one model and its own site patterns; the batch
+ * holds any mix, e.g. 20-state protein models with 4 rate classes and
+ * 61-state codon models, with uneven pattern counts.  No reference
+ * counterpart beyond Likelihood_c's slot (lib/likelihood_c.ml:1-33): the
+ * reference scores one tree at a time. */
+typedef struct {
+  pgpu_tree tree;            /* brlen required; 2..255 tips */
+  pgpu_model model;          /* 2..64 states, 1..4 rate classes */
+  pgpu_tip_codes codes;      /* 1..255 codes */
+  const uint8_t *tip_codes;  /* DEVICE [n_tips][ld_pat] codes (pad with any valid code) */
+  const double *weights;     /* DEVICE [n_pat] or NULL */
+  size_t n_pat;
+  size_t ld_pat;             /* row stride in bytes: multiple of 128, >= n_pat rounded up to 128 */
+} pgpu_variant;
+
+typedef struct pgpu_batch pgpu_batch;
+
+/* Validates the variants, builds their schedules, and solves the models'
+ * eigen systems (FP64, on the GPU).  The device buffers the variants point
+ * to must outlive the batch. */
+pgpu_status pgpu_batch_create(pgpu_ctx *ctx, const pgpu_variant *variants, int n_variants,
+                              pgpu_batch **out);
+void pgpu_batch_destroy(pgpu_batch *batch);
+
+/* Scores every variant, asynchronously on the context's stream and without
+ * host synchronisation or allocation, so the call can be captured in a CUDA
+ * graph: FP64 P matrices, then one persistent tensor-core launch
+ * (tcgen05.mma kind::tf32, FP32 accumulate, FP32 vectors, per-pattern power-
+ * of-two scalers), then the per-variant compensated sums into
+ * lnl_dev[n_variants]; site_lnl_dev (or NULL) receives every pattern's lnL,
+ * variants one after another. */
+pgpu_status pgpu_batch_run(pgpu_ctx *ctx, pgpu_batch *batch, double *lnl_dev,
+                           double *site_lnl_dev);
+
+/* The FP64 comparison form over the first `sample` patterns of every variant
+ * (lnl_dev[v] = weighted FP64 lnL of those patterns). */
+pgpu_status pgpu_batch_run_fp64(pgpu_ctx *ctx, pgpu_batch *batch, size_t sample, double *lnl_dev);
+
+long long pgpu_batch_work_items(const pgpu_batch *batch);
+long long pgpu_batch_patterns(const pgpu_batch *batch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -62,6 +62,18 @@ class PgpuTipCodes(C.Structure):
     ]
 
 
+class PgpuVariant(C.Structure):
+    _fields_ = [
+        ("tree", PgpuTree),
+        ("model", PgpuModel),
+        ("codes", PgpuTipCodes),
+        ("tip_codes", C.c_void_p),
+        ("weights", C.c_void_p),
+        ("n_pat", C.c_size_t),
+        ("ld_pat", C.c_size_t),
+    ]
+
+
 _P = C.c_void_p
 _SZ = C.c_size_t
 _I = C.c_int
@@ -90,6 +102,12 @@ SIGNATURES: dict[str, tuple] = {
                             C.POINTER(PgpuTipCodes), _P, _P, _SZ, _I, _DP, _P]),
     "pgpu_prune_lnl_dev": (_I, [_P, C.POINTER(PgpuTree), C.POINTER(PgpuModel),
                                 C.POINTER(PgpuTipCodes), _P, _SZ, _P, _SZ, _I, _P, _P]),
+    "pgpu_batch_create": (_I, [_P, C.POINTER(PgpuVariant), _I, C.POINTER(_P)]),
+    "pgpu_batch_destroy": (None, [_P]),
+    "pgpu_batch_run": (_I, [_P, _P, _P, _P]),
+    "pgpu_batch_run_fp64": (_I, [_P, _P, _SZ, _P]),
+    "pgpu_batch_work_items": (C.c_longlong, [_P]),
+    "pgpu_batch_patterns": (C.c_longlong, [_P]),
 }
 
 _lib = None

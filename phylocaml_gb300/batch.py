@@ -1,0 +1,118 @@
+"""Batched likelihood of many variants (tree, model, patterns) on the GPU
+tensor cores: the pgpu_batch_* entry points of the C ABI.
+
+Each variant is independent -- a 20-state protein model with four Gamma rate
+classes, a 61-state codon model, or anything up to 64 states and four
+classes -- and the whole batch runs as FP64 P-matrix setup plus one
+persistent tcgen05 kernel (csrc/batch.cu).  Tip codes and weights stay on
+the device; the batch handle keeps everything else.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native
+from .tree import RootedTree
+
+
+@dataclass
+class Variant:
+    tree: RootedTree
+    q: np.ndarray
+    pi: np.ndarray
+    rates: np.ndarray
+    probs: np.ndarray
+    code_table: np.ndarray      # [n_codes, S]
+    tip_codes: object           # device uint8 tensor [n_tips, ld_pat], ld_pat % 128 == 0
+    weights: object | None      # device float64 tensor [n_pat] or None
+    n_pat: int
+
+    @staticmethod
+    def ld_for(n_pat: int) -> int:
+        return max(128, (n_pat + 127) // 128 * 128)
+
+
+class Batch:
+    def __init__(self, variants: list[Variant], ctx: _native.Context | None = None):
+        self.ctx = ctx or _native.default_context()
+        self.variants = variants
+        self._keep = []
+        arr = (_native.PgpuVariant * len(variants))()
+        dp = C.POINTER(C.c_double)
+        for k, v in enumerate(variants):
+            t, keep = _native.make_tree(v.tree.left, v.tree.right, v.tree.brlen)
+            self._keep.append(keep)
+            mats = [np.ascontiguousarray(a, np.float64) for a in (v.q, v.pi, v.rates, v.probs,
+                                                                   v.code_table)]
+            self._keep.append(mats)
+            x = arr[k]
+            x.tree = t
+            x.model.n_states = mats[0].shape[0]
+            x.model.n_rates = len(mats[2])
+            x.model.Q, x.model.pi, x.model.rates, x.model.probs = (m.ctypes.data_as(dp) for m in mats[:4])
+            x.codes.n_codes = mats[4].shape[0]
+            x.codes.table = mats[4].ctypes.data_as(dp)
+            x.tip_codes = _native.ptr(v.tip_codes)
+            x.weights = _native.ptr(v.weights)
+            x.n_pat = v.n_pat
+            x.ld_pat = v.tip_codes.shape[1]
+        h = C.c_void_p()
+        self.ctx.call("pgpu_batch_create", arr, len(variants), C.byref(h))
+        self.h = h
+        self.n_var = len(variants)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.pgpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def work_items(self) -> int:
+        return int(self.ctx.lib.pgpu_batch_work_items(self.h))
+
+    @property
+    def patterns(self) -> int:
+        return int(self.ctx.lib.pgpu_batch_patterns(self.h))
+
+    def run_dev(self, lnl_dev, site_lnl_dev=None) -> None:
+        """Asynchronous on the context's stream (graph-capturable)."""
+        self.ctx.call("pgpu_batch_run", self.h, _native.ptr(lnl_dev), _native.ptr(site_lnl_dev))
+
+    def run(self, site_lnl: bool = False):
+        import torch
+        dev = torch.device(f"cuda:{self.ctx.device}")
+        out = torch.zeros(self.n_var, dtype=torch.float64, device=dev)
+        site = torch.zeros(self.patterns, dtype=torch.float64, device=dev) if site_lnl else None
+        torch.cuda.synchronize(dev)
+        self.run_dev(out, site)
+        self.ctx.synchronize()
+        res = out.cpu().numpy()
+        return (res, site.cpu().numpy()) if site_lnl else res
+
+    def run_fp64(self, sample: int) -> np.ndarray:
+        import torch
+        dev = torch.device(f"cuda:{self.ctx.device}")
+        out = torch.zeros(self.n_var, dtype=torch.float64, device=dev)
+        torch.cuda.synchronize(dev)
+        self.ctx.call("pgpu_batch_run_fp64", self.h, int(sample), _native.ptr(out))
+        self.ctx.synchronize()
+        return out.cpu().numpy()
+
+
+def device_codes(codes: np.ndarray, device) -> object:
+    """Copies [n_tips, n_pat] uint8 codes to a device tensor padded to the
+    batch row stride (padding code 0)."""
+    import torch
+    n_tips, n_pat = codes.shape
+    t = torch.zeros((n_tips, Variant.ld_for(n_pat)), dtype=torch.uint8, device=device)
+    t[:, :n_pat] = torch.from_numpy(np.ascontiguousarray(codes)).to(device)
+    return t

@@ -1,0 +1,975 @@
+// Batched likelihood of many trees, models and pattern sets of uneven size,
+// for 20-state (protein) and 61-state (codon) models, on the tensor cores.
+//
+// Reference: the likelihood character is a stub in phylocaml
+// (Likelihood_c.median_2, lib/likelihood_c.ml:15); P matrices follow
+// MlModel.compose (lib/mlModel.ml:585-587, P[i][j] = Pr(j | i, t)).  Every
+// variant is an independent (tree, model, patterns) problem.
+//
+// Design (one GB300, one launch for all variants):
+//   setup kernels  the FP64 Jacobi eigen systems (pmatrix.cu), then per
+//                  variant, internal branch and rate class the FP32 B operand
+//                  B[n=i][k=j] = P(t r)[i][j] in the tcgen05 K-major
+//                  core-matrix layout, and per tip branch the FP64-formed tip
+//                  rows tab[c][i] = sum_j P[i][j] code_tab[c][j];
+//   batch_tc_kernel  persistent, one CTA per SM, over work items
+//                  (variant, tile of 128 patterns).  A tile's conditional
+//                  likelihood vectors live in tensor memory (TMEM lane =
+//                  pattern, columns = states) and are the A operand of
+//                  tcgen05.mma.kind::tf32 for internal children; D (FP32) is
+//                  accumulated in TMEM.  Tip children need no MMA: their rows
+//                  come from the staged tip table.  Rate classes are separate
+//                  passes with their own power-of-two scalers, joined at the
+//                  root with a log-sum-exp in FP64.
+//     warp 4       producer: per postorder step, bulk-copies the B blocks of
+//                  internal children, the tip-table blocks and tip-code rows
+//                  of tip children into a shared ring slot;
+//     warp 5       MMA issuer (lane 0) and TMEM allocator;
+//     warps 0-3    epilogue: thread = pattern; reads D rows (tcgen05.ld) or
+//                  tip rows, forms the product, rescales, writes the parent's
+//                  vector back into TMEM (tcgen05.st).
+//   Producer, MMA and epilogue move in lockstep per step through mbarriers
+//   (mma_bar: MMA -> epilogue, epi_bar: epilogue -> MMA), so a step's MMA
+//   never reads a vector before it is written and no mbarrier phase can be
+//   skipped.  Every wait is bounded.
+//   batch_fp64_kernel  the FP64 comparison form on a sample of patterns.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "pgpu_internal.cuh"
+#include "pmatrix.cuh"
+
+namespace {
+
+constexpr int BT_M = 128;          // patterns per tile (TMEM lanes)
+constexpr int BT_SP = 64;          // register bound on padded states
+constexpr int BT_ST = 4;           // ring slots (power of two)
+constexpr int BT_THREADS = 288;    // 8 epilogue warps (thread 0 issues MMAs), producer
+constexpr int BT_TMEM_COLS = 512;
+
+struct BVar {
+  int n_tips, n_ops, S, R, n_codes;
+  int Kp, Np, SpT, NCp;            // padded K (A columns), N (D columns), odd tip-row stride, padded code rows
+  int n_slots;                     // TMEM stack slots available
+  int n_tiles;
+  long long n_pat;
+  long long ld;                    // tip-code row stride in bytes (n_tiles * 128)
+  const uint8_t *codes;            // [n_tips][ld] device tip codes of this variant
+  const double *weights;           // [n_pat] device weights or null
+  long long pat_off;               // first pattern of the variant in the site outputs
+  long long ops_off;               // int4 entries into the ops array
+  long long bmat_off;              // floats into the B array
+  long long tip_off;               // floats into the tip-row array
+  long long pi_off;                // doubles into the pi array
+  long long brlen_off;             // doubles into the branch-length array ([2n-2])
+  long long rates_off;             // doubles into the rates array ([R])
+  long long ctab_off;              // doubles into the code-table array ([n_codes][S])
+  int group, group_idx;            // eigen system: model group_idx of the group of this S
+  double probs[4];
+};
+
+// op.x = internal index k, op.y = first child, op.z = second child,
+// op.w = slot_a | slot_b << 8 | slot_out << 16 (TMEM stack positions)
+
+__device__ __forceinline__ uint32_t su32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// K-major, no-swizzle shared-memory descriptor: 8-row x 16-byte core
+// matrices, K-adjacent ones LBO apart, 8-row groups SBO apart.
+__device__ __forceinline__ uint64_t smem_desc(const void *base, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((su32(base) >> 4) & 0x3FFF);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// byte offset of element (row n, col k) of a K-major core-matrix tile of
+// 32-bit values with Kp columns
+__host__ __device__ inline size_t cm_off(int n, int k, int Kp) {
+  return (size_t)(n / 8) * (size_t)(Kp / 4) * 128 + (size_t)(k / 4) * 128 + (n % 8) * 16 + (k % 4) * 4;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t ta, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+      "[%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(ta));
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ void two_sum_d(double a, double b, double &s, double &e) {
+  s = a + b;
+  const double bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ void warp_csum_d(double &s, double &c) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double s2 = __shfl_xor_sync(0xffffffffu, s, o);
+    const double c2 = __shfl_xor_sync(0xffffffffu, c, o);
+    double t, e;
+    two_sum_d(s, s2, t, e);
+    s = t;
+    c = c + c2 + e;
+  }
+}
+
+struct BatchArgs {
+  const BVar *vars;
+  const int2 *work;               // [n_work] (variant, tile)
+  long long n_work;
+  const int4 *ops;
+  const float *bmat;
+  const float *tiptab;
+  const double *pis;
+  double *site_lnl;               // [total patterns] or null
+  double2 *partials;              // [n_work]
+  int *flag;
+  int slot_bytes;                 // ring slot size
+};
+
+// ring slot layout: [0,128) codes of child a, [128,256) codes of child b,
+// then block a and block b (each the larger of a B block and a tip block)
+__device__ __forceinline__ int blk_bytes(const BVar &v) {
+  const int b = v.Np * v.Kp * 4, t = v.NCp * v.SpT * 4;
+  return ((b > t ? b : t) + 127) & ~127;
+}
+
+__global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs p) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ uint64_t full[BT_ST], empty[BT_ST], mma_bar;
+  __shared__ uint32_t tmem_base;
+  __shared__ float xch[2][BT_M];
+  __shared__ double xchd[2][BT_M];
+  __shared__ double2 red[4];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (warp == 8) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     su32(&tmem_base)),
+                 "r"(BT_TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < BT_ST; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1 + 8);   // the MMA commit + 8 epilogue warps
+    }
+    mbar_init(&mma_bar, 1);
+    fence_mbarrier_init();
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+
+  if (warp == 8) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      long long seq = 0;
+      bool ok = true;
+      for (long long w = blockIdx.x; w < p.n_work && ok; w += gridDim.x) {
+        const int2 wk = __ldg(p.work + w);
+        const BVar &v = p.vars[wk.x];
+        const int BB = blk_bytes(v);
+        const uint32_t bmat_bytes = (uint32_t)(v.Np * v.Kp * 4);
+        const uint32_t tip_bytes = (uint32_t)(v.NCp * v.SpT * 4);
+        for (int r = 0; r < v.R && ok; ++r) {
+          for (int i = 0; i < v.n_ops; ++i, ++seq) {
+            const int slot = (int)(seq & (BT_ST - 1));
+            const long long round = seq / BT_ST;
+            if (round > 0 && !mbar_wait_bounded(&empty[slot], (uint32_t)((round - 1) & 1), p.flag)) {
+              ok = false;
+              break;
+            }
+            const int4 op = __ldg(p.ops + v.ops_off + i);
+            unsigned char *sl = smem + (size_t)slot * p.slot_bytes;
+            uint32_t tx = 0;
+            for (int h = 0; h < 2; ++h) {
+              const int ch = h == 0 ? op.y : op.z;
+              tx += ch < v.n_tips ? 128u + tip_bytes : bmat_bytes;
+            }
+            mbar_arrive_expect_tx(&full[slot], tx);
+            for (int h = 0; h < 2; ++h) {
+              const int ch = h == 0 ? op.y : op.z;
+              unsigned char *blk = sl + 256 + (size_t)h * BB;
+              if (ch < v.n_tips) {
+                bulk_g2s(sl + h * 128, v.codes + (long long)ch * v.ld + (long long)wk.y * 128, 128u,
+                         &full[slot]);
+                bulk_g2s(blk, p.tiptab + v.tip_off + ((long long)ch * v.R + r) * v.NCp * v.SpT,
+                         tip_bytes, &full[slot]);
+              } else {
+                bulk_g2s(blk,
+                         p.bmat + v.bmat_off +
+                             ((long long)(ch - v.n_tips) * v.R + r) * (long long)v.Np * v.Kp,
+                         bmat_bytes, &full[slot]);
+              }
+            }
+          }
+        }
+      }
+      for (long long s = seq - BT_ST; s < seq; ++s)
+        if (s >= 0) (void)mbar_wait_bounded(&full[s & (BT_ST - 1)], (uint32_t)((s / BT_ST) & 1), p.flag);
+    }
+  } else {
+    // ------------------------------------------------------------ epilogue
+    // warp w: TMEM lanes 32 (w % 4) ..; states [hf B, hf B + B) of the row,
+    // B = Kp / 2.  Thread 0 also issues every step's MMAs, right after the
+    // previous step's vectors are in TMEM.
+    const int q = warp & 3, hf = warp >> 2;
+    const int m = 32 * q + lane;                          // pattern within the tile
+    const uint32_t lane_base = (uint32_t)(32 * q) << 16;
+    long long seq = 0;
+    bool ok = true;
+    for (long long w = blockIdx.x; w < p.n_work && ok; w += gridDim.x) {
+      const int2 wk = __ldg(p.work + w);
+      const BVar &v = p.vars[wk.x];
+      const int BB = blk_bytes(v);
+      const long long pat = (long long)wk.y * BT_M + m;
+      const bool active = pat < v.n_pat;
+      const int S = v.S, B = v.Kp / 2, e0 = hf * B;       // my states: e0 .. e0 + B - 1
+      const uint32_t LBO = 128, SBO = (uint32_t)(v.Kp / 4) * 128;
+      uint32_t idesc = 0;
+      idesc |= 1u << 4;
+      idesc |= 2u << 7;
+      idesc |= 2u << 10;
+      idesc |= (uint32_t)(v.Np >> 3) << 17;
+      idesc |= (uint32_t)(BT_M >> 4) << 24;
+      double lnr[4];
+      float acc[BT_SP / 2];
+      for (int r = 0; r < v.R && ok; ++r) {
+        int escale = 0;
+        for (int i = 0; i < v.n_ops; ++i, ++seq) {
+          const int slot = (int)(seq & (BT_ST - 1));
+          const int4 op = __ldg(p.ops + v.ops_off + i);
+          const unsigned char *sl = smem + (size_t)slot * p.slot_bytes;
+          // ---- issue this step's MMAs (internal children) ----
+          if (tid == 0) {
+            bool got = mbar_wait_bounded(&full[slot], (uint32_t)((seq / BT_ST) & 1), p.flag);
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            bool any = false;
+            for (int h = 0; h < 2 && got; ++h) {
+              const int ch = h == 0 ? op.y : op.z;
+              if (ch < v.n_tips) continue;
+              any = true;
+              const int sa = (op.w >> (8 * h)) & 0xff;
+              const uint32_t d_col = (uint32_t)(h * v.Np);
+              const uint32_t a_col = (uint32_t)(2 * v.Np + sa * v.Kp);
+              const unsigned char *blk = sl + 256 + (size_t)h * BB;
+              for (int ks = 0; ks < v.Kp / 8; ++ks) {
+                const uint64_t bd = smem_desc(blk + (size_t)ks * 2 * LBO, LBO, SBO);
+                const uint32_t accf = ks > 0 ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, q;\n\t}" ::"r"(tmem + d_col),
+                    "r"(tmem + a_col + (uint32_t)(ks * 8)), "l"(bd), "r"(idesc), "r"(accf)
+                    : "memory");
+              }
+            }
+            if (any) {
+              asm volatile(
+                  "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                      su32(&mma_bar))
+                  : "memory");
+              asm volatile(
+                  "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                      su32(&empty[slot]))
+                  : "memory");
+            } else {
+              mbar_arrive(&mma_bar);
+              mbar_arrive(&empty[slot]);
+            }
+          }
+          // ---- epilogue of this step ----
+          bool got = mbar_wait_bounded(&full[slot], (uint32_t)((seq / BT_ST) & 1), p.flag);
+          got = got && mbar_wait_bounded(&mma_bar, (uint32_t)(seq & 1), p.flag);
+          got = __all_sync(0xffffffffu, got);
+          if (!got) {
+            ok = false;
+            atomicOr(p.flag, PGPU_FLAG_TIMEOUT);
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+          for (int e = 0; e < BT_SP / 2; ++e) acc[e] = 1.0f;
+          for (int h = 0; h < 2 && ok; ++h) {
+            const int ch = h == 0 ? op.y : op.z;
+            if (ch < v.n_tips) {
+              int code = sl[h * 128 + m];
+              if (code >= v.n_codes) {
+                if (active && hf == 0) atomicOr(p.flag, PGPU_FLAG_BADCODE);
+                code = 0;
+              }
+              const float *row = reinterpret_cast<const float *>(sl + 256 + (size_t)h * BB) +
+                                 (size_t)code * v.SpT + e0;
+#pragma unroll
+              for (int e = 0; e < BT_SP / 2; ++e)
+                if (e < B && e0 + e < S) acc[e] *= row[e];
+            } else {
+              // the (at most three) 16-column chunks that cover my states, all
+              // loads in flight before one wait
+              const int c_first = (e0 / 16) * 16;
+              float d[3][16];
+#pragma unroll
+              for (int u = 0; u < 3; ++u) {
+                const int c0 = c_first + 16 * u;
+                if (c0 < v.Np && c0 < e0 + B)
+                  tmem_ld16(tmem + lane_base + (uint32_t)(h * v.Np + c0), d[u]);
+              }
+              asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+              for (int u = 0; u < 3; ++u) {
+                const int c0 = c_first + 16 * u;
+                if (c0 < v.Np && c0 < e0 + B) {
+#pragma unroll
+                  for (int j = 0; j < 16; ++j) {
+                    const int e = c0 + j - e0;
+                    if (e >= 0 && e < B && c0 + j < S) acc[e < BT_SP / 2 ? e : 0] *= d[u][j];
+                  }
+                }
+              }
+            }
+          }
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&empty[slot]);
+          // rescale by an exact power of two; the two halves of a row agree
+          float mx = 0.0f;
+#pragma unroll
+          for (int e = 0; e < BT_SP / 2; ++e)
+            if (e < B && e0 + e < S) mx = fmaxf(mx, acc[e]);
+          xch[hf][m] = mx;
+          // the exchange barrier also makes the timeout verdict uniform over
+          // the epilogue warps, so none can leave the loop alone
+          {
+            uint32_t all_ok;
+            asm volatile(
+                "{\n\t.reg .pred a, b;\n\tsetp.ne.u32 a, %1, 0;\n\t"
+                "bar.red.and.pred b, 1, 256, a;\n\tselp.u32 %0, 1, 0, b;\n\t}"
+                : "=r"(all_ok)
+                : "r"((uint32_t)ok)
+                : "memory");
+            ok = all_ok != 0;
+          }
+          mx = fmaxf(mx, xch[hf ^ 1][m]);
+          if (mx < 0x1p-32f && mx > 0.0f) {
+            int ex;
+            (void)frexpf(mx, &ex);
+            escale += ex;
+            const int k1 = min(-ex, 120), k2 = -ex - k1;
+            const float f1 = __int_as_float((127 + k1) << 23), f2 = __int_as_float((127 + k2) << 23);
+#pragma unroll
+            for (int e = 0; e < BT_SP / 2; ++e) acc[e] = acc[e] * f1 * f2;
+          }
+#pragma unroll
+          for (int e = 0; e < BT_SP / 2; ++e)
+            if (e >= B || e0 + e >= S) acc[e] = 0.0f;
+          // into the TMEM stack slot: my K columns e0 .. e0 + B - 1
+          const int so = (op.w >> 16) & 0xff;
+          const uint32_t col = (uint32_t)(2 * v.Np + so * v.Kp + e0);
+#pragma unroll
+          for (int c0 = 0; c0 < BT_SP / 2; c0 += 4)
+            if (c0 < B) {
+              asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(
+                               tmem + lane_base + col + (uint32_t)c0),
+                           "r"(__float_as_uint(acc[c0])), "r"(__float_as_uint(acc[c0 + 1])),
+                           "r"(__float_as_uint(acc[c0 + 2])), "r"(__float_as_uint(acc[c0 + 3]))
+                           : "memory");
+            }
+          asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          // every vector of this step is in TMEM before the next MMA issues
+          asm volatile("bar.sync 1, 256;" ::: "memory");
+          if (!ok) break;
+        }
+        if (!ok) break;
+        // root of this rate pass (both halves of the row)
+        double Lp = 0.0;
+        const double *pi = p.pis + v.pi_off;
+        for (int e = 0; e < B; ++e)
+          if (e0 + e < S) Lp += pi[e0 + e] * (double)acc[e];
+        xchd[hf][m] = Lp;
+        asm volatile("bar.sync 1, 256;" ::: "memory");
+        const double L = Lp + xchd[hf ^ 1][m];
+        lnr[r] = log(L) + (double)escale * 0.69314718055994530942;
+        asm volatile("bar.sync 1, 256;" ::: "memory");
+      }
+      // join the rate classes: log sum_r probs[r] exp(lnr[r])
+      double s = 0.0, comp = 0.0;
+      if (ok && active && hf == 0) {
+        double mxl = -INFINITY;
+        for (int r = 0; r < v.R; ++r) mxl = fmax(mxl, lnr[r]);
+        double sum = 0.0;
+        for (int r = 0; r < v.R; ++r) sum += v.probs[r] * exp(lnr[r] - mxl);
+        const double lnl = mxl + log(sum);
+        if (p.site_lnl) p.site_lnl[v.pat_off + pat] = lnl;
+        s = v.weights ? v.weights[pat] * lnl : lnl;
+      }
+      if (hf == 0) {
+        warp_csum_d(s, comp);
+        if (lane == 0) red[q] = make_double2(s, comp);
+      }
+      asm volatile("bar.sync 1, 256;" ::: "memory");
+      if (tid == 0) {
+        double ss = 0.0, cc = 0.0;
+        for (int k = 0; k < 4; ++k) {
+          double t, e;
+          two_sum_d(ss, red[k].x, t, e);
+          ss = t;
+          cc += e + red[k].y;
+        }
+        p.partials[w] = make_double2(ss, cc);
+      }
+      asm volatile("bar.sync 1, 256;" ::: "memory");
+    }
+    // the last MMAs finish before TMEM is released
+    if (tid == 0 && seq > 0) (void)mbar_wait_bounded(&mma_bar, (uint32_t)((seq - 1) & 1), p.flag);
+  }
+
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 8)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BT_TMEM_COLS));
+}
+
+// Per variant: sum its tiles' (sum, compensation) pairs in tile order.
+__global__ void batch_finalize_kernel(const double2 *partials, const long long *tile_base,
+                                      const int *n_tiles, int n_var, double *out) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n_var) return;
+  double s = 0.0, c = 0.0;
+  for (int t = 0; t < n_tiles[v]; ++t) {
+    const double2 x = partials[tile_base[v] + t];
+    double u, e;
+    two_sum_d(s, x.x, u, e);
+    s = u;
+    c += e + x.y;
+  }
+  out[v] = s + c;
+}
+
+// Setup: for every branch of every variant of one state count S and every
+// rate class, P = U diag(exp(lambda r t)) Ui in FP64 (shared memory), then
+//   tip branch      tip rows tab[c][i] = sum_j P[i][j] code_tab[c][j]  (float)
+//   internal branch B block B[n=i][k=j] = P[i][j] in the core-matrix layout
+struct SetupArgs {
+  const BVar *vars;
+  const int *members;             // variants of this group
+  const double *U, *lam, *Ui;     // group eigen systems [g][S][S], [g][S], [g][S][S]
+  const int *status;              // [g]
+  const double *brlen, *rates, *ctab;
+  float *bmat, *tiptab;
+  int *flag;
+  int S;
+};
+
+__global__ void __launch_bounds__(256) batch_setup_kernel(const SetupArgs a) {
+  extern __shared__ __align__(16) double P[];   // [S][S] then e[S]
+  const int S = a.S, SS = S * S;
+  const int vi = a.members[blockIdx.z];
+  const BVar &v = a.vars[vi];
+  const int c = blockIdx.x, r = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
+  const int n_br = 2 * v.n_tips - 2;
+  if (c >= n_br || r >= v.R) return;
+  const int g = v.group_idx;
+  if (a.status[g]) {
+    if (c == 0 && r == 0 && tid == 0) atomicOr(a.flag, pgpu_model_flag(a.status[g]));
+    return;
+  }
+  const double *U = a.U + (size_t)g * SS, *Ui = a.Ui + (size_t)g * SS, *lam = a.lam + (size_t)g * S;
+  double *e = P + SS;
+  const double t = a.brlen[v.brlen_off + c], rate = a.rates[v.rates_off + r];
+  const bool ident = !(t >= 1e-10);
+  for (int k = tid; k < S; k += nt) e[k] = exp(lam[k] * rate * t);
+  __syncthreads();
+  for (int o = tid; o < SS; o += nt) {
+    const int i = o / S, j = o % S;
+    double x = 0.0;
+    if (ident) {
+      x = i == j ? 1.0 : 0.0;
+    } else {
+      for (int k = 0; k < S; ++k) x = fma(U[i * S + k] * e[k], Ui[k * S + j], x);
+    }
+    P[o] = fmax(x, 0.0);   // transition probabilities: clamp eigen-product noise below 0
+  }
+  __syncthreads();
+  if (c < v.n_tips) {
+    float *out = a.tiptab + v.tip_off + ((size_t)c * v.R + r) * v.NCp * v.SpT;
+    const double *ct = a.ctab + v.ctab_off;
+    for (int o = tid; o < v.NCp * v.SpT; o += nt) {
+      const int code = o / v.SpT, i = o % v.SpT;
+      double y = 0.0;
+      if (i < S && code < v.n_codes)
+        for (int j = 0; j < S; ++j) y = fma(P[i * S + j], ct[code * S + j], y);
+      out[o] = (float)y;
+    }
+  } else {
+    unsigned char *out = reinterpret_cast<unsigned char *>(
+        a.bmat + v.bmat_off + ((size_t)(c - v.n_tips) * v.R + r) * (size_t)v.Np * v.Kp);
+    for (int o = tid; o < v.Np * v.Kp; o += nt) {
+      const int n = o / v.Kp, k = o % v.Kp;
+      const float x = (n < S && k < S) ? (float)P[n * S + k] : 0.0f;   // P >= 0 after clamping
+      *reinterpret_cast<float *>(out + cm_off(n, k, v.Kp)) = x;
+    }
+  }
+}
+
+// The FP64 comparison form over the first `sample` patterns of every
+// variant: one CTA per (variant, block of 32 patterns), thread = pattern,
+// all rate classes and states in FP64; the stack of vectors in shared
+// memory, each branch's P rebuilt in shared memory from the eigen system.
+struct F64Args {
+  const BVar *vars;
+  const int4 *ops;
+  const double *U, *lam, *Ui;     // per group, indexed through vars[].group / group_idx
+  long long gU[8], gL[8];         // group bases (doubles) into U/Ui and lam
+  const double *brlen, *rates, *ctab, *pis;
+  double2 *partials;              // [n_var][blocks]
+  int blocks;                     // blocks per variant
+  long long sample;
+  int max_depth;
+};
+
+constexpr int F64_NP = 32;
+
+__global__ void __launch_bounds__(F64_NP) batch_fp64_kernel(const F64Args a) {
+  extern __shared__ __align__(16) double sm[];
+  const int vi = blockIdx.y, blk = blockIdx.x, tid = threadIdx.x;
+  const BVar &v = a.vars[vi];
+  const int S = v.S, SS = S * S, R = v.R;
+  double *P = sm;                                   // [S][S]
+  double *e = P + SS;                               // [S]
+  double *stk = e + 64;                             // [depth][S][32]
+  const long long n_use = min(a.sample, v.n_pat);
+  const long long pat = (long long)blk * F64_NP + tid;
+  const bool active = pat < n_use;
+  const double *U = a.U + a.gU[v.group] + (size_t)v.group_idx * SS;
+  const double *Ui = a.Ui + a.gU[v.group] + (size_t)v.group_idx * SS;
+  const double *lam = a.lam + a.gL[v.group] + (size_t)v.group_idx * S;
+  const double *ct = a.ctab + v.ctab_off;
+  double lnr[4];
+  double x[2][64];
+  for (int r = 0; r < R; ++r) {
+    int sp = 0;
+    long long esc = 0;
+    for (int i = 0; i < v.n_ops; ++i) {
+      const int4 op = a.ops[v.ops_off + i];
+      // pop the internal children (b above a)
+      for (int h = 1; h >= 0; --h) {
+        const int ch = h == 0 ? op.y : op.z;
+        if (ch >= v.n_tips) {
+          --sp;
+          for (int j = 0; j < S; ++j) x[h][j] = stk[((size_t)sp * S + j) * F64_NP + tid];
+        }
+      }
+      double out[64];
+      for (int j = 0; j < S; ++j) out[j] = 1.0;
+      for (int h = 0; h < 2; ++h) {
+        const int ch = h == 0 ? op.y : op.z;
+        __syncthreads();
+        const double t = a.brlen[v.brlen_off + ch], rate = a.rates[v.rates_off + r];
+        const bool ident = !(t >= 1e-10);
+        for (int k = tid; k < S; k += F64_NP) e[k] = exp(lam[k] * rate * t);
+        __syncthreads();
+        for (int o = tid; o < SS; o += F64_NP) {
+          const int ii = o / S, jj = o % S;
+          double y = 0.0;
+          if (ident) y = ii == jj ? 1.0 : 0.0;
+          else
+            for (int k = 0; k < S; ++k) y = fma(U[ii * S + k] * e[k], Ui[k * S + jj], y);
+          P[o] = fmax(y, 0.0);
+        }
+        __syncthreads();
+        if (ch < v.n_tips) {
+          int code = active ? v.codes[(long long)ch * v.ld + pat] : 0;
+          if (code >= v.n_codes) code = 0;
+          for (int j = 0; j < S; ++j) x[h][j] = ct[code * S + j];
+        }
+        for (int ii = 0; ii < S; ++ii) {
+          double y = 0.0;
+          for (int jj = 0; jj < S; ++jj) y = fma(P[ii * S + jj], x[h][jj], y);
+          out[ii] *= y;
+        }
+      }
+      double mx = 0.0;
+      for (int j = 0; j < S; ++j) mx = fmax(mx, out[j]);
+      if (mx > 0.0 && mx < 0x1p-256) {
+        int ex;
+        (void)frexp(mx, &ex);
+        esc += ex;
+        for (int j = 0; j < S; ++j) out[j] = ldexp(out[j], -ex);
+      }
+      if (i + 1 < v.n_ops) {
+        for (int j = 0; j < S; ++j) stk[((size_t)sp * S + j) * F64_NP + tid] = out[j];
+        ++sp;
+      } else {
+        double L = 0.0;
+        for (int j = 0; j < S; ++j) L += a.pis[v.pi_off + j] * out[j];
+        lnr[r] = log(L) + (double)esc * 0.69314718055994530942;
+      }
+    }
+  }
+  double s = 0.0, c = 0.0;
+  if (active) {
+    double mxl = -INFINITY;
+    for (int r = 0; r < R; ++r) mxl = fmax(mxl, lnr[r]);
+    double sum = 0.0;
+    for (int r = 0; r < R; ++r) sum += v.probs[r] * exp(lnr[r] - mxl);
+    const double lnl = mxl + log(sum);
+    s = v.weights ? v.weights[pat] * lnl : lnl;
+  }
+  warp_csum_d(s, c);
+  if (tid == 0) a.partials[(size_t)vi * a.blocks + blk] = make_double2(s, c);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+struct pgpu_batch {
+  int n_var = 0;
+  int max_depth = 0;
+  long long n_work = 0, total_pat = 0;
+  std::vector<BVar> hvars;
+  std::vector<int> group_S;                     // state count of each group
+  std::vector<std::vector<int>> group_members;  // variant ids per group
+  // device
+  BVar *vars = nullptr;
+  int2 *work = nullptr;
+  int4 *ops = nullptr;
+  float *bmat = nullptr, *tiptab = nullptr;
+  double *pis = nullptr, *brlen = nullptr, *rates = nullptr, *ctab = nullptr;
+  double *Q = nullptr, *U = nullptr, *Ui = nullptr, *lam = nullptr;
+  int *status = nullptr, *members = nullptr;
+  long long *tile_base = nullptr;
+  int *n_tiles = nullptr;
+  double2 *partials = nullptr;
+  std::vector<long long> gQ, gL, gM;            // group bases (doubles, doubles, ints)
+  int slot_bytes = 0;
+};
+
+namespace {
+
+template <typename T>
+pgpu_status upload(pgpu_ctx *ctx, T **dst, const std::vector<T> &src) {
+  const size_t bytes = std::max<size_t>(src.size() * sizeof(T), 16);
+  PGPU_CUDA(ctx, cudaMalloc(reinterpret_cast<void **>(dst), bytes));
+  if (!src.empty())
+    PGPU_CUDA(ctx, cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return PGPU_OK;
+}
+
+void free_batch(pgpu_batch *b) {
+  void *ptrs[] = {b->vars, b->work,   b->ops, b->bmat,   b->tiptab,  b->pis,      b->brlen,
+                  b->rates, b->ctab,  b->Q,   b->U,      b->Ui,      b->lam,      b->status,
+                  b->members, b->tile_base, b->n_tiles, b->partials};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  delete b;
+}
+
+}  // namespace
+
+extern "C" {
+
+pgpu_status pgpu_batch_create(pgpu_ctx *ctx, const pgpu_variant *vs, int n_var, pgpu_batch **out) {
+  if (!ctx || !out) return PGPU_ERR_ARG;
+  *out = nullptr;
+  if (!vs || n_var < 1) return pgpu_set_err(ctx, PGPU_ERR_ARG, "batch: no variants");
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  pgpu_batch *b = new pgpu_batch();
+  b->n_var = n_var;
+  std::vector<int4> ops;
+  std::vector<int2> work;
+  std::vector<double> pis, brl, rts, ctab, Qg;
+  std::vector<long long> tile_base;
+  std::vector<int> ntiles, members;
+  long long bm_off = 0, tt_off = 0, pat_off = 0;
+  size_t max_blk = 0;
+  auto fail = [&](pgpu_status st, const char *msg, int v) {
+    free_batch(b);
+    return pgpu_set_err(ctx, st, "batch: variant %d: %s", v, msg);
+  };
+  for (int vi = 0; vi < n_var; ++vi) {
+    const pgpu_variant &x = vs[vi];
+    const pgpu_model &m = x.model;
+    if (!x.tree.brlen || !m.Q || !m.pi || !m.rates || !m.probs || !x.codes.table || !x.tip_codes)
+      return fail(PGPU_ERR_ARG, "null field", vi);
+    if (m.n_states < 2 || m.n_states > 64) return fail(PGPU_ERR_LIMIT, "2..64 states", vi);
+    if (m.n_rates < 1 || m.n_rates > 4) return fail(PGPU_ERR_LIMIT, "1..4 rate classes", vi);
+    if (x.codes.n_codes < 1 || x.codes.n_codes > 255) return fail(PGPU_ERR_ARG, "1..255 codes", vi);
+    if (x.tree.n_tips < 2 || x.tree.n_tips > 255) return fail(PGPU_ERR_LIMIT, "2..255 tips", vi);
+    const long long nt = (long long)((x.n_pat + BT_M - 1) / BT_M);
+    if (x.ld_pat % 128 != 0 || (long long)x.ld_pat < nt * BT_M || ((uintptr_t)x.tip_codes & 15))
+      return fail(PGPU_ERR_ARG, "ld_pat must be a multiple of 128 covering the padded tiles", vi);
+    TreeSchedule sch;
+    pgpu_status st = pgpu_build_schedule(ctx, &x.tree, &sch);
+    if (st != PGPU_OK) {
+      free_batch(b);
+      return st;
+    }
+    const int n = x.tree.n_tips, S = m.n_states, R = m.n_rates;
+    BVar v{};
+    v.n_tips = n;
+    v.n_ops = n - 1;
+    v.S = S;
+    v.R = R;
+    v.n_codes = x.codes.n_codes;
+    v.Kp = (S + 7) / 8 * 8;
+    v.Np = (S + 15) / 16 * 16;
+    v.SpT = S | 1;                        // odd row stride: distinct codes, distinct banks
+    v.NCp = (x.codes.n_codes + 3) / 4 * 4; // rows padded so a block is a multiple of 16 bytes
+    v.n_slots = (BT_TMEM_COLS - 2 * v.Np) / v.Kp;
+    v.n_tiles = (int)nt;
+    v.n_pat = (long long)x.n_pat;
+    v.ld = (long long)x.ld_pat;
+    v.codes = x.tip_codes;
+    v.weights = x.weights;
+    v.pat_off = pat_off;
+    v.ops_off = (long long)ops.size();
+    v.bmat_off = bm_off;
+    v.tip_off = tt_off;
+    v.pi_off = (long long)pis.size();
+    v.brlen_off = (long long)brl.size();
+    v.rates_off = (long long)rts.size();
+    v.ctab_off = (long long)ctab.size();
+    for (int r = 0; r < 4; ++r) v.probs[r] = r < R ? m.probs[r] : 0.0;
+    if (sch.max_depth > v.n_slots) return fail(PGPU_ERR_LIMIT, "tree too deep for the TMEM stack", vi);
+    b->max_depth = std::max(b->max_depth, sch.max_depth);
+    // TMEM stack positions from the stack simulation
+    int sp = 0;
+    for (const SchedOp &o : sch.ops) {
+      int sa = 0, sb = 0;
+      if (o.b >= n) sb = --sp;
+      if (o.a >= n) sa = --sp;
+      const int so = sp++;
+      ops.push_back(make_int4(o.k, o.a, o.b, sa | (sb << 8) | (so << 16)));
+    }
+    for (long long t = 0; t < nt; ++t) work.push_back(make_int2(vi, (int)t));
+    tile_base.push_back((long long)work.size() - nt);
+    ntiles.push_back((int)nt);
+    pis.insert(pis.end(), m.pi, m.pi + S);
+    brl.insert(brl.end(), x.tree.brlen, x.tree.brlen + 2 * n - 2);
+    rts.insert(rts.end(), m.rates, m.rates + R);
+    ctab.insert(ctab.end(), x.codes.table, x.codes.table + (size_t)v.n_codes * S);
+    bm_off += (long long)(n - 2) * R * v.Np * v.Kp;
+    tt_off += (long long)n * R * v.NCp * v.SpT;
+    bm_off = (bm_off + 3) / 4 * 4;
+    tt_off = (tt_off + 3) / 4 * 4;
+    pat_off += v.n_pat;
+    const size_t blk = std::max<size_t>((size_t)v.Np * v.Kp * 4, (size_t)v.NCp * v.SpT * 4);
+    max_blk = std::max(max_blk, (blk + 127) & ~size_t(127));
+    // eigen group by state count
+    int g = -1;
+    for (size_t k = 0; k < b->group_S.size(); ++k)
+      if (b->group_S[k] == S) g = (int)k;
+    if (g < 0) {
+      g = (int)b->group_S.size();
+      b->group_S.push_back(S);
+      b->group_members.emplace_back();
+    }
+    v.group = g;
+    v.group_idx = (int)b->group_members[g].size();
+    b->group_members[g].push_back(vi);
+    b->hvars.push_back(v);
+  }
+  if (b->group_S.size() > 8) return fail(PGPU_ERR_LIMIT, "at most 8 distinct state counts", 0);
+  // group layout of Q / pi / eigen arrays
+  std::vector<double> Qall, PIall;
+  long long q_acc = 0, l_acc = 0;
+  for (size_t g = 0; g < b->group_S.size(); ++g) {
+    const int S = b->group_S[g];
+    b->gQ.push_back(q_acc);
+    b->gL.push_back(l_acc);
+    b->gM.push_back((long long)members.size());
+    for (int vi : b->group_members[g]) {
+      Qall.insert(Qall.end(), vs[vi].model.Q, vs[vi].model.Q + (size_t)S * S);
+      PIall.insert(PIall.end(), vs[vi].model.pi, vs[vi].model.pi + S);
+      members.push_back(vi);
+    }
+    q_acc += (long long)b->group_members[g].size() * S * S;
+    l_acc += (long long)b->group_members[g].size() * S;
+  }
+  b->n_work = (long long)work.size();
+  b->total_pat = pat_off;
+  b->slot_bytes = (int)(256 + 2 * max_blk);
+  pgpu_status st = PGPU_OK;
+  if (st == PGPU_OK) st = upload(ctx, &b->vars, b->hvars);
+  if (st == PGPU_OK) st = upload(ctx, &b->work, work);
+  if (st == PGPU_OK) st = upload(ctx, &b->ops, ops);
+  if (st == PGPU_OK) st = upload(ctx, &b->pis, pis);
+  if (st == PGPU_OK) st = upload(ctx, &b->brlen, brl);
+  if (st == PGPU_OK) st = upload(ctx, &b->rates, rts);
+  if (st == PGPU_OK) st = upload(ctx, &b->ctab, ctab);
+  if (st == PGPU_OK) st = upload(ctx, &b->Q, Qall);
+  if (st == PGPU_OK) st = upload(ctx, &b->tile_base, tile_base);
+  if (st == PGPU_OK) st = upload(ctx, &b->n_tiles, ntiles);
+  if (st == PGPU_OK) st = upload(ctx, &b->members, members);
+  std::vector<double> pig(PIall);
+  double *dpig = nullptr;
+  if (st == PGPU_OK) st = upload(ctx, &dpig, pig);
+  auto alloc = [&](void **p, size_t bytes) -> pgpu_status {
+    PGPU_CUDA(ctx, cudaMalloc(p, std::max<size_t>(bytes, 16)));
+    return PGPU_OK;
+  };
+  if (st == PGPU_OK) st = alloc((void **)&b->bmat, (size_t)bm_off * 4);
+  if (st == PGPU_OK) st = alloc((void **)&b->tiptab, (size_t)tt_off * 4);
+  if (st == PGPU_OK) st = alloc((void **)&b->U, (size_t)q_acc * 8);
+  if (st == PGPU_OK) st = alloc((void **)&b->Ui, (size_t)q_acc * 8);
+  if (st == PGPU_OK) st = alloc((void **)&b->lam, (size_t)l_acc * 8);
+  if (st == PGPU_OK) st = alloc((void **)&b->status, (size_t)n_var * 4);
+  if (st == PGPU_OK) st = alloc((void **)&b->partials, (size_t)std::max<long long>(b->n_work, 1) * 16);
+  // the eigen systems depend on the models only: solved once here
+  if (st == PGPU_OK) {
+    for (size_t g = 0; g < b->group_S.size() && st == PGPU_OK; ++g) {
+      const int S = b->group_S[g];
+      st = pgpu_launch_eig(ctx, b->Q + b->gQ[g], dpig + b->gL[g], S,
+                           (int)b->group_members[g].size(), b->U + b->gQ[g], b->lam + b->gL[g],
+                           b->Ui + b->gQ[g], b->status + b->gM[g]);
+    }
+  }
+  if (st == PGPU_OK) {
+    std::vector<int> hst(n_var, 0);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(hst.data(), b->status, (size_t)n_var * 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) st = pgpu_set_err(ctx, PGPU_ERR_CUDA, "batch: %s", cudaGetErrorString(e));
+    for (int k = 0; k < n_var && st == PGPU_OK; ++k)
+      if (hst[k]) st = pgpu_set_err(ctx, hst[k], "batch: model %d failed its eigendecomposition (%d)", k, hst[k]);
+  }
+  if (dpig) cudaFree(dpig);
+  if (st != PGPU_OK) {
+    free_batch(b);
+    return st;
+  }
+  *out = b;
+  return PGPU_OK;
+}
+
+void pgpu_batch_destroy(pgpu_batch *b) {
+  if (b) free_batch(b);
+}
+
+pgpu_status pgpu_batch_run(pgpu_ctx *ctx, pgpu_batch *b, double *lnl_dev, double *site_lnl_dev) {
+  if (!ctx || !b || !lnl_dev) return PGPU_ERR_ARG;
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  // B blocks and tip rows for every branch (FP64 P from the eigen systems)
+  for (size_t g = 0; g < b->group_S.size(); ++g) {
+    const int S = b->group_S[g];
+    SetupArgs a;
+    a.vars = b->vars;
+    a.members = b->members + b->gM[g];
+    a.U = b->U + b->gQ[g];
+    a.lam = b->lam + b->gL[g];
+    a.Ui = b->Ui + b->gQ[g];
+    a.status = b->status + b->gM[g];
+    a.brlen = b->brlen;
+    a.rates = b->rates;
+    a.ctab = b->ctab;
+    a.bmat = b->bmat;
+    a.tiptab = b->tiptab;
+    a.flag = ctx->d_flag;
+    a.S = S;
+    int max_tips = 0, max_R = 0;
+    for (int vi : b->group_members[g]) {
+      max_tips = std::max(max_tips, b->hvars[vi].n_tips);
+      max_R = std::max(max_R, b->hvars[vi].R);
+    }
+    const size_t smem = sizeof(double) * ((size_t)S * S + S);
+    PGPU_CUDA(ctx, cudaFuncSetAttribute(batch_setup_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)std::max<size_t>(smem, 1024)));
+    batch_setup_kernel<<<dim3(2 * max_tips - 2, max_R, (unsigned)b->group_members[g].size()), 256, smem,
+                         ctx->stream>>>(a);
+    PGPU_TRY(pgpu_after_launch(ctx, "batch_setup_kernel"));
+  }
+  BatchArgs a;
+  a.vars = b->vars;
+  a.work = b->work;
+  a.n_work = b->n_work;
+  a.ops = b->ops;
+  a.bmat = b->bmat;
+  a.tiptab = b->tiptab;
+  a.pis = b->pis;
+  a.site_lnl = site_lnl_dev;
+  a.partials = b->partials;
+  a.flag = ctx->d_flag;
+  a.slot_bytes = b->slot_bytes;
+  // at least 120 KB, so that one CTA (which holds all 512 TMEM columns)
+  // occupies each SM
+  const size_t smem = std::max<size_t>((size_t)BT_ST * b->slot_bytes, 120 * 1024);
+  if (smem > ctx->smem_optin)
+    return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "batch: %zu bytes of shared memory needed", smem);
+  PGPU_CUDA(ctx, cudaFuncSetAttribute(batch_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)std::max<size_t>(smem, 48 * 1024)));
+  const long long grid = std::min<long long>(ctx->num_sms, b->n_work);
+  batch_tc_kernel<<<(unsigned)std::max<long long>(grid, 1), BT_THREADS, smem, ctx->stream>>>(a);
+  PGPU_TRY(pgpu_after_launch(ctx, "batch_tc_kernel"));
+  batch_finalize_kernel<<<(b->n_var + 127) / 128, 128, 0, ctx->stream>>>(b->partials, b->tile_base,
+                                                                        b->n_tiles, b->n_var, lnl_dev);
+  return pgpu_after_launch(ctx, "batch_finalize_kernel");
+}
+
+pgpu_status pgpu_batch_run_fp64(pgpu_ctx *ctx, pgpu_batch *b, size_t sample, double *lnl_dev) {
+  if (!ctx || !b || !lnl_dev || sample == 0) return PGPU_ERR_ARG;
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  F64Args a;
+  a.vars = b->vars;
+  a.ops = b->ops;
+  a.U = b->U;
+  a.Ui = b->Ui;
+  a.lam = b->lam;
+  for (size_t g = 0; g < 8; ++g) {
+    a.gU[g] = g < b->gQ.size() ? b->gQ[g] : 0;
+    a.gL[g] = g < b->gL.size() ? b->gL[g] : 0;
+  }
+  a.brlen = b->brlen;
+  a.rates = b->rates;
+  a.ctab = b->ctab;
+  a.pis = b->pis;
+  long long max_pat = 0;
+  int max_S = 0;
+  for (const BVar &v : b->hvars) {
+    max_pat = std::max(max_pat, std::min<long long>(v.n_pat, (long long)sample));
+    max_S = std::max(max_S, v.S);
+  }
+  a.blocks = (int)((max_pat + F64_NP - 1) / F64_NP);
+  a.sample = (long long)sample;
+  a.max_depth = b->max_depth;
+  double2 *dpart = nullptr;
+  PGPU_TRY(pgpu_buf(ctx, BUF_D, (size_t)a.blocks * b->n_var * sizeof(double2), (void **)&dpart));
+  a.partials = dpart;
+  const size_t smem = sizeof(double) * ((size_t)max_S * max_S + 64 + (size_t)b->max_depth * max_S * F64_NP);
+  if (smem > ctx->smem_optin) return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "batch fp64: tree too deep");
+  PGPU_CUDA(ctx, cudaFuncSetAttribute(batch_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)std::max<size_t>(smem, 48 * 1024)));
+  batch_fp64_kernel<<<dim3(a.blocks, b->n_var), F64_NP, smem, ctx->stream>>>(a);
+  PGPU_TRY(pgpu_after_launch(ctx, "batch_fp64_kernel"));
+  // per variant: blocks * F64_NP patterns, partials at [v * blocks]
+  std::vector<long long> base(b->n_var);
+  std::vector<int> cnt(b->n_var, a.blocks);
+  for (int v = 0; v < b->n_var; ++v) base[v] = (long long)v * a.blocks;
+  long long *dbase = nullptr;
+  int *dcnt = nullptr;
+  PGPU_TRY(pgpu_buf(ctx, BUF_E, base.size() * 8, (void **)&dbase));
+  PGPU_TRY(pgpu_buf(ctx, BUF_F, cnt.size() * 4, (void **)&dcnt));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(dbase, base.data(), base.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(dcnt, cnt.data(), cnt.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+  batch_finalize_kernel<<<(b->n_var + 127) / 128, 128, 0, ctx->stream>>>(dpart, dbase, dcnt,
+                                                                        b->n_var, lnl_dev);
+  return pgpu_after_launch(ctx, "batch_finalize_kernel");
+}
+
+long long pgpu_batch_work_items(const pgpu_batch *b) { return b ? b->n_work : 0; }
+long long pgpu_batch_patterns(const pgpu_batch *b) { return b ? b->total_pat : 0; }
+
+}  // extern "C"

@@ -201,3 +201,80 @@ def prune_workload(n_tips: int, n_sites: int, seed: int, mean_brlen: float = 0.1
         inject_ambiguity(masks, ambiguity, rng)
     pats, w, _ = compress_patterns(masks)
     return tr, spec, pats, w
+
+
+# ---- protein and codon models ------------------------------------------------
+
+# The standard genetic code, codons in TCAG order (first base slowest).
+_BASES = "TCAG"
+_AMINO = "FFLLSSSSYY**CC*WLLLLPPPPHHQQRRRRIIIMTTTTNNKKSSRRVVVVAAAADDEEGGGG"
+SENSE_CODONS = [a + b + c for a in _BASES for b in _BASES for c in _BASES
+                if _AMINO[16 * _BASES.index(a) + 4 * _BASES.index(b) + _BASES.index(c)] != "*"]
+
+
+def _aa(codon: str) -> str:
+    return _AMINO[16 * _BASES.index(codon[0]) + 4 * _BASES.index(codon[1]) + _BASES.index(codon[2])]
+
+
+def normalize_q(q: np.ndarray, pi: np.ndarray) -> np.ndarray:
+    q = q.copy()
+    np.fill_diagonal(q, 0.0)
+    np.fill_diagonal(q, -q.sum(axis=1))
+    return q / float(-(np.diag(q) * pi).sum())
+
+
+def protein_model(rng: np.random.Generator):
+    """Random reversible 20-state Q: exchangeabilities ~ LogNormal(0, 1),
+    frequencies ~ Dirichlet(1 x 20), mean rate 1."""
+    ex = rng.lognormal(0.0, 1.0, (20, 20))
+    ex = np.triu(ex, 1)
+    ex = ex + ex.T
+    pi = rng.dirichlet(np.ones(20))
+    return normalize_q(ex * pi[None, :], pi), pi
+
+
+_CODON_STRUCT = None
+
+
+def _codon_struct():
+    """(single-change mask, transition mask, non-synonymous mask) over the
+    61 sense codons, built once."""
+    global _CODON_STRUCT
+    if _CODON_STRUCT is None:
+        n = len(SENSE_CODONS)
+        single = np.zeros((n, n), bool)
+        ts = np.zeros((n, n), bool)
+        nonsyn = np.zeros((n, n), bool)
+        purine = set("AG")
+        for i, a in enumerate(SENSE_CODONS):
+            for j, b in enumerate(SENSE_CODONS):
+                diff = [k for k in range(3) if a[k] != b[k]]
+                if len(diff) != 1:
+                    continue
+                x, y = a[diff[0]], b[diff[0]]
+                single[i, j] = True
+                ts[i, j] = (x in purine) == (y in purine)
+                nonsyn[i, j] = _aa(a) != _aa(b)
+        _CODON_STRUCT = (single, ts, nonsyn)
+    return _CODON_STRUCT
+
+
+def codon_model(kappa: float, omega: float, pi: np.ndarray | None = None):
+    """Goldman-Yang (1994) style 61-state codon Q: single-nucleotide changes
+    only, transitions x kappa, non-synonymous changes x omega, target
+    frequency pi_j (uniform by default), mean rate 1."""
+    n = len(SENSE_CODONS)
+    pi = np.full(n, 1.0 / n) if pi is None else np.asarray(pi, np.float64)
+    single, ts, nonsyn = _codon_struct()
+    q = np.where(single, pi[None, :], 0.0)
+    q = np.where(ts, q * kappa, q)
+    q = np.where(nonsyn, q * omega, q)
+    return normalize_q(q, pi), pi
+
+
+def state_code_table(S: int) -> np.ndarray:
+    """[S + 1, S] tip partials: code c < S is state c, code S is missing."""
+    t = np.zeros((S + 1, S))
+    t[np.arange(S), np.arange(S)] = 1.0
+    t[S] = 1.0
+    return t

@@ -88,3 +88,20 @@ def test_fitch_workload_shapes():
     assert w.min() >= 1 and w.max() <= 8
     amb = np.isin(masks, [1, 2, 4, 8], invert=True).mean()
     assert 0.03 < amb < 0.07
+
+
+def test_codon_and_protein_models():
+    q, pi = synth.codon_model(2.5, 0.4)
+    assert q.shape == (61, 61) and len(synth.SENSE_CODONS) == 61
+    assert np.allclose(q.sum(axis=1), 0.0, atol=1e-14)
+    assert abs(-(np.diag(q) * pi).sum() - 1.0) < 1e-12
+    assert np.allclose(pi[:, None] * q, (pi[:, None] * q).T, atol=1e-14)   # reversible
+    # only single-nucleotide changes have a rate
+    for i, a in enumerate(synth.SENSE_CODONS[:10]):
+        for j, b in enumerate(synth.SENSE_CODONS):
+            if i != j and sum(x != y for x, y in zip(a, b)) > 1:
+                assert q[i, j] == 0.0
+    qp, pp = synth.protein_model(np.random.default_rng(3))
+    assert qp.shape == (20, 20) and np.allclose(pp[:, None] * qp, (pp[:, None] * qp).T)
+    t = synth.state_code_table(20)
+    assert t.shape == (21, 20) and (t[20] == 1).all() and (t[:20].sum(1) == 1).all()
