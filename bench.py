@@ -432,7 +432,7 @@ def bench_prune(args, rank, world, local):
             float(out.item())
 
     forms = {}
-    for prec in (32, 48):
+    for prec in [f for f in (32, 48) if f in args.prune_forms]:
         clk = ClockSampler(local)
         clk.start()
         el, per, launches, lnl = timed(prec, args.steps)
@@ -440,16 +440,20 @@ def bench_prune(args, rank, world, local):
                               (el * 1e-3), "lnl": lnl, "launches": launches, "clocks": clk.stop(),
                               "per_launch_ms": per}
     k64 = max(3, min(args.steps, 10))
-    el, per, launches, lnl = timed(64, k64)
-    forms["fp64"] = {"ms_per_step": el / k64, "value": world * units * k64 / (el * 1e-3), "lnl": lnl,
-                     "launches": launches, "per_launch_ms": per}
+    if 64 in args.prune_forms:
+        el, per, launches, lnl = timed(64, k64)
+        forms["fp64"] = {"ms_per_step": el / k64, "value": world * units * k64 / (el * 1e-3),
+                         "lnl": lnl, "launches": launches, "per_launch_ms": per}
     for f in forms.values():
         f["dlnl_vs_oracle"] = None if exp is None else f["lnl"] - exp
         f["within_gate"] = None if exp is None else abs(f["lnl"] - exp) <= PRUNE_GATE
 
     # headline: fastest FP32-unit form inside the gate
-    cand = [(FORMS[p], p) for p in (32, 48) if forms[FORMS[p]]["within_gate"]]
-    head_name, head_prec = min(cand, key=lambda x: forms[x[0]]["ms_per_step"]) if cand else ("fp32x2", 48)
+    present = [(FORMS[p], p) for p in (32, 48) if FORMS[p] in forms]
+    cand = [fp for fp in present if forms[fp[0]]["within_gate"]] or present
+    if not cand:
+        raise SystemExit("bench: --prune-forms must include 32 or 48")
+    head_name, head_prec = min(cand, key=lambda x: forms[x[0]]["ms_per_step"])
     head = forms[head_name]
 
     # end to end through the host-buffer call (pinned host tips and weights)
@@ -481,8 +485,9 @@ def bench_prune(args, rank, world, local):
                    "n_tips": tr.n_tips, "n_patterns": n_pat, "n_rates": R, "form": head_name,
                    "l2": "each step reads the 228 MB tip-code matrix (> L2) once; no flush"},
         "forms": forms,
-        "fp64_form": {"value": forms["fp64"]["value"], "ms_per_step": forms["fp64"]["ms_per_step"],
-                      "speedup_of_headline": head["value"] / forms["fp64"]["value"]},
+        "fp64_form": None if "fp64" not in forms else {
+            "value": forms["fp64"]["value"], "ms_per_step": forms["fp64"]["ms_per_step"],
+            "speedup_of_headline": head["value"] / forms["fp64"]["value"]},
         "dlnl": {"oracle_lnl": exp, "headline_vs_oracle": head["dlnl_vs_oracle"],
                  "gate": PRUNE_GATE, "within_gate": head["within_gate"]},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": lane_peak, "unit": "Tinst/s",
@@ -590,7 +595,7 @@ def bench_batch(args, rank, world, local):
     from phylocaml_gb300.batch import Batch
     dev = torch.device(f"cuda:{local}")
     torch.cuda.set_device(dev)
-    variants = batch_data(rank, dev)
+    variants = batch_data(rank, dev, args.batch_variants)
     ctx = _native.Context(local)
     stream = torch.cuda.Stream(dev)
     torch.cuda.synchronize(dev)
@@ -704,8 +709,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=["prune", "fitch", "batch", "all"], default="all")
+    # smaller runs for profiler captures: a subset of the pruning forms, fewer batch variants
+    ap.add_argument("--prune-forms", default="32,48,64")
+    ap.add_argument("--batch-variants", type=int, default=BATCH_VARIANTS)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    args.prune_forms = {int(f) for f in args.prune_forms.split(",") if f}
     rank, world, local = dist_info()
     head = args.workload if args.workload in ("fitch", "batch") else "prune"
 

@@ -274,6 +274,99 @@ pgpu_status pgpu_batch_run_fp64(pgpu_ctx *ctx, pgpu_batch *batch, size_t sample,
 long long pgpu_batch_work_items(const pgpu_batch *batch);
 long long pgpu_batch_patterns(const pgpu_batch *batch);
 
+/* ---------------------------------------------------------------------------
+ * SPR rearrangements (Tree.break / Tree.join, lib/tree.ml:299-494; the
+ * neighbourhood enumerators lib/treeNeighborhoods.ml:27-75 are TODOs there)
+ *
+ * An engine holds one unrooted tree over fixed DNA data (4 states, 1..8 rate
+ * classes) and, on the GPU, the conditional likelihood vectors of both sides
+ * of every edge.  A move (p, u, c, y) cuts edge (p,u), carries p's side away,
+ * joins u's two other neighbours into one edge (lengths added) and puts u in
+ * the middle of edge (c,y) (half its length on each side); the pruned branch
+ * keeps its length.  Moves are listed in a fixed order per tree; indices refer
+ * to the current tree's list.  `precision` is 32, 48 (float pairs) or 64, as
+ * for pgpu_prune_lnl.
+ * ------------------------------------------------------------------------- */
+typedef struct pgpu_spr pgpu_spr;
+
+/* tip_codes_dev: DEVICE [n_tips][ld_pat]; weights_dev: DEVICE [n_pat] or NULL
+ * (all 1); both must outlive the engine. */
+pgpu_status pgpu_spr_create(pgpu_ctx *ctx, const pgpu_model *model, const pgpu_tip_codes *codes,
+                            int32_t n_tips, const uint8_t *tip_codes_dev, size_t ld_pat,
+                            const double *weights_dev, size_t n_pat, int precision,
+                            pgpu_spr **out);
+void pgpu_spr_destroy(pgpu_spr *spr);
+/* The tree as a rooted postorder (root ignored: its two branches become one
+ * edge); brlen required. */
+pgpu_status pgpu_spr_set_tree(pgpu_spr *spr, const pgpu_tree *tree);
+/* The current tree, rooted on the edge above tip 0 (half of it each side):
+ * left/right [n_tips-1], brlen [2 n_tips - 2]. */
+pgpu_status pgpu_spr_get_tree(pgpu_spr *spr, int32_t *left, int32_t *right, double *brlen);
+/* lnL of the current tree (host scalar) and optionally every pattern's. */
+pgpu_status pgpu_spr_lnl(pgpu_spr *spr, double *lnl, double *site_lnl);
+pgpu_status pgpu_spr_n_moves(pgpu_spr *spr, size_t *n_moves);
+/* Node ids of every move, in the numbering of pgpu_spr_get_tree. */
+pgpu_status pgpu_spr_moves(pgpu_spr *spr, int32_t *p, int32_t *u, int32_t *c, int32_t *y, size_t cap);
+/* lnL of the tree after each move (no branch-length optimisation), into
+ * DEVICE lnl_dev[n_moves]. */
+pgpu_status pgpu_spr_scan(pgpu_spr *spr, double *lnl_dev);
+/* The same for k chosen moves only; lnl is a host array [k]. */
+pgpu_status pgpu_spr_score(pgpu_spr *spr, const int64_t *move_idx, size_t k, double *lnl);
+/* Fitch (parsimony) length of the tree after each move into DEVICE
+ * len_dev[n_moves]; tree_len receives the current tree's. */
+pgpu_status pgpu_spr_fitch(pgpu_spr *spr, uint64_t *len_dev, uint64_t *tree_len);
+/* 64 FP32 features per move into DEVICE X_dev[n_moves][64]: subtree sizes,
+ * the branch lengths at the prune and regraft points, the Fitch length
+ * change, and pattern-averaged state profiles of the sides involved. */
+pgpu_status pgpu_spr_features(pgpu_spr *spr, float *X_dev);
+pgpu_status pgpu_spr_apply(pgpu_spr *spr, int64_t move_idx);
+/* Newton steps on all branch lengths at once, up to `passes` rounds or until
+ * a round gains less than tol; lnl (or NULL) receives the final lnL. */
+pgpu_status pgpu_spr_optimize(pgpu_spr *spr, int passes, double tol, double *lnl);
+/* Edge lengths and endpoints of the engine's unrooted tree [2 n_tips - 3]. */
+pgpu_status pgpu_spr_lengths(pgpu_spr *spr, double *len, int32_t *ea, int32_t *eb);
+
+/* ---------------------------------------------------------------------------
+ * Learned SPR ranking: BF16 MLP 64 -> 256 -> 256 -> 256 -> 1 (GELU), FP32
+ * accumulation on the tensor cores (tcgen05.mma kind::f16), FP32 master
+ * weights, AdamW.  Inputs are the 64 move features of pgpu_spr_features,
+ * normalised per column with statistics set by pgpu_mlp_fit_norm.  The flat
+ * parameter vector is W1[256][64], b1[256], W2[256][256], b2, W3[256][256],
+ * b3, w4[256], b4.
+ * ------------------------------------------------------------------------- */
+typedef struct pgpu_mlp pgpu_mlp;
+
+long long pgpu_mlp_n_params(void);
+/* He-uniform weights from `seed`; training batches of up to max_batch rows. */
+pgpu_status pgpu_mlp_create(pgpu_ctx *ctx, uint64_t seed, int max_batch, pgpu_mlp **out);
+void pgpu_mlp_destroy(pgpu_mlp *mlp);
+pgpu_status pgpu_mlp_get_params(pgpu_mlp *mlp, float *host);
+pgpu_status pgpu_mlp_set_params(pgpu_mlp *mlp, const float *host);
+pgpu_status pgpu_mlp_get_norm(pgpu_mlp *mlp, float *mu, float *inv_sd);
+/* column means and inverse standard deviations of DEVICE X_dev[n][64] */
+pgpu_status pgpu_mlp_fit_norm(pgpu_mlp *mlp, const float *X_dev, size_t n);
+/* y_dev[n] = network(X_dev[n][64]) (device arrays, asynchronous) */
+pgpu_status pgpu_mlp_forward(pgpu_mlp *mlp, const float *X_dev, size_t n, float *y_dev);
+/* Gradients of sum_i sw_i (y_i - t_i)^2 / sum_i sw_i (sw_dev NULL: all 1)
+ * into the host vector grad[n_params]; loss (or NULL) gets the loss. */
+pgpu_status pgpu_mlp_grads(pgpu_mlp *mlp, const float *X_dev, const float *t_dev, const float *sw_dev,
+                           size_t n, float *grad, float *loss);
+/* One AdamW step (beta 0.9 / 0.999, eps 1e-8, decoupled weight decay on the
+ * weight matrices) on that loss; loss (or NULL: no synchronisation). */
+pgpu_status pgpu_mlp_train_step(pgpu_mlp *mlp, const float *X_dev, const float *t_dev,
+                                const float *sw_dev, size_t n, float lr, float weight_decay,
+                                float *loss);
+
+/* Random-addition parsimony tree (host only): taxa join in a seeded random
+ * order, each where it adds the fewest Fitch steps.  tip_codes is HOST
+ * [n_tips][ld]; code_mask[c] holds the state bits of code c; every branch
+ * gets length brlen.  length (or NULL) receives the tree's Fitch length. */
+pgpu_status pgpu_parsimony_stepwise(int32_t n_tips, const uint8_t *tip_codes, size_t ld,
+                                    size_t n_pat, const uint8_t *code_mask, int n_codes,
+                                    const double *weights, uint64_t seed, double brlen,
+                                    int32_t *left, int32_t *right, double *brlen_out,
+                                    uint64_t *length);
+
 #ifdef __cplusplus
 }
 #endif

@@ -108,6 +108,23 @@ SIGNATURES: dict[str, tuple] = {
     "pgpu_batch_run_fp64": (_I, [_P, _P, _SZ, _P]),
     "pgpu_batch_work_items": (C.c_longlong, [_P]),
     "pgpu_batch_patterns": (C.c_longlong, [_P]),
+    "pgpu_spr_create": (_I, [_P, C.POINTER(PgpuModel), C.POINTER(PgpuTipCodes), C.c_int32, _P, _SZ,
+                             _P, _SZ, _I, C.POINTER(_P)]),
+    "pgpu_spr_destroy": (None, [_P]),
+    "pgpu_spr_set_tree": (_I, [_P, C.POINTER(PgpuTree)]),
+    "pgpu_spr_get_tree": (_I, [_P, _P, _P, _P]),
+    "pgpu_spr_lnl": (_I, [_P, _DP, _P]),
+    "pgpu_spr_n_moves": (_I, [_P, C.POINTER(_SZ)]),
+    "pgpu_spr_moves": (_I, [_P, _P, _P, _P, _P, _SZ]),
+    "pgpu_spr_scan": (_I, [_P, _P]),
+    "pgpu_spr_score": (_I, [_P, _P, _SZ, _P]),
+    "pgpu_spr_fitch": (_I, [_P, _P, _U64P]),
+    "pgpu_spr_features": (_I, [_P, _P]),
+    "pgpu_spr_apply": (_I, [_P, C.c_int64]),
+    "pgpu_spr_optimize": (_I, [_P, _I, C.c_double, _DP]),
+    "pgpu_spr_lengths": (_I, [_P, _P, _P, _P]),
+    "pgpu_parsimony_stepwise": (_I, [C.c_int32, _P, _SZ, _SZ, _P, _I, _P, C.c_uint64, C.c_double,
+                                     _P, _P, _P, _U64P]),
 }
 
 _lib = None

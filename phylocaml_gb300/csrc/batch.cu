@@ -37,6 +37,7 @@
 #include <cmath>
 #include <vector>
 
+#include "forms.cuh"
 #include "pgpu_internal.cuh"
 #include "pmatrix.cuh"
 
@@ -442,19 +443,13 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
 }
 
 // Per variant: sum its tiles' (sum, compensation) pairs in tile order.
-__global__ void batch_finalize_kernel(const double2 *partials, const long long *tile_base,
-                                      const int *n_tiles, int n_var, double *out) {
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(256) batch_finalize_kernel(const double2 *partials,
+                                                            const long long *tile_base,
+                                                            const int *n_tiles, int n_var, double *out) {
+  const int v = blockIdx.x;
   if (v >= n_var) return;
-  double s = 0.0, c = 0.0;
-  for (int t = 0; t < n_tiles[v]; ++t) {
-    const double2 x = partials[tile_base[v] + t];
-    double u, e;
-    two_sum_d(s, x.x, u, e);
-    s = u;
-    c += e + x.y;
-  }
-  out[v] = s + c;
+  const double sum = pgpu_forms::csum_block<256>(partials + tile_base[v], n_tiles[v]);
+  if (threadIdx.x == 0) out[v] = sum;
 }
 
 // Setup: for every branch of every variant of one state count S and every
@@ -914,7 +909,7 @@ pgpu_status pgpu_batch_run(pgpu_ctx *ctx, pgpu_batch *b, double *lnl_dev, double
   const long long grid = std::min<long long>(ctx->num_sms, b->n_work);
   batch_tc_kernel<<<(unsigned)std::max<long long>(grid, 1), BT_THREADS, smem, ctx->stream>>>(a);
   PGPU_TRY(pgpu_after_launch(ctx, "batch_tc_kernel"));
-  batch_finalize_kernel<<<(b->n_var + 127) / 128, 128, 0, ctx->stream>>>(b->partials, b->tile_base,
+  batch_finalize_kernel<<<b->n_var, 256, 0, ctx->stream>>>(b->partials, b->tile_base,
                                                                         b->n_tiles, b->n_var, lnl_dev);
   return pgpu_after_launch(ctx, "batch_finalize_kernel");
 }
@@ -964,7 +959,7 @@ pgpu_status pgpu_batch_run_fp64(pgpu_ctx *ctx, pgpu_batch *b, size_t sample, dou
   PGPU_TRY(pgpu_buf(ctx, BUF_F, cnt.size() * 4, (void **)&dcnt));
   PGPU_CUDA(ctx, cudaMemcpyAsync(dbase, base.data(), base.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
   PGPU_CUDA(ctx, cudaMemcpyAsync(dcnt, cnt.data(), cnt.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-  batch_finalize_kernel<<<(b->n_var + 127) / 128, 128, 0, ctx->stream>>>(dpart, dbase, dcnt,
+  batch_finalize_kernel<<<b->n_var, 256, 0, ctx->stream>>>(dpart, dbase, dcnt,
                                                                         b->n_var, lnl_dev);
   return pgpu_after_launch(ctx, "batch_finalize_kernel");
 }

@@ -22,7 +22,7 @@
 //                    to the pattern's integer scaler e_s.
 // The root log-likelihoods are weighted and summed in FP64 with error-free
 // TwoSum steps (a compensated reduction), one (sum, compensation) pair per
-// CTA; prune_finalize_kernel adds the pairs in CTA order with Neumaier's
+// CTA; prune_finalize_kernel adds the pairs in contiguous chunks with Neumaier's
 // method, so the result does not depend on scheduling.
 //
 // T = float is the FP32 form, T = double the FP64 comparison form; both use
@@ -32,9 +32,11 @@
 #include <cmath>
 
 #include "pgpu_internal.cuh"
+#include "forms.cuh"
 #include "pmatrix.cuh"
 
 namespace {
+using namespace pgpu_forms;
 
 struct PruneArgs {
   const uint8_t *tip_codes;   // [n_tips][ld_pat]
@@ -53,171 +55,10 @@ struct PruneArgs {
   int n_tips, n_ops, n_codes, R, NP, depth;
 };
 
-__device__ __forceinline__ void two_sum(double a, double b, double &s, double &e) {
-  s = a + b;
-  const double bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-
-// compensated sum of (s, c) pairs over the 32 lanes of a warp
-__device__ __forceinline__ void warp_csum(double &s, double &c) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const double s2 = __shfl_xor_sync(0xffffffffu, s, o);
-    const double c2 = __shfl_xor_sync(0xffffffffu, c, o);
-    double t, e;
-    two_sum(s, s2, t, e);
-    s = t;
-    c = c + c2 + e;
-  }
-}
-
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
 constexpr int PR_STAGES = 8;      // ring depth in postorder steps (power of two)
 constexpr int PR_THREADS = 256;   // consumer threads per CTA
-
-// ---- the three arithmetic forms -------------------------------------------
-// Fp32  values float;  P buffer holds fl32(P - I);  y_i = x_i + sum_j D_ij x_j
-// Fp64  values double; P buffer holds P;            y_i = sum_j P_ij x_j
-// Ff32  values are unevaluated float pairs (hi + lo, about 48 significant
-//       bits); P buffer holds (hi, lo) pairs of P - I; every sum and product
-//       is an error-free float transformation, so the only roundings are of
-//       the order of 2^-48.  Sites that share subtree patterns share their
-//       rounding errors, which then add up linearly over the patterns; the
-//       pair form keeps that sum far below 1e-3 where plain FP32 cannot.
-
-struct ff {
-  float h, l;
-};
-
-__device__ __forceinline__ ff two_sum(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  const float bb = __fsub_rn(s, a);
-  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-  return {s, e};
-}
-__device__ __forceinline__ ff fast_two_sum(float a, float b) {   // |a| >= |b| or a == 0
-  const float s = __fadd_rn(a, b);
-  return {s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-__device__ __forceinline__ ff ff_mul(ff a, ff b) {
-  const float p = __fmul_rn(a.h, b.h);
-  float e = __fmaf_rn(a.h, b.h, -p);
-  e = __fmaf_rn(a.h, b.l, e);
-  e = __fmaf_rn(a.l, b.h, e);
-  return fast_two_sum(p, e);
-}
-
-// 2^k as a float for 0 <= k <= 127
-__device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
-
-struct Fp32 {
-  using V = float;
-  using Coef = float;
-  static constexpr float thresh = 0x1p-32f;
-  __device__ static V zero() { return 0.0f; }
-  __device__ static float mag(V v) { return v; }
-  __device__ static double to_d(V v) { return (double)v; }
-  __device__ static V mul(V a, V b) { return a * b; }
-  __device__ static V scale(V v, int k) { return v * pow2f(k); }
-  __device__ static void load_tip(const void *tab, size_t at, V *y) {
-    const float4 v = reinterpret_cast<const float4 *>(tab)[at];
-    y[0] = v.x;
-    y[1] = v.y;
-    y[2] = v.z;
-    y[3] = v.w;
-  }
-  // y[i] = x[i] + sum_j D[i][j] x[j]
-  __device__ static void rows(const Coef *D, const V *x, V *y) {
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const float4 d = reinterpret_cast<const float4 *>(D)[i];
-      float s = d.x * x[0];
-      s = fmaf(d.y, x[1], s);
-      s = fmaf(d.z, x[2], s);
-      s = fmaf(d.w, x[3], s);
-      y[i] = x[i] + s;
-    }
-  }
-};
-
-struct Fp64 {
-  using V = double;
-  using Coef = double;
-  static constexpr double thresh = 0x1p-256;
-  __device__ static V zero() { return 0.0; }
-  __device__ static double mag(V v) { return v; }
-  __device__ static double to_d(V v) { return v; }
-  __device__ static V mul(V a, V b) { return a * b; }
-  __device__ static V scale(V v, int k) { return v * __longlong_as_double((long long)(1023 + k) << 52); }
-  __device__ static void load_tip(const void *tab, size_t at, V *y) {
-    const double2 a = reinterpret_cast<const double2 *>(tab)[2 * at];
-    const double2 b = reinterpret_cast<const double2 *>(tab)[2 * at + 1];
-    y[0] = a.x;
-    y[1] = a.y;
-    y[2] = b.x;
-    y[3] = b.y;
-  }
-  __device__ static void rows(const Coef *P, const V *x, V *y) {
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const double2 a = reinterpret_cast<const double2 *>(P)[2 * i];
-      const double2 b = reinterpret_cast<const double2 *>(P)[2 * i + 1];
-      double s = a.x * x[0];
-      s = fma(a.y, x[1], s);
-      s = fma(b.x, x[2], s);
-      s = fma(b.y, x[3], s);
-      y[i] = s;
-    }
-  }
-};
-
-struct Ff32 {
-  using V = ff;
-  using Coef = float2;
-  static constexpr float thresh = 0x1p-32f;
-  __device__ static V zero() { return {0.0f, 0.0f}; }
-  __device__ static float mag(V v) { return v.h; }
-  __device__ static double to_d(V v) { return (double)v.h + (double)v.l; }
-  __device__ static V mul(V a, V b) { return ff_mul(a, b); }
-  __device__ static V scale(V v, int k) {
-    const float f = pow2f(k);
-    return {v.h * f, v.l * f};
-  }
-  __device__ static void load_tip(const void *tab, size_t at, V *y) {
-    const float4 a = reinterpret_cast<const float4 *>(tab)[2 * at];
-    const float4 b = reinterpret_cast<const float4 *>(tab)[2 * at + 1];
-    y[0] = {a.x, a.y};
-    y[1] = {a.z, a.w};
-    y[2] = {b.x, b.y};
-    y[3] = {b.z, b.w};
-  }
-  __device__ static void rows(const Coef *D, const V *x, V *y) {
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const float4 d01 = reinterpret_cast<const float4 *>(D)[2 * i];
-      const float4 d23 = reinterpret_cast<const float4 *>(D)[2 * i + 1];
-      const float dh[4] = {d01.x, d01.z, d23.x, d23.z};
-      const float dl[4] = {d01.y, d01.w, d23.y, d23.w};
-      // c = sum_j D_ij x_j with the exact product errors and sum errors kept
-      float sh = 0.0f, sl = 0.0f;
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const float ph = __fmul_rn(dh[j], x[j].h);
-        float pe = __fmaf_rn(dh[j], x[j].h, -ph);
-        pe = __fmaf_rn(dh[j], x[j].l, pe);
-        pe = __fmaf_rn(dl[j], x[j].h, pe);
-        const ff t = two_sum(sh, ph);
-        sh = t.h;
-        sl = __fadd_rn(sl, __fadd_rn(t.l, pe));
-      }
-      // y = x + c
-      const ff t = two_sum(x[i].h, sh);
-      y[i] = fast_two_sum(t.h, __fadd_rn(t.l, __fadd_rn(x[i].l, sl)));
-    }
-  }
-};
 
 // Shared memory of one CTA: PR_STAGES per-op slots, then the CLV stack.
 // A slot holds everything one postorder step reads, staged by the producer:
@@ -439,18 +280,10 @@ __global__ void __launch_bounds__(32 + PR_THREADS) prune_tree_kernel(const Prune
 }
 
 // Neumaier sum of the per-CTA (sum, compensation) pairs in CTA order.
-__global__ void __launch_bounds__(32) prune_finalize_kernel(const double2 *partials, int n,
-                                                           double *out) {
-  if (threadIdx.x != 0) return;
-  double s = 0.0, c = 0.0;
-  for (int i = 0; i < n; ++i) {
-    const double2 v = partials[i];
-    double t, e;
-    two_sum(s, v.x, t, e);
-    s = t;
-    c += e + v.y;
-  }
-  out[0] = s + c;
+__global__ void __launch_bounds__(1024) prune_finalize_kernel(const double2 *partials, int n,
+                                                             double *out) {
+  const double v = csum_block<1024>(partials, n);
+  if (threadIdx.x == 0) out[0] = v;
 }
 
 template <typename Pol, int RT>
@@ -513,6 +346,7 @@ pgpu_status pgpu_stage_commit(pgpu_ctx *ctx, size_t bytes) {
 }
 
 namespace {
+using namespace pgpu_forms;
 
 pgpu_status check_model(pgpu_ctx *ctx, const pgpu_model *m, const pgpu_tip_codes *codes) {
   if (!m || !m->Q || !m->pi || !m->rates || !m->probs)
@@ -644,7 +478,7 @@ pgpu_status prune_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *m,
   if (precision == 32) PGPU_TRY(launch_prune<Fp32>(ctx, a, RT));
   else if (precision == 48) PGPU_TRY(launch_prune<Ff32>(ctx, a, RT));
   else PGPU_TRY(launch_prune<Fp64>(ctx, a, RT));
-  prune_finalize_kernel<<<1, 32, 0, ctx->stream>>>((const double2 *)dpart, (int)n_tiles, lnl_dev);
+  prune_finalize_kernel<<<1, 1024, 0, ctx->stream>>>((const double2 *)dpart, (int)n_tiles, lnl_dev);
   return pgpu_after_launch(ctx, "prune_finalize_kernel");
 }
 

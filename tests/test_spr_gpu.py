@@ -1,0 +1,146 @@
+"""GPU: the SPR engine (pgpu_spr_*) against the CPU restatement of the moves
+(oracle/spr_oracle.py) and the FP64 pruning and Fitch oracles."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import spr_oracle as SO
+from phylocaml_gb300 import mlmodel as M, spr, synth, tree as T
+
+pytestmark = pytest.mark.gpu
+
+# move lnL tolerances per form, relative to |lnL| (FP64, float pairs) or
+# absolute per weighted pattern (plain FP32)
+TOL = {64: ("rel", 1e-10), 48: ("rel", 1e-9), 32: ("per_pat", 2e-6)}
+
+
+def close(got, exp, prec, wsum):
+    kind, tol = TOL[prec]
+    lim = tol * np.abs(exp) if kind == "rel" else tol * wsum
+    return np.abs(np.asarray(got) - np.asarray(exp)) <= lim + 1e-12
+
+
+@pytest.fixture(scope="module")
+def small(ctx):
+    import torch
+    tr, spec, pats, w = synth.prune_workload(10, 400, seed=31, mean_brlen=0.15, ambiguity=0.05)
+    q, pi, rates, probs = synth.host_model(spec)
+    model = M.create(spec, ctx)
+    dev = torch.device("cuda:0")
+    tips = torch.from_numpy(pats).to(dev)
+    wd = torch.from_numpy(w).to(dev)
+    return dict(tr=tr, q=q, pi=pi, rates=rates, probs=probs, model=model, pats=pats, w=w,
+                tips=tips, wd=wd, table=synth.dna_code_table())
+
+
+def engine(d, ctx, prec):
+    e = spr.SprEngine(d["tips"], d["pats"].shape[1], d["model"], d["table"], d["wd"], prec, ctx)
+    e.set_tree(d["tr"])
+    return e
+
+
+def oracle_lnl(d, adj):
+    return SO.lnl(adj, d["tr"].n_tips, d["q"], d["pi"], d["rates"], d["probs"], d["pats"],
+                  d["table"], d["w"])
+
+
+@pytest.mark.parametrize("prec", [64, 48, 32])
+def test_tree_lnl_and_every_move(small, ctx, prec):
+    d = small
+    n = d["tr"].n_tips
+    e = engine(d, ctx, prec)
+    cur = e.get_tree()
+    adj = SO.unroot(cur.left, cur.right, cur.brlen)
+    wsum = float(d["w"].sum())
+    assert close(e.lnl(), oracle_lnl(d, adj), prec, wsum)
+    mv = e.moves()
+    assert sorted(zip(mv.p, mv.u, mv.c, mv.y)) == sorted(SO.moves(adj, n))
+    got = e.scan().cpu().numpy()
+    exp = np.array([oracle_lnl(d, SO.apply_move(adj, *mv[i])) for i in range(len(mv))])
+    ok = close(got, exp, prec, wsum)
+    assert ok.all(), (np.flatnonzero(~ok)[:5], np.max(np.abs(got - exp)))
+    e.close()
+
+
+def test_fitch_of_every_move(small, ctx):
+    d = small
+    n = d["tr"].n_tips
+    e = engine(d, ctx, 48)
+    cur = e.get_tree()
+    adj = SO.unroot(cur.left, cur.right, cur.brlen)
+    masks = spr.code_masks(d["table"])
+    lens, tree_len = e.fitch()
+    assert tree_len == SO.fitch_length(adj, n, d["pats"], masks, d["w"])
+    mv = e.moves()
+    exp = [SO.fitch_length(SO.apply_move(adj, *mv[i]), n, d["pats"], masks, d["w"])
+           for i in range(len(mv))]
+    assert lens.cpu().numpy().tolist() == exp
+    X = e.features().cpu().numpy()
+    assert X.shape == (len(mv), spr.N_FEATURES) and np.isfinite(X).all()
+    dF = (np.array(exp, np.float64) - tree_len) * 100.0 / d["w"].sum()
+    assert np.allclose(X[:, 8], dF, rtol=1e-6, atol=1e-6)
+    e.close()
+
+
+def test_score_apply_and_optimize(small, ctx):
+    d = small
+    n = d["tr"].n_tips
+    e = engine(d, ctx, 64)
+    full = e.scan().cpu().numpy()
+    rng = np.random.default_rng(5)
+    pick = rng.choice(len(full), size=min(17, len(full)), replace=False)
+    got = e.score(pick)
+    assert np.allclose(got, full[pick], rtol=1e-12, atol=0)
+    best = int(np.argmax(full))
+    cur = e.get_tree()
+    adj = SO.unroot(cur.left, cur.right, cur.brlen)
+    mv = e.moves()[best]
+    e.apply(best)
+    assert abs(e.lnl() - full[best]) <= 1e-10 * abs(full[best])
+    new = e.get_tree()
+    new_adj = SO.unroot(new.left, new.right, new.brlen)
+    assert SO.splits(new_adj, n) == SO.splits(SO.apply_move(adj, *mv), n)
+    before = e.lnl()
+    after = e.optimize(40, 1e-8)
+    assert after >= before - 1e-9
+    t = e.get_tree()
+    adj_t = SO.unroot(t.left, t.right, t.brlen)
+    assert abs(oracle_lnl(d, adj_t) - after) <= 1e-9 * abs(after)
+    # every branch is at a local optimum: a 2 % change of any one does not help
+    for a in list(adj_t)[:6]:
+        for b in list(adj_t[a])[:1]:
+            for f in (0.98, 1.02):
+                alt = {v: dict(nb) for v, nb in adj_t.items()}
+                alt[a][b] = alt[b][a] = adj_t[a][b] * f
+                assert oracle_lnl(d, alt) <= after + 1e-4
+    e.close()
+
+
+def test_deep_tree_rescaling(ctx):
+    """A 48-tip caterpillar with long branches drives every vector through
+    the power-of-two rescaling."""
+    import torch
+    rng = np.random.default_rng(7)
+    n = 48
+    tr = T.caterpillar(n, 1.5)
+    spec = synth.random_gtr_spec(rng, 0.5)
+    q, pi, rates, probs = synth.host_model(spec)
+    pats = rng.choice(np.array([1, 2, 4, 8], np.uint8), size=(n, 300))
+    w = rng.integers(1, 4, size=300).astype(np.float64)
+    dev = torch.device("cuda:0")
+    d = dict(tr=tr, q=q, pi=pi, rates=rates, probs=probs, model=M.create(spec, ctx), pats=pats,
+             w=w, tips=torch.from_numpy(pats).to(dev), wd=torch.from_numpy(w).to(dev),
+             table=synth.dna_code_table())
+    e = engine(d, ctx, 48)
+    cur = e.get_tree()
+    adj = SO.unroot(cur.left, cur.right, cur.brlen)
+    lnl = e.lnl()
+    exp = oracle_lnl(d, adj)
+    assert lnl < -1000 and abs(lnl - exp) <= 1e-9 * abs(exp)
+    full = e.scan().cpu().numpy()
+    mv = e.moves()
+    idx = rng.choice(len(mv), size=25, replace=False)
+    exp = np.array([oracle_lnl(d, SO.apply_move(adj, *mv[i])) for i in idx])
+    assert np.all(np.abs(full[idx] - exp) <= 1e-9 * np.abs(exp))
+    e.close()

@@ -1,0 +1,56 @@
+"""CPU: the SPR restatement (oracle/spr_oracle.py) and the random-addition
+parsimony start tree (host code of libphylo_gpu.so, no GPU needed)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import spr_oracle as SO
+from phylocaml_gb300 import spr, synth, tree as T
+
+
+@pytest.mark.parametrize("n", [5, 7, 12])
+def test_oracle_neighbourhood_size(n):
+    """Distinct SPR neighbours of an unrooted binary tree: 2(n-3)(2n-7)."""
+    tr = T.yule(n, np.random.default_rng(n), 0.1)
+    adj = SO.unroot(tr.left, tr.right, tr.brlen)
+    base = SO.splits(adj, n)
+    tops = {SO.splits(SO.apply_move(adj, *m), n) for m in SO.moves(adj, n)} - {base}
+    assert len(tops) == 2 * (n - 3) * (2 * n - 7)
+
+
+def test_oracle_move_keeps_total_length():
+    tr = T.yule(9, np.random.default_rng(3), 0.2)
+    adj = SO.unroot(tr.left, tr.right, tr.brlen)
+    total = sum(t for a in adj for b, t in adj[a].items() if a < b)
+    for m in SO.moves(adj, 9)[:40]:
+        new = SO.apply_move(adj, *m)
+        assert abs(sum(t for a in new for b, t in new[a].items() if a < b) - total) < 1e-12
+
+
+def test_oracle_reroot_roundtrip():
+    tr = T.yule(11, np.random.default_rng(4), 0.2)
+    adj = SO.unroot(tr.left, tr.right, tr.brlen)
+    l, r, b = SO.reroot(adj, 11)
+    adj2 = SO.unroot(l, r, b)
+    assert SO.splits(adj2, 11) == SO.splits(adj, 11)
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_parsimony_start(seed):
+    tr, spec, pats, w = synth.prune_workload(20, 600, seed=seed, mean_brlen=0.1, ambiguity=0.05)
+    table = synth.dna_code_table()
+    start, length = spr.parsimony_start(pats, table, w, seed=seed, brlen=0.05)
+    n = 20
+    adj = SO.unroot(start.left, start.right, start.brlen)
+    assert len(adj) == 2 * n - 2 and all(len(adj[v]) == (1 if v < n else 3) for v in adj)
+    masks = spr.code_masks(table)
+    assert length == SO.fitch_length(adj, n, pats, masks, w)
+    # no single SPR move of the start tree is shorter by more than what
+    # stepwise addition can miss; at least it is far better than the true
+    # tree's random relabelling
+    rnd = T.yule(n, np.random.default_rng(99), 0.1)
+    adj_r = SO.unroot(rnd.left, rnd.right, rnd.brlen)
+    assert length < SO.fitch_length(adj_r, n, pats, masks, w)
+    again, length2 = spr.parsimony_start(pats, table, w, seed=seed, brlen=0.05)
+    assert length2 == length and (again.left == start.left).all()
