@@ -123,6 +123,17 @@ SIGNATURES: dict[str, tuple] = {
     "pgpu_spr_apply": (_I, [_P, C.c_int64]),
     "pgpu_spr_optimize": (_I, [_P, _I, C.c_double, _DP]),
     "pgpu_spr_lengths": (_I, [_P, _P, _P, _P]),
+    "pgpu_mlp_n_params": (C.c_longlong, []),
+    "pgpu_mlp_create": (_I, [_P, C.c_uint64, _I, C.POINTER(_P)]),
+    "pgpu_mlp_destroy": (None, [_P]),
+    "pgpu_mlp_get_params": (_I, [_P, _P]),
+    "pgpu_mlp_set_params": (_I, [_P, _P]),
+    "pgpu_mlp_get_norm": (_I, [_P, _P, _P]),
+    "pgpu_mlp_fit_norm": (_I, [_P, _P, _SZ]),
+    "pgpu_mlp_forward": (_I, [_P, _P, _SZ, _P]),
+    "pgpu_mlp_grads": (_I, [_P, _P, _P, _P, _SZ, _P, C.POINTER(C.c_float)]),
+    "pgpu_mlp_train_step": (_I, [_P, _P, _P, _P, _SZ, C.c_float, C.c_float,
+                                 C.POINTER(C.c_float)]),
     "pgpu_parsimony_stepwise": (_I, [C.c_int32, _P, _SZ, _SZ, _P, _I, _P, C.c_uint64, C.c_double,
                                      _P, _P, _P, _U64P]),
 }

@@ -1,0 +1,187 @@
+"""SPR hill climbing on the GPU: plain exhaustive SPR and the learned proposal.
+
+phylocaml's tree search is a TODO (lib/treeNeighborhoods.ml:27-75); these are
+the two searches the learned part is judged by.  Both start from the same
+tree, score moves with the same exact kernel (SprEngine.scan / score: the
+lnL of the rearranged tree, no branch-length re-estimation), accept the best
+move when it gains more than ``eps``, re-estimate branch lengths a few
+Newton rounds after each accepted move, and stop at a tree where no SPR move
+gains more than ``eps``.  Both finish with the same full branch-length
+optimisation, so trees of equal topology end at equal lnL.
+
+* ``exhaustive_spr`` scores every move every round.
+* ``learned_spr`` scores every move once to train the network (the first,
+  exhaustive round), then each round ranks all moves with the MLP on their
+  features and scores only the top k exactly; the network keeps training
+  on every exactly scored move.  When none of the k gains, it falls back to
+  an exhaustive round, so it also stops only where no move gains.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .spr import SprEngine
+from .tree import RootedTree
+
+
+@dataclass
+class SearchResult:
+    lnl: float                 # after the final branch-length optimisation
+    lnl_search: float          # when the move search stopped
+    rounds: int
+    accepted: int
+    exact_moves: int           # moves whose lnL was computed exactly
+    exhaustive_rounds: int
+    seconds: float
+    tree: RootedTree
+    trace: list = field(default_factory=list)   # (seconds, lnL) after each accepted move
+    train_seconds: float = 0.0
+
+
+def _target(dl):
+    """Training target: asinh of the lnL change (keeps the thousands of very
+    bad moves from swamping the few good ones)."""
+    return np.arcsinh(dl)
+
+
+def exhaustive_spr(eng: SprEngine, eps: float = 1e-3, smooth_passes: int = 2,
+                   final_passes: int = 60, max_rounds: int = 10000) -> SearchResult:
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lnl = eng.lnl()
+    rounds = accepted = exact = 0
+    trace = []
+    while rounds < max_rounds:
+        rounds += 1
+        scores = eng.scan().cpu().numpy()
+        exact += scores.size
+        best = int(np.argmax(scores))
+        gain = float(scores[best]) - lnl
+        if not gain > eps:
+            break
+        eng.apply(best)
+        lnl = eng.optimize(smooth_passes, 1e-4)
+        accepted += 1
+        trace.append((time.perf_counter() - t0, lnl))
+    lnl_search = lnl
+    final = eng.optimize(final_passes, 1e-8)
+    torch.cuda.synchronize()
+    return SearchResult(final, lnl_search, rounds, accepted, exact, rounds,
+                        time.perf_counter() - t0, eng.get_tree(), trace)
+
+
+class _Replay:
+    """Exactly scored moves (features, target) kept on the device."""
+
+    def __init__(self, torch, device, cap: int):
+        self.torch = torch
+        self.X = torch.empty((cap, 64), dtype=torch.float32, device=device)
+        self.t = torch.empty(cap, dtype=torch.float32, device=device)
+        self.cap, self.n, self.pos = cap, 0, 0
+
+    def add(self, X, t):
+        k = X.shape[0]
+        if k >= self.cap:
+            X, t, k = X[-self.cap:], t[-self.cap:], self.cap
+        end = self.pos + k
+        if end <= self.cap:
+            self.X[self.pos:end] = X
+            self.t[self.pos:end] = t
+        else:
+            a = self.cap - self.pos
+            self.X[self.pos:] = X[:a]
+            self.t[self.pos:] = t[:a]
+            self.X[:k - a] = X[a:]
+            self.t[:k - a] = t[a:]
+        self.pos = end % self.cap
+        self.n = min(self.cap, self.n + k)
+
+    def sample(self, gen, b):
+        idx = self.torch.randint(0, self.n, (b,), device=self.X.device, generator=gen)
+        return self.X[idx].contiguous(), self.t[idx].contiguous()
+
+
+def learned_spr(eng: SprEngine, net, k: int = 32, eps: float = 1e-3, smooth_passes: int = 2,
+                final_passes: int = 60, boot_steps: int = 400, round_steps: int = 8,
+                batch: int = 1024, lr: float = 2e-3, seed: int = 0,
+                max_rounds: int = 10000) -> SearchResult:
+    """``net`` is a phylocaml_gb300.mlp.MLP with max_batch >= batch."""
+    import torch
+    dev = eng.device
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    train_s = 0.0
+    lnl = eng.lnl()
+    rounds = accepted = exact = exhaustive = 0
+    trace = []
+    replay = _Replay(torch, dev, 1 << 20)
+    recent = _Replay(torch, dev, 1 << 14)
+    fitted = False
+
+    def train(steps):
+        nonlocal train_s
+        t = time.perf_counter()
+        half = batch // 2
+        for _ in range(steps):
+            Xa, ta = replay.sample(gen, batch - half if recent.n else batch)
+            if recent.n:
+                Xb, tb = recent.sample(gen, half)
+                Xa, ta = torch.cat([Xa, Xb]), torch.cat([ta, tb])
+            net.train_step(Xa, ta, None, lr, 1e-4, sync=False)
+        train_s += time.perf_counter() - t
+
+    def exhaustive_round():
+        nonlocal exact, exhaustive, fitted
+        X = eng.features()
+        scores = eng.scan().cpu().numpy()
+        exact += scores.size
+        exhaustive += 1
+        if not fitted:
+            net.fit_norm(X)
+            fitted = True
+        replay.add(X, torch.from_numpy(_target(scores - lnl).astype(np.float32)).to(dev))
+        return scores
+
+    while rounds < max_rounds:
+        rounds += 1
+        if rounds == 1:
+            scores = exhaustive_round()
+            train(boot_steps)
+            best = int(np.argmax(scores))
+            gain = float(scores[best]) - lnl
+        else:
+            X = eng.features()
+            pred = net.forward(X).cpu().numpy()
+            kk = min(k, pred.size)
+            top_h = np.argpartition(-pred, kk - 1)[:kk]
+            got = eng.score(top_h)
+            exact += kk
+            tgt = torch.from_numpy(_target(got - lnl).astype(np.float32)).to(dev)
+            Xk = X[torch.from_numpy(top_h).to(dev)]
+            recent.add(Xk, tgt)
+            replay.add(Xk, tgt)
+            j = int(np.argmax(got))
+            best, gain = int(top_h[j]), float(got[j]) - lnl
+            if not gain > eps:
+                # nothing among the network's picks: fall back to every move
+                scores = exhaustive_round()
+                best = int(np.argmax(scores))
+                gain = float(scores[best]) - lnl
+            train(round_steps)
+        if not gain > eps:
+            break
+        eng.apply(best)
+        lnl = eng.optimize(smooth_passes, 1e-4)
+        accepted += 1
+        trace.append((time.perf_counter() - t0, lnl))
+    lnl_search = lnl
+    final = eng.optimize(final_passes, 1e-8)
+    torch.cuda.synchronize()
+    return SearchResult(final, lnl_search, rounds, accepted, exact, exhaustive,
+                        time.perf_counter() - t0, eng.get_tree(), trace, train_s)
