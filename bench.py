@@ -702,13 +702,99 @@ def bench_batch(args, rank, world, local):
     return rec
 
 
+
+# ---- learned SPR proposal vs exhaustive SPR --------------------------------
+SPR_TAXA, SPR_SITES = 256, 50_000
+
+
+def bench_spr(args, rank, world, local):
+    """256-taxon, 50,000-site DNA alignment simulated as the prune workload
+    (GTR+Gamma4, branch lengths ~ Exp(0.1)), search from a random-addition
+    parsimony tree.  Both arms start from the same tree (branch lengths
+    optimised), score moves with the same exact kernel (float-pair form) and
+    stop where no SPR move gains more than 1e-3; the learned arm ranks all
+    moves with the MLP and scores the top 32 exactly, falling back to an
+    exhaustive round when none of its picks gains.  `value` = learned wall
+    time / exhaustive wall time."""
+    import torch
+    from phylocaml_gb300 import _native, mlmodel as M, mlp, search, spr, synth
+    from oracle import spr_oracle as SO
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    tr, spec, pats, w = synth.prune_workload(SPR_TAXA, SPR_SITES, seed=6 + rank, mean_brlen=0.1)
+    table = synth.dna_code_table()
+    n_pat = pats.shape[1]
+    ctx = _native.Context(local)
+    model = M.create(spec, ctx)
+    tips = torch.from_numpy(pats).to(dev)
+    wd = torch.from_numpy(w).to(dev)
+    t = time.perf_counter()
+    start, plen = spr.parsimony_start(pats, table, w, seed=6 + rank, brlen=0.05)
+    t_start = time.perf_counter() - t
+    eng = spr.SprEngine(tips, n_pat, model, table, wd, 48, ctx)
+    eng.set_tree(start)
+    l0 = eng.optimize(20, 1e-6)
+    start_opt = eng.get_tree()
+    nm = eng.n_moves
+    # one exhaustive scan through the C ABI (it synchronises on return)
+    out = torch.empty(nm, dtype=torch.float64, device=dev)
+    for _ in range(2):
+        eng.scan(out)
+    torch.cuda.synchronize(dev)
+    reps = 3
+    t = time.perf_counter()
+    for _ in range(reps):
+        eng.scan(out)
+    scan_ms = (time.perf_counter() - t) / reps * 1e3
+    arms = {}
+    for arm in ("exhaustive", "learned"):
+        eng.set_tree(start_opt)
+        if arm == "exhaustive":
+            r = search.exhaustive_spr(eng)
+        else:
+            net = mlp.MLP(seed=1, max_batch=1024, ctx=ctx)
+            r = search.learned_spr(eng, net)
+            net.close()
+        arms[arm] = r
+    ex, le = arms["exhaustive"], arms["learned"]
+    n = SPR_TAXA
+    same = SO.splits(SO.unroot(ex.tree.left, ex.tree.right, ex.tree.brlen), n) == \
+        SO.splits(SO.unroot(le.tree.left, le.tree.right, le.tree.brlen), n)
+
+    def arm_rec(r):
+        return {"seconds": r.seconds, "final_lnl": r.lnl, "search_lnl": r.lnl_search,
+                "rounds": r.rounds, "accepted_moves": r.accepted, "exactly_scored_moves": r.exact_moves,
+                "exhaustive_rounds": r.exhaustive_rounds,
+                "timing_s": {k: round(v, 4) for k, v in r.timing.items()}}
+    # full-tree equivalent: re-pruning every neighbour would update
+    # (n - 2) internal nodes x patterns per move
+    rec = {
+        "metric": "wall time to the SPR optimum, learned proposal / exhaustive SPR (same final lnL +-1e-3)",
+        "value": le.seconds / ex.seconds, "unit": "ratio", "higher_is_better": False,
+        "target": "<= 1/3",
+        "config": {"workload": "learned SPR: 256-taxon Yule tree (BL ~ Exp(0.1)), 50,000 GTR+Gamma4 "
+                               "DNA sites compressed to weighted patterns, random-addition parsimony "
+                               "start, MLP 64-256-256-256-1 (BF16, FP32 accumulate), top-32 proposals",
+                   "n_patterns": n_pat, "n_moves": nm, "precision": "fp32x2"},
+        "start": {"parsimony_length": plen, "seconds": t_start, "lnl_after_brlen": l0},
+        "exhaustive": arm_rec(ex), "learned": arm_rec(le),
+        "dlnl_learned_minus_exhaustive": le.lnl - ex.lnl,
+        "reaches_exhaustive_optimum": bool(le.lnl >= ex.lnl - 1e-3),
+        "same_topology": bool(same),
+        "scan": {"ms_per_exhaustive_scan": scan_ms, "moves_per_s": nm / (scan_ms * 1e-3),
+                 "full_tree_equivalent_updates_per_s": nm * (n - 2) * n_pat / (scan_ms * 1e-3)},
+    }
+    eng.close()
+    ctx.close()
+    return rec
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["prune", "fitch", "batch", "all"], default="all")
+    ap.add_argument("--workload", choices=["prune", "fitch", "batch", "spr", "all"], default="all")
     # smaller runs for profiler captures: a subset of the pruning forms, fewer batch variants
     ap.add_argument("--prune-forms", default="32,48,64")
     ap.add_argument("--batch-variants", type=int, default=BATCH_VARIANTS)
@@ -716,7 +802,7 @@ def main():
     args.warmup = max(args.warmup, 3)
     args.prune_forms = {int(f) for f in args.prune_forms.split(",") if f}
     rank, world, local = dist_info()
-    head = args.workload if args.workload in ("fitch", "batch") else "prune"
+    head = args.workload if args.workload in ("fitch", "batch", "spr") else "prune"
 
     if args.impl == "reference":
         if rank != 0:
@@ -739,9 +825,13 @@ def main():
             rec["fitch"] = bench_fitch(args, rank, world, local)
             args.steps = steps_given if steps_given is not None else 3
             rec["batch"] = bench_batch(args, rank, world, local)
+            if rank == 0:
+                rec["spr"] = bench_spr(args, rank, world, local)
     elif head == "batch":
         args.steps = steps_given if steps_given is not None else 3
         rec = bench_batch(args, rank, world, local)
+    elif head == "spr":
+        rec = bench_spr(args, rank, world, local)
     else:
         args.steps = steps_given if steps_given is not None else 2000
         rec = bench_fitch(args, rank, world, local)

@@ -26,6 +26,7 @@
 // HBM traffic is therefore the compulsory minimum: each tip row read once,
 // each internal row written once, plus weights and per-site counts.
 #include <algorithm>
+#include <cstring>
 
 #include "pgpu_internal.cuh"
 
@@ -352,6 +353,221 @@ __global__ void __launch_bounds__(160) fitch_tree_kernel(const FitchTreeArgs p) 
   }
 }
 
+// ---------------------------------------------------------------------------
+// tree kernel, segmented form.  One CTA of FS_K warps per 128-word slice
+// (4 words per thread): the postorder is cut into up to FS_K disjoint
+// subtrees (segments), warp w walks segment w with its own stack, and each
+// thread keeps its next FS_P tip slices in flight with cp.async (LDGSTS)
+// into a per-warp ring.  Segment results meet in shared memory, where warp 0
+// finishes the few nodes above the segments.  Splitting the walk multiplies
+// the warps per SM by up to FS_K, which the single postorder walk cannot.
+// ---------------------------------------------------------------------------
+constexpr int FS_K = 4;   // segments (warps) per CTA
+constexpr int FS_P = 4;   // tip slices in flight per thread
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, bool valid) {
+  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(valid ? 16 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+struct FitchSplitArgs {
+  const uint32_t *tips, *weights;
+  uint32_t *node_sets, *site_cost;
+  unsigned long long *total;
+  const int4 *ops, *seg, *top;
+  const int32_t *tip_seq;
+  size_t ld, n_words, n_sites;
+  int32_t n_tips;
+  int n_seg, n_top, depth;
+};
+
+__host__ __device__ inline size_t split_smem(int depth) {
+  // per warp: ring [FS_P][32] + stack [depth][32] uint4; then segment and
+  // top results [FS_K][32] uint4 each; then the per-site count exchange
+  return (size_t)FS_K * (FS_P + depth) * 32 * 16 + 2 * (size_t)FS_K * 32 * 16 + 32 * 32 * 4;
+}
+
+template <int LB>
+__global__ void __launch_bounds__(FS_K * 32) fitch_tree_split_kernel(const FitchSplitArgs p) {
+  constexpr int PER = Lanes<LB>::PER;
+  constexpr uint32_t FLUSH = Lanes<LB>::FLUSH;
+  constexpr uint32_t LSB = Lanes<LB>::H >> (LB - 1);
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  uint4 *ring = reinterpret_cast<uint4 *>(smem) + (size_t)w * (FS_P + p.depth) * 32;
+  uint4 *stk = ring + FS_P * 32;
+  uint4 *segres = reinterpret_cast<uint4 *>(smem) + (size_t)FS_K * (FS_P + p.depth) * 32;
+  uint4 *topres = segres + FS_K * 32;
+  uint32_t *sitecnt = reinterpret_cast<uint32_t *>(topres + FS_K * 32);   // [32 lanes][4*PER]
+  const size_t word0 = (size_t)blockIdx.x * 128 + 4 * (size_t)lane;
+  const bool active = word0 < p.ld;
+  uint4 valid;
+  valid.x = valid_lanes<LB>(word0 + 0, p.n_sites);
+  valid.y = valid_lanes<LB>(word0 + 1, p.n_sites);
+  valid.z = valid_lanes<LB>(word0 + 2, p.n_sites);
+  valid.w = valid_lanes<LB>(word0 + 3, p.n_sites);
+  const uint32_t *col = p.tips + (active ? word0 : 0);
+  uint4 cnt = make_uint4(0, 0, 0, 0);
+  uint32_t acc[4][PER];
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int l = 0; l < PER; ++l) acc[q][l] = 0;
+  uint32_t since = 0;
+  auto count = [&](const uint4 &e) {
+    cnt.x += e.x & valid.x & LSB;
+    cnt.y += e.y & valid.y & LSB;
+    cnt.z += e.z & valid.z & LSB;
+    cnt.w += e.w & valid.w & LSB;
+    if (LB < 32 && ++since == FLUSH) {
+#pragma unroll
+      for (int l = 0; l < PER; ++l) {
+        acc[0][l] += (cnt.x >> (l * LB)) & FLUSH;
+        acc[1][l] += (cnt.y >> (l * LB)) & FLUSH;
+        acc[2][l] += (cnt.z >> (l * LB)) & FLUSH;
+        acc[3][l] += (cnt.w >> (l * LB)) & FLUSH;
+      }
+      cnt = make_uint4(0, 0, 0, 0);
+      since = 0;
+    }
+  };
+  auto store = [&](int k, const uint4 &med) {
+    if (active) __stcs(reinterpret_cast<uint4 *>(p.node_sets + (size_t)k * p.ld + word0), med);
+  };
+
+  // ---- phase 1: warp w walks segment w ----
+  if (w < p.n_seg) {
+    const int4 sg = p.seg[w];   // {op_off, n_ops, tip_off, n_tips}
+    const int32_t *tseq = p.tip_seq + sg.z;
+    int issued = 0, consumed = 0;
+    auto issue = [&]() {
+      if (issued < sg.w)
+        cp_async16(&ring[(issued % FS_P) * 32 + lane], col + (size_t)__ldg(tseq + issued) * p.ld, active);
+      cp_async_commit();   // empty groups keep the count in step
+      ++issued;
+    };
+#pragma unroll
+    for (int j = 0; j < FS_P; ++j) issue();
+    int sp = 0;
+    uint4 top = make_uint4(0, 0, 0, 0);
+    bool top_valid = false;
+    auto pop = [&]() -> uint4 {
+      if (top_valid) {
+        top_valid = false;
+        return top;
+      }
+      return stk[(--sp) * 32 + lane];
+    };
+    const int4 *ops = p.ops + sg.x;
+    int4 op = __ldg(ops);
+    for (int i = 0; i < sg.y; ++i) {
+      const int4 next = i + 1 < sg.y ? __ldg(ops + i + 1) : op;
+      const bool ta = op.y < p.n_tips, tb = op.z < p.n_tips;
+      uint4 x = make_uint4(0, 0, 0, 0), y = make_uint4(0, 0, 0, 0);
+      if (!tb) y = pop();
+      if (!ta) x = pop();
+      // a step's tips are the next ones of the sequence: the first needs all
+      // copy groups but the FS_P-1 newest, the second all but the FS_P-2 newest
+      if (ta) {
+        cp_async_wait<FS_P - 1>();
+        x = ring[(consumed % FS_P) * 32 + lane];
+        ++consumed;
+        if (tb) {
+          cp_async_wait<FS_P - 2>();
+          y = ring[(consumed % FS_P) * 32 + lane];
+          ++consumed;
+        }
+      } else if (tb) {
+        cp_async_wait<FS_P - 1>();
+        y = ring[(consumed % FS_P) * 32 + lane];
+        ++consumed;
+      }
+      uint4 e;
+      const uint4 med = fitch_quad<LB>(x, y, valid, e);
+      count(e);
+      // slots read this step are refilled only once their values are in use
+      while (issued < consumed + FS_P) issue();
+      if (top_valid) stk[(sp++) * 32 + lane] = top;
+      top = med;
+      top_valid = true;
+      store(op.x, med);
+      op = next;
+    }
+    cp_async_wait<0>();
+    segres[w * 32 + lane] = top;
+  }
+  __syncthreads();
+  // ---- phase 2: warp 0 joins the segments ----
+  if (w == 0) {
+    for (int i = 0; i < p.n_top; ++i) {
+      const int4 op = __ldg(p.top + i);
+      uint4 c[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int ref = h == 0 ? op.y : op.z;
+        if (ref >= 0)
+          c[h] = active ? __ldcs(reinterpret_cast<const uint4 *>(col + (size_t)ref * p.ld))
+                        : make_uint4(0, 0, 0, 0);
+        else if (ref > -100)
+          c[h] = segres[(-1 - ref) * 32 + lane];
+        else
+          c[h] = topres[(-100 - ref) * 32 + lane];
+      }
+      uint4 e;
+      const uint4 med = fitch_quad<LB>(c[0], c[1], valid, e);
+      count(e);
+      topres[i * 32 + lane] = med;
+      store(op.x, med);
+    }
+  }
+  // ---- phase 3: per-site counts of all warps, then the weighted total ----
+  if (LB < 32) {
+#pragma unroll
+    for (int l = 0; l < PER; ++l) {
+      acc[0][l] += (cnt.x >> (l * LB)) & FLUSH;
+      acc[1][l] += (cnt.y >> (l * LB)) & FLUSH;
+      acc[2][l] += (cnt.z >> (l * LB)) & FLUSH;
+      acc[3][l] += (cnt.w >> (l * LB)) & FLUSH;
+    }
+  } else {
+    acc[0][0] += cnt.x;
+    acc[1][0] += cnt.y;
+    acc[2][0] += cnt.z;
+    acc[3][0] += cnt.w;
+  }
+  for (int i = tid; i < 32 * 4 * PER; i += FS_K * 32) sitecnt[i] = 0;
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int l = 0; l < PER; ++l)
+      if (acc[q][l]) atomicAdd(&sitecnt[(q * PER + l) * 32 + lane], acc[q][l]);
+  __syncthreads();
+  if (w == 0) {
+    unsigned long long wsum = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const size_t s0 = (word0 + q) * PER;
+#pragma unroll
+      for (int l = 0; l < PER; ++l) {
+        const size_t s = s0 + l;
+        if (active && s < p.n_sites) {
+          const uint32_t v = sitecnt[(q * PER + l) * 32 + lane];
+          if (p.site_cost) p.site_cost[s] = v;
+          const uint32_t wt = p.weights ? __ldg(p.weights + s) : 1u;
+          wsum += (unsigned long long)wt * v;
+        }
+      }
+    }
+    wsum = warp_sum_u64(wsum);
+    if (lane == 0 && wsum) atomicAdd(p.total, wsum);
+  }
+}
+
 template <int LB>
 pgpu_status launch_pair(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b, const uint32_t *w,
                         uint32_t *out, size_t n_words, size_t n_sites,
@@ -443,6 +659,149 @@ cudaError_t launch_tree(cudaStream_t stream, int lb, const FitchTreeArgs &args, 
   }
 }
 
+
+// Cuts the postorder into up to FS_K segments: repeatedly split the largest
+// remaining subtree at its root (the root joins the top part) while fewer
+// than FS_K subtrees remain and the largest has at least two internal
+// nodes.  Each segment is scheduled like the whole tree (Sethi-Ullman order:
+// the child with the larger stack need first).
+pgpu_status build_split(pgpu_ctx *ctx, const pgpu_tree *tree, SplitSchedule *out) {
+  TreeSchedule check;
+  PGPU_TRY(pgpu_build_schedule(ctx, tree, &check));   // validates the tree
+  const int32_t n = tree->n_tips, n_int = n - 1;
+  const int32_t *L = tree->left, *R = tree->right;
+  std::vector<int32_t> size(n_int, 1), need(2 * n - 1, 0);
+  std::vector<uint8_t> swp(n_int, 0);
+  for (int32_t k = 0; k < n_int; ++k) {
+    const int32_t a = L[k], b = R[k];
+    if (a >= n) size[k] += size[a - n];
+    if (b >= n) size[k] += size[b - n];
+    const int32_t ha = a >= n, hb = b >= n;
+    const int32_t a_first = std::max(need[a], ha + need[b]);
+    const int32_t b_first = std::max(need[b], hb + need[a]);
+    swp[k] = b_first < a_first;
+    need[n + k] = std::max(std::min(a_first, b_first), 1);
+  }
+  std::vector<int32_t> heap{n_int - 1};
+  std::vector<uint8_t> is_top(n_int, 0);
+  auto by_size = [&](int32_t x, int32_t y) { return size[x] < size[y]; };
+  int n_split = 0;
+  while ((int)heap.size() < FS_K && !heap.empty() && n_split < FS_K) {
+    std::pop_heap(heap.begin(), heap.end(), by_size);
+    const int32_t k = heap.back();
+    if (size[k] < 2) {
+      std::push_heap(heap.begin(), heap.end(), by_size);
+      break;
+    }
+    heap.pop_back();
+    is_top[k] = 1;
+    ++n_split;
+    for (const int32_t c : {L[k], R[k]})
+      if (c >= n) {
+        heap.push_back(c - n);
+        std::push_heap(heap.begin(), heap.end(), by_size);
+      }
+  }
+  std::sort(heap.begin(), heap.end(), [&](int32_t x, int32_t y) { return size[x] > size[y]; });
+  SplitSchedule sp;
+  sp.n_seg = (int)heap.size();
+  std::vector<int32_t> seg_of(n_int, -1), top_of(n_int, -1);
+  for (int i = 0; i < sp.n_seg; ++i) seg_of[heap[i]] = i;
+  for (int i = 0; i < sp.n_seg; ++i) {
+    const int32_t root = heap[i];
+    const int op_off = (int)sp.ops.size(), tip_off = (int)sp.tips.size();
+    struct Fr {
+      int32_t v;
+      bool done;
+    };
+    std::vector<Fr> st{{n + root, false}};
+    int height = 0, depth = 0;
+    while (!st.empty()) {
+      const Fr f = st.back();
+      st.pop_back();
+      const int32_t k = f.v - n;
+      const int32_t first = swp[k] ? R[k] : L[k], second = swp[k] ? L[k] : R[k];
+      if (!f.done) {
+        st.push_back({f.v, true});
+        if (second >= n) st.push_back({second, false});
+        if (first >= n) st.push_back({first, false});
+        continue;
+      }
+      sp.ops.push_back(make_int4(k, first, second, 0));
+      if (first < n) sp.tips.push_back(first);
+      if (second < n) sp.tips.push_back(second);
+      height += 1 - (first >= n) - (second >= n);
+      depth = std::max(depth, height);
+    }
+    sp.max_depth = std::max(sp.max_depth, depth);
+    sp.seg.push_back(make_int4(op_off, (int)sp.ops.size() - op_off, tip_off, (int)sp.tips.size() - tip_off));
+  }
+  int n_top = 0;
+  for (int32_t k = 0; k < n_int; ++k) {
+    if (!is_top[k]) continue;
+    int32_t ref[2];
+    for (int h = 0; h < 2; ++h) {
+      const int32_t c = h == 0 ? L[k] : R[k];
+      ref[h] = c < n ? c : seg_of[c - n] >= 0 ? -1 - seg_of[c - n] : -100 - top_of[c - n];
+    }
+    top_of[k] = n_top++;
+    sp.top.push_back(make_int4(k, ref[0], ref[1], 0));
+  }
+  if (n_top > FS_K)
+    return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: %d joining nodes (at most %d)", n_top, FS_K);
+  *out = std::move(sp);
+  return PGPU_OK;
+}
+
+// the split schedule of `tree`, resident in BUF_SPLIT ({ops, seg, top, tips})
+pgpu_status split_device(pgpu_ctx *ctx, const pgpu_tree *tree, const int4 **ops, const int4 **seg,
+                         const int4 **top, const int32_t **tips) {
+  const int32_t n_int = tree->n_tips - 1;
+  const bool hit = ctx->split_valid && (int32_t)ctx->split_left.size() == n_int &&
+                   std::memcmp(ctx->split_left.data(), tree->left, n_int * 4) == 0 &&
+                   std::memcmp(ctx->split_right.data(), tree->right, n_int * 4) == 0;
+  const SplitSchedule &sp = ctx->split;
+  if (!hit) {
+    ctx->split_valid = false;
+    PGPU_TRY(build_split(ctx, tree, &ctx->split));
+    const size_t bytes = 16 * (sp.ops.size() + sp.seg.size() + sp.top.size()) + 4 * sp.tips.size();
+    void *d;
+    PGPU_TRY(pgpu_buf(ctx, BUF_SPLIT, std::max<size_t>(bytes, 16), &d));
+    std::vector<unsigned char> h(std::max<size_t>(bytes, 16));
+    size_t off = 0;
+    auto put = [&](const void *src, size_t b) {
+      if (b) std::memcpy(h.data() + off, src, b);
+      off += b;
+    };
+    put(sp.ops.data(), 16 * sp.ops.size());
+    put(sp.seg.data(), 16 * sp.seg.size());
+    put(sp.top.data(), 16 * sp.top.size());
+    put(sp.tips.data(), 4 * sp.tips.size());
+    PGPU_CUDA(ctx, cudaMemcpyAsync(d, h.data(), bytes, cudaMemcpyHostToDevice, ctx->stream));
+    PGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // h is a temporary
+    ctx->split_left.assign(tree->left, tree->left + n_int);
+    ctx->split_right.assign(tree->right, tree->right + n_int);
+    ctx->split_valid = true;
+  }
+  const int4 *base = static_cast<const int4 *>(ctx->buf[BUF_SPLIT]);
+  *ops = base;
+  *seg = base + sp.ops.size();
+  *top = *seg + sp.seg.size();
+  *tips = reinterpret_cast<const int32_t *>(*top + sp.top.size());
+  return PGPU_OK;
+}
+
+template <int LB>
+cudaError_t launch_split(cudaStream_t stream, const FitchSplitArgs &a, size_t tiles) {
+  const size_t smem = split_smem(a.depth);
+  cudaError_t e = cudaFuncSetAttribute(fitch_tree_split_kernel<LB>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)std::max<size_t>(smem, 48 * 1024));
+  if (e != cudaSuccess) return e;
+  fitch_tree_split_kernel<LB><<<(unsigned)tiles, FS_K * 32, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
 pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips, size_t ld,
                      const uint32_t *weights, size_t n_sites, int lb, uint32_t *node_sets,
                      uint32_t *site_cost, uint64_t *total) {
@@ -454,40 +813,39 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
                         ld, n_words);
   if (((uintptr_t)tips | (uintptr_t)node_sets) & 15)
     return pgpu_set_err(ctx, PGPU_ERR_ARG, "fitch_tree: tip and node rows must be 16-byte aligned");
-  const TreeSchedule *sch;
-  const int4 *dops;
-  const int32_t *dseq;
-  PGPU_TRY(pgpu_schedule_device(ctx, tree, &sch, &dops, &dseq));
-  const int32_t n = tree->n_tips;
+  if (!tree || tree->n_tips < 2) return pgpu_set_err(ctx, PGPU_ERR_ARG, "fitch_tree: need at least 2 tips");
+  FitchSplitArgs a;
+  PGPU_TRY(split_device(ctx, tree, &a.ops, &a.seg, &a.top, &a.tip_seq));
   cudaStream_t s = ctx->stream;
   PGPU_CUDA(ctx, cudaMemsetAsync(total, 0, sizeof(uint64_t), s));
   if (n_words == 0) return PGPU_OK;
-
-  const int depth = sch->max_depth;
-  const FitchPlan pl = fitch_plan(n_words, depth, ctx->num_sms, ctx->smem_optin);
-  if (pl.smem > ctx->smem_optin)
+  const SplitSchedule &sp = ctx->split;
+  a.tips = tips;
+  a.weights = weights;
+  a.node_sets = node_sets;
+  a.site_cost = site_cost;
+  a.total = reinterpret_cast<unsigned long long *>(total);
+  a.ld = ld;
+  a.n_words = n_words;
+  a.n_sites = n_sites;
+  a.n_tips = tree->n_tips;
+  a.n_seg = sp.n_seg;
+  a.n_top = (int)sp.top.size();
+  a.depth = std::max(sp.max_depth, 1);
+  if (split_smem(a.depth) > ctx->smem_optin)
     return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: tree needs a stack of %d rows; too deep",
-                        depth);
-  FitchTreeArgs args;
-  args.tips = tips;
-  args.weights = weights;
-  args.node_sets = node_sets;
-  args.site_cost = site_cost;
-  args.total = reinterpret_cast<unsigned long long *>(total);
-  args.ops = dops;
-  args.tip_seq = dseq;
-  args.flag = ctx->d_flag;
-  args.ld = ld;
-  args.n_words = n_words;
-  args.n_sites = n_sites;
-  args.n_tips = n;
-  args.n_ops = (int32_t)sch->ops.size();
-  args.W = (int)pl.W;
-  args.depth = depth;
-  const cudaError_t e = launch_tree(ctx->stream, lb, args, pl);
+                        a.depth);
+  const size_t tiles = (n_words + 127) / 128;
+  cudaError_t e;
+  switch (lb) {
+    case 4: e = launch_split<4>(s, a, tiles); break;
+    case 8: e = launch_split<8>(s, a, tiles); break;
+    case 16: e = launch_split<16>(s, a, tiles); break;
+    default: e = launch_split<32>(s, a, tiles); break;
+  }
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
-    return pgpu_set_err(ctx, PGPU_ERR_CUDA, "launch of fitch_tree_kernel failed: %s",
+    return pgpu_set_err(ctx, PGPU_ERR_CUDA, "launch of fitch_tree_split_kernel failed: %s",
                         cudaGetErrorString(e));
   }
   ctx->launches++;

@@ -30,6 +30,7 @@ enum {
   BUF_H,
   BUF_I,
   BUF_J,
+  BUF_SPLIT,
   BUF_COUNT
 };
 
@@ -46,6 +47,19 @@ struct TreeSchedule {
   std::vector<SchedOp> ops;        // evaluation order
   std::vector<int32_t> tip_seq;    // tips in the order the ops read them
   int max_depth = 0;               // largest stack height reached
+};
+
+// The postorder cut into up to 4 disjoint subtrees (segments), each a
+// stack-machine schedule of its own, plus the few nodes above them (top).
+// Segment ops read tips from their own tip sequence and internal children
+// from their own stack; a top op's child reference is a tip id (>= 0), a
+// segment result (-1 - s) or an earlier top result (-100 - t).
+struct SplitSchedule {
+  int n_seg = 0, max_depth = 0;
+  std::vector<int4> ops;       // segment ops, segments one after another
+  std::vector<int32_t> tips;   // segment tip sequences, one after another
+  std::vector<int4> seg;       // {op_off, n_ops, tip_off, n_tips}
+  std::vector<int4> top;       // {k, ref_a, ref_b, 0} in postorder
 };
 
 struct pgpu_ctx {
@@ -66,6 +80,10 @@ struct pgpu_ctx {
   bool sched_valid = false;
   std::vector<int32_t> sched_left, sched_right;
   TreeSchedule sched;
+  // the last tree's segment schedule, resident in BUF_SPLIT
+  bool split_valid = false;
+  std::vector<int32_t> split_left, split_right;
+  SplitSchedule split;
   // double-buffered pinned staging of small per-call parameters
   void *stage_h[2] = {};
   void *stage_d[2] = {};

@@ -90,10 +90,11 @@ struct PruneLayout {
   }
 };
 
-// One CTA: 32 producer threads + PR_THREADS consumers.  Consumer c works on
-// pattern c / RT of the tile and rate class c % RT (RT lanes per pattern,
-// R <= RT of them active).  Each thread holds the 4 state values of its rate
-// class; the RT lanes of a pattern agree on rescaling through shuffles.
+// One CTA: 32 producer threads + PR_THREADS consumers.  Consumer warp w
+// works on rate class w % RT (R <= RT of them active) for 32 patterns of the
+// tile; each thread holds the 4 state values of one (pattern, rate class)
+// and its own power-of-two scaler.  All lanes of a warp read the same
+// coefficient block (a shared-memory broadcast).
 template <typename Pol, int RT>
 __global__ void __launch_bounds__(32 + PR_THREADS) prune_tree_kernel(const PruneArgs p) {
   using V = typename Pol::V;
@@ -102,6 +103,7 @@ __global__ void __launch_bounds__(32 + PR_THREADS) prune_tree_kernel(const Prune
   constexpr int ST = PR_STAGES, NT = PR_THREADS;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ double2 red[NT / 32];
+  __shared__ double2 xch[RT][NT / RT];   // per pattern and rate class: (part, scaler)
   const int NP = p.NP, R = p.R, NC = p.n_codes;
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);     // [ST]
   uint64_t *empty = full + ST;                              // [ST]
@@ -157,8 +159,10 @@ __global__ void __launch_bounds__(32 + PR_THREADS) prune_tree_kernel(const Prune
     return;
   }
 
-  const int c = tid - 32, lane = tid & 31;
-  const int pl = c / RT, r = c % RT;
+  // consumer warp w works on rate class w % RT for 32 patterns, so every
+  // coefficient read of a warp is a broadcast of one rate's P block
+  const int c = tid - 32, lane = tid & 31, cwarp = c >> 5;
+  const int r = cwarp % RT, pl = (cwarp / RT) * 32 + lane;
   const size_t pat = tile0 + pl;
   const bool active = pat < p.n_pat;
   const bool rate_on = r < R;
@@ -220,12 +224,11 @@ __global__ void __launch_bounds__(32 + PR_THREADS) prune_tree_kernel(const Prune
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[slot]);
-    // exact power-of-two rescaling, agreed by the RT lanes of the pattern;
-    // rare, so the group maximum is formed only when some lane needs it
+    // exact power-of-two rescaling of this rate class's vector (each rate
+    // class keeps its own scaler; the root aligns them); rare, so the warp
+    // only enters when some lane needs it
     auto mx = fmax(fmax(Pol::mag(acc[0]), Pol::mag(acc[1])), fmax(Pol::mag(acc[2]), Pol::mag(acc[3])));
     if (__any_sync(0xffffffffu, mx < Pol::thresh && mx > 0)) {
-#pragma unroll
-      for (int o = 1; o < RT; o <<= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
       if (mx < Pol::thresh && mx > 0) {
         int ex;
         (void)frexp((double)mx, &ex);
@@ -251,7 +254,8 @@ __global__ void __launch_bounds__(32 + PR_THREADS) prune_tree_kernel(const Prune
     top_valid = true;
   }
 
-  // root: sum over rate classes of probs[r] * sum_i pi_i x_i, in FP64
+  // root: sum over rate classes of probs[r] 2^e_r sum_i pi_i x_i, in FP64;
+  // the rate classes of a pattern meet in shared memory
   double part = 0.0;
   if (ok && rate_on) {
     double lr = 0.0;
@@ -259,13 +263,22 @@ __global__ void __launch_bounds__(32 + PR_THREADS) prune_tree_kernel(const Prune
     for (int e = 0; e < 4; ++e) lr += p.pi[e] * Pol::to_d(top[e]);
     part = p.probs[r] * lr;
   }
-#pragma unroll
-  for (int o = 1; o < RT; o <<= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  xch[r][pl] = make_double2(part, (double)escale);
+  asm volatile("bar.sync 1, %0;" ::"r"(NT) : "memory");
   double s = 0.0, comp = 0.0;
-  if (ok && active && r == 0) {
-    const double lnl = log(part) + (double)escale * 0.69314718055994530942;
-    if (p.site_lnl) p.site_lnl[pat] = lnl;
-    s = p.weights ? p.weights[pat] * lnl : lnl;
+  if (r == 0) {
+    int emax = -0x7fffffff;
+    for (int q = 0; q < R; ++q) emax = max(emax, (int)xch[q][pl].y);
+    double site = 0.0;
+    for (int q = 0; q < R; ++q) {
+      const double2 v = xch[q][pl];
+      site += ldexp(v.x, (int)v.y - emax);
+    }
+    if (ok && active) {
+      const double lnl = log(site) + (double)emax * 0.69314718055994530942;
+      if (p.site_lnl) p.site_lnl[pat] = lnl;
+      s = p.weights ? p.weights[pat] * lnl : lnl;
+    }
   }
   warp_csum(s, comp);
   const int cw = c >> 5;

@@ -12,9 +12,10 @@ optimisation, so trees of equal topology end at equal lnL.
 * ``exhaustive_spr`` scores every move every round.
 * ``learned_spr`` scores every move once to train the network (the first,
   exhaustive round), then each round ranks all moves with the MLP on their
-  features and scores only the top k exactly; the network keeps training
-  on every exactly scored move.  When none of the k gains, it falls back to
-  an exhaustive round, so it also stops only where no move gains.
+  features and scores only the top k exactly (then the next widen*k - k
+  when none of those gains); the network keeps training on every exactly
+  scored move.  When none of them gains, it falls back to an exhaustive
+  round, so it also stops only where no move gains.
 """
 from __future__ import annotations
 
@@ -39,12 +40,15 @@ class SearchResult:
     tree: RootedTree
     trace: list = field(default_factory=list)   # (seconds, lnL) after each accepted move
     train_seconds: float = 0.0
+    timing: dict = field(default_factory=dict)  # seconds per phase
 
 
 def _target(dl):
-    """Training target: asinh of the lnL change (keeps the thousands of very
-    bad moves from swamping the few good ones)."""
-    return np.arcsinh(dl)
+    """Training target: the lnL change, floored at -100 and scaled by 1/10.
+    Only the order of the best few moves matters; moves that lose more
+    than 100 log units are all equally useless, and the floor keeps them from
+    dominating the squared loss."""
+    return np.maximum(dl, -100.0) / 10.0
 
 
 def exhaustive_spr(eng: SprEngine, eps: float = 1e-3, smooth_passes: int = 2,
@@ -55,23 +59,30 @@ def exhaustive_spr(eng: SprEngine, eps: float = 1e-3, smooth_passes: int = 2,
     lnl = eng.lnl()
     rounds = accepted = exact = 0
     trace = []
+    tm = {"scan": 0.0, "smooth": 0.0, "final": 0.0}
     while rounds < max_rounds:
         rounds += 1
+        t = time.perf_counter()
         scores = eng.scan().cpu().numpy()
+        tm["scan"] += time.perf_counter() - t
         exact += scores.size
         best = int(np.argmax(scores))
         gain = float(scores[best]) - lnl
         if not gain > eps:
             break
+        t = time.perf_counter()
         eng.apply(best)
         lnl = eng.optimize(smooth_passes, 1e-4)
+        tm["smooth"] += time.perf_counter() - t
         accepted += 1
         trace.append((time.perf_counter() - t0, lnl))
     lnl_search = lnl
+    t = time.perf_counter()
     final = eng.optimize(final_passes, 1e-8)
     torch.cuda.synchronize()
+    tm["final"] = time.perf_counter() - t
     return SearchResult(final, lnl_search, rounds, accepted, exact, rounds,
-                        time.perf_counter() - t0, eng.get_tree(), trace)
+                        time.perf_counter() - t0, eng.get_tree(), trace, 0.0, tm)
 
 
 class _Replay:
@@ -106,10 +117,13 @@ class _Replay:
 
 
 def learned_spr(eng: SprEngine, net, k: int = 32, eps: float = 1e-3, smooth_passes: int = 2,
-                final_passes: int = 60, boot_steps: int = 400, round_steps: int = 8,
+                final_passes: int = 60, boot_steps: int = 1000, round_steps: int = 8, widen: int = 8,
                 batch: int = 1024, lr: float = 2e-3, seed: int = 0,
-                max_rounds: int = 10000) -> SearchResult:
-    """``net`` is a phylocaml_gb300.mlp.MLP with max_batch >= batch."""
+                max_rounds: int = 10000, diag: list | None = None) -> SearchResult:
+    """``net`` is a phylocaml_gb300.mlp.MLP with max_batch >= batch.  With
+    ``diag`` a list, one record per round is appended: how many of the
+    network's picks gained, and after a fallback the number of gaining moves
+    and the network's rank of the best one."""
     import torch
     dev = eng.device
     gen = torch.Generator(device=dev)
@@ -120,9 +134,14 @@ def learned_spr(eng: SprEngine, net, k: int = 32, eps: float = 1e-3, smooth_pass
     lnl = eng.lnl()
     rounds = accepted = exact = exhaustive = 0
     trace = []
+    # every exactly scored move; and the best of them (the top 1 % of each
+    # exhaustive round and every move the network proposed), which fill half
+    # of each training batch so that the rare good moves shape the ranking
     replay = _Replay(torch, dev, 1 << 20)
-    recent = _Replay(torch, dev, 1 << 14)
+    recent = _Replay(torch, dev, 1 << 16)
     fitted = False
+    tm = {"exhaustive": 0.0, "features": 0.0, "rank": 0.0, "score": 0.0, "train": 0.0,
+          "smooth": 0.0, "final": 0.0}
 
     def train(steps):
         nonlocal train_s
@@ -134,10 +153,13 @@ def learned_spr(eng: SprEngine, net, k: int = 32, eps: float = 1e-3, smooth_pass
                 Xb, tb = recent.sample(gen, half)
                 Xa, ta = torch.cat([Xa, Xb]), torch.cat([ta, tb])
             net.train_step(Xa, ta, None, lr, 1e-4, sync=False)
+        torch.cuda.synchronize()
         train_s += time.perf_counter() - t
+        tm["train"] += time.perf_counter() - t
 
     def exhaustive_round():
         nonlocal exact, exhaustive, fitted
+        t = time.perf_counter()
         X = eng.features()
         scores = eng.scan().cpu().numpy()
         exact += scores.size
@@ -145,7 +167,12 @@ def learned_spr(eng: SprEngine, net, k: int = 32, eps: float = 1e-3, smooth_pass
         if not fitted:
             net.fit_norm(X)
             fitted = True
-        replay.add(X, torch.from_numpy(_target(scores - lnl).astype(np.float32)).to(dev))
+        tgt = torch.from_numpy(_target(scores - lnl).astype(np.float32)).to(dev)
+        replay.add(X, tgt)
+        top = np.argpartition(-scores, max(1, scores.size // 100) - 1)[:max(1, scores.size // 100)]
+        ti = torch.from_numpy(top).to(dev)
+        recent.add(X[ti], tgt[ti])
+        tm["exhaustive"] += time.perf_counter() - t
         return scores
 
     while rounds < max_rounds:
@@ -156,32 +183,61 @@ def learned_spr(eng: SprEngine, net, k: int = 32, eps: float = 1e-3, smooth_pass
             best = int(np.argmax(scores))
             gain = float(scores[best]) - lnl
         else:
+            t = time.perf_counter()
             X = eng.features()
+            tm["features"] += time.perf_counter() - t
+            t = time.perf_counter()
             pred = net.forward(X).cpu().numpy()
-            kk = min(k, pred.size)
-            top_h = np.argpartition(-pred, kk - 1)[:kk]
-            got = eng.score(top_h)
-            exact += kk
-            tgt = torch.from_numpy(_target(got - lnl).astype(np.float32)).to(dev)
-            Xk = X[torch.from_numpy(top_h).to(dev)]
-            recent.add(Xk, tgt)
-            replay.add(Xk, tgt)
-            j = int(np.argmax(got))
-            best, gain = int(top_h[j]), float(got[j]) - lnl
+            tm["rank"] += time.perf_counter() - t
+            order = None
+            lo = 0
+            gain = -np.inf
+            # the network's top k, then the next (widen - 1) k, exactly scored
+            for kk in (k, k * widen):
+                kk = min(kk, pred.size)
+                if kk <= lo:
+                    break
+                if order is None or kk > len(order):
+                    order = np.argsort(-pred)[:kk] if kk * 8 >= pred.size else \
+                        np.argpartition(-pred, kk - 1)[:kk]
+                    order = order[np.argsort(-pred[order])]
+                top_h = order[lo:kk]
+                t = time.perf_counter()
+                got = eng.score(top_h)
+                tm["score"] += time.perf_counter() - t
+                exact += len(top_h)
+                tgt = torch.from_numpy(_target(got - lnl).astype(np.float32)).to(dev)
+                Xk = X[torch.from_numpy(top_h).to(dev)]
+                recent.add(Xk, tgt)
+                replay.add(Xk, tgt)
+                j = int(np.argmax(got))
+                best, gain = int(top_h[j]), float(got[j]) - lnl
+                lo = kk
+                if gain > eps:
+                    break
+            rec = {"round": rounds, "picked": int(lo), "gain": gain}
             if not gain > eps:
                 # nothing among the network's picks: fall back to every move
                 scores = exhaustive_round()
                 best = int(np.argmax(scores))
                 gain = float(scores[best]) - lnl
+                rec.update(fallback=True, n_gaining=int(np.sum(scores - lnl > eps)),
+                           best_rank=int(np.sum(pred > pred[best])), fallback_gain=gain)
+            if diag is not None:
+                diag.append(rec)
             train(round_steps)
         if not gain > eps:
             break
+        t = time.perf_counter()
         eng.apply(best)
         lnl = eng.optimize(smooth_passes, 1e-4)
+        tm["smooth"] += time.perf_counter() - t
         accepted += 1
         trace.append((time.perf_counter() - t0, lnl))
     lnl_search = lnl
+    t = time.perf_counter()
     final = eng.optimize(final_passes, 1e-8)
     torch.cuda.synchronize()
+    tm["final"] = time.perf_counter() - t
     return SearchResult(final, lnl_search, rounds, accepted, exact, exhaustive,
-                        time.perf_counter() - t0, eng.get_tree(), trace, train_s)
+                        time.perf_counter() - t0, eng.get_tree(), trace, train_s, tm)
