@@ -75,6 +75,10 @@ const char *pgpu_last_error(const pgpu_ctx *ctx);
  * (handle 0) therefore cannot be selected -- pass an explicit stream. */
 pgpu_status pgpu_set_stream(pgpu_ctx *ctx, void *cuda_stream);
 pgpu_status pgpu_synchronize(pgpu_ctx *ctx);
+/* The cudaStream_t the context's work runs on (its own stream unless
+ * pgpu_set_stream chose another), for callers that order their own work
+ * against it with events. */
+void *pgpu_get_stream(const pgpu_ctx *ctx);
 /* Number of kernels this library launched on ctx since creation. */
 uint64_t pgpu_kernel_launches(const pgpu_ctx *ctx);
 /* Library version as 10000*major + 100*minor + patch. */

@@ -88,6 +88,7 @@ SIGNATURES: dict[str, tuple] = {
     "pgpu_set_stream": (_I, [_P, _P]),
     "pgpu_synchronize": (_I, [_P]),
     "pgpu_kernel_launches": (C.c_uint64, [_P]),
+    "pgpu_get_stream": (_P, [_P]),
     "pgpu_version": (_I, []),
     "pgpu_tree_schedule": (_I, [_P, C.POINTER(PgpuTree), _P, C.POINTER(C.c_int32)]),
     "pgpu_fitch_median2": (_I, [_P, _P, _P, _P, _SZ, _I, _U64P]),
@@ -237,6 +238,27 @@ class Context:
 
     def synchronize(self) -> None:
         self.call("pgpu_synchronize")
+
+    # The context's stream is a non-blocking CUDA stream: it does not wait
+    # for PyTorch's current stream, nor PyTorch for it.  Wrappers that hand
+    # tensors across call these around their asynchronous library calls.
+    def _ext(self):
+        import torch
+        h = self.lib.pgpu_get_stream(self.h)
+        if getattr(self, "_ext_handle", None) != h:
+            self._ext_stream = torch.cuda.ExternalStream(h, device=torch.device("cuda", self.device))
+            self._ext_handle = h
+        return self._ext_stream
+
+    def after_torch(self) -> None:
+        """Library work issued from now on waits for PyTorch's queued work."""
+        import torch
+        self._ext().wait_stream(torch.cuda.current_stream(torch.device("cuda", self.device)))
+
+    def before_torch(self) -> None:
+        """PyTorch work issued from now on waits for the library's queued work."""
+        import torch
+        torch.cuda.current_stream(torch.device("cuda", self.device)).wait_stream(self._ext())
 
 
 _default: Context | None = None

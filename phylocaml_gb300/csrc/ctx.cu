@@ -154,4 +154,6 @@ pgpu_status pgpu_synchronize(pgpu_ctx *ctx) {
 
 uint64_t pgpu_kernel_launches(const pgpu_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
+void *pgpu_get_stream(const pgpu_ctx *ctx) { return ctx ? static_cast<void *>(ctx->stream) : nullptr; }
+
 }  // extern "C"

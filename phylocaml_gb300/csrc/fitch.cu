@@ -385,24 +385,30 @@ struct FitchSplitArgs {
   int n_seg, n_top, depth;
 };
 
+// rows of one warp's region: ring [FS_P][32] then stack [depth][32] uint4;
+// after the walk the ring's first row holds the segment's result and warp
+// 0's stack holds the joining nodes' results, so it has at least FS_K rows
+__host__ __device__ inline int split_rows(int depth) { return FS_P + (depth > FS_K ? depth : FS_K); }
 __host__ __device__ inline size_t split_smem(int depth) {
-  // per warp: ring [FS_P][32] + stack [depth][32] uint4; then segment and
-  // top results [FS_K][32] uint4 each; then the per-site count exchange
-  return (size_t)FS_K * (FS_P + depth) * 32 * 16 + 2 * (size_t)FS_K * 32 * 16 + 32 * 32 * 4;
+  return (size_t)FS_K * split_rows(depth) * 32 * 16 + 32 * 32 * 4;   // + per-site counts
 }
 
 template <int LB>
-__global__ void __launch_bounds__(FS_K * 32) fitch_tree_split_kernel(const FitchSplitArgs p) {
+__global__ void __launch_bounds__(FS_K * 32, 8) fitch_tree_split_kernel(const FitchSplitArgs p) {
   constexpr int PER = Lanes<LB>::PER;
   constexpr uint32_t FLUSH = Lanes<LB>::FLUSH;
   constexpr uint32_t LSB = Lanes<LB>::H >> (LB - 1);
   extern __shared__ __align__(128) unsigned char smem[];
   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-  uint4 *ring = reinterpret_cast<uint4 *>(smem) + (size_t)w * (FS_P + p.depth) * 32;
+  const int rows = split_rows(p.depth);
+  uint4 *region = reinterpret_cast<uint4 *>(smem);
+  uint4 *ring = region + (size_t)w * rows * 32;
   uint4 *stk = ring + FS_P * 32;
-  uint4 *segres = reinterpret_cast<uint4 *>(smem) + (size_t)FS_K * (FS_P + p.depth) * 32;
-  uint4 *topres = segres + FS_K * 32;
-  uint32_t *sitecnt = reinterpret_cast<uint32_t *>(topres + FS_K * 32);   // [32 lanes][4*PER]
+  // per-site counts of the CTA's 128 words, shared by its warps (they all
+  // work on the same words): [4 * PER][32 lanes]
+  uint32_t *sitecnt = reinterpret_cast<uint32_t *>(region + (size_t)FS_K * rows * 32);
+  for (int i = tid; i < 32 * 4 * PER; i += FS_K * 32) sitecnt[i] = 0;
+  __syncthreads();
   const size_t word0 = (size_t)blockIdx.x * 128 + 4 * (size_t)lane;
   const bool active = word0 < p.ld;
   uint4 valid;
@@ -411,27 +417,27 @@ __global__ void __launch_bounds__(FS_K * 32) fitch_tree_split_kernel(const Fitch
   valid.z = valid_lanes<LB>(word0 + 2, p.n_sites);
   valid.w = valid_lanes<LB>(word0 + 3, p.n_sites);
   const uint32_t *col = p.tips + (active ? word0 : 0);
-  uint4 cnt = make_uint4(0, 0, 0, 0);
-  uint32_t acc[4][PER];
-#pragma unroll
-  for (int q = 0; q < 4; ++q)
-#pragma unroll
-    for (int l = 0; l < PER; ++l) acc[q][l] = 0;
+  uint4 cnt = make_uint4(0, 0, 0, 0);   // LB-bit lane counters
   uint32_t since = 0;
+  // LB-bit lane counters into the shared per-site counts
+  auto flush = [&]() {
+    const uint32_t c4[4] = {cnt.x, cnt.y, cnt.z, cnt.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int l = 0; l < PER; ++l) {
+        const uint32_t v = LB < 32 ? (c4[q] >> (l * LB)) & FLUSH : c4[q];
+        if (v) atomicAdd(&sitecnt[(q * PER + l) * 32 + lane], v);
+      }
+    cnt = make_uint4(0, 0, 0, 0);
+  };
   auto count = [&](const uint4 &e) {
     cnt.x += e.x & valid.x & LSB;
     cnt.y += e.y & valid.y & LSB;
     cnt.z += e.z & valid.z & LSB;
     cnt.w += e.w & valid.w & LSB;
     if (LB < 32 && ++since == FLUSH) {
-#pragma unroll
-      for (int l = 0; l < PER; ++l) {
-        acc[0][l] += (cnt.x >> (l * LB)) & FLUSH;
-        acc[1][l] += (cnt.y >> (l * LB)) & FLUSH;
-        acc[2][l] += (cnt.z >> (l * LB)) & FLUSH;
-        acc[3][l] += (cnt.w >> (l * LB)) & FLUSH;
-      }
-      cnt = make_uint4(0, 0, 0, 0);
+      flush();
       since = 0;
     }
   };
@@ -498,7 +504,7 @@ __global__ void __launch_bounds__(FS_K * 32) fitch_tree_split_kernel(const Fitch
       op = next;
     }
     cp_async_wait<0>();
-    segres[w * 32 + lane] = top;
+    ring[lane] = top;   // the segment's result, in its (idle) ring's first row
   }
   __syncthreads();
   // ---- phase 2: warp 0 joins the segments ----
@@ -513,39 +519,19 @@ __global__ void __launch_bounds__(FS_K * 32) fitch_tree_split_kernel(const Fitch
           c[h] = active ? __ldcs(reinterpret_cast<const uint4 *>(col + (size_t)ref * p.ld))
                         : make_uint4(0, 0, 0, 0);
         else if (ref > -100)
-          c[h] = segres[(-1 - ref) * 32 + lane];
+          c[h] = region[(size_t)(-1 - ref) * rows * 32 + lane];
         else
-          c[h] = topres[(-100 - ref) * 32 + lane];
+          c[h] = stk[(-100 - ref) * 32 + lane];
       }
       uint4 e;
       const uint4 med = fitch_quad<LB>(c[0], c[1], valid, e);
       count(e);
-      topres[i * 32 + lane] = med;
+      stk[i * 32 + lane] = med;   // warp 0's stack is idle now
       store(op.x, med);
     }
   }
-  // ---- phase 3: per-site counts of all warps, then the weighted total ----
-  if (LB < 32) {
-#pragma unroll
-    for (int l = 0; l < PER; ++l) {
-      acc[0][l] += (cnt.x >> (l * LB)) & FLUSH;
-      acc[1][l] += (cnt.y >> (l * LB)) & FLUSH;
-      acc[2][l] += (cnt.z >> (l * LB)) & FLUSH;
-      acc[3][l] += (cnt.w >> (l * LB)) & FLUSH;
-    }
-  } else {
-    acc[0][0] += cnt.x;
-    acc[1][0] += cnt.y;
-    acc[2][0] += cnt.z;
-    acc[3][0] += cnt.w;
-  }
-  for (int i = tid; i < 32 * 4 * PER; i += FS_K * 32) sitecnt[i] = 0;
-  __syncthreads();
-#pragma unroll
-  for (int q = 0; q < 4; ++q)
-#pragma unroll
-    for (int l = 0; l < PER; ++l)
-      if (acc[q][l]) atomicAdd(&sitecnt[(q * PER + l) * 32 + lane], acc[q][l]);
+  // ---- phase 3: the per-site counts, then the weighted total ----
+  flush();
   __syncthreads();
   if (w == 0) {
     unsigned long long wsum = 0;

@@ -295,5 +295,4 @@ struct Ff32 {
   }
 };
 
-
 }  // namespace pgpu_forms

@@ -719,8 +719,9 @@ __global__ void __launch_bounds__(256) spr_feature_kernel(const FeatArgs a) {
   f[3] = logf((float)t_pu + 1e-4f);
   f[4] = logf((float)(t_s + t_g) + 1e-4f);
   f[5] = logf((float)t_c + 1e-4f);
-  f[6] = logf((float)t_s + 1e-4f);
-  f[7] = logf((float)t_g + 1e-4f);
+  // u's other two neighbours are unordered: only symmetric functions of them
+  f[6] = logf((float)fmin(t_s, t_g) + 1e-4f);
+  f[7] = logf((float)fmax(t_s, t_g) + 1e-4f);
   // parsimony: length of the rearranged tree minus the current length
   const double lenT = (double)a.lenF[a.nd];
   // remaining tree joined at (s,g) plus the pruned subtree, then the new join
@@ -742,17 +743,18 @@ __global__ void __launch_bounds__(256) spr_feature_kernel(const FeatArgs a) {
   float dot_c = 0.0f, dot_s = 0.0f;
 #pragma unroll
   for (int e = 0; e < 4; ++e) {
+    const float mean_sg = 0.5f * (ss[e] + sg[e]), diff_sg = fabsf(ss[e] - sg[e]);
     f[16 + e] = sp[e];
     f[20 + e] = sc_[e];
     f[24 + e] = sy[e];
-    f[28 + e] = ss[e];
-    f[32 + e] = sg[e];
+    f[28 + e] = mean_sg;
+    f[32 + e] = diff_sg;
     f[36 + e] = sp[e] * sc_[e];
     f[40 + e] = sp[e] * sy[e];
-    f[44 + e] = sp[e] * ss[e];
-    f[48 + e] = sp[e] * sg[e];
+    f[44 + e] = sp[e] * mean_sg;
+    f[48 + e] = sp[e] * diff_sg;
     dot_c += sp[e] * sc_[e];
-    dot_s += sp[e] * ss[e];
+    dot_s += sp[e] * mean_sg;
   }
   f[52] = dot_c;
   f[53] = dot_s;
@@ -973,8 +975,8 @@ pgpu_status upload(pgpu_spr *s, T *dst, const T *src, size_t n) {
   return PGPU_OK;
 }
 
-int p32_mode(int prec) { return prec == 32 ? P32_MINUS_I : prec == 48 ? P32_MINUS_I_PAIRS : P32_PLAIN; }
-int tip_form(int prec) { return prec == 32 ? 0 : prec == 48 ? 1 : 2; }
+int p32_mode(int prec) { return prec == 32 ? P32_MINUS_I : prec == 64 ? P32_PLAIN : P32_MINUS_I_PAIRS; }
+int tip_form(int prec) { return prec == 32 ? 0 : prec == 64 ? 2 : 1; }
 
 pgpu_status compose(pgpu_spr *s, const double *t_dev, int n_br, void *out) {
   return pgpu_launch_compose(s->ctx, s->U, s->lam, s->Ui, 4, t_dev, n_br, s->rates, s->R,

@@ -76,21 +76,29 @@ class MLP:
         self._chk(self.lib.pgpu_mlp_get_norm(self.h, mu.ctypes.data, inv.ctypes.data), "pgpu_mlp_get_norm")
         return mu, inv
 
+    # Every call below reads tensors PyTorch may still be writing and/or
+    # writes tensors PyTorch will read: the library's stream waits for
+    # PyTorch's first, and PyTorch waits for the library's afterwards.
     def fit_norm(self, X_dev) -> None:
+        self.ctx.after_torch()
         self._chk(self.lib.pgpu_mlp_fit_norm(self.h, _native.ptr(X_dev), int(X_dev.shape[0])),
                   "pgpu_mlp_fit_norm")
+        self.ctx.before_torch()
 
     def forward(self, X_dev, out=None):
         n = int(X_dev.shape[0])
         if out is None:
             out = self.torch.empty(max(n, 1), dtype=self.torch.float32, device=X_dev.device)
+        self.ctx.after_torch()
         self._chk(self.lib.pgpu_mlp_forward(self.h, _native.ptr(X_dev), n, _native.ptr(out)),
                   "pgpu_mlp_forward")
+        self.ctx.before_torch()
         return out[:n]
 
     def grads(self, X_dev, t_dev, sw_dev=None):
         g = np.empty(self.n_params, np.float32)
         loss = C.c_float(0.0)
+        self.ctx.after_torch()
         self._chk(self.lib.pgpu_mlp_grads(self.h, _native.ptr(X_dev), _native.ptr(t_dev),
                                           _native.ptr(sw_dev), int(X_dev.shape[0]), g.ctypes.data,
                                           C.byref(loss)), "pgpu_mlp_grads")
@@ -99,8 +107,10 @@ class MLP:
     def train_step(self, X_dev, t_dev, sw_dev=None, lr: float = 1e-3, weight_decay: float = 1e-4,
                    sync: bool = True):
         loss = C.c_float(0.0)
+        self.ctx.after_torch()
         self._chk(self.lib.pgpu_mlp_train_step(self.h, _native.ptr(X_dev), _native.ptr(t_dev),
                                                _native.ptr(sw_dev), int(X_dev.shape[0]), lr,
                                                weight_decay, C.byref(loss) if sync else None),
                   "pgpu_mlp_train_step")
+        self.ctx.before_torch()
         return float(loss.value) if sync else None

@@ -87,6 +87,7 @@ class SprEngine:
         codes, self._keep_c = tip_code_table(code_table)
         h = _native._P()
         ld = int(tip_codes_dev.stride(0))
+        self.ctx.after_torch()
         st = self.lib.pgpu_spr_create(self.ctx.h, C.byref(m), C.byref(codes), self.n_tips,
                                       _native.ptr(tip_codes_dev), ld, _native.ptr(weights_dev),
                                       self.n_pat, precision, C.byref(h))
@@ -156,7 +157,9 @@ class SprEngine:
         nm = self.n_moves
         if out is None:
             out = self.torch.empty(nm, dtype=self.torch.float64, device=self.device)
+        self.ctx.after_torch()
         self._check(self.lib.pgpu_spr_scan(self.h, _native.ptr(out)), "pgpu_spr_scan")
+        self.ctx.before_torch()
         return out
 
     def score(self, idx) -> np.ndarray:
@@ -173,7 +176,9 @@ class SprEngine:
         if out is None:
             out = self.torch.empty(max(nm, 1), dtype=self.torch.int64, device=self.device)
         tl = C.c_uint64(0)
+        self.ctx.after_torch()
         self._check(self.lib.pgpu_spr_fitch(self.h, _native.ptr(out), C.byref(tl)), "pgpu_spr_fitch")
+        self.ctx.before_torch()
         return out[:nm], int(tl.value)
 
     def features(self, out=None):
@@ -181,7 +186,9 @@ class SprEngine:
         if out is None:
             out = self.torch.empty((max(nm, 1), N_FEATURES), dtype=self.torch.float32,
                                    device=self.device)
+        self.ctx.after_torch()
         self._check(self.lib.pgpu_spr_features(self.h, _native.ptr(out)), "pgpu_spr_features")
+        self.ctx.before_torch()
         return out[:nm]
 
     def apply(self, i: int) -> None:

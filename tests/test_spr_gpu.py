@@ -144,3 +144,33 @@ def test_deep_tree_rescaling(ctx):
     exp = np.array([oracle_lnl(d, SO.apply_move(adj, *mv[i])) for i in idx])
     assert np.all(np.abs(full[idx] - exp) <= 1e-9 * np.abs(exp))
     e.close()
+
+
+def test_features_do_not_depend_on_numbering(small, ctx):
+    """The same move gets the same features whatever the engine's internal
+    node and edge numbering (two engines holding one tree, one of them after
+    a move and its inverse bookkeeping)."""
+    d = small
+    n = d["tr"].n_tips
+    a = engine(d, ctx, 48)
+    s = a.scan().cpu().numpy()
+    a.apply(int(np.argmax(s)))
+    b = engine(d, ctx, 48)
+    b.set_tree(a.get_tree())
+
+    def by_move(e):
+        X = e.features().cpu().numpy()
+        t = e.get_tree()
+        adj = SO.unroot(t.left, t.right, t.brlen)
+        m = e.moves()
+
+        def tips(x, y):
+            return frozenset(v for v in SO.side(adj, x, y) if v < n)
+        return {(tips(int(m.p[i]), int(m.u[i])), tips(int(m.c[i]), int(m.y[i])),
+                 tips(int(m.y[i]), int(m.c[i]))): X[i] for i in range(len(m))}
+    fa, fb = by_move(a), by_move(b)
+    assert fa.keys() == fb.keys()
+    worst = max(float(np.max(np.abs(fa[k] - fb[k]))) for k in fa)
+    assert worst < 1e-4, worst
+    a.close()
+    b.close()
