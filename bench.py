@@ -279,8 +279,8 @@ def bench_fitch(args, rank, world, local):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                      "peak_source": peak_src, "algorithmic_bytes": alg_bytes,
-                     "traffic": profile_traffic("fitch_tree_kernel_1024x1e6"),
-                     "kernel": "fitch_tree_kernel<4>", "per_launch_ms": per_launch_ms},
+                     "traffic": profile_traffic("fitch_tree_split_kernel_1024x1e6"),
+                     "kernel": "fitch_tree_split_kernel<4>", "per_launch_ms": per_launch_ms},
         "e2e": {"value": units / e2e_s, "unit": "node-site updates/s",
                 "h2d_bytes_per_step": int(words.nbytes + w.nbytes),
                 "d2h_bytes_per_step": int(pin_out.nbytes + pin_sc.nbytes + 8),
@@ -349,9 +349,12 @@ def bench_fitch_reference(args):
 PRUNE_TAXA, PRUNE_SITES, PRUNE_BL = 512, 500_000, 0.05
 PRUNE_GATE = 1e-3
 FORMS = {32: "fp32", 48: "fp32x2", 64: "fp64"}
-# FP32 lane instructions per node-pattern-rate of each form (counted from
-# csrc/prune.cu: two children x 4 rows, then the product and the rescale test)
-FP32_INSTR_PER_NODE_RATE = {32: 2 * 4 * 5 + 4 + 6, 48: 2 * 4 * 59 + 4 * 6 + 6}
+# FP32 lane instructions of each form, counted from csrc/forms.cuh: per row of
+# a P x child product (internal children only; tip children are table rows),
+# and per node and rate class for the product of the two children and the
+# rescale test
+FP32_INSTR_PER_ROW = {32: 5, 48: 43}
+FP32_INSTR_PER_NODE = {32: 4 + 6, 48: 4 * 7 + 6}
 
 
 def prune_data(rank):
@@ -472,7 +475,9 @@ def bench_prune(args, rank, world, local):
     sm_mhz = clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
     lane_peak = n_sm * 128 * sm_mhz * 1e6 / 1e12            # Tinst/s at the sampled clock
-    instr = FP32_INSTR_PER_NODE_RATE[head_prec] * R * units
+    internal_children = int(np.sum(tr.left >= tr.n_tips) + np.sum(tr.right >= tr.n_tips))
+    instr = R * n_pat * (internal_children * 4 * FP32_INSTR_PER_ROW[head_prec] +
+                         tr.n_internal * FP32_INSTR_PER_NODE[head_prec])
     achieved = instr / (head["per_launch_ms"] * 1e-3) / 1e12
     rec = {
         "metric": "node-site-pattern updates/s on 1 GB300, FP32 vs FP64 form at |dlnL|<=1e-3",

@@ -35,6 +35,7 @@
 //   batch_fp64_kernel  the FP64 comparison form on a sample of patterns.
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "forms.cuh"
@@ -146,6 +147,123 @@ __device__ __forceinline__ int blk_bytes(const BVar &v) {
   return ((b > t ? b : t) + 127) & ~127;
 }
 
+
+// What one epilogue step reads.
+struct EpiIn {
+  int4 op;
+  const unsigned char *sl;   // the step's ring slot
+  int BB;                    // bytes of one child block in the slot
+  uint32_t tmem, lane_base;
+  int m;                     // pattern within the tile (TMEM lane)
+  bool active, last;
+  const double *pi;
+};
+
+// One postorder step for the half row of states [HF*KP/2, (HF+1)*KP/2):
+// the product of the two children (tip rows from the slot, or the MMA
+// results from TMEM), rescaled by a power of two agreed with the other half,
+// written into the node's TMEM stack slot.  KP is a template parameter so
+// that every state index is a compile-time constant and the vectors stay
+// in registers.
+template <int KP>
+__device__ __forceinline__ void epi_step(const BVar &v, const BatchArgs &p, const EpiIn &in, int hf,
+                                         int lane, int slot, uint64_t *empty, float (*xch)[BT_M],
+                                         int &escale, bool &ok, double &Lp) {
+  constexpr int B = KP / 2;
+  const int S = v.S;
+  float acc[B];
+#pragma unroll
+  for (int e = 0; e < B; ++e) acc[e] = 1.0f;
+  // e0 = hf * B: both halves are compiled, the warp takes its own
+  auto half = [&](auto HFc) {
+    constexpr int HF = decltype(HFc)::value;
+    constexpr int e0 = HF * B;
+    constexpr int c_first = (e0 / 16) * 16;
+    constexpr int n_chunks = (e0 - c_first + B + 15) / 16;
+    for (int h = 0; h < 2 && ok; ++h) {
+      const int ch = h == 0 ? in.op.y : in.op.z;
+      if (ch < v.n_tips) {
+        int code = in.sl[h * 128 + in.m];
+        if (code >= v.n_codes) {
+          if (in.active && HF == 0) atomicOr(p.flag, PGPU_FLAG_BADCODE);
+          code = 0;
+        }
+        const float *row =
+            reinterpret_cast<const float *>(in.sl + 256 + (size_t)h * in.BB) + (size_t)code * v.SpT + e0;
+#pragma unroll
+        for (int e = 0; e < B; ++e)
+          if (e0 + e < S) acc[e] *= row[e];
+      } else {
+        float d[n_chunks][16];
+#pragma unroll
+        for (int u = 0; u < n_chunks; ++u)
+          tmem_ld16(in.tmem + in.lane_base + (uint32_t)(h * v.Np + c_first + 16 * u), d[u]);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int e = 0; e < B; ++e) {
+          constexpr int dummy = 0;
+          (void)dummy;
+          const int col = e0 + e - c_first;
+          if (e0 + e < S) acc[e] *= d[col / 16][col % 16];
+        }
+      }
+    }
+  };
+  if (hf == 0) half(std::integral_constant<int, 0>{});
+  else half(std::integral_constant<int, 1>{});
+  __syncwarp();
+  if (lane == 0) mbar_arrive(&empty[slot]);
+  const int e0 = hf * B;
+  // rescale by an exact power of two; the two halves of a row agree
+  float mx = 0.0f;
+#pragma unroll
+  for (int e = 0; e < B; ++e)
+    if (e0 + e < S) mx = fmaxf(mx, acc[e]);
+  xch[hf][in.m] = mx;
+  // the exchange barrier also makes the timeout verdict uniform over the
+  // epilogue warps, so none can leave the loop alone
+  {
+    uint32_t all_ok;
+    asm volatile(
+        "{\n\t.reg .pred a, b;\n\tsetp.ne.u32 a, %1, 0;\n\t"
+        "bar.red.and.pred b, 1, 256, a;\n\tselp.u32 %0, 1, 0, b;\n\t}"
+        : "=r"(all_ok)
+        : "r"((uint32_t)ok)
+        : "memory");
+    ok = all_ok != 0;
+  }
+  mx = fmaxf(mx, xch[hf ^ 1][in.m]);
+  if (mx < 0x1p-32f && mx > 0.0f) {
+    int ex;
+    (void)frexpf(mx, &ex);
+    escale += ex;
+    const int k1 = min(-ex, 120), k2 = -ex - k1;
+    const float f1 = __int_as_float((127 + k1) << 23), f2 = __int_as_float((127 + k2) << 23);
+#pragma unroll
+    for (int e = 0; e < B; ++e) acc[e] = acc[e] * f1 * f2;
+  }
+#pragma unroll
+  for (int e = 0; e < B; ++e)
+    if (e0 + e >= S) acc[e] = 0.0f;
+  // into the TMEM stack slot: my K columns e0 .. e0 + B - 1
+  const int so = (in.op.w >> 16) & 0xff;
+  const uint32_t col = (uint32_t)(2 * v.Np + so * v.Kp + e0);
+#pragma unroll
+  for (int c0 = 0; c0 < B; c0 += 4)
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(
+                     in.tmem + in.lane_base + col + (uint32_t)c0),
+                 "r"(__float_as_uint(acc[c0])), "r"(__float_as_uint(acc[c0 + 1])),
+                 "r"(__float_as_uint(acc[c0 + 2])), "r"(__float_as_uint(acc[c0 + 3]))
+                 : "memory");
+  if (in.last) {
+    double l = 0.0;
+#pragma unroll
+    for (int e = 0; e < B; ++e)
+      if (e0 + e < S) l += in.pi[e0 + e] * (double)acc[e];
+    Lp = l;
+  }
+}
+
 __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs p) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint64_t full[BT_ST], empty[BT_ST], mma_bar;
@@ -247,7 +365,7 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
       idesc |= (uint32_t)(v.Np >> 3) << 17;
       idesc |= (uint32_t)(BT_M >> 4) << 24;
       double lnr[4];
-      float acc[BT_SP / 2];
+      double Lp = 0.0;   // this half row's share of the root likelihood
       for (int r = 0; r < v.R && ok; ++r) {
         int escale = 0;
         for (int i = 0; i < v.n_ops; ++i, ++seq) {
@@ -300,91 +418,17 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
             atomicOr(p.flag, PGPU_FLAG_TIMEOUT);
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-          for (int e = 0; e < BT_SP / 2; ++e) acc[e] = 1.0f;
-          for (int h = 0; h < 2 && ok; ++h) {
-            const int ch = h == 0 ? op.y : op.z;
-            if (ch < v.n_tips) {
-              int code = sl[h * 128 + m];
-              if (code >= v.n_codes) {
-                if (active && hf == 0) atomicOr(p.flag, PGPU_FLAG_BADCODE);
-                code = 0;
-              }
-              const float *row = reinterpret_cast<const float *>(sl + 256 + (size_t)h * BB) +
-                                 (size_t)code * v.SpT + e0;
-#pragma unroll
-              for (int e = 0; e < BT_SP / 2; ++e)
-                if (e < B && e0 + e < S) acc[e] *= row[e];
-            } else {
-              // the (at most three) 16-column chunks that cover my states, all
-              // loads in flight before one wait
-              const int c_first = (e0 / 16) * 16;
-              float d[3][16];
-#pragma unroll
-              for (int u = 0; u < 3; ++u) {
-                const int c0 = c_first + 16 * u;
-                if (c0 < v.Np && c0 < e0 + B)
-                  tmem_ld16(tmem + lane_base + (uint32_t)(h * v.Np + c0), d[u]);
-              }
-              asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-              for (int u = 0; u < 3; ++u) {
-                const int c0 = c_first + 16 * u;
-                if (c0 < v.Np && c0 < e0 + B) {
-#pragma unroll
-                  for (int j = 0; j < 16; ++j) {
-                    const int e = c0 + j - e0;
-                    if (e >= 0 && e < B && c0 + j < S) acc[e < BT_SP / 2 ? e : 0] *= d[u][j];
-                  }
-                }
-              }
-            }
+          EpiIn in{op, sl, BB, tmem, lane_base, m, active, i == v.n_ops - 1, p.pis + v.pi_off};
+          switch (v.Kp) {
+            case 8: epi_step<8>(v, p, in, hf, lane, slot, empty, xch, escale, ok, Lp); break;
+            case 16: epi_step<16>(v, p, in, hf, lane, slot, empty, xch, escale, ok, Lp); break;
+            case 24: epi_step<24>(v, p, in, hf, lane, slot, empty, xch, escale, ok, Lp); break;
+            case 32: epi_step<32>(v, p, in, hf, lane, slot, empty, xch, escale, ok, Lp); break;
+            case 40: epi_step<40>(v, p, in, hf, lane, slot, empty, xch, escale, ok, Lp); break;
+            case 48: epi_step<48>(v, p, in, hf, lane, slot, empty, xch, escale, ok, Lp); break;
+            case 56: epi_step<56>(v, p, in, hf, lane, slot, empty, xch, escale, ok, Lp); break;
+            default: epi_step<64>(v, p, in, hf, lane, slot, empty, xch, escale, ok, Lp); break;
           }
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&empty[slot]);
-          // rescale by an exact power of two; the two halves of a row agree
-          float mx = 0.0f;
-#pragma unroll
-          for (int e = 0; e < BT_SP / 2; ++e)
-            if (e < B && e0 + e < S) mx = fmaxf(mx, acc[e]);
-          xch[hf][m] = mx;
-          // the exchange barrier also makes the timeout verdict uniform over
-          // the epilogue warps, so none can leave the loop alone
-          {
-            uint32_t all_ok;
-            asm volatile(
-                "{\n\t.reg .pred a, b;\n\tsetp.ne.u32 a, %1, 0;\n\t"
-                "bar.red.and.pred b, 1, 256, a;\n\tselp.u32 %0, 1, 0, b;\n\t}"
-                : "=r"(all_ok)
-                : "r"((uint32_t)ok)
-                : "memory");
-            ok = all_ok != 0;
-          }
-          mx = fmaxf(mx, xch[hf ^ 1][m]);
-          if (mx < 0x1p-32f && mx > 0.0f) {
-            int ex;
-            (void)frexpf(mx, &ex);
-            escale += ex;
-            const int k1 = min(-ex, 120), k2 = -ex - k1;
-            const float f1 = __int_as_float((127 + k1) << 23), f2 = __int_as_float((127 + k2) << 23);
-#pragma unroll
-            for (int e = 0; e < BT_SP / 2; ++e) acc[e] = acc[e] * f1 * f2;
-          }
-#pragma unroll
-          for (int e = 0; e < BT_SP / 2; ++e)
-            if (e >= B || e0 + e >= S) acc[e] = 0.0f;
-          // into the TMEM stack slot: my K columns e0 .. e0 + B - 1
-          const int so = (op.w >> 16) & 0xff;
-          const uint32_t col = (uint32_t)(2 * v.Np + so * v.Kp + e0);
-#pragma unroll
-          for (int c0 = 0; c0 < BT_SP / 2; c0 += 4)
-            if (c0 < B) {
-              asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(
-                               tmem + lane_base + col + (uint32_t)c0),
-                           "r"(__float_as_uint(acc[c0])), "r"(__float_as_uint(acc[c0 + 1])),
-                           "r"(__float_as_uint(acc[c0 + 2])), "r"(__float_as_uint(acc[c0 + 3]))
-                           : "memory");
-            }
           asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
           // every vector of this step is in TMEM before the next MMA issues
@@ -393,10 +437,6 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
         }
         if (!ok) break;
         // root of this rate pass (both halves of the row)
-        double Lp = 0.0;
-        const double *pi = p.pis + v.pi_off;
-        for (int e = 0; e < B; ++e)
-          if (e0 + e < S) Lp += pi[e0 + e] * (double)acc[e];
         xchd[hf][m] = Lp;
         asm volatile("bar.sync 1, 256;" ::: "memory");
         const double L = Lp + xchd[hf ^ 1][m];

@@ -354,15 +354,18 @@ __global__ void __launch_bounds__(160) fitch_tree_kernel(const FitchTreeArgs p) 
 }
 
 // ---------------------------------------------------------------------------
-// tree kernel, segmented form.  One CTA of FS_K warps per 128-word slice
-// (4 words per thread): the postorder is cut into up to FS_K disjoint
-// subtrees (segments), warp w walks segment w with its own stack, and each
-// thread keeps its next FS_P tip slices in flight with cp.async (LDGSTS)
-// into a per-warp ring.  Segment results meet in shared memory, where warp 0
-// finishes the few nodes above the segments.  Splitting the walk multiplies
-// the warps per SM by up to FS_K, which the single postorder walk cannot.
+// tree kernel, segmented form.  One CTA of FS_W warps per 128-word slice
+// (4 words per thread): the postorder is cut into up to FS_S disjoint
+// subtrees (segments), dealt to the warps longest first; each warp walks its
+// segments one after another with its own stack, and each thread keeps its
+// next FS_P tip slices in flight with cp.async (LDGSTS) into a per-warp ring.
+// A finished segment's result stays at the bottom of its warp's stack; warp
+// 0 then finishes the few nodes above the segments.  Splitting the walk
+// multiplies the warps per SM by FS_W, which a single postorder walk cannot,
+// and dealing more segments than warps keeps the warps' loads even.
 // ---------------------------------------------------------------------------
-constexpr int FS_K = 4;   // segments (warps) per CTA
+constexpr int FS_W = 4;   // warps per CTA
+constexpr int FS_S = 8;   // segments at most
 constexpr int FS_P = 4;   // tip slices in flight per thread
 
 __device__ __forceinline__ void cp_async16(void *dst, const void *src, bool valid) {
@@ -378,36 +381,36 @@ struct FitchSplitArgs {
   const uint32_t *tips, *weights;
   uint32_t *node_sets, *site_cost;
   unsigned long long *total;
-  const int4 *ops, *seg, *top;
+  const int4 *ops, *seg, *top, *wseg;   // wseg[w] = {first segment, count}
   const int32_t *tip_seq;
   size_t ld, n_words, n_sites;
   int32_t n_tips;
-  int n_seg, n_top, depth;
+  int n_top, rows;                       // rows: ring + stack rows per warp
 };
 
-// rows of one warp's region: ring [FS_P][32] then stack [depth][32] uint4;
-// after the walk the ring's first row holds the segment's result and warp
-// 0's stack holds the joining nodes' results, so it has at least FS_K rows
-__host__ __device__ inline int split_rows(int depth) { return FS_P + (depth > FS_K ? depth : FS_K); }
-__host__ __device__ inline size_t split_smem(int depth) {
-  return (size_t)FS_K * split_rows(depth) * 32 * 16 + 32 * 32 * 4;   // + per-site counts
+// one warp's region: ring [FS_P][32] then stack [rows - FS_P][32] uint4
+// (its finished segments' results at the bottom, the walk above them); after
+// the walks the rings hold the joining nodes' results, FS_W * FS_P >= FS_S
+static_assert(FS_W * FS_P >= FS_S, "joining results overlay the rings");
+__host__ __device__ inline size_t split_smem(int rows) {
+  return (size_t)FS_W * rows * 32 * 16 + 32 * 32 * 4;   // + per-site counts
 }
 
 template <int LB>
-__global__ void __launch_bounds__(FS_K * 32, 8) fitch_tree_split_kernel(const FitchSplitArgs p) {
+__global__ void __launch_bounds__(FS_W * 32, 8) fitch_tree_split_kernel(const FitchSplitArgs p) {
   constexpr int PER = Lanes<LB>::PER;
   constexpr uint32_t FLUSH = Lanes<LB>::FLUSH;
   constexpr uint32_t LSB = Lanes<LB>::H >> (LB - 1);
   extern __shared__ __align__(128) unsigned char smem[];
   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-  const int rows = split_rows(p.depth);
+  const int rows = p.rows;
   uint4 *region = reinterpret_cast<uint4 *>(smem);
   uint4 *ring = region + (size_t)w * rows * 32;
-  uint4 *stk = ring + FS_P * 32;
+  uint4 *stk0 = ring + FS_P * 32;
   // per-site counts of the CTA's 128 words, shared by its warps (they all
   // work on the same words): [4 * PER][32 lanes]
-  uint32_t *sitecnt = reinterpret_cast<uint32_t *>(region + (size_t)FS_K * rows * 32);
-  for (int i = tid; i < 32 * 4 * PER; i += FS_K * 32) sitecnt[i] = 0;
+  uint32_t *sitecnt = reinterpret_cast<uint32_t *>(region + (size_t)FS_W * rows * 32);
+  for (int i = tid; i < 32 * 4 * PER; i += FS_W * 32) sitecnt[i] = 0;
   __syncthreads();
   const size_t word0 = (size_t)blockIdx.x * 128 + 4 * (size_t)lane;
   const bool active = word0 < p.ld;
@@ -445,14 +448,20 @@ __global__ void __launch_bounds__(FS_K * 32, 8) fitch_tree_split_kernel(const Fi
     if (active) __stcs(reinterpret_cast<uint4 *>(p.node_sets + (size_t)k * p.ld + word0), med);
   };
 
-  // ---- phase 1: warp w walks segment w ----
-  if (w < p.n_seg) {
-    const int4 sg = p.seg[w];   // {op_off, n_ops, tip_off, n_tips}
+  // ---- phase 1: warp w walks its segments ----
+  const int4 ws = p.wseg[w];
+  for (int q = 0; q < ws.y; ++q) {
+    const int4 sg = p.seg[ws.x + q];   // {op_off, n_ops, tip_off, n_tips}
+    uint4 *stk = stk0 + (q + 1) * 32;  // rows below hold earlier results
     const int32_t *tseq = p.tip_seq + sg.z;
     int issued = 0, consumed = 0;
+    int32_t next_tip = sg.w > 0 ? __ldg(tseq) : 0;
     auto issue = [&]() {
-      if (issued < sg.w)
-        cp_async16(&ring[(issued % FS_P) * 32 + lane], col + (size_t)__ldg(tseq + issued) * p.ld, active);
+      if (issued < sg.w) {
+        const int32_t tip = next_tip;
+        if (issued + 1 < sg.w) next_tip = __ldg(tseq + issued + 1);
+        cp_async16(&ring[(issued % FS_P) * 32 + lane], col + (size_t)tip * p.ld, active);
+      }
       cp_async_commit();   // empty groups keep the count in step
       ++issued;
     };
@@ -504,10 +513,12 @@ __global__ void __launch_bounds__(FS_K * 32, 8) fitch_tree_split_kernel(const Fi
       op = next;
     }
     cp_async_wait<0>();
-    ring[lane] = top;   // the segment's result, in its (idle) ring's first row
+    stk0[q * 32 + lane] = top;   // this segment's result
   }
   __syncthreads();
   // ---- phase 2: warp 0 joins the segments ----
+  // reference of a child: tip id (>= 0), segment result -1 - (warp * 32 +
+  // row), joining result -1000 - t (kept in the idle rings, FS_P per warp)
   if (w == 0) {
     for (int i = 0; i < p.n_top; ++i) {
       const int4 op = __ldg(p.top + i);
@@ -515,18 +526,21 @@ __global__ void __launch_bounds__(FS_K * 32, 8) fitch_tree_split_kernel(const Fi
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int ref = h == 0 ? op.y : op.z;
-        if (ref >= 0)
+        if (ref >= 0) {
           c[h] = active ? __ldcs(reinterpret_cast<const uint4 *>(col + (size_t)ref * p.ld))
                         : make_uint4(0, 0, 0, 0);
-        else if (ref > -100)
-          c[h] = region[(size_t)(-1 - ref) * rows * 32 + lane];
-        else
-          c[h] = stk[(-100 - ref) * 32 + lane];
+        } else if (ref > -1000) {
+          const int at = -1 - ref;
+          c[h] = region[((size_t)(at >> 5) * rows + FS_P + (at & 31)) * 32 + lane];
+        } else {
+          const int t = -1000 - ref;
+          c[h] = region[((size_t)(t / FS_P) * rows + t % FS_P) * 32 + lane];
+        }
       }
       uint4 e;
       const uint4 med = fitch_quad<LB>(c[0], c[1], valid, e);
       count(e);
-      stk[i * 32 + lane] = med;   // warp 0's stack is idle now
+      region[((size_t)(i / FS_P) * rows + i % FS_P) * 32 + lane] = med;
       store(op.x, med);
     }
   }
@@ -646,11 +660,12 @@ cudaError_t launch_tree(cudaStream_t stream, int lb, const FitchTreeArgs &args, 
 }
 
 
-// Cuts the postorder into up to FS_K segments: repeatedly split the largest
+// Cuts the postorder into up to FS_S segments: repeatedly split the largest
 // remaining subtree at its root (the root joins the top part) while fewer
-// than FS_K subtrees remain and the largest has at least two internal
-// nodes.  Each segment is scheduled like the whole tree (Sethi-Ullman order:
-// the child with the larger stack need first).
+// than FS_S subtrees remain and the largest has at least two internal nodes.
+// Each segment is scheduled like the whole tree (Sethi-Ullman order: the
+// child with the larger stack need first).  Segments go to the FS_W warps
+// longest first, each to the least loaded warp.
 pgpu_status build_split(pgpu_ctx *ctx, const pgpu_tree *tree, SplitSchedule *out) {
   TreeSchedule check;
   PGPU_TRY(pgpu_build_schedule(ctx, tree, &check));   // validates the tree
@@ -672,7 +687,7 @@ pgpu_status build_split(pgpu_ctx *ctx, const pgpu_tree *tree, SplitSchedule *out
   std::vector<uint8_t> is_top(n_int, 0);
   auto by_size = [&](int32_t x, int32_t y) { return size[x] < size[y]; };
   int n_split = 0;
-  while ((int)heap.size() < FS_K && !heap.empty() && n_split < FS_K) {
+  while ((int)heap.size() < FS_S && !heap.empty() && n_split < FS_S) {
     std::pop_heap(heap.begin(), heap.end(), by_size);
     const int32_t k = heap.back();
     if (size[k] < 2) {
@@ -688,60 +703,78 @@ pgpu_status build_split(pgpu_ctx *ctx, const pgpu_tree *tree, SplitSchedule *out
         std::push_heap(heap.begin(), heap.end(), by_size);
       }
   }
+  // longest first onto the least loaded warp
   std::sort(heap.begin(), heap.end(), [&](int32_t x, int32_t y) { return size[x] > size[y]; });
+  std::vector<std::vector<int32_t>> per_warp(FS_W);
+  std::vector<int64_t> load(FS_W, 0);
+  for (const int32_t r : heap) {
+    const int w = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    per_warp[w].push_back(r);
+    load[w] += size[r];
+  }
   SplitSchedule sp;
   sp.n_seg = (int)heap.size();
-  std::vector<int32_t> seg_of(n_int, -1), top_of(n_int, -1);
-  for (int i = 0; i < sp.n_seg; ++i) seg_of[heap[i]] = i;
-  for (int i = 0; i < sp.n_seg; ++i) {
-    const int32_t root = heap[i];
-    const int op_off = (int)sp.ops.size(), tip_off = (int)sp.tips.size();
-    struct Fr {
-      int32_t v;
-      bool done;
-    };
-    std::vector<Fr> st{{n + root, false}};
-    int height = 0, depth = 0;
-    while (!st.empty()) {
-      const Fr f = st.back();
-      st.pop_back();
-      const int32_t k = f.v - n;
-      const int32_t first = swp[k] ? R[k] : L[k], second = swp[k] ? L[k] : R[k];
-      if (!f.done) {
-        st.push_back({f.v, true});
-        if (second >= n) st.push_back({second, false});
-        if (first >= n) st.push_back({first, false});
-        continue;
+  std::vector<int32_t> ref_of(n_int, 0);   // reference of a segment root
+  int max_need = 1;
+  for (int w = 0; w < FS_W; ++w) {
+    sp.wseg.push_back(make_int4((int)sp.seg.size(), (int)per_warp[w].size(), 0, 0));
+    for (int q = 0; q < (int)per_warp[w].size(); ++q) {
+      const int32_t root = per_warp[w][q];
+      ref_of[root] = -1 - (w * 32 + q);
+      const int op_off = (int)sp.ops.size(), tip_off = (int)sp.tips.size();
+      struct Fr {
+        int32_t v;
+        bool done;
+      };
+      std::vector<Fr> st{{n + root, false}};
+      int height = 0, depth = 0;
+      while (!st.empty()) {
+        const Fr f = st.back();
+        st.pop_back();
+        const int32_t k = f.v - n;
+        const int32_t first = swp[k] ? R[k] : L[k], second = swp[k] ? L[k] : R[k];
+        if (!f.done) {
+          st.push_back({f.v, true});
+          if (second >= n) st.push_back({second, false});
+          if (first >= n) st.push_back({first, false});
+          continue;
+        }
+        sp.ops.push_back(make_int4(k, first, second, 0));
+        if (first < n) sp.tips.push_back(first);
+        if (second < n) sp.tips.push_back(second);
+        height += 1 - (first >= n) - (second >= n);
+        depth = std::max(depth, height);
       }
-      sp.ops.push_back(make_int4(k, first, second, 0));
-      if (first < n) sp.tips.push_back(first);
-      if (second < n) sp.tips.push_back(second);
-      height += 1 - (first >= n) - (second >= n);
-      depth = std::max(depth, height);
+      // the walk's stack starts above the q earlier results and this one
+      max_need = std::max(max_need, q + 1 + depth);
+      sp.seg.push_back(make_int4(op_off, (int)sp.ops.size() - op_off, tip_off,
+                                 (int)sp.tips.size() - tip_off));
     }
-    sp.max_depth = std::max(sp.max_depth, depth);
-    sp.seg.push_back(make_int4(op_off, (int)sp.ops.size() - op_off, tip_off, (int)sp.tips.size() - tip_off));
   }
+  if (sp.n_seg > 32) return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: too many segments");
+  sp.rows = FS_P + max_need;
+  std::vector<int32_t> top_of(n_int, -1);
   int n_top = 0;
   for (int32_t k = 0; k < n_int; ++k) {
     if (!is_top[k]) continue;
     int32_t ref[2];
     for (int h = 0; h < 2; ++h) {
       const int32_t c = h == 0 ? L[k] : R[k];
-      ref[h] = c < n ? c : seg_of[c - n] >= 0 ? -1 - seg_of[c - n] : -100 - top_of[c - n];
+      ref[h] = c < n ? c : !is_top[c - n] ? ref_of[c - n] : -1000 - top_of[c - n];
     }
     top_of[k] = n_top++;
     sp.top.push_back(make_int4(k, ref[0], ref[1], 0));
   }
-  if (n_top > FS_K)
-    return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: %d joining nodes (at most %d)", n_top, FS_K);
+  if (n_top > FS_W * FS_P)
+    return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: %d joining nodes (at most %d)", n_top,
+                        FS_W * FS_P);
   *out = std::move(sp);
   return PGPU_OK;
 }
 
 // the split schedule of `tree`, resident in BUF_SPLIT ({ops, seg, top, tips})
 pgpu_status split_device(pgpu_ctx *ctx, const pgpu_tree *tree, const int4 **ops, const int4 **seg,
-                         const int4 **top, const int32_t **tips) {
+                         const int4 **top, const int4 **wseg, const int32_t **tips) {
   const int32_t n_int = tree->n_tips - 1;
   const bool hit = ctx->split_valid && (int32_t)ctx->split_left.size() == n_int &&
                    std::memcmp(ctx->split_left.data(), tree->left, n_int * 4) == 0 &&
@@ -750,7 +783,8 @@ pgpu_status split_device(pgpu_ctx *ctx, const pgpu_tree *tree, const int4 **ops,
   if (!hit) {
     ctx->split_valid = false;
     PGPU_TRY(build_split(ctx, tree, &ctx->split));
-    const size_t bytes = 16 * (sp.ops.size() + sp.seg.size() + sp.top.size()) + 4 * sp.tips.size();
+    const size_t bytes =
+        16 * (sp.ops.size() + sp.seg.size() + sp.top.size() + sp.wseg.size()) + 4 * sp.tips.size();
     void *d;
     PGPU_TRY(pgpu_buf(ctx, BUF_SPLIT, std::max<size_t>(bytes, 16), &d));
     std::vector<unsigned char> h(std::max<size_t>(bytes, 16));
@@ -762,6 +796,7 @@ pgpu_status split_device(pgpu_ctx *ctx, const pgpu_tree *tree, const int4 **ops,
     put(sp.ops.data(), 16 * sp.ops.size());
     put(sp.seg.data(), 16 * sp.seg.size());
     put(sp.top.data(), 16 * sp.top.size());
+    put(sp.wseg.data(), 16 * sp.wseg.size());
     put(sp.tips.data(), 4 * sp.tips.size());
     PGPU_CUDA(ctx, cudaMemcpyAsync(d, h.data(), bytes, cudaMemcpyHostToDevice, ctx->stream));
     PGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // h is a temporary
@@ -773,18 +808,19 @@ pgpu_status split_device(pgpu_ctx *ctx, const pgpu_tree *tree, const int4 **ops,
   *ops = base;
   *seg = base + sp.ops.size();
   *top = *seg + sp.seg.size();
-  *tips = reinterpret_cast<const int32_t *>(*top + sp.top.size());
+  *wseg = *top + sp.top.size();
+  *tips = reinterpret_cast<const int32_t *>(*wseg + sp.wseg.size());
   return PGPU_OK;
 }
 
 template <int LB>
 cudaError_t launch_split(cudaStream_t stream, const FitchSplitArgs &a, size_t tiles) {
-  const size_t smem = split_smem(a.depth);
+  const size_t smem = split_smem(a.rows);
   cudaError_t e = cudaFuncSetAttribute(fitch_tree_split_kernel<LB>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)std::max<size_t>(smem, 48 * 1024));
   if (e != cudaSuccess) return e;
-  fitch_tree_split_kernel<LB><<<(unsigned)tiles, FS_K * 32, smem, stream>>>(a);
+  fitch_tree_split_kernel<LB><<<(unsigned)tiles, FS_W * 32, smem, stream>>>(a);
   return cudaGetLastError();
 }
 
@@ -801,7 +837,7 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
     return pgpu_set_err(ctx, PGPU_ERR_ARG, "fitch_tree: tip and node rows must be 16-byte aligned");
   if (!tree || tree->n_tips < 2) return pgpu_set_err(ctx, PGPU_ERR_ARG, "fitch_tree: need at least 2 tips");
   FitchSplitArgs a;
-  PGPU_TRY(split_device(ctx, tree, &a.ops, &a.seg, &a.top, &a.tip_seq));
+  PGPU_TRY(split_device(ctx, tree, &a.ops, &a.seg, &a.top, &a.wseg, &a.tip_seq));
   cudaStream_t s = ctx->stream;
   PGPU_CUDA(ctx, cudaMemsetAsync(total, 0, sizeof(uint64_t), s));
   if (n_words == 0) return PGPU_OK;
@@ -815,12 +851,11 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
   a.n_words = n_words;
   a.n_sites = n_sites;
   a.n_tips = tree->n_tips;
-  a.n_seg = sp.n_seg;
   a.n_top = (int)sp.top.size();
-  a.depth = std::max(sp.max_depth, 1);
-  if (split_smem(a.depth) > ctx->smem_optin)
+  a.rows = sp.rows;
+  if (split_smem(a.rows) > ctx->smem_optin)
     return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: tree needs a stack of %d rows; too deep",
-                        a.depth);
+                        a.rows);
   const size_t tiles = (n_words + 127) / 128;
   cudaError_t e;
   switch (lb) {

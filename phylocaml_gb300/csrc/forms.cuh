@@ -64,9 +64,9 @@ __device__ __forceinline__ double csum_block(const double2 *p, long long n) {
 // Fp32  values float;  P buffer holds fl32(P - I);  y_i = x_i + sum_j D_ij x_j
 // Fp64  values double; P buffer holds P;            y_i = sum_j P_ij x_j
 // Ff32  values are unevaluated float pairs (hi + lo, about 48 significant
-//       bits); P buffer holds (hi, lo) pairs of P - I; every sum and product
-//       is an error-free float transformation, so the only roundings are of
-//       the order of 2^-48.  Sites that share subtree patterns share their
+//       bits); P buffer holds (hi, lo) pairs of P; every sum and product is
+//       an error-free float transformation, so the only roundings are of the
+//       order of 2^-48.  Sites that share subtree patterns share their
 //       rounding errors, which then add up linearly over the patterns; the
 //       pair form keeps that sum far below 1e-3 where plain FP32 cannot.
 
@@ -269,28 +269,32 @@ struct Ff32 {
     y[2] = {b.x, b.y};
     y[3] = {b.z, b.w};
   }
-  __device__ static void rows(const Coef *D, const V *x, V *y) {
+  // y_i = sum_j P_ij x_j with P as (hi, lo) pairs: every product exact
+  // (TwoProduct), the hi products summed with TwoSum, the small cross terms
+  // (P_hi x_lo, P_lo x_hi) and all rounding errors gathered in one float.
+  // The terms are all non-negative, so the pair keeps about 48 bits.
+  __device__ static void rows(const Coef *P, const V *x, V *y) {
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      const float4 d01 = reinterpret_cast<const float4 *>(D)[2 * i];
-      const float4 d23 = reinterpret_cast<const float4 *>(D)[2 * i + 1];
-      const float dh[4] = {d01.x, d01.z, d23.x, d23.z};
-      const float dl[4] = {d01.y, d01.w, d23.y, d23.w};
-      // c = sum_j D_ij x_j with the exact product errors and sum errors kept
-      float sh = 0.0f, sl = 0.0f;
+      const float4 d01 = reinterpret_cast<const float4 *>(P)[2 * i];
+      const float4 d23 = reinterpret_cast<const float4 *>(P)[2 * i + 1];
+      const float ph[4] = {d01.x, d01.z, d23.x, d23.z};
+      const float pl[4] = {d01.y, d01.w, d23.y, d23.w};
+      float sh = __fmul_rn(ph[0], x[0].h);
+      float lo = __fmaf_rn(ph[0], x[0].h, -sh);
+      lo = __fmaf_rn(ph[0], x[0].l, lo);
+      lo = __fmaf_rn(pl[0], x[0].h, lo);
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const float ph = __fmul_rn(dh[j], x[j].h);
-        float pe = __fmaf_rn(dh[j], x[j].h, -ph);
-        pe = __fmaf_rn(dh[j], x[j].l, pe);
-        pe = __fmaf_rn(dl[j], x[j].h, pe);
-        const ff t = two_sum(sh, ph);
+      for (int j = 1; j < 4; ++j) {
+        const float p = __fmul_rn(ph[j], x[j].h);
+        float e = __fmaf_rn(ph[j], x[j].h, -p);
+        e = __fmaf_rn(ph[j], x[j].l, e);
+        e = __fmaf_rn(pl[j], x[j].h, e);
+        const ff t = two_sum(sh, p);
         sh = t.h;
-        sl = __fadd_rn(sl, __fadd_rn(t.l, pe));
+        lo = __fadd_rn(lo, __fadd_rn(t.l, e));
       }
-      // y = x + c
-      const ff t = two_sum(x[i].h, sh);
-      y[i] = fast_two_sum(t.h, __fadd_rn(t.l, __fadd_rn(x[i].l, sl)));
+      y[i] = fast_two_sum(sh, lo);
     }
   }
 };

@@ -49,16 +49,18 @@ struct TreeSchedule {
   int max_depth = 0;               // largest stack height reached
 };
 
-// The postorder cut into up to 4 disjoint subtrees (segments), each a
-// stack-machine schedule of its own, plus the few nodes above them (top).
-// Segment ops read tips from their own tip sequence and internal children
-// from their own stack; a top op's child reference is a tip id (>= 0), a
-// segment result (-1 - s) or an earlier top result (-100 - t).
+// The postorder cut into disjoint subtrees (segments), each a stack-machine
+// schedule of its own, dealt to the warps of a CTA, plus the few nodes above
+// them (top).  Segment ops read tips from their own tip sequence and
+// internal children from their own stack; a top op's child reference is a
+// tip id (>= 0), a segment result (-1 - (warp * 32 + row)) or an earlier
+// top result (-1000 - t).
 struct SplitSchedule {
-  int n_seg = 0, max_depth = 0;
+  int n_seg = 0, rows = 0;     // rows: ring + stack rows one warp needs
   std::vector<int4> ops;       // segment ops, segments one after another
   std::vector<int32_t> tips;   // segment tip sequences, one after another
-  std::vector<int4> seg;       // {op_off, n_ops, tip_off, n_tips}
+  std::vector<int4> seg;       // {op_off, n_ops, tip_off, n_tips}, by warp
+  std::vector<int4> wseg;      // per warp {first segment, count, 0, 0}
   std::vector<int4> top;       // {k, ref_a, ref_b, 0} in postorder
 };
 

@@ -231,8 +231,9 @@ __global__ void __launch_bounds__(256) compose_kernel(const ComposeArgs p) {
     const size_t off = ((size_t)b * R + r) * SS + (size_t)i * S + j;
     if (p.P) p.P[off] = v;
     if (p.P32) {
-      const double d = (p.p32_mode != P32_PLAIN && i == j) ? v - 1.0 : v;
-      if (p.p32_mode == P32_MINUS_I_PAIRS) {
+      const bool minus_i = p.p32_mode == P32_MINUS_I || p.p32_mode == P32_MINUS_I_PAIRS;
+      const double d = (minus_i && i == j) ? v - 1.0 : v;
+      if (p.p32_mode == P32_MINUS_I_PAIRS || p.p32_mode == P32_PAIRS) {
         const float hi = (float)d;
         p.P32[2 * off] = hi;
         p.P32[2 * off + 1] = (float)(d - (double)hi);

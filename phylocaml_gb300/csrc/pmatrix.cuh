@@ -19,7 +19,8 @@ pgpu_status pgpu_launch_eig(pgpu_ctx *ctx, const double *Q_dev, const double *pi
 enum P32Mode {
   P32_PLAIN = 0,          // fl32(P)
   P32_MINUS_I = 1,        // fl32(P - I)
-  P32_MINUS_I_PAIRS = 2   // (hi, lo) float pairs of P - I, two floats per entry
+  P32_MINUS_I_PAIRS = 2,  // (hi, lo) float pairs of P - I, two floats per entry
+  P32_PAIRS = 3           // (hi, lo) float pairs of P
 };
 pgpu_status pgpu_launch_compose(pgpu_ctx *ctx, const double *U_dev, const double *lam_dev,
                                 const double *Ui_dev, int S, const double *t_dev, int n_br,

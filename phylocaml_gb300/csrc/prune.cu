@@ -454,7 +454,7 @@ pgpu_status prune_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *m,
   PGPU_TRY(pgpu_launch_compose(ctx, dU, dlam, dUi, S, rebase(d, lay.brlen), n_br,
                                rebase(d, lay.rates), R, precision == 64 ? (double *)dP : nullptr,
                                precision == 64 ? nullptr : (float *)dP, false, dst,
-                               precision == 32 ? P32_MINUS_I : precision == 48 ? P32_MINUS_I_PAIRS
+                               precision == 32 ? P32_MINUS_I : precision == 48 ? P32_PAIRS
                                                                                : P32_PLAIN));
   // tip rows in FP64, stored in the form's value type
   const size_t tt_vals = (size_t)n * R * codes->n_codes * S;
