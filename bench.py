@@ -726,7 +726,8 @@ def bench_spr(args, rank, world, local):
     from oracle import spr_oracle as SO
     dev = torch.device(f"cuda:{local}")
     torch.cuda.set_device(dev)
-    tr, spec, pats, w = synth.prune_workload(SPR_TAXA, SPR_SITES, seed=6 + rank, mean_brlen=0.1)
+    tr, spec, pats, w = synth.prune_workload(args.spr_taxa, args.spr_sites, seed=6 + rank,
+                                             mean_brlen=0.1)
     table = synth.dna_code_table()
     n_pat = pats.shape[1]
     ctx = _native.Context(local)
@@ -762,7 +763,7 @@ def bench_spr(args, rank, world, local):
             net.close()
         arms[arm] = r
     ex, le = arms["exhaustive"], arms["learned"]
-    n = SPR_TAXA
+    n = args.spr_taxa
     same = SO.splits(SO.unroot(ex.tree.left, ex.tree.right, ex.tree.brlen), n) == \
         SO.splits(SO.unroot(le.tree.left, le.tree.right, le.tree.brlen), n)
 
@@ -777,9 +778,10 @@ def bench_spr(args, rank, world, local):
         "metric": "wall time to the SPR optimum, learned proposal / exhaustive SPR (same final lnL +-1e-3)",
         "value": le.seconds / ex.seconds, "unit": "ratio", "higher_is_better": False,
         "target": "<= 1/3",
-        "config": {"workload": "learned SPR: 256-taxon Yule tree (BL ~ Exp(0.1)), 50,000 GTR+Gamma4 "
-                               "DNA sites compressed to weighted patterns, random-addition parsimony "
-                               "start, MLP 64-256-256-256-1 (BF16, FP32 accumulate), top-32 proposals",
+        "config": {"workload": f"learned SPR: {args.spr_taxa}-taxon Yule tree (BL ~ Exp(0.1)), "
+                               f"{args.spr_sites:,} GTR+Gamma4 DNA sites compressed to weighted patterns, "
+                               "random-addition parsimony start, MLP 64-256-256-256-1 (BF16, FP32 "
+                               "accumulate), top-32 proposals",
                    "n_patterns": n_pat, "n_moves": nm, "precision": "fp32x2"},
         "start": {"parsimony_length": plen, "seconds": t_start, "lnl_after_brlen": l0},
         "exhaustive": arm_rec(ex), "learned": arm_rec(le),
@@ -803,6 +805,8 @@ def main():
     # smaller runs for profiler captures: a subset of the pruning forms, fewer batch variants
     ap.add_argument("--prune-forms", default="32,48,64")
     ap.add_argument("--batch-variants", type=int, default=BATCH_VARIANTS)
+    ap.add_argument("--spr-taxa", type=int, default=SPR_TAXA)
+    ap.add_argument("--spr-sites", type=int, default=SPR_SITES)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     args.prune_forms = {int(f) for f in args.prune_forms.split(",") if f}

@@ -45,7 +45,6 @@
 namespace {
 
 constexpr int BT_M = 128;          // patterns per tile (TMEM lanes)
-constexpr int BT_SP = 64;          // register bound on padded states
 constexpr int BT_ST = 4;           // ring slots (power of two)
 constexpr int BT_THREADS = 288;    // 8 epilogue warps (thread 0 issues MMAs), producer
 constexpr int BT_TMEM_COLS = 512;
@@ -54,6 +53,7 @@ struct BVar {
   int n_tips, n_ops, S, R, n_codes;
   int Kp, Np, SpT, NCp;            // padded K (A columns), N (D columns), odd tip-row stride, padded code rows
   int n_slots;                     // TMEM stack slots available
+  int RP;                          // rate classes per pass (1 or 2): their MMAs share a step
   int n_tiles;
   long long n_pat;
   long long ld;                    // tip-code row stride in bytes (n_tiles * 128)
@@ -159,22 +159,26 @@ struct EpiIn {
   const double *pi;
 };
 
-// One postorder step for the half row of states [HF*KP/2, (HF+1)*KP/2):
-// the product of the two children (tip rows from the slot, or the MMA
-// results from TMEM), rescaled by a power of two agreed with the other half,
-// written into the node's TMEM stack slot.  KP is a template parameter so
-// that every state index is a compile-time constant and the vectors stay
-// in registers.
-template <int KP>
+// One postorder step for the half row of states [hf*KP/2, (hf+1)*KP/2) of
+// the RP rate classes of this pass: the product of the two children (tip
+// rows from the slot, or the MMA results from TMEM), rescaled by a power of
+// two agreed with the other half, written into the node's TMEM stack slot.
+// KP and RP are template parameters so that every state index is a
+// compile-time constant and the vectors stay in registers.  TMEM columns:
+// D of child h, rate q at (h*RP + q)*Np; stack slot s, rate q at
+// 2*RP*Np + (s*RP + q)*Kp.
+template <int KP, int RP>
 __device__ __forceinline__ void epi_step(const BVar &v, const BatchArgs &p, const EpiIn &in, int hf,
-                                         int lane, int slot, uint64_t *empty, float (*xch)[BT_M],
-                                         int &escale, bool &ok, double &Lp) {
+                                         int lane, int slot, uint64_t *empty, float (*xch)[RP][BT_M],
+                                         int *escale, bool &ok, double *Lp) {
   constexpr int B = KP / 2;
   const int S = v.S;
-  float acc[B];
+  float acc[RP][B];
 #pragma unroll
-  for (int e = 0; e < B; ++e) acc[e] = 1.0f;
-  // e0 = hf * B: both halves are compiled, the warp takes its own
+  for (int q = 0; q < RP; ++q)
+#pragma unroll
+    for (int e = 0; e < B; ++e) acc[q][e] = 1.0f;
+  // both halves are compiled; the warp takes its own (hf is warp-uniform)
   auto half = [&](auto HFc) {
     constexpr int HF = decltype(HFc)::value;
     constexpr int e0 = HF * B;
@@ -188,23 +192,27 @@ __device__ __forceinline__ void epi_step(const BVar &v, const BatchArgs &p, cons
           if (in.active && HF == 0) atomicOr(p.flag, PGPU_FLAG_BADCODE);
           code = 0;
         }
-        const float *row =
-            reinterpret_cast<const float *>(in.sl + 256 + (size_t)h * in.BB) + (size_t)code * v.SpT + e0;
 #pragma unroll
-        for (int e = 0; e < B; ++e)
-          if (e0 + e < S) acc[e] *= row[e];
+        for (int q = 0; q < RP; ++q) {
+          const float *row = reinterpret_cast<const float *>(in.sl + 256 + (size_t)(h * RP + q) * in.BB) +
+                             (size_t)code * v.SpT + e0;
+#pragma unroll
+          for (int e = 0; e < B; ++e)
+            if (e0 + e < S) acc[q][e] *= row[e];
+        }
       } else {
-        float d[n_chunks][16];
 #pragma unroll
-        for (int u = 0; u < n_chunks; ++u)
-          tmem_ld16(in.tmem + in.lane_base + (uint32_t)(h * v.Np + c_first + 16 * u), d[u]);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        for (int q = 0; q < RP; ++q) {
+          float d[n_chunks][16];
 #pragma unroll
-        for (int e = 0; e < B; ++e) {
-          constexpr int dummy = 0;
-          (void)dummy;
-          const int col = e0 + e - c_first;
-          if (e0 + e < S) acc[e] *= d[col / 16][col % 16];
+          for (int u = 0; u < n_chunks; ++u)
+            tmem_ld16(in.tmem + in.lane_base + (uint32_t)((h * RP + q) * v.Np + c_first + 16 * u), d[u]);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int e = 0; e < B; ++e) {
+            const int col = e0 + e - c_first;
+            if (e0 + e < S) acc[q][e] *= d[col / 16][col % 16];
+          }
         }
       }
     }
@@ -214,12 +222,16 @@ __device__ __forceinline__ void epi_step(const BVar &v, const BatchArgs &p, cons
   __syncwarp();
   if (lane == 0) mbar_arrive(&empty[slot]);
   const int e0 = hf * B;
-  // rescale by an exact power of two; the two halves of a row agree
-  float mx = 0.0f;
+  // rescale by an exact power of two per rate class; the two halves agree
+  float mx[RP];
 #pragma unroll
-  for (int e = 0; e < B; ++e)
-    if (e0 + e < S) mx = fmaxf(mx, acc[e]);
-  xch[hf][in.m] = mx;
+  for (int q = 0; q < RP; ++q) {
+    mx[q] = 0.0f;
+#pragma unroll
+    for (int e = 0; e < B; ++e)
+      if (e0 + e < S) mx[q] = fmaxf(mx[q], acc[q][e]);
+    xch[hf][q][in.m] = mx[q];
+  }
   // the exchange barrier also makes the timeout verdict uniform over the
   // epilogue warps, so none can leave the loop alone
   {
@@ -232,44 +244,62 @@ __device__ __forceinline__ void epi_step(const BVar &v, const BatchArgs &p, cons
         : "memory");
     ok = all_ok != 0;
   }
-  mx = fmaxf(mx, xch[hf ^ 1][in.m]);
-  if (mx < 0x1p-32f && mx > 0.0f) {
-    int ex;
-    (void)frexpf(mx, &ex);
-    escale += ex;
-    const int k1 = min(-ex, 120), k2 = -ex - k1;
-    const float f1 = __int_as_float((127 + k1) << 23), f2 = __int_as_float((127 + k2) << 23);
-#pragma unroll
-    for (int e = 0; e < B; ++e) acc[e] = acc[e] * f1 * f2;
-  }
-#pragma unroll
-  for (int e = 0; e < B; ++e)
-    if (e0 + e >= S) acc[e] = 0.0f;
-  // into the TMEM stack slot: my K columns e0 .. e0 + B - 1
   const int so = (in.op.w >> 16) & 0xff;
-  const uint32_t col = (uint32_t)(2 * v.Np + so * v.Kp + e0);
 #pragma unroll
-  for (int c0 = 0; c0 < B; c0 += 4)
-    asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(
-                     in.tmem + in.lane_base + col + (uint32_t)c0),
-                 "r"(__float_as_uint(acc[c0])), "r"(__float_as_uint(acc[c0 + 1])),
-                 "r"(__float_as_uint(acc[c0 + 2])), "r"(__float_as_uint(acc[c0 + 3]))
-                 : "memory");
-  if (in.last) {
-    double l = 0.0;
+  for (int q = 0; q < RP; ++q) {
+    const float m2 = fmaxf(mx[q], xch[hf ^ 1][q][in.m]);
+    if (m2 < 0x1p-32f && m2 > 0.0f) {
+      int ex;
+      (void)frexpf(m2, &ex);
+      escale[q] += ex;
+      const int k1 = min(-ex, 120), k2 = -ex - k1;
+      const float f1 = __int_as_float((127 + k1) << 23), f2 = __int_as_float((127 + k2) << 23);
+#pragma unroll
+      for (int e = 0; e < B; ++e) acc[q][e] = acc[q][e] * f1 * f2;
+    }
 #pragma unroll
     for (int e = 0; e < B; ++e)
-      if (e0 + e < S) l += in.pi[e0 + e] * (double)acc[e];
-    Lp = l;
+      if (e0 + e >= S) acc[q][e] = 0.0f;
+    // into the TMEM stack slot: my K columns e0 .. e0 + B - 1
+    const uint32_t col = (uint32_t)(2 * RP * v.Np + (so * RP + q) * v.Kp + e0);
+#pragma unroll
+    for (int c0 = 0; c0 < B; c0 += 4)
+      asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(
+                       in.tmem + in.lane_base + col + (uint32_t)c0),
+                   "r"(__float_as_uint(acc[q][c0])), "r"(__float_as_uint(acc[q][c0 + 1])),
+                   "r"(__float_as_uint(acc[q][c0 + 2])), "r"(__float_as_uint(acc[q][c0 + 3]))
+                   : "memory");
+    if (in.last) {
+      double l = 0.0;
+#pragma unroll
+      for (int e = 0; e < B; ++e)
+        if (e0 + e < S) l += in.pi[e0 + e] * (double)acc[q][e];
+      Lp[q] = l;
+    }
   }
+}
+
+template <int KP>
+__device__ __forceinline__ void epi_dispatch(const BVar &v, const BatchArgs &p, const EpiIn &in, int hf,
+                                             int lane, int slot, uint64_t *empty, float (*xch1)[1][BT_M],
+                                             float (*xch2)[2][BT_M], int *escale, bool &ok,
+                                             double *Lp) {
+  if constexpr (KP <= 32) {
+    if (v.RP == 2) {
+      epi_step<KP, 2>(v, p, in, hf, lane, slot, empty, xch2, escale, ok, Lp);
+      return;
+    }
+  }
+  epi_step<KP, 1>(v, p, in, hf, lane, slot, empty, xch1, escale, ok, Lp);
 }
 
 __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs p) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint64_t full[BT_ST], empty[BT_ST], mma_bar;
   __shared__ uint32_t tmem_base;
-  __shared__ float xch[2][BT_M];
-  __shared__ double xchd[2][BT_M];
+  __shared__ float xch2[2][2][BT_M];   // per half, rate class of the pass, lane: max entry
+  __shared__ double xchd[2][2][BT_M];
+  float(*xch1)[1][BT_M] = reinterpret_cast<float(*)[1][BT_M]>(&xch2[0][0][0]);
   __shared__ double2 red[4];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -303,7 +333,8 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
         const int BB = blk_bytes(v);
         const uint32_t bmat_bytes = (uint32_t)(v.Np * v.Kp * 4);
         const uint32_t tip_bytes = (uint32_t)(v.NCp * v.SpT * 4);
-        for (int r = 0; r < v.R && ok; ++r) {
+        const int RP = v.RP;
+        for (int r0 = 0; r0 < v.R && ok; r0 += RP) {
           for (int i = 0; i < v.n_ops; ++i, ++seq) {
             const int slot = (int)(seq & (BT_ST - 1));
             const long long round = seq / BT_ST;
@@ -316,22 +347,24 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
             uint32_t tx = 0;
             for (int h = 0; h < 2; ++h) {
               const int ch = h == 0 ? op.y : op.z;
-              tx += ch < v.n_tips ? 128u + tip_bytes : bmat_bytes;
+              tx += ch < v.n_tips ? 128u + RP * tip_bytes : RP * bmat_bytes;
             }
             mbar_arrive_expect_tx(&full[slot], tx);
             for (int h = 0; h < 2; ++h) {
               const int ch = h == 0 ? op.y : op.z;
-              unsigned char *blk = sl + 256 + (size_t)h * BB;
-              if (ch < v.n_tips) {
+              if (ch < v.n_tips)
                 bulk_g2s(sl + h * 128, v.codes + (long long)ch * v.ld + (long long)wk.y * 128, 128u,
                          &full[slot]);
-                bulk_g2s(blk, p.tiptab + v.tip_off + ((long long)ch * v.R + r) * v.NCp * v.SpT,
-                         tip_bytes, &full[slot]);
-              } else {
-                bulk_g2s(blk,
-                         p.bmat + v.bmat_off +
-                             ((long long)(ch - v.n_tips) * v.R + r) * (long long)v.Np * v.Kp,
-                         bmat_bytes, &full[slot]);
+              for (int q = 0; q < RP; ++q) {
+                unsigned char *blk = sl + 256 + (size_t)(h * RP + q) * BB;
+                if (ch < v.n_tips)
+                  bulk_g2s(blk, p.tiptab + v.tip_off + ((long long)ch * v.R + r0 + q) * v.NCp * v.SpT,
+                           tip_bytes, &full[slot]);
+                else
+                  bulk_g2s(blk,
+                           p.bmat + v.bmat_off +
+                               ((long long)(ch - v.n_tips) * v.R + r0 + q) * (long long)v.Np * v.Kp,
+                           bmat_bytes, &full[slot]);
               }
             }
           }
@@ -356,7 +389,6 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
       const int BB = blk_bytes(v);
       const long long pat = (long long)wk.y * BT_M + m;
       const bool active = pat < v.n_pat;
-      const int S = v.S, B = v.Kp / 2, e0 = hf * B;       // my states: e0 .. e0 + B - 1
       const uint32_t LBO = 128, SBO = (uint32_t)(v.Kp / 4) * 128;
       uint32_t idesc = 0;
       idesc |= 1u << 4;
@@ -365,9 +397,10 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
       idesc |= (uint32_t)(v.Np >> 3) << 17;
       idesc |= (uint32_t)(BT_M >> 4) << 24;
       double lnr[4];
-      double Lp = 0.0;   // this half row's share of the root likelihood
-      for (int r = 0; r < v.R && ok; ++r) {
-        int escale = 0;
+      double Lp[2] = {0.0, 0.0};   // this half row's share of the root likelihoods
+      const int RP = v.RP;
+      for (int r0 = 0; r0 < v.R && ok; r0 += RP) {
+        int escale[2] = {0, 0};
         for (int i = 0; i < v.n_ops; ++i, ++seq) {
           const int slot = (int)(seq & (BT_ST - 1));
           const int4 op = __ldg(p.ops + v.ops_off + i);
@@ -382,17 +415,19 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
               if (ch < v.n_tips) continue;
               any = true;
               const int sa = (op.w >> (8 * h)) & 0xff;
-              const uint32_t d_col = (uint32_t)(h * v.Np);
-              const uint32_t a_col = (uint32_t)(2 * v.Np + sa * v.Kp);
-              const unsigned char *blk = sl + 256 + (size_t)h * BB;
-              for (int ks = 0; ks < v.Kp / 8; ++ks) {
-                const uint64_t bd = smem_desc(blk + (size_t)ks * 2 * LBO, LBO, SBO);
-                const uint32_t accf = ks > 0 ? 1u : 0u;
-                asm volatile(
-                    "{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %4, 0;\n\t"
-                    "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, q;\n\t}" ::"r"(tmem + d_col),
-                    "r"(tmem + a_col + (uint32_t)(ks * 8)), "l"(bd), "r"(idesc), "r"(accf)
-                    : "memory");
+              for (int q = 0; q < RP; ++q) {
+                const uint32_t d_col = (uint32_t)((h * RP + q) * v.Np);
+                const uint32_t a_col = (uint32_t)(2 * RP * v.Np + (sa * RP + q) * v.Kp);
+                const unsigned char *blk = sl + 256 + (size_t)(h * RP + q) * BB;
+                for (int ks = 0; ks < v.Kp / 8; ++ks) {
+                  const uint64_t bd = smem_desc(blk + (size_t)ks * 2 * LBO, LBO, SBO);
+                  const uint32_t accf = ks > 0 ? 1u : 0u;
+                  asm volatile(
+                      "{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %4, 0;\n\t"
+                      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, q;\n\t}" ::"r"(tmem + d_col),
+                      "r"(tmem + a_col + (uint32_t)(ks * 8)), "l"(bd), "r"(idesc), "r"(accf)
+                      : "memory");
+                }
               }
             }
             if (any) {
@@ -419,16 +454,18 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           EpiIn in{op, sl, BB, tmem, lane_base, m, active, i == v.n_ops - 1, p.pis + v.pi_off};
+#define EPI(K) epi_dispatch<K>(v, p, in, hf, lane, slot, empty, xch1, xch2, escale, ok, Lp)
           switch (v.Kp) {
-            case 8: epi_step<8>(v, p, in, hf, lane, slot, empty, xch, escale, ok, Lp); break;
-            case 16: epi_step<16>(v, p, in, hf, lane, slot, empty, xch, escale, ok, Lp); break;
-            case 24: epi_step<24>(v, p, in, hf, lane, slot, empty, xch, escale, ok, Lp); break;
-            case 32: epi_step<32>(v, p, in, hf, lane, slot, empty, xch, escale, ok, Lp); break;
-            case 40: epi_step<40>(v, p, in, hf, lane, slot, empty, xch, escale, ok, Lp); break;
-            case 48: epi_step<48>(v, p, in, hf, lane, slot, empty, xch, escale, ok, Lp); break;
-            case 56: epi_step<56>(v, p, in, hf, lane, slot, empty, xch, escale, ok, Lp); break;
-            default: epi_step<64>(v, p, in, hf, lane, slot, empty, xch, escale, ok, Lp); break;
+            case 8: EPI(8); break;
+            case 16: EPI(16); break;
+            case 24: EPI(24); break;
+            case 32: EPI(32); break;
+            case 40: EPI(40); break;
+            case 48: EPI(48); break;
+            case 56: EPI(56); break;
+            default: EPI(64); break;
           }
+#undef EPI
           asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
           // every vector of this step is in TMEM before the next MMA issues
@@ -436,11 +473,13 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
           if (!ok) break;
         }
         if (!ok) break;
-        // root of this rate pass (both halves of the row)
-        xchd[hf][m] = Lp;
+        // roots of this pass's rate classes (both halves of the row)
+        for (int q = 0; q < RP; ++q) xchd[hf][q][m] = Lp[q];
         asm volatile("bar.sync 1, 256;" ::: "memory");
-        const double L = Lp + xchd[hf ^ 1][m];
-        lnr[r] = log(L) + (double)escale * 0.69314718055994530942;
+        for (int q = 0; q < RP; ++q) {
+          const double L = Lp[q] + xchd[hf ^ 1][q][m];
+          lnr[r0 + q] = log(L) + (double)escale[q] * 0.69314718055994530942;
+        }
         asm volatile("bar.sync 1, 256;" ::: "memory");
       }
       // join the rate classes: log sum_r probs[r] exp(lnr[r])
@@ -781,6 +820,9 @@ pgpu_status pgpu_batch_create(pgpu_ctx *ctx, const pgpu_variant *vs, int n_var, 
     v.ctab_off = (long long)ctab.size();
     for (int r = 0; r < 4; ++r) v.probs[r] = r < R ? m.probs[r] : 0.0;
     if (sch.max_depth > v.n_slots) return fail(PGPU_ERR_LIMIT, "tree too deep for the TMEM stack", vi);
+    // two rate classes per pass when their D columns and stacks fit in TMEM
+    v.RP = 1;
+    if (R % 2 == 0 && v.Kp <= 32 && (BT_TMEM_COLS - 4 * v.Np) / (2 * v.Kp) >= sch.max_depth) v.RP = 2;
     b->max_depth = std::max(b->max_depth, sch.max_depth);
     // TMEM stack positions from the stack simulation
     int sp = 0;
@@ -804,7 +846,7 @@ pgpu_status pgpu_batch_create(pgpu_ctx *ctx, const pgpu_variant *vs, int n_var, 
     tt_off = (tt_off + 3) / 4 * 4;
     pat_off += v.n_pat;
     const size_t blk = std::max<size_t>((size_t)v.Np * v.Kp * 4, (size_t)v.NCp * v.SpT * 4);
-    max_blk = std::max(max_blk, (blk + 127) & ~size_t(127));
+    max_blk = std::max(max_blk, (size_t)v.RP * ((blk + 127) & ~size_t(127)));
     // eigen group by state count
     int g = -1;
     for (size_t k = 0; k < b->group_S.size(); ++k)
