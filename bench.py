@@ -225,9 +225,8 @@ def bench_fitch(args, rank, world, local):
     launches = ctx.launches - launches0
     elapsed_ms = t_start.elapsed_time(t_end)
     if world > 1:
-        t = torch.tensor([elapsed_ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+        from phylocaml_gb300 import shard
+        elapsed_ms = shard.max_over_ranks(elapsed_ms, dev)
     per_launch_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
 
     # parity on this run: a slice of sites against the restated bv_fitch
@@ -428,9 +427,8 @@ def bench_prune(args, rank, world, local):
         torch.cuda.synchronize(dev)
         el = t0.elapsed_time(t1)
         if world > 1:
-            tt = torch.tensor([el], device=dev, dtype=torch.float64)
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            el = float(tt.item())
+            from phylocaml_gb300 import shard
+            el = shard.max_over_ranks(el, dev)
         return el, statistics.mean(a.elapsed_time(b) for a, b in ev), ctx.launches - l0, \
             float(out.item())
 
@@ -657,9 +655,8 @@ def bench_batch(args, rank, world, local):
     ungraphed_ms = e0.elapsed_time(e1)
     el = t0.elapsed_time(t1)
     if world > 1:
-        tt = torch.tensor([el], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        el = float(tt.item())
+        from phylocaml_gb300 import shard
+        el = shard.max_over_ranks(el, dev)
     launches = ctx.launches - l0 if graph is None else k * 4
     # FP64 comparison on the first BATCH_SAMPLE patterns of every variant
     f64 = b.run_fp64(BATCH_SAMPLE)
