@@ -592,6 +592,19 @@ def batch_data(rank, device, n_var=BATCH_VARIANTS):
     return out
 
 
+def batch_traffic(work_items: int):
+    """DRAM bytes of one batch launch, from the ncu capture of the 8-variant
+    case scaled by the work items (the traffic is per (variant, tile))."""
+    t = profile_traffic("batch_tc_kernel_8var")
+    p = REPO / "profiles" / "batch_tc_kernel_8var.md"
+    if t is None or not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("work_items_per_launch:"):
+            return t * work_items / float(line.split(":", 1)[1])
+    return None
+
+
 def bench_batch(args, rank, world, local):
     import torch
     from phylocaml_gb300 import _native
@@ -679,9 +692,9 @@ def bench_batch(args, rank, world, local):
         "metric": "node-site-pattern updates/s, 2,048 protein/codon variants in one persistent launch",
         "value": world * units * k / (el * 1e-3), "unit": "node-site-pattern updates/s",
         "ms_per_step": el / k, "steps": k, "dtype": "tf32 (fp32 accumulate)",
-        "config": {"workload": "batch: 2,048 variants x 128 taxa, patterns ~ U{5,000..200,000}; "
-                               "even: 20-state LogNormal/Dirichlet Q + Gamma4; odd: 61-state codon "
-                               "Q (kappa ~ U(1,4), omega ~ U(0.1,1))",
+        "config": {"workload": f"batch: {len(variants):,} variants x 128 taxa, patterns ~ "
+                               "U{5,000..200,000}; even: 20-state LogNormal/Dirichlet Q + Gamma4; "
+                               "odd: 61-state codon Q (kappa ~ U(1,4), omega ~ U(0.1,1))",
                    "patterns": n_pat_total, "work_items": b.work_items,
                    "graph_captured": graph is not None, "ungraphed_ms_per_step": ungraphed_ms},
         "lnl_error_vs_fp64": {"sample_patterns_per_variant": BATCH_SAMPLE,
@@ -694,7 +707,9 @@ def bench_batch(args, rank, world, local):
         "roofline": {"bound": "tensor", "achieved": flops / per_s / 1e12, "peak": tf32_peak,
                      "unit": "TFLOP/s", "frac": flops / per_s / 1e12 / tf32_peak,
                      "peak_source": f"derived: TF32 dense = half the {peak_src} BF16 figure",
-                     "algorithmic_flops_per_step": flops, "kernel": "batch_tc_kernel"},
+                     "algorithmic_flops_per_step": flops, "kernel": "batch_tc_kernel",
+                     "traffic": batch_traffic(b.work_items),
+                     "traffic_note": "ncu DRAM bytes of the 8-variant launch scaled by work items"},
         "gpu_launches": int(launches), "clocks": clk,
     }
     if graph is None:
