@@ -230,8 +230,7 @@ __global__ void __launch_bounds__(32 + PR_THREADS) prune_tree_kernel(const Prune
     auto mx = fmax(fmax(Pol::mag(acc[0]), Pol::mag(acc[1])), fmax(Pol::mag(acc[2]), Pol::mag(acc[3])));
     if (__any_sync(0xffffffffu, mx < Pol::thresh && mx > 0)) {
       if (mx < Pol::thresh && mx > 0) {
-        int ex;
-        (void)frexp((double)mx, &ex);
+        const int ex = frexp_exp(mx);
         escale += ex;
         // two steps when the largest entry is subnormal, so each factor
         // stays a normal power of two

@@ -57,8 +57,7 @@ __device__ __forceinline__ void rescale(typename Pol::V *acc, int &sc) {
 #pragma unroll
     for (int o = 1; o < RT; o <<= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (mx < Pol::thresh && mx > 0) {
-      int ex;
-      (void)frexp((double)mx, &ex);
+      const int ex = frexp_exp(mx);
       sc += ex;
       const int k1 = min(-ex, 120), k2 = -ex - k1;
 #pragma unroll
