@@ -352,8 +352,8 @@ FORMS = {32: "fp32", 48: "fp32x2", 64: "fp64"}
 # a P x child product (internal children only; tip children are table rows),
 # and per node and rate class for the product of the two children and the
 # rescale test
-FP32_INSTR_PER_ROW = {32: 5, 48: 43}
-FP32_INSTR_PER_NODE = {32: 4 + 6, 48: 4 * 7 + 6}
+FP32_INSTR_PER_ROW = {32: 5, 48: 37}
+FP32_INSTR_PER_NODE = {32: 4 + 6, 48: 4 * 4 + 6}
 
 
 def prune_data(rank):

@@ -269,7 +269,15 @@ struct Ff32 {
   __device__ static V zero() { return {0.0f, 0.0f}; }
   __device__ static float mag(V v) { return v.h; }
   __device__ static double to_d(V v) { return (double)v.h + (double)v.l; }
-  __device__ static V mul(V a, V b) { return ff_mul(a, b); }
+  // exact product left unnormalised: the low word stays within a few ulps
+  // of the high word, which every consumer of the pair tolerates
+  __device__ static V mul(V a, V b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return {p, e};
+  }
   __device__ static V scale(V v, int k) {
     const float f = pow2f(k);
     return {v.h * f, v.l * f};
@@ -283,9 +291,10 @@ struct Ff32 {
     y[3] = {b.z, b.w};
   }
   // y_i = sum_j P_ij x_j with P as (hi, lo) pairs: every product exact
-  // (TwoProduct), the hi products summed with TwoSum, the small cross terms
-  // (P_hi x_lo, P_lo x_hi) and all rounding errors gathered in one float.
-  // The terms are all non-negative, so the pair keeps about 48 bits.
+  // (TwoProduct), the hi products summed exactly (the terms are
+  // non-negative, so max/min orders them for Fast2Sum), the small cross
+  // terms (P_hi x_lo, P_lo x_hi) and all rounding errors gathered in one
+  // float.  The pair keeps about 48 bits and is left unnormalised.
   __device__ static void rows(const Coef *P, const V *x, V *y) {
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -303,11 +312,11 @@ struct Ff32 {
         float e = __fmaf_rn(ph[j], x[j].h, -p);
         e = __fmaf_rn(ph[j], x[j].l, e);
         e = __fmaf_rn(pl[j], x[j].h, e);
-        const ff t = two_sum(sh, p);
+        const ff t = fast_two_sum(fmaxf(sh, p), fminf(sh, p));
         sh = t.h;
         lo = __fadd_rn(lo, __fadd_rn(t.l, e));
       }
-      y[i] = fast_two_sum(sh, lo);
+      y[i] = {sh, lo};
     }
   }
 };
