@@ -57,10 +57,22 @@ struct PruneArgs {
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
-constexpr int PR_STAGES = 8;      // ring depth in postorder steps (power of two)
 constexpr int PR_THREADS = 256;   // consumer threads per CTA
 
-// Shared memory of one CTA: PR_STAGES per-op slots, then the CLV stack.
+// Ring depth in postorder steps (a power of two) and the CTAs each SM should
+// hold.  The pair form's slots and stack are twice the FP32 form's, so its
+// ring is shorter to fit three CTAs (27 warps) per SM.
+template <typename Pol> struct PruneTune {
+  static constexpr int stages = 8, min_ctas = 1;
+};
+template <> struct PruneTune<pgpu_forms::Ff32> {
+  static constexpr int stages = 4, min_ctas = 3;
+};
+template <> struct PruneTune<pgpu_forms::Fp32> {
+  static constexpr int stages = 8, min_ctas = 4;
+};
+
+// Shared memory of one CTA: the ring of per-op slots, then the CLV stack.
 // A slot holds everything one postorder step reads, staged by the producer:
 //   [0, NP)            tip codes of child a (if a is a tip)
 //   [NP, 2 NP)         tip codes of child b
@@ -83,7 +95,7 @@ struct PruneLayout {
   }
   __host__ __device__ static size_t ring_off() { return 128; }
   __host__ __device__ static size_t stk_off(int NP, int R, int n_codes) {
-    return ring_off() + (size_t)PR_STAGES * slot_bytes(NP, R, n_codes);
+    return ring_off() + (size_t)PruneTune<Pol>::stages * slot_bytes(NP, R, n_codes);
   }
   __host__ __device__ static size_t bytes(int NP, int R, int n_codes, int depth) {
     return stk_off(NP, R, n_codes) + (size_t)depth * 4 * PR_THREADS * sizeof(V);
@@ -96,11 +108,12 @@ struct PruneLayout {
 // and its own power-of-two scaler.  All lanes of a warp read the same
 // coefficient block (a shared-memory broadcast).
 template <typename Pol, int RT>
-__global__ void __launch_bounds__(32 + PR_THREADS) prune_tree_kernel(const PruneArgs p) {
+__global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
+    prune_tree_kernel(const PruneArgs p) {
   using V = typename Pol::V;
   using Coef = typename Pol::Coef;
   using L = PruneLayout<Pol>;
-  constexpr int ST = PR_STAGES, NT = PR_THREADS;
+  constexpr int ST = PruneTune<Pol>::stages, NT = PR_THREADS;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ double2 red[NT / 32];
   __shared__ double2 xch[RT][NT / RT];   // per pattern and rate class: (part, scaler)
@@ -167,30 +180,25 @@ __global__ void __launch_bounds__(32 + PR_THREADS) prune_tree_kernel(const Prune
   const bool active = pat < p.n_pat;
   const bool rate_on = r < R;
 
+  // The stack discipline is fixed by the schedule: in postorder the result
+  // of step i - 1 is always the second child of step i when that child is
+  // internal, else its first child when that one is internal; a step with
+  // two tip children leaves it pending (push), and a step with two internal
+  // children takes its first child from the stack (pop).  So the top of the
+  // stack lives in registers and each step is one of four straight-line
+  // cases, chosen by a warp-uniform branch.
   V top[4];
-  bool top_valid = false;
+  V *my = stk + c;   // this thread's column of the stack: entry (k, e) at my[(4 k + e) NT]
   int sp = 0, escale = 0;
+  uint32_t code_max = 0;
   bool ok = true;
-
-  auto pop = [&](V *dst) {
-    if (top_valid) {
-#pragma unroll
-      for (int e = 0; e < 4; ++e) dst[e] = top[e];
-      top_valid = false;
-    } else {
-      --sp;
-#pragma unroll
-      for (int e = 0; e < 4; ++e) dst[e] = stk[((size_t)sp * 4 + e) * NT + c];
-    }
-  };
+  const size_t tipb = L::tip_off(NP, R) + (size_t)r * NC * 4 * sizeof(V);
+  const size_t coefb = L::coef_off(NP) + (size_t)r * 16 * sizeof(Coef);
 
   for (int i = 0; i < p.n_ops && ok; ++i) {
     const int slot = i & (ST - 1);
     const int4 op = __ldg(p.ops + i);
-    const int a = op.y, b = op.z;
-    V xa[4], xb[4];
-    if (b >= p.n_tips) pop(xb);
-    if (a >= p.n_tips) pop(xa);
+    const int kind = (op.y >= p.n_tips ? 1 : 0) | (op.z >= p.n_tips ? 2 : 0);
     const bool got =
         __all_sync(0xffffffffu, mbar_wait_bounded(&full[slot], (i / ST) & 1, p.flag));
     if (!got) {
@@ -200,24 +208,52 @@ __global__ void __launch_bounds__(32 + PR_THREADS) prune_tree_kernel(const Prune
     const unsigned char *sl = ring + (size_t)slot * SB;
     V acc[4];
     if (rate_on) {
-      V y[2][4];
+      auto tip = [&](int h, V *y) {
+        const uint32_t code = sl[h * NP + pl];
+        code_max = max(code_max, code);
+        Pol::load_tip(sl + tipb + h * TB, min(code, (uint32_t)NC - 1u), y);
+      };
+      auto coef = [&](int h) { return reinterpret_cast<const Coef *>(sl + coefb + h * CB); };
+      V y0[4], y1[4];
+      switch (kind) {
+        case 0:   // two tips; the previous result waits on the stack
+          if (i > 0) {
+            if (sp < p.depth) {
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int ch = h == 0 ? a : b;
-        if (ch < p.n_tips) {
-          int code = sl[h * NP + pl];
-          if (code >= NC) {
-            if (active && r == 0) atomicOr(p.flag, PGPU_FLAG_BADCODE);
-            code = 0;
+              for (int e = 0; e < 4; ++e) my[(4 * sp + e) * NT] = top[e];
+              ++sp;
+            } else {
+              ok = false;   // schedule and stack size disagree
+            }
           }
-          Pol::load_tip(sl + L::tip_off(NP, R) + h * TB, (size_t)r * NC + code, y[h]);
-        } else {
-          Pol::rows(reinterpret_cast<const Coef *>(sl + L::coef_off(NP) + h * CB) + r * 16,
-                    h == 0 ? xa : xb, y[h]);
+          tip(0, y0);
+          tip(1, y1);
+          break;
+        case 1:   // internal first child (the previous result), tip second
+          Pol::rows(coef(0), top, y0);
+          tip(1, y1);
+          break;
+        case 2:   // tip first, internal second child (the previous result)
+          tip(0, y0);
+          Pol::rows(coef(1), top, y1);
+          break;
+        default: {   // both internal: the first from the stack
+          V xa[4];
+          if (sp > 0) {
+            --sp;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) xa[e] = my[(4 * sp + e) * NT];
+          } else {
+            ok = false;   // schedule and stack disagree
+#pragma unroll
+            for (int e = 0; e < 4; ++e) xa[e] = Pol::zero();
+          }
+          Pol::rows(coef(0), xa, y0);
+          Pol::rows(coef(1), top, y1);
         }
       }
 #pragma unroll
-      for (int e = 0; e < 4; ++e) acc[e] = Pol::mul(y[0][e], y[1][e]);
+      for (int e = 0; e < 4; ++e) acc[e] = Pol::mul(y0[e], y1[e]);
     } else {
 #pragma unroll
       for (int e = 0; e < 4; ++e) acc[e] = Pol::zero();
@@ -243,15 +279,10 @@ __global__ void __launch_bounds__(32 + PR_THREADS) prune_tree_kernel(const Prune
         }
       }
     }
-    if (top_valid) {
-#pragma unroll
-      for (int e = 0; e < 4; ++e) stk[((size_t)sp * 4 + e) * NT + c] = top[e];
-      ++sp;
-    }
 #pragma unroll
     for (int e = 0; e < 4; ++e) top[e] = acc[e];
-    top_valid = true;
   }
+  if (active && r == 0 && rate_on && code_max >= (uint32_t)NC) atomicOr(p.flag, PGPU_FLAG_BADCODE);
 
   // root: sum over rate classes of probs[r] 2^e_r sum_i pi_i x_i, in FP64;
   // the rate classes of a pattern meet in shared memory
