@@ -117,6 +117,7 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ double2 red[NT / 32];
   __shared__ double2 xch[RT][NT / RT];   // per pattern and rate class: (part, scaler)
+  __shared__ int step_kind[ST];          // per slot: which of the consumer's step cases
   const int NP = p.NP, R = p.R, NC = p.n_codes;
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);     // [ST]
   uint64_t *empty = full + ST;                              // [ST]
@@ -153,6 +154,11 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
           const int ch = h == 0 ? op.y : op.z;
           tx += ch < p.n_tips ? code_bytes + (uint32_t)TB : (uint32_t)CB;
         }
+        // bit 0: first child internal, bit 1: second child internal; 4 marks
+        // the first step, which has no earlier result to set aside.  The
+        // arrive below releases this store to the consumers' wait.
+        const int kind = (op.y >= p.n_tips ? 1 : 0) | (op.z >= p.n_tips ? 2 : 0);
+        step_kind[slot] = i == 0 ? 4 : kind;
         mbar_arrive_expect_tx(&full[slot], tx);
         for (int h = 0; h < 2; ++h) {
           const int ch = h == 0 ? op.y : op.z;
@@ -179,6 +185,9 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
   const size_t pat = tile0 + pl;
   const bool active = pat < p.n_pat;
   const bool rate_on = r < R;
+  // warps of a rate class beyond R (R < RT) repeat class R - 1 and are
+  // dropped at the root, so the step loop has no branch on the rate
+  const int rr = min(r, R - 1);
 
   // The stack discipline is fixed by the schedule: in postorder the result
   // of step i - 1 is always the second child of step i when that child is
@@ -192,22 +201,21 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
   int sp = 0, escale = 0;
   uint32_t code_max = 0;
   bool ok = true;
-  const size_t tipb = L::tip_off(NP, R) + (size_t)r * NC * 4 * sizeof(V);
-  const size_t coefb = L::coef_off(NP) + (size_t)r * 16 * sizeof(Coef);
+  const size_t tipb = L::tip_off(NP, R) + (size_t)rr * NC * 4 * sizeof(V);
+  const size_t coefb = L::coef_off(NP) + (size_t)rr * 16 * sizeof(Coef);
 
   for (int i = 0; i < p.n_ops && ok; ++i) {
     const int slot = i & (ST - 1);
-    const int4 op = __ldg(p.ops + i);
-    const int kind = (op.y >= p.n_tips ? 1 : 0) | (op.z >= p.n_tips ? 2 : 0);
     const bool got =
         __all_sync(0xffffffffu, mbar_wait_bounded(&full[slot], (i / ST) & 1, p.flag));
     if (!got) {
       ok = false;
       break;
     }
+    const int kind = step_kind[slot];
     const unsigned char *sl = ring + (size_t)slot * SB;
     V acc[4];
-    if (rate_on) {
+    {
       auto tip = [&](int h, V *y) {
         const uint32_t code = sl[h * NP + pl];
         code_max = max(code_max, code);
@@ -217,15 +225,17 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
       V y0[4], y1[4];
       switch (kind) {
         case 0:   // two tips; the previous result waits on the stack
-          if (i > 0) {
-            if (sp < p.depth) {
+          if (sp < p.depth) {
 #pragma unroll
-              for (int e = 0; e < 4; ++e) my[(4 * sp + e) * NT] = top[e];
-              ++sp;
-            } else {
-              ok = false;   // schedule and stack size disagree
-            }
+            for (int e = 0; e < 4; ++e) my[(4 * sp + e) * NT] = top[e];
+            ++sp;
+          } else {
+            ok = false;   // schedule and stack size disagree
           }
+          tip(0, y0);
+          tip(1, y1);
+          break;
+        case 4:   // the first step: two tips, nothing to set aside
           tip(0, y0);
           tip(1, y1);
           break;
@@ -237,7 +247,7 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
           tip(0, y0);
           Pol::rows(coef(1), top, y1);
           break;
-        default: {   // both internal: the first from the stack
+        default: {   // 3, both internal: the first from the stack
           V xa[4];
           if (sp > 0) {
             --sp;
@@ -254,18 +264,16 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
       }
 #pragma unroll
       for (int e = 0; e < 4; ++e) acc[e] = Pol::mul(y0[e], y1[e]);
-    } else {
-#pragma unroll
-      for (int e = 0; e < 4; ++e) acc[e] = Pol::zero();
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[slot]);
     // exact power-of-two rescaling of this rate class's vector (each rate
     // class keeps its own scaler; the root aligns them); rare, so the warp
-    // only enters when some lane needs it
+    // only enters when some lane needs it.  An all-zero vector (a site the
+    // tree cannot produce) rescales to zeros again and ends as log 0 = -inf.
     auto mx = fmax(fmax(Pol::mag(acc[0]), Pol::mag(acc[1])), fmax(Pol::mag(acc[2]), Pol::mag(acc[3])));
-    if (__any_sync(0xffffffffu, mx < Pol::thresh && mx > 0)) {
-      if (mx < Pol::thresh && mx > 0) {
+    if (__any_sync(0xffffffffu, mx < Pol::thresh)) {
+      if (mx < Pol::thresh) {
         const int ex = frexp_exp(mx);
         escale += ex;
         // two steps when the largest entry is subnormal, so each factor

@@ -125,13 +125,14 @@ def test_small_config_fp64_and_fp32(ctx, orc):
 
 
 @pytest.mark.parametrize("shape", ["yule", "caterpillar", "balanced"])
-@pytest.mark.parametrize("rates", ["constant", "gamma4", "custom8"])
+@pytest.mark.parametrize("rates", ["constant", "gamma3", "gamma4", "custom8"])
 def test_trees_and_rate_classes(ctx, orc, shape, rates):
     from phylocaml_gb300 import likelihood as Lk
     rng = np.random.default_rng(hash((shape, rates)) % 2**32)
     tr = {"yule": lambda: T.yule(64, rng, 0.1), "caterpillar": lambda: T.caterpillar(150, 0.05),
           "balanced": lambda: T.balanced(128, 0.08)}[shape]()
-    sv = {"constant": ("Constant",), "gamma4": ("DiscreteGamma", 4, 0.7),
+    sv = {"constant": ("Constant",), "gamma3": ("DiscreteGamma", 3, 0.9),
+          "gamma4": ("DiscreteGamma", 4, 0.7),
           "custom8": ("DiscreteCustom", [(r, 1 / 8) for r in np.linspace(0.2, 1.8, 8)])}[rates]
     spec = M.Spec(("GTR", rng.uniform(0.5, 2, 5)), sv, ("Empirical", rng.dirichlet([5] * 4)))
     m = M.create(spec, ctx)
