@@ -71,6 +71,9 @@ template <> struct PruneTune<pgpu_forms::Ff32> {
 template <> struct PruneTune<pgpu_forms::Fp32> {
   static constexpr int stages = 8, min_ctas = 4;
 };
+// Steps per ring barrier: the producer stages PR_GROUP consecutive steps
+// under one mbarrier phase, so the consumers wait and release once per group.
+constexpr int PR_GROUP = 2;
 
 // Shared memory of one CTA: the ring of per-op slots, then the CLV stack.
 // A slot holds everything one postorder step reads, staged by the producer:
@@ -113,14 +116,15 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
   using V = typename Pol::V;
   using Coef = typename Pol::Coef;
   using L = PruneLayout<Pol>;
-  constexpr int ST = PruneTune<Pol>::stages, NT = PR_THREADS;
+  constexpr int ST = PruneTune<Pol>::stages, NT = PR_THREADS, G = PR_GROUP, NB = ST / G;
+  static_assert(ST % G == 0 && (NB & (NB - 1)) == 0, "ring depth must be a power-of-two number of groups");
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ double2 red[NT / 32];
   __shared__ double2 xch[RT][NT / RT];   // per pattern and rate class: (part, scaler)
-  __shared__ int step_kind[ST];          // per slot: which of the consumer's step cases
+  __shared__ int step_kind[ST];          // per step slot: which of the consumer's step cases
   const int NP = p.NP, R = p.R, NC = p.n_codes;
-  uint64_t *full = reinterpret_cast<uint64_t *>(smem);     // [ST]
-  uint64_t *empty = full + ST;                              // [ST]
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem);     // [NB]
+  uint64_t *empty = full + NB;                              // [NB]
   const size_t SB = L::slot_bytes(NP, R, NC);
   unsigned char *ring = smem + L::ring_off();               // [ST][SB]
   V *stk = reinterpret_cast<V *>(smem + L::stk_off(NP, R, NC));   // [depth][4][NT]
@@ -129,7 +133,7 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
   const size_t CB = L::coef_bytes(R), TB = L::tip_bytes(R, NC);
 
   if (tid == 0) {
-    for (int s = 0; s < ST; ++s) {
+    for (int s = 0; s < NB; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], NT / 32);
     }
@@ -143,37 +147,47 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
       const uint32_t code_bytes = (uint32_t)min((size_t)NP, p.ld_pat - tile0);
       const unsigned char *Pg = static_cast<const unsigned char *>(p.P);
       const unsigned char *Tg = static_cast<const unsigned char *>(p.tiptab);
-      int issued = 0;
-      for (int i = 0; i < p.n_ops; ++i) {
-        const int slot = i & (ST - 1), round = i / ST;
-        if (round > 0 && !mbar_wait_bounded(&empty[slot], (round - 1) & 1, p.flag)) break;
-        const int4 op = __ldg(p.ops + i);
-        unsigned char *sl = ring + (size_t)slot * SB;
+      // step i goes into step slot i % ST; group q (steps qG .. qG + G - 1)
+      // completes barrier q % NB once per pass over the ring
+      int groups = 0;
+      for (int g0 = 0; g0 < p.n_ops; g0 += G) {
+        const int q = g0 / G, b = q & (NB - 1), round = q / NB;
+        if (round > 0 && !mbar_wait_bounded(&empty[b], (round - 1) & 1, p.flag)) break;
+        const int gn = min(G, p.n_ops - g0);
+        int4 ops[G];
         uint32_t tx = 0;
-        for (int h = 0; h < 2; ++h) {
-          const int ch = h == 0 ? op.y : op.z;
-          tx += ch < p.n_tips ? code_bytes + (uint32_t)TB : (uint32_t)CB;
+        for (int k = 0; k < gn; ++k) {
+          const int4 op = __ldg(p.ops + g0 + k);
+          ops[k] = op;
+          for (int h = 0; h < 2; ++h) {
+            const int ch = h == 0 ? op.y : op.z;
+            tx += ch < p.n_tips ? code_bytes + (uint32_t)TB : (uint32_t)CB;
+          }
+          // bit 0: first child internal, bit 1: second child internal; 4
+          // marks the first step, which has no earlier result to set aside.
+          // The arrive below releases these stores to the consumers' wait.
+          const int kind = (op.y >= p.n_tips ? 1 : 0) | (op.z >= p.n_tips ? 2 : 0);
+          step_kind[(g0 + k) & (ST - 1)] = g0 + k == 0 ? 4 : kind;
         }
-        // bit 0: first child internal, bit 1: second child internal; 4 marks
-        // the first step, which has no earlier result to set aside.  The
-        // arrive below releases this store to the consumers' wait.
-        const int kind = (op.y >= p.n_tips ? 1 : 0) | (op.z >= p.n_tips ? 2 : 0);
-        step_kind[slot] = i == 0 ? 4 : kind;
-        mbar_arrive_expect_tx(&full[slot], tx);
-        for (int h = 0; h < 2; ++h) {
-          const int ch = h == 0 ? op.y : op.z;
-          if (ch < p.n_tips) {
-            bulk_g2s(sl + (size_t)h * NP, p.tip_codes + (size_t)ch * p.ld_pat + tile0, code_bytes,
-                     &full[slot]);
-            bulk_g2s(sl + L::tip_off(NP, R) + h * TB, Tg + (size_t)ch * TB, (uint32_t)TB, &full[slot]);
-          } else {
-            bulk_g2s(sl + L::coef_off(NP) + h * CB, Pg + (size_t)ch * CB, (uint32_t)CB, &full[slot]);
+        mbar_arrive_expect_tx(&full[b], tx);
+        for (int k = 0; k < gn; ++k) {
+          unsigned char *sl = ring + (size_t)((g0 + k) & (ST - 1)) * SB;
+          for (int h = 0; h < 2; ++h) {
+            const int ch = h == 0 ? ops[k].y : ops[k].z;
+            if (ch < p.n_tips) {
+              bulk_g2s(sl + (size_t)h * NP, p.tip_codes + (size_t)ch * p.ld_pat + tile0, code_bytes,
+                       &full[b]);
+              bulk_g2s(sl + L::tip_off(NP, R) + h * TB, Tg + (size_t)ch * TB, (uint32_t)TB, &full[b]);
+            } else {
+              bulk_g2s(sl + L::coef_off(NP) + h * CB, Pg + (size_t)ch * CB, (uint32_t)CB, &full[b]);
+            }
           }
         }
-        issued = i + 1;
+        groups = q + 1;
       }
-      for (int i = max(0, issued - ST); i < issued; ++i)
-        (void)mbar_wait_bounded(&full[i & (ST - 1)], (i / ST) & 1, p.flag);
+      // do not leave while copies into this CTA's shared memory are in flight
+      for (int q = max(0, groups - NB); q < groups; ++q)
+        (void)mbar_wait_bounded(&full[q & (NB - 1)], (q / NB) & 1, p.flag);
     }
     return;
   }
@@ -204,14 +218,18 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
   const size_t tipb = L::tip_off(NP, R) + (size_t)rr * NC * 4 * sizeof(V);
   const size_t coefb = L::coef_off(NP) + (size_t)rr * 16 * sizeof(Coef);
 
-  for (int i = 0; i < p.n_ops && ok; ++i) {
-    const int slot = i & (ST - 1);
-    const bool got =
-        __all_sync(0xffffffffu, mbar_wait_bounded(&full[slot], (i / ST) & 1, p.flag));
+  for (int g0 = 0; g0 < p.n_ops && ok; g0 += G) {
+    const int q = g0 / G, b = q & (NB - 1);
+    const bool got = __all_sync(0xffffffffu, mbar_wait_bounded(&full[b], (q / NB) & 1, p.flag));
     if (!got) {
       ok = false;
       break;
     }
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+    const int i = g0 + k;
+    if (i >= p.n_ops) break;
+    const int slot = i & (ST - 1);
     const int kind = step_kind[slot];
     const unsigned char *sl = ring + (size_t)slot * SB;
     V acc[4];
@@ -265,8 +283,6 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
 #pragma unroll
       for (int e = 0; e < 4; ++e) acc[e] = Pol::mul(y0[e], y1[e]);
     }
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[slot]);
     // exact power-of-two rescaling of this rate class's vector (each rate
     // class keeps its own scaler; the root aligns them); rare, so the warp
     // only enters when some lane needs it.  An all-zero vector (a site the
@@ -289,6 +305,10 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
     }
 #pragma unroll
     for (int e = 0; e < 4; ++e) top[e] = acc[e];
+    }
+    // this warp is done with the group's step slots
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[b]);
   }
   if (active && r == 0 && rate_on && code_max >= (uint32_t)NC) atomicOr(p.flag, PGPU_FLAG_BADCODE);
 
