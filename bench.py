@@ -620,10 +620,12 @@ def bench_batch(args, rank, world, local):
     n_pat_total = b.patterns
     units = sum((v.tree.n_internal) * v.n_pat for v in variants)
     flops = 0.0   # unpadded tensor-core MACs x 2: internal children only
+    spill = 0.0   # bytes a design that writes and re-reads every internal vector in HBM would move
     for v in variants:
         S = v.q.shape[0]
         internal_children = int(np.sum(v.tree.left >= v.tree.n_tips) + np.sum(v.tree.right >= v.tree.n_tips))
         flops += 2.0 * S * S * internal_children * len(v.rates) * v.n_pat
+        spill += 2.0 * v.tree.n_internal * v.n_pat * (4 * S * len(v.rates) + 4)
     lnl = torch.zeros(len(variants), dtype=torch.float64, device=dev)
     site = torch.zeros(n_pat_total, dtype=torch.float64, device=dev)
     for _ in range(args.warmup):
@@ -682,7 +684,8 @@ def bench_batch(args, rank, world, local):
     bad_tc = np.flatnonzero(~np.isfinite(tc_sample))
     bad_64 = np.flatnonzero(~np.isfinite(f64))
     ok = np.isfinite(tc_sample) & np.isfinite(f64)
-    err = np.abs(tc_sample - f64)[ok]
+    signed = (tc_sample - f64)[ok]
+    err = np.abs(signed)
     rel = err / np.abs(f64[ok])
     n_nonfinite_sites = int(np.sum(~np.isfinite(site_h)))
     peaks, peak_src = load_peaks()
@@ -700,6 +703,7 @@ def bench_batch(args, rank, world, local):
         "lnl_error_vs_fp64": {"sample_patterns_per_variant": BATCH_SAMPLE,
                               "max_abs": float(err.max()), "median_abs": float(np.median(err)),
                               "max_rel": float(rel.max()), "median_rel": float(np.median(rel)),
+                              "median_signed": float(np.median(signed)),
                               "per_variant_abs_first8": [float(x) for x in err[:8]],
                               "nonfinite_variants_tc": bad_tc[:16].tolist(),
                               "nonfinite_variants_fp64": bad_64[:16].tolist(),
@@ -709,7 +713,15 @@ def bench_batch(args, rank, world, local):
                      "peak_source": f"derived: TF32 dense = half the {peak_src} BF16 figure",
                      "algorithmic_flops_per_step": flops, "kernel": "batch_tc_kernel",
                      "traffic": batch_traffic(b.work_items),
-                     "traffic_note": "ncu DRAM bytes of the 8-variant launch scaled by work items"},
+                     "traffic_note": "ncu DRAM bytes of the 8-variant launch scaled by work items",
+                     # the materialising roofline: every internal vector written and
+                     # read once in HBM, bound max(bytes / HBM, flops / TF32); this
+                     # kernel keeps the vectors in TMEM, so these bytes never move
+                     "spill_model": {"bytes_per_step": spill,
+                                     "bound_ms": 1e3 * max(spill / (peaks["hbm_gbs"] * 1e9),
+                                                           flops / (tf32_peak * 1e12)),
+                                     "frac": 1e3 * max(spill / (peaks["hbm_gbs"] * 1e9),
+                                                       flops / (tf32_peak * 1e12)) / (el / k)}},
         "gpu_launches": int(launches), "clocks": clk,
     }
     if graph is None:

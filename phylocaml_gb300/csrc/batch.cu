@@ -95,6 +95,14 @@ __host__ __device__ inline size_t cm_off(int n, int k, int Kp) {
   return (size_t)(n / 8) * (size_t)(Kp / 4) * 128 + (size_t)(k / 4) * 128 + (n % 8) * 16 + (k % 4) * 4;
 }
 
+// x rounded to the nearest TF32 value (10-bit mantissa), as bits: the MMA
+// then reads an unbiased operand instead of one whose low bits are dropped
+__device__ __forceinline__ uint32_t tf32_bits(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
 __device__ __forceinline__ void tmem_ld16(uint32_t ta, float *v) {
   uint32_t r[16];
   asm volatile(
@@ -266,8 +274,8 @@ __device__ __forceinline__ void epi_step(const BVar &v, const BatchArgs &p, cons
     for (int c0 = 0; c0 < B; c0 += 4)
       asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(
                        in.tmem + in.lane_base + col + (uint32_t)c0),
-                   "r"(__float_as_uint(acc[q][c0])), "r"(__float_as_uint(acc[q][c0 + 1])),
-                   "r"(__float_as_uint(acc[q][c0 + 2])), "r"(__float_as_uint(acc[q][c0 + 3]))
+                   "r"(tf32_bits(acc[q][c0])), "r"(tf32_bits(acc[q][c0 + 1])),
+                   "r"(tf32_bits(acc[q][c0 + 2])), "r"(tf32_bits(acc[q][c0 + 3]))
                    : "memory");
     if (in.last) {
       double l = 0.0;
@@ -592,7 +600,7 @@ __global__ void __launch_bounds__(256) batch_setup_kernel(const SetupArgs a) {
     for (int o = tid; o < v.Np * v.Kp; o += nt) {
       const int n = o / v.Kp, k = o % v.Kp;
       const float x = (n < S && k < S) ? (float)P[n * S + k] : 0.0f;   // P >= 0 after clamping
-      *reinterpret_cast<float *>(out + cm_off(n, k, v.Kp)) = x;
+      *reinterpret_cast<uint32_t *>(out + cm_off(n, k, v.Kp)) = tf32_bits(x);
     }
   }
 }
