@@ -297,6 +297,143 @@ def bench_fitch(args, rank, world, local):
     return rec
 
 
+def bench_tcm(args, rank, world, local):
+    """Cost-matrix medians over the Fitch workload's tree and sites, with the
+    integer cost matrix of a GTR model at branch length 0.1
+    (MlModel.integerized_model) under the general median rule."""
+    import torch
+    from phylocaml_gb300 import _native, synth, costmatrix as CM, mlmodel as M
+    from oracle import tcm_oracle as TO
+
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    tr, masks, w = synth.fitch_workload(FITCH_TAXA, FITCH_SITES, seed=1 + rank, ambiguity=0.03)
+    words = synth.pack_lanes(masks, 4)
+    n_sites, nw = FITCH_SITES, words.shape[1]
+    ld = (nw + 3) // 4 * 4
+    units = tr.n_internal * n_sites
+    ctx = _native.Context(local)
+    stream = torch.cuda.Stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    spec = M.Spec(("GTR", [1.3, 0.7, 1.8, 0.6, 1.1]), ("Constant",),
+                  ("Empirical", [0.28, 0.22, 0.24, 0.26]))
+    tcm = CM.integerized_model(M.create(spec, ctx), 0.1, 4, ctx).astype(np.int32)
+    cm = CM.CostMatrix(tcm, mode="general")
+    tips = torch.zeros((tr.n_tips, ld), dtype=torch.int32, device=dev)
+    tips[:, :nw] = torch.from_numpy(words.view(np.int32)).to(dev)
+    wd = torch.from_numpy(w.view(np.int32)).to(dev)
+    out = torch.empty((tr.n_internal, ld), dtype=torch.int32, device=dev)
+    sc = torch.empty(n_sites, dtype=torch.int32, device=dev)
+    tot = torch.zeros(1, dtype=torch.int64, device=dev)
+    torch.cuda.synchronize(dev)
+    keep: list = []
+
+    def step():
+        cm.tree_cost_dev(tr, tips, ld, n_sites, wd, out, sc, tot, ctx, keep)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    launches0 = ctx.launches
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for i in range(args.steps):
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+    t_end.record(stream)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    clk = clocks.stop()
+    launches = ctx.launches - launches0
+    elapsed_ms = t_start.elapsed_time(t_end)
+    if world > 1:
+        from phylocaml_gb300 import shard
+        elapsed_ms = shard.max_over_ranks(elapsed_ms, dev)
+    per_launch_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    keep.clear()
+
+    # parity on this run: a slice of sites against the restatement
+    check = 20_000
+    cost, assign = TO.fill_tables(tcm, TO.GENERAL, cm.symmetric)
+    exp_node, exp_site, _ = TO.tree_cost(tr.left, tr.right, masks[:, :check], cost, assign)
+    got = synth.unpack_lanes(out[:, : check // 8].cpu().numpy().view(np.uint32), check, 4)
+    sc_host = sc.cpu().numpy().view(np.uint32)
+    parity = bool(np.array_equal(got, exp_node)) and \
+        bool(np.array_equal(sc_host[:check].astype(np.int64), exp_site)) and \
+        int(tot.item()) == int((sc_host.astype(np.uint64) * w.astype(np.uint64)).sum())
+
+    # end to end through the host-buffer C-ABI call
+    ctx.set_stream(None)
+    pin_tips = torch.from_numpy(words.view(np.int32)).pin_memory().numpy().view(np.uint32)
+    pin_w = torch.from_numpy(w.view(np.int32)).pin_memory().numpy().view(np.uint32)
+    pin_out = torch.empty((tr.n_internal, nw), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    pin_sc = torch.empty(n_sites, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    import ctypes as C
+    t_tree, tkeep = _native.make_tree(tr.left, tr.right)
+    total = C.c_uint64(0)
+
+    def e2e_step():
+        ctx.call("pgpu_tcm_tree", C.byref(t_tree), pin_tips.ctypes.data, pin_w.ctypes.data,
+                 n_sites, cm.table.ctypes.data, pin_out.ctypes.data, pin_sc.ctypes.data,
+                 C.byref(total))
+
+    for _ in range(min(args.warmup, 3)):
+        e2e_step()
+    e2e_steps = max(3, min(args.steps, 30))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_ok = np.array_equal(pin_out, out[:, :nw].cpu().numpy().view(np.uint32))
+
+    peaks, peak_src = load_peaks()
+    alg_bytes = 4 * (tr.n_tips * nw + tr.n_internal * nw) + 4 * n_sites + 4 * n_sites
+    achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
+    rec = {
+        "metric": "node-site updates/s (cost-matrix medians, 1,024 taxa x 1e6 sites)",
+        "value": world * units * args.steps / (elapsed_ms * 1e-3), "unit": "node-site updates/s",
+        "ms_per_step": elapsed_ms / args.steps, "steps": args.steps,
+        "dtype": "u32 (4-bit lanes, integer costs)",
+        "config": {"workload": "tcm: the Fitch workload's 1,024-taxon tree and 1e6 sites; integer "
+                               "cost matrix of GTR at t = 0.1 (sigma 4), general median rule",
+                   "tcm": tcm.tolist(), "l2": "inputs (512 MB tips) exceed L2; no flush"},
+        "parity": {"bit_exact_vs_oracle": parity, "checked_sites": check,
+                   "e2e_matches_device": bool(e2e_ok)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "peak_source": peak_src,
+                     "algorithmic_bytes": alg_bytes, "traffic": profile_traffic("tcm_tree_kernel_1024x1e6"),
+                     "kernel": "tcm_tree_kernel", "per_launch_ms": per_launch_ms},
+        "e2e": {"value": units / e2e_s, "unit": "node-site updates/s",
+                "h2d_bytes_per_step": int(words.nbytes + w.nbytes),
+                "d2h_bytes_per_step": int(pin_out.nbytes + pin_sc.nbytes + 8),
+                "ms_per_step": e2e_s * 1e3},
+        "gpu_launches": int(launches), "clocks": clk,
+    }
+    if rank == 0:   # the restatement (numpy, one core) on a bounded sample
+        s = 100_000
+        t0 = time.perf_counter()
+        TO.tree_cost(tr.left, tr.right, masks[:, :s], cost, assign)
+        dt = time.perf_counter() - t0
+        rec["cpu_baseline"] = {"value": tr.n_internal * s / dt, "unit": "node-site updates/s",
+                               "cores": 1, "kind": "port",
+                               "sample": f"{tr.n_tips} taxa x {s:,} of {n_sites:,} sites, "
+                                         f"oracle/tcm_oracle.py tree_cost, {dt:.1f} s"}
+    del tkeep
+    ctx.close()
+    return rec
+
+
 def bench_fitch_reference(args):
     from phylocaml_gb300 import synth
     tr, masks, w = synth.fitch_workload(FITCH_TAXA, FITCH_SITES, seed=1, ambiguity=0.03)
@@ -825,7 +962,8 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["prune", "fitch", "batch", "spr", "all"], default="all")
+    ap.add_argument("--workload", choices=["prune", "fitch", "tcm", "batch", "spr", "all"],
+                    default="all")
     # smaller runs for profiler captures: a subset of the pruning forms, fewer batch variants
     ap.add_argument("--prune-forms", default="32,48,64")
     ap.add_argument("--batch-variants", type=int, default=BATCH_VARIANTS)
@@ -835,7 +973,7 @@ def main():
     args.warmup = max(args.warmup, 3)
     args.prune_forms = {int(f) for f in args.prune_forms.split(",") if f}
     rank, world, local = dist_info()
-    head = args.workload if args.workload in ("fitch", "batch", "spr") else "prune"
+    head = args.workload if args.workload in ("fitch", "tcm", "batch", "spr") else "prune"
 
     if args.impl == "reference":
         if rank != 0:
@@ -856,6 +994,8 @@ def main():
         if args.workload == "all":
             args.steps = steps_given if steps_given is not None else 2000
             rec["fitch"] = bench_fitch(args, rank, world, local)
+            args.steps = steps_given if steps_given is not None else 200
+            rec["tcm"] = bench_tcm(args, rank, world, local)
             args.steps = steps_given if steps_given is not None else 3
             rec["batch"] = bench_batch(args, rank, world, local)
             if rank == 0:
@@ -865,6 +1005,9 @@ def main():
         rec = bench_batch(args, rank, world, local)
     elif head == "spr":
         rec = bench_spr(args, rank, world, local)
+    elif head == "tcm":
+        args.steps = steps_given if steps_given is not None else 200
+        rec = bench_tcm(args, rank, world, local)
     else:
         args.steps = steps_given if steps_given is not None else 2000
         rec = bench_fitch(args, rank, world, local)

@@ -170,6 +170,47 @@ pgpu_status pgpu_fitch_tree_noalloc(const pgpu_tree *tree, const uint32_t *tips_
                                     uint32_t *site_cost_dev, uint64_t *total_dev,
                                     void *cuda_stream);
 
+/* ---- cost-matrix (TCM) medians of state sets ----
+ * The median rule a transformation cost matrix declares
+ * (lib/costMatrix.ml:145-149): find_median_general (:68-86), _metric
+ * (:104-122, medians drawn from the union of the two sets) or _equal
+ * (:89-101, intersection or union at the matrix's equal / unequal cost). */
+enum { PGPU_TCM_GENERAL = 0, PGPU_TCM_METRIC = 1, PGPU_TCM_EQUAL = 2 };
+
+/* Host-only (ctx may be NULL): CostMatrix.Make.create (lib/costMatrix.ml:
+ * 168-183, fill_cm :141-166) for a bit-flag alphabet of n_states (1..4)
+ * atomic states.  tcm is the row-major n_states x n_states cost of atomic
+ * state i to j, each in [0, 2^25].  For every pair of codes a, b in 0..15:
+ *   table[a*16 + b]   packed for the kernels: cost << 4 | median code, or
+ *                     0x80000000 where the pair has no median (a code 0 or
+ *                     a code with bits at or above n_states);
+ *   cost, assign      (optional) the same as plain integers, INT64_MAX / 0
+ *                     where there is no median (the reference's inf, 0).
+ * symmetric != 0 fills a <= b and mirrors it, as the reference does for a
+ * matrix declared symmetric. */
+pgpu_status pgpu_tcm_tables(pgpu_ctx *ctx, const int32_t *tcm, int n_states, int mode,
+                            int symmetric, uint32_t *table, int64_t *cost, int32_t *assign);
+
+/* A tree's postorder under a cost-matrix character (Node.Make1D.median_2,
+ * lib/node.ml:183-198, with CostMatrix.Make.median, lib/costMatrix.ml:194):
+ * internal node k takes table's median code of its children's codes and
+ * adds table's cost.  Sites are 4-bit codes, eight to a word, as for
+ * pgpu_fitch_tree with lane_bits 4; node_sets, site_cost and total as
+ * there, site_cost[s] the sum of the costs over the internal nodes (the
+ * call fails with PGPU_ERR_OVERFLOW if that could exceed 2^32 - 1).  A code
+ * without a median in a site returns PGPU_ERR_ARG. */
+pgpu_status pgpu_tcm_tree(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
+                          const uint32_t *weights, size_t n_sites, const uint32_t *table,
+                          uint32_t *node_sets, uint32_t *site_cost, uint64_t *total);
+
+/* Device-pointer form of pgpu_tcm_tree, asynchronous on the context's
+ * stream; rows ld_words apart, table a host array of 256 entries (staged).
+ * *total_dev is overwritten. */
+pgpu_status pgpu_tcm_tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips_dev,
+                              size_t ld_words, const uint32_t *weights_dev, size_t n_sites,
+                              const uint32_t *table, uint32_t *node_sets_dev,
+                              uint32_t *site_cost_dev, uint64_t *total_dev);
+
 /* ---- substitution models and transition matrices (FP64 on the GPU) ----
  * Q is row-major, rows sum to zero, and reversible with respect to pi
  * (pi_i Q_ij = pi_j Q_ji) -- the models MlModel.create builds

@@ -97,6 +97,9 @@ SIGNATURES: dict[str, tuple] = {
     "pgpu_fitch_tree": (_I, [_P, C.POINTER(PgpuTree), _P, _P, _SZ, _I, _P, _P, _U64P]),
     "pgpu_fitch_tree_dev": (_I, [_P, C.POINTER(PgpuTree), _P, _SZ, _P, _SZ, _I, _P, _P, _P]),
     "pgpu_fitch_tree_noalloc": (_I, [C.POINTER(PgpuTree), _P, _SZ, _P, _SZ, _I, _P, _P, _P, _P]),
+    "pgpu_tcm_tables": (_I, [_P, _P, _I, _I, _I, _P, _P, _P]),
+    "pgpu_tcm_tree": (_I, [_P, C.POINTER(PgpuTree), _P, _P, _SZ, _P, _P, _P, _P]),
+    "pgpu_tcm_tree_dev": (_I, [_P, C.POINTER(PgpuTree), _P, _SZ, _P, _SZ, _P, _P, _P, _P]),
     "pgpu_model_diagonalize": (_I, [_P, _P, _P, _I, _P, _P, _P]),
     "pgpu_model_compose": (_I, [_P, _P, _P, _P, _I, _P, _SZ, _P]),
     "pgpu_prune_lnl": (_I, [_P, C.POINTER(PgpuTree), C.POINTER(PgpuModel),

@@ -1623,16 +1623,24 @@ pgpu_status pgpu_spr_optimize(pgpu_spr *s, int passes, double tol, double *lnl_o
     PGPU_CUDA(s->ctx, cudaMemcpyAsync(nl.data(), s->newlen, ne * 8, cudaMemcpyDeviceToHost, s->ctx->stream));
     PGPU_TRY(sync_check(s, "spr_optimize"));
     old = s->T.len;
-    // take the joint Newton step; halve it while the likelihood drops
+    // take the joint Newton step; halve it until the likelihood rises
     double alpha = 1.0, got = cur;
     bool accepted = false;
-    for (int tries = 0; tries < 5 && !accepted; ++tries, alpha *= 0.5) {
+    for (int tries = 0; tries < 10 && !accepted; ++tries, alpha *= 0.5) {
       for (int e = 0; e < ne; ++e) s->T.len[e] = old[e] + alpha * (nl[e] - old[e]);
       invalidate(s);
       PGPU_TRY(pgpu_spr_lnl(s, &got, nullptr));
-      accepted = got >= cur - 1e-9 * std::fabs(cur);
+      accepted = got > cur;
     }
-    if (!accepted) {
+    // the edges' steps interfere: take them a quarter of the edges at a time
+    for (int g = 0; g < 4 && !accepted; ++g) {
+      s->T.len = old;
+      for (int e = g; e < ne; e += 4) s->T.len[e] = nl[e];
+      invalidate(s);
+      PGPU_TRY(pgpu_spr_lnl(s, &got, nullptr));
+      accepted = got > cur;
+    }
+    if (!accepted) {   // no step improves: converged as far as Newton can see
       s->T.len = old;
       invalidate(s);
       PGPU_TRY(pgpu_spr_lnl(s, &got, nullptr));

@@ -52,7 +52,7 @@ def _target(dl):
 
 
 def exhaustive_spr(eng: SprEngine, eps: float = 1e-3, smooth_passes: int = 2,
-                   final_passes: int = 60, max_rounds: int = 10000) -> SearchResult:
+                   final_passes: int = 200, max_rounds: int = 10000) -> SearchResult:
     import torch
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -78,7 +78,7 @@ def exhaustive_spr(eng: SprEngine, eps: float = 1e-3, smooth_passes: int = 2,
         trace.append((time.perf_counter() - t0, lnl))
     lnl_search = lnl
     t = time.perf_counter()
-    final = eng.optimize(final_passes, 1e-8)
+    final = eng.optimize(final_passes, 1e-6)
     torch.cuda.synchronize()
     tm["final"] = time.perf_counter() - t
     return SearchResult(final, lnl_search, rounds, accepted, exact, rounds,
@@ -117,7 +117,7 @@ class _Replay:
 
 
 def learned_spr(eng: SprEngine, net, k: int = 32, eps: float = 1e-3, smooth_passes: int = 2,
-                final_passes: int = 60, boot_steps: int = 1000, round_steps: int = 8, widen: int = 8,
+                final_passes: int = 200, boot_steps: int = 1000, round_steps: int = 8, widen: int = 8,
                 batch: int = 1024, lr: float = 2e-3, seed: int = 0,
                 max_rounds: int = 10000, diag: list | None = None) -> SearchResult:
     """``net`` is a phylocaml_gb300.mlp.MLP with max_batch >= batch.  With
@@ -236,7 +236,7 @@ def learned_spr(eng: SprEngine, net, k: int = 32, eps: float = 1e-3, smooth_pass
         trace.append((time.perf_counter() - t0, lnl))
     lnl_search = lnl
     t = time.perf_counter()
-    final = eng.optimize(final_passes, 1e-8)
+    final = eng.optimize(final_passes, 1e-6)
     torch.cuda.synchronize()
     tm["final"] = time.perf_counter() - t
     return SearchResult(final, lnl_search, rounds, accepted, exact, exhaustive,
