@@ -264,3 +264,97 @@ def compose(model: Model, t, ctx: _native.Context | None = None) -> np.ndarray:
     ctx.call("pgpu_model_compose", model.u.ctypes.data, model.lam.ctypes.data,
              model.ui.ctypes.data, S, ts.ctypes.data, len(ts), out.ctypes.data)
     return out[0] if np.ndim(t) == 0 else out
+
+
+# ---- model-parameter optimisation hooks ------------------------------------
+# MlModel.gen_subst_opt_func / gen_rates_opt_func / gen_prior_opt_func
+# (lib/mlModel.ml:822-829, "todo" in the reference): each returns the model's
+# current free parameters as a vector and a function that builds the model
+# for another vector.  Vectors are unconstrained, so any optimiser can move
+# them: positive parameters (exchangeabilities, kappa, the Gamma shape) as
+# logs, base frequencies as logs relative to the last state.
+
+def _with(model: Model, ctx, **changes) -> Model:
+    from dataclasses import replace
+    return create(replace(model.spec, **changes), ctx)
+
+
+def gen_subst_opt_func(model: Model, ctx: _native.Context | None = None):
+    """Substitution parameters: GTR's free exchangeabilities (the last is fixed
+    at 1, lib/mlModel.ml:396-400), kappa of K2P/F84/HKY85, (alpha, beta) of
+    TN93; JC69, F81 and a given matrix have none."""
+    s = model.spec.substitution
+    a = model.spec.alphabet_size
+    name = s[0]
+    if name == "GTR":
+        co = np.asarray(s[1] if len(s) > 1 and len(s[1]) else np.ones(((a - 2) * (a + 1)) // 2),
+                        np.float64)
+        return np.log(co), lambda x: _with(model, ctx, substitution=("GTR", list(np.exp(x))))
+    if name in ("K2P", "F84", "HKY85"):
+        return np.log([float(s[1])]), lambda x: _with(model, ctx, substitution=(name, float(np.exp(x[0]))))
+    if name == "TN93":
+        return (np.log([float(s[1][0]), float(s[1][1])]),
+                lambda x: _with(model, ctx, substitution=(name, (float(np.exp(x[0])), float(np.exp(x[1]))))))
+    return np.zeros(0), lambda x: model
+
+
+def gen_rates_opt_func(model: Model, ctx: _native.Context | None = None):
+    """Site-rate parameters: the shape of DiscreteGamma; Constant and a
+    custom rate list have none."""
+    sv = model.spec.site_variation
+    if sv[0] == "DiscreteGamma":
+        k = sv[1]
+        return np.log([float(sv[2])]), lambda x: _with(model, ctx,
+                                                       site_variation=("DiscreteGamma", k, float(np.exp(x[0]))))
+    return np.zeros(0), lambda x: model
+
+
+def gen_prior_opt_func(model: Model, ctx: _native.Context | None = None):
+    """Base frequencies: a - 1 log-ratios against the last state.  JC69 and
+    K2P have uniform stationary frequencies whatever the priors field holds,
+    so they have none."""
+    if model.spec.substitution[0] in ("JC69", "K2P"):
+        return np.zeros(0), lambda x: model
+    pi = np.asarray(model.priors, np.float64)
+
+    def build(x):
+        e = np.exp(np.append(np.asarray(x, np.float64), 0.0))
+        return _with(model, ctx, base_priors=("Empirical", list(e / e.sum())))
+
+    return np.log(pi[:-1] / pi[-1]), build
+
+
+HOOKS = {"subst": gen_subst_opt_func, "rates": gen_rates_opt_func, "prior": gen_prior_opt_func}
+
+
+def optimize_model(model: Model, lnl_of, hooks=("subst", "rates", "prior"), rounds: int = 8,
+                   tol: float = 1e-4, ctx: _native.Context | None = None):
+    """Maximise lnl_of(model) over the hooks' parameters, one hook at a time
+    (L-BFGS with forward-difference gradients, each difference one more
+    lnL), until a round gains less than tol.  Returns (model, lnl, calls)."""
+    from scipy.optimize import minimize
+    calls = 0
+    best = lnl_of(model)
+    calls += 1
+    for _ in range(rounds):
+        start = best
+        for h in hooks:
+            x0, build = HOOKS[h](model, ctx)
+            if len(x0) == 0:
+                continue
+            cache = {}
+
+            def neg(x):
+                nonlocal calls
+                key = tuple(np.round(x, 12))
+                if key not in cache:
+                    calls += 1
+                    cache[key] = -lnl_of(build(x))
+                return cache[key]
+
+            res = minimize(neg, x0, method="L-BFGS-B", options={"eps": 1e-5, "maxiter": 60})
+            if -res.fun > best:
+                model, best = build(res.x), -res.fun
+        if best - start < tol:
+            break
+    return model, best, calls

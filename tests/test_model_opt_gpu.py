@@ -1,0 +1,62 @@
+"""GPU: the model-parameter optimisation hooks (lib/mlModel.ml:822-829) and a
+maximum-likelihood fit of GTR + Gamma4 + base frequencies through them, with
+the tree's lnL from the float-pair pruning kernel, checked against the same
+fit on the oracle's FP64 lnL."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle import mlmodel_oracle as O
+from phylocaml_gb300 import likelihood as Lk, mlmodel as M, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def test_hooks_round_trip(ctx):
+    spec = M.Spec(("GTR", [1.3, 0.4, 2.2, 0.9, 1.7]), ("DiscreteGamma", 4, 0.6),
+                  ("Empirical", [0.31, 0.19, 0.22, 0.28]))
+    m = M.create(spec, ctx)
+    for name, hook in M.HOOKS.items():
+        x0, build = hook(m, ctx)
+        back = build(x0)
+        np.testing.assert_allclose(back.q, m.q, rtol=1e-12, atol=1e-14)
+        np.testing.assert_allclose(back.rates, m.rates, rtol=1e-12)
+        np.testing.assert_allclose(back.priors, m.priors, rtol=1e-12)
+    assert len(M.gen_subst_opt_func(m, ctx)[0]) == 5
+    assert len(M.gen_rates_opt_func(m, ctx)[0]) == 1
+    assert len(M.gen_prior_opt_func(m, ctx)[0]) == 3
+    jc = M.create(M.Spec(("JC69",)), ctx)
+    assert [len(h(jc, ctx)[0]) for h in M.HOOKS.values()] == [0, 0, 0]
+    hky = M.create(M.Spec(("HKY85", 2.5), ("Constant",), ("Empirical", [0.3, 0.2, 0.2, 0.3])), ctx)
+    x, b = M.gen_subst_opt_func(hky, ctx)
+    assert b(x + np.log(2.0)).spec.substitution[1] == pytest.approx(5.0)
+
+
+def test_ml_fit_reaches_the_truth_and_matches_the_oracle(ctx, orc):
+    tr, spec, pats, w = synth.prune_workload(32, 6000, seed=21, mean_brlen=0.1)
+    table = synth.dna_code_table()
+    truth = M.create(M.Spec(spec.substitution, spec.site_variation, spec.base_priors), ctx)
+
+    def gpu_lnl(m):
+        return Lk.tree_lnl(tr, m, pats, table, w, 48, ctx)
+
+    def cpu_lnl(m):
+        P = O.pmatrices(m.q, m.priors, m.rates, tr.brlen)
+        return orc.prune_lnl(tr.left, tr.right, P, m.priors, m.probs, pats, table, w, n_threads=4)
+
+    start = M.create(M.Spec(("GTR", [1.0] * 5), ("DiscreteGamma", 4, 1.0), "Equal"), ctx)
+    fit, best, calls = M.optimize_model(start, gpu_lnl, ctx=ctx)
+    at_truth = gpu_lnl(truth)
+    assert best >= gpu_lnl(start) + 10.0
+    assert best >= at_truth - 1e-3           # the maximum is at least the truth's value
+    assert calls < 2000
+    fit_cpu, best_cpu, _ = M.optimize_model(start, cpu_lnl, ctx=ctx)
+    assert abs(best - best_cpu) <= 2e-2
+    np.testing.assert_allclose(fit.spec.substitution[1], fit_cpu.spec.substitution[1], rtol=2e-2)
+    assert fit.spec.site_variation[2] == pytest.approx(fit_cpu.spec.site_variation[2], rel=2e-2)
+    np.testing.assert_allclose(fit.priors, fit_cpu.priors, atol=2e-3)
+    # the estimates are near the simulating values
+    assert fit.spec.site_variation[2] == pytest.approx(spec.site_variation[2], rel=0.3)
+    np.testing.assert_allclose(fit.priors, truth.priors, atol=0.02)
