@@ -186,6 +186,8 @@ __device__ __forceinline__ void epi_step(const BVar &v, const BatchArgs &p, cons
   for (int q = 0; q < RP; ++q)
 #pragma unroll
     for (int e = 0; e < B; ++e) acc[q][e] = 1.0f;
+  // states S .. KP-1 need no masks: the tip rows and the B blocks are zero
+  // there, so every vector's padding is a product of zeros
   // both halves are compiled; the warp takes its own (hf is warp-uniform)
   auto half = [&](auto HFc) {
     constexpr int HF = decltype(HFc)::value;
@@ -206,7 +208,7 @@ __device__ __forceinline__ void epi_step(const BVar &v, const BatchArgs &p, cons
                              (size_t)code * v.SpT + e0;
 #pragma unroll
           for (int e = 0; e < B; ++e)
-            if (e0 + e < S) acc[q][e] *= row[e];
+            acc[q][e] *= row[e];
         }
       } else {
 #pragma unroll
@@ -219,7 +221,7 @@ __device__ __forceinline__ void epi_step(const BVar &v, const BatchArgs &p, cons
 #pragma unroll
           for (int e = 0; e < B; ++e) {
             const int col = e0 + e - c_first;
-            if (e0 + e < S) acc[q][e] *= d[col / 16][col % 16];
+            acc[q][e] *= d[col / 16][col % 16];
           }
         }
       }
@@ -237,7 +239,7 @@ __device__ __forceinline__ void epi_step(const BVar &v, const BatchArgs &p, cons
     mx[q] = 0.0f;
 #pragma unroll
     for (int e = 0; e < B; ++e)
-      if (e0 + e < S) mx[q] = fmaxf(mx[q], acc[q][e]);
+      mx[q] = fmaxf(mx[q], acc[q][e]);
     xch[hf][q][in.m] = mx[q];
   }
   // the exchange barrier also makes the timeout verdict uniform over the
@@ -265,9 +267,6 @@ __device__ __forceinline__ void epi_step(const BVar &v, const BatchArgs &p, cons
 #pragma unroll
       for (int e = 0; e < B; ++e) acc[q][e] = acc[q][e] * f1 * f2;
     }
-#pragma unroll
-    for (int e = 0; e < B; ++e)
-      if (e0 + e >= S) acc[q][e] = 0.0f;
     // into the TMEM stack slot: my K columns e0 .. e0 + B - 1
     const uint32_t col = (uint32_t)(2 * RP * v.Np + (so * RP + q) * v.Kp + e0);
 #pragma unroll
@@ -810,7 +809,7 @@ pgpu_status pgpu_batch_create(pgpu_ctx *ctx, const pgpu_variant *vs, int n_var, 
     v.n_codes = x.codes.n_codes;
     v.Kp = (S + 7) / 8 * 8;
     v.Np = (S + 15) / 16 * 16;
-    v.SpT = S | 1;                        // odd row stride: distinct codes, distinct banks
+    v.SpT = v.Kp | 1;                     // odd row stride (distinct codes, distinct banks), entries S.. zero
     v.NCp = (x.codes.n_codes + 3) / 4 * 4; // rows padded so a block is a multiple of 16 bytes
     v.n_slots = (BT_TMEM_COLS - 2 * v.Np) / v.Kp;
     v.n_tiles = (int)nt;
