@@ -863,9 +863,42 @@ def bench_batch(args, rank, world, local):
     }
     if graph is None:
         rec["config"]["graph_capture_error"] = capture_error
+    if rank == 0:
+        rec["cpu_baseline"] = batch_cpu_rate(variants, units)
     b.close()
     ctx.close()
     return rec
+
+
+def batch_cpu_rate(variants, units):
+    """The FP64 pruning restatement (oracle/prune_oracle.c) on all host cores,
+    timed on a pattern sample of the first 20-state and the first 61-state
+    variant, and weighted by the batch's own mix of the two."""
+    import oracle
+    from oracle import mlmodel_oracle as O
+    cores = os.cpu_count() or 1
+    per_kind, samples = {}, []
+    for v in variants:
+        S = v.q.shape[0]
+        if S in per_kind:
+            continue
+        s = min(v.n_pat, 20_000 if S <= 20 else 6_000)
+        codes = np.ascontiguousarray(v.tip_codes[:, :s].cpu().numpy())
+        P = O.pmatrices(v.q, v.pi, v.rates, v.tree.brlen)
+        t0 = time.perf_counter()
+        oracle.prune_lnl(v.tree.left, v.tree.right, P, v.pi, v.probs, codes, v.code_table, None,
+                         n_threads=cores)
+        dt = time.perf_counter() - t0
+        per_kind[S] = v.tree.n_internal * s / dt
+        samples.append(f"{S}-state: {s:,} patterns in {dt:.2f} s")
+        if len(per_kind) == 2:
+            break
+    t_cpu = sum(v.tree.n_internal * v.n_pat / per_kind[v.q.shape[0]] for v in variants
+                if v.q.shape[0] in per_kind)
+    return {"value": units / t_cpu, "unit": "node-site-pattern updates/s", "cores": cores,
+            "kind": "port", "per_state_count": {str(k): r for k, r in per_kind.items()},
+            "sample": "FP64 restatement (oracle/prune_oracle.c), " + "; ".join(samples) +
+                      "; the batch's time at those rates"}
 
 
 
