@@ -1,7 +1,7 @@
 """SPR hill climbing on the GPU: plain exhaustive SPR and the learned proposal.
 
 phylocaml's tree search is a TODO (lib/treeNeighborhoods.ml:27-75); these are
-the two searches the learned part is judged by.  Both start from the same
+the two searches the learned proposal is compared with each other by.  Both start from the same
 tree, score moves with the same exact kernel (SprEngine.scan / score: the
 lnL of the rearranged tree, no branch-length re-estimation), accept the best
 move when it gains more than ``eps``, re-estimate branch lengths a few
