@@ -1,7 +1,8 @@
 """SPR hill climbing on the GPU: plain exhaustive SPR and the learned proposal.
 
-phylocaml's tree search is a TODO (lib/treeNeighborhoods.ml:27-75); these are
-the two searches the learned proposal is compared with each other by.  Both start from the same
+phylocaml's tree search is a TODO (lib/treeNeighborhoods.ml:27-75); here are an
+exhaustive search and a learned-proposal search, compared on wall time to
+the same optimum.  Both start from the same
 tree, score moves with the same exact kernel (SprEngine.scan / score: the
 lnL of the rearranged tree, no branch-length re-estimation), accept the best
 move when it gains more than ``eps``, re-estimate branch lengths a few
