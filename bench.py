@@ -872,17 +872,19 @@ def bench_batch(args, rank, world, local):
 
 def batch_cpu_rate(variants, units):
     """The FP64 pruning restatement (oracle/prune_oracle.c) on all host cores,
-    timed on a pattern sample of the first 20-state and the first 61-state
-    variant, and weighted by the batch's own mix of the two."""
+    timed on the largest 20-state and 61-state variants, and weighted by the
+    batch's own mix of the two."""
     import oracle
     from oracle import mlmodel_oracle as O
     cores = os.cpu_count() or 1
     per_kind, samples = {}, []
-    for v in variants:
+    largest = {}
+    for v in variants:   # the variant with the most patterns of each state count
         S = v.q.shape[0]
-        if S in per_kind:
-            continue
-        s = min(v.n_pat, 20_000 if S <= 20 else 6_000)
+        if S not in largest or v.n_pat > largest[S].n_pat:
+            largest[S] = v
+    for S, v in largest.items():
+        s = min(v.n_pat, 200_000 if S <= 20 else 100_000)   # a few seconds each
         codes = np.ascontiguousarray(v.tip_codes[:, :s].cpu().numpy())
         P = O.pmatrices(v.q, v.pi, v.rates, v.tree.brlen)
         t0 = time.perf_counter()
@@ -891,8 +893,6 @@ def batch_cpu_rate(variants, units):
         dt = time.perf_counter() - t0
         per_kind[S] = v.tree.n_internal * s / dt
         samples.append(f"{S}-state: {s:,} patterns in {dt:.2f} s")
-        if len(per_kind) == 2:
-            break
     t_cpu = sum(v.tree.n_internal * v.n_pat / per_kind[v.q.shape[0]] for v in variants
                 if v.q.shape[0] in per_kind)
     return {"value": units / t_cpu, "unit": "node-site-pattern updates/s", "cores": cores,
