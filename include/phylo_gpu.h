@@ -99,8 +99,11 @@ pgpu_status pgpu_tree_schedule(pgpu_ctx *ctx, const pgpu_tree *tree, int32_t *op
  * lowest lane in the lowest bits.  lane_bits 8 with one state bit per
  * alphabet code is the reference's BV8 layout (lib/bitvector/bv.h:29-34);
  * lane_bits 4 packs the four nucleotides (A=1, C=2, G=4, T=8,
- * lib/alphabet.ml:301-307) eight sites to a word.  Lanes past the last site
- * are ignored on input and written as zero. */
+ * lib/alphabet.ml:301-307) eight sites to a word.  lane_bits 64 is BV64:
+ * site s is the 64-bit element in words 2s (low half) and 2s + 1, the
+ * little-endian layout of a uint64_t array.  Lanes past the last site are
+ * ignored on input and written as zero.  pgpu_fitch_tree_noalloc takes
+ * lane_bits 4..32 only. */
 
 /* Bitvector.BVn.fitch_median_2 (lib/bitvector.mli:94; bv_CAML_fitch_median2,
  * lib/bitvector/bv.c:463-480, and bv_fitch, bv.c:148-160).  out[i] = a&b,

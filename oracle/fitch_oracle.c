@@ -12,7 +12,8 @@
  *                      restates NonAdditive_c.median_2 (lib/nonAdditive_c.ml:19-35).
  *   orc_fitch_tree_packed
  *                      the same rule over packed lanes of 4/8/16/32 bits in
- *                      uint32 words, lane by lane, with per-site union counts
+ *                      uint32 words (or 64-bit elements as word pairs, low
+ *                      word first), lane by lane, with per-site union counts
  *                      and the weighted total.
  *
  * Tree convention: tips are ids 0..n_tips-1; internal node k has id n_tips+k
@@ -141,6 +142,18 @@ double orc_nonadditive_median2(const int64_t *xs, const int64_t *ys,
 
 /* ---- packed lanes ------------------------------------------------------- */
 
+/* 64-bit lanes (BV64): site s is words 2s (low) and 2s+1 (high) */
+static uint64_t lane_get64(const uint32_t *row, uint64_t site)
+{
+  return (uint64_t)row[2 * site] | ((uint64_t)row[2 * site + 1] << 32);
+}
+
+static void lane_set64(uint32_t *row, uint64_t site, uint64_t v)
+{
+  row[2 * site] = (uint32_t)v;
+  row[2 * site + 1] = (uint32_t)(v >> 32);
+}
+
 static uint32_t lane_get(const uint32_t *row, uint64_t site, int lb)
 {
   uint64_t per = 32u / (unsigned)lb;
@@ -172,9 +185,11 @@ int orc_fitch_tree_packed(int32_t n_tips, const int32_t *left, const int32_t *ri
   int32_t k, n_int = n_tips - 1;
   uint64_t s, tot = 0;
   uint32_t *cnt;
-  if (lane_bits != 4 && lane_bits != 8 && lane_bits != 16 && lane_bits != 32) return -1;
+  if (lane_bits != 4 && lane_bits != 8 && lane_bits != 16 && lane_bits != 32 && lane_bits != 64)
+    return -1;
   if (n_tips < 2) return -1;
-  if (ld_words * (32u / (unsigned)lane_bits) < n_sites) return -1;
+  if (lane_bits == 64 ? ld_words < 2 * n_sites : ld_words * (32u / (unsigned)lane_bits) < n_sites)
+    return -1;
   cnt = (uint32_t *)calloc(n_sites ? n_sites : 1, sizeof(uint32_t));
   memset(node_sets, 0, (size_t)n_int * ld_words * sizeof(uint32_t));
   for (k = 0; k < n_int; ++k) {
@@ -187,6 +202,12 @@ int orc_fitch_tree_packed(int32_t n_tips, const int32_t *left, const int32_t *ri
     uint64_t nc = 0;
     if (l >= n_tips + k || r >= n_tips + k || l < 0 || r < 0) { free(cnt); return -1; }
     for (s = 0; s < n_sites; ++s) {
+      if (lane_bits == 64) {
+        uint64_t a = lane_get64(ra, s), b = lane_get64(rb, s), m = a & b;
+        if (m == 0) { m = a | b; cnt[s]++; nc++; }
+        lane_set64(rc, s, m);
+        continue;
+      }
       uint32_t a = lane_get(ra, s, lane_bits), b = lane_get(rb, s, lane_bits);
       uint32_t m = a & b;
       if (m == 0) { m = a | b; cnt[s]++; nc++; }

@@ -5,8 +5,8 @@ a C custom block (lib/bitvector/bv.h:57-63) and compute fitch_median_2 and
 distance with scalar loops (lib/bitvector/bv.c:46-55, 148-160).  Here a
 vector is packed lanes of ``lane_bits`` bits in uint32 words; the median
 and the distance run as GPU kernels through the C ABI.  ``BV4`` (4-bit
-lanes, eight DNA sites per word) has no reference counterpart; ``BV64`` is
-not provided (no lane wider than 32 bits).
+lanes, eight DNA sites per word) has no reference counterpart; ``BV64``
+keeps each 64-bit element as two words, low word first.
 
 Functions keep the reference's names and argument meaning:
 ``fitch_median_2 s t -> (median, added cost)``, ``distance s t -> int``.
@@ -44,8 +44,8 @@ class BV:
     """One element width of the Bitvector.BV signature."""
 
     def __init__(self, lane_bits: int, ctx: _native.Context | None = None):
-        if lane_bits not in (4, 8, 16, 32):
-            raise ValueError("lane_bits must be 4, 8, 16 or 32")
+        if lane_bits not in (4, 8, 16, 32, 64):
+            raise ValueError("lane_bits must be 4, 8, 16, 32 or 64")
         self.lane_bits = lane_bits
         self.max_width = lane_bits
         self._ctx = ctx
@@ -66,9 +66,9 @@ class BV:
 
     def of_array(self, width: int, elts) -> Vector:
         a = np.asarray(elts, dtype=np.uint64)
-        if (a >> np.uint64(self.lane_bits)).any():
+        if self.lane_bits < 64 and (a >> np.uint64(self.lane_bits)).any():
             raise ValueError("element does not fit the lane width")
-        w = pack_lanes(a.astype(np.uint32)[None, :], self.lane_bits)[0]
+        w = pack_lanes((a if self.lane_bits == 64 else a.astype(np.uint32))[None, :], self.lane_bits)[0]
         return Vector(w, len(a), width, self.lane_bits)
 
     # -- accessors (bitvector.mli:29-50) --
@@ -85,6 +85,10 @@ class BV:
         return int(unpack_lanes(v.words[None, :], v.chars, self.lane_bits)[0, i])
 
     def set_elt(self, v: Vector, i: int, x: int) -> None:
+        if self.lane_bits == 64:
+            v.words[2 * i] = np.uint32(x & 0xFFFFFFFF)
+            v.words[2 * i + 1] = np.uint32((x >> 32) & 0xFFFFFFFF)
+            return
         per = 32 // self.lane_bits
         mask = 0xFFFFFFFF if self.lane_bits == 32 else (1 << self.lane_bits) - 1
         sh = (i % per) * self.lane_bits
@@ -133,3 +137,4 @@ BV4 = BV(4)
 BV8 = BV(8)
 BV16 = BV(16)
 BV32 = BV(32)
+BV64 = BV(64)

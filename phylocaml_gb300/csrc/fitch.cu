@@ -115,6 +115,99 @@ __global__ void __launch_bounds__(256) fitch_pair_kernel(const uint32_t *__restr
   block_add_u64(acc, count, red);
 }
 
+// 64-bit elements (Bitvector.BV64, lib/bitvector.ml): one character per
+// element, two 32-bit words (low word first); the median takes the union
+// when the whole element's intersection is empty.
+template <bool WEIGHTED, bool WRITE>
+__global__ void __launch_bounds__(256) fitch_pair64_kernel(const uint2 *__restrict__ a,
+                                                           const uint2 *__restrict__ b,
+                                                           const uint32_t *__restrict__ weights,
+                                                           uint2 *__restrict__ out, size_t n,
+                                                           unsigned long long *count) {
+  __shared__ unsigned long long red[8];
+  unsigned long long acc = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const uint2 x = __ldg(a + i), y = __ldg(b + i);
+    uint2 m = make_uint2(x.x & y.x, x.y & y.y);
+    const bool empty = (m.x | m.y) == 0u;
+    if (empty) m = make_uint2(x.x | y.x, x.y | y.y);
+    if (WRITE) out[i] = m;
+    if (empty) acc += WEIGHTED ? __ldg(weights + i) : 1u;
+  }
+  block_add_u64(acc, count, red);
+}
+
+// The whole postorder over 64-bit elements: one thread per element walks
+// the schedule; the last result stays in registers, a step with two tip
+// children sets it aside on a shared-memory stack and a step with two
+// internal children takes its first child back.
+struct Fitch64Args {
+  const uint2 *tips;          // [n_tips][ld / 2]
+  const uint32_t *weights;    // [n] or null
+  uint2 *node_sets;           // [n_int][ld / 2]
+  uint32_t *site_cost;        // [n] or null
+  unsigned long long *total;
+  const int4 *ops;
+  size_t ld2, n;              // row stride in elements, elements
+  int32_t n_tips, n_ops, depth;
+};
+
+constexpr int F64_THREADS = 128;
+
+__global__ void __launch_bounds__(F64_THREADS) fitch_tree64_kernel(const Fitch64Args p) {
+  extern __shared__ uint2 stk64[];   // [depth][F64_THREADS]
+  __shared__ unsigned long long red[F64_THREADS / 32];
+  const int t = threadIdx.x;
+  const size_t i = (size_t)blockIdx.x * F64_THREADS + t;
+  const bool on = i < p.n;
+  auto tip = [&](int ch) { return on ? __ldg(p.tips + (size_t)ch * p.ld2 + i) : make_uint2(0, 0); };
+  uint2 top = make_uint2(0, 0);
+  uint32_t cnt = 0;
+  int sp = 0;
+  bool ok = true;
+  for (int k = 0; k < p.n_ops && ok; ++k) {
+    const int4 op = __ldg(p.ops + k);
+    const int kind = (op.y >= p.n_tips ? 1 : 0) | (op.z >= p.n_tips ? 2 : 0);
+    uint2 x, y;
+    if (kind == 0) {
+      if (k > 0) {
+        if (sp < p.depth) stk64[sp++ * F64_THREADS + t] = top;
+        else ok = false;
+      }
+      x = tip(op.y);
+      y = tip(op.z);
+    } else if (kind == 1) {
+      x = top;
+      y = tip(op.z);
+    } else if (kind == 2) {
+      x = tip(op.y);
+      y = top;
+    } else {
+      if (sp > 0) {
+        x = stk64[--sp * F64_THREADS + t];
+      } else {
+        ok = false;
+        x = make_uint2(0, 0);
+      }
+      y = top;
+    }
+    uint2 m = make_uint2(x.x & y.x, x.y & y.y);
+    if ((m.x | m.y) == 0u) {
+      m = make_uint2(x.x | y.x, x.y | y.y);
+      ++cnt;
+    }
+    if (on) p.node_sets[(size_t)op.x * p.ld2 + i] = m;
+    top = m;
+  }
+  unsigned long long acc = 0;
+  if (on && ok) {
+    if (p.site_cost) p.site_cost[i] = cnt;
+    acc = (unsigned long long)(p.weights ? __ldg(p.weights + i) : 1u) * cnt;
+  }
+  block_add_u64(acc, p.total, red);
+}
+
 // ---------------------------------------------------------------------------
 // tree kernel
 // ---------------------------------------------------------------------------
@@ -588,6 +681,7 @@ pgpu_status launch_pair(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b, con
 }
 
 bool lane_bits_ok(int lb) { return lb == 4 || lb == 8 || lb == 16 || lb == 32; }
+bool lane_bits_ok64(int lb) { return lane_bits_ok(lb) || lb == 64; }
 
 size_t words_for(size_t n_sites, int lb) { return (n_sites * (size_t)lb + 31) / 32; }
 
@@ -595,7 +689,8 @@ size_t words_for(size_t n_sites, int lb) { return (n_sites * (size_t)lb + 31) / 
 pgpu_status pair_host(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b, const uint32_t *w,
                       uint32_t *out, size_t n_sites, int lb, uint64_t *result, int mode) {
   if (!ctx) return PGPU_ERR_ARG;
-  if (!lane_bits_ok(lb)) return pgpu_set_err(ctx, PGPU_ERR_ARG, "lane_bits must be 4, 8, 16 or 32");
+  if (!lane_bits_ok64(lb))
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "lane_bits must be 4, 8, 16, 32 or 64");
   if (!a || !b || !result || (mode != 2 && !out) || (mode == 1 && !w))
     return pgpu_set_err(ctx, PGPU_ERR_ARG, "fitch: null buffer");
   PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -616,7 +711,20 @@ pgpu_status pair_host(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b, const
     const uint32_t *pa = (const uint32_t *)da, *pb = (const uint32_t *)db,
                    *pw = (const uint32_t *)dw;
     uint32_t *po = (uint32_t *)dout;
-    switch (lb) {
+    if (lb == 64) {
+      const int threads = 256;
+      size_t blocks = (n_sites + threads - 1) / threads;
+      blocks = std::min<size_t>(std::max<size_t>(blocks, 1), (size_t)ctx->num_sms * 8);
+      const uint2 *a2 = (const uint2 *)pa, *b2 = (const uint2 *)pb;
+      uint2 *o2 = (uint2 *)po;
+      if (mode == 0)
+        fitch_pair64_kernel<false, true><<<(unsigned)blocks, threads, 0, s>>>(a2, b2, pw, o2, n_sites, cnt);
+      else if (mode == 1)
+        fitch_pair64_kernel<true, true><<<(unsigned)blocks, threads, 0, s>>>(a2, b2, pw, o2, n_sites, cnt);
+      else
+        fitch_pair64_kernel<false, false><<<(unsigned)blocks, threads, 0, s>>>(a2, b2, pw, o2, n_sites, cnt);
+      PGPU_TRY(pgpu_after_launch(ctx, "fitch_pair64_kernel"));
+    } else switch (lb) {
       case 4: PGPU_TRY(launch_pair<4>(ctx, pa, pb, pw, po, n_words, n_sites, cnt, mode)); break;
       case 8: PGPU_TRY(launch_pair<8>(ctx, pa, pb, pw, po, n_words, n_sites, cnt, mode)); break;
       case 16: PGPU_TRY(launch_pair<16>(ctx, pa, pb, pw, po, n_words, n_sites, cnt, mode)); break;
@@ -824,10 +932,44 @@ cudaError_t launch_split(cudaStream_t stream, const FitchSplitArgs &a, size_t ti
   return cudaGetLastError();
 }
 
+// 64-bit elements: the element kernel over the plain schedule
+pgpu_status tree64_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips, size_t ld,
+                       const uint32_t *weights, size_t n_sites, uint32_t *node_sets,
+                       uint32_t *site_cost, uint64_t *total) {
+  const TreeSchedule *sch;
+  const int4 *d_ops;
+  const int32_t *d_seq;
+  PGPU_TRY(pgpu_schedule_device(ctx, tree, &sch, &d_ops, &d_seq));
+  cudaStream_t s = ctx->stream;
+  PGPU_CUDA(ctx, cudaMemsetAsync(total, 0, sizeof(uint64_t), s));
+  if (n_sites == 0) return PGPU_OK;
+  Fitch64Args a;
+  a.tips = reinterpret_cast<const uint2 *>(tips);
+  a.weights = weights;
+  a.node_sets = reinterpret_cast<uint2 *>(node_sets);
+  a.site_cost = site_cost;
+  a.total = reinterpret_cast<unsigned long long *>(total);
+  a.ops = d_ops;
+  a.ld2 = ld / 2;
+  a.n = n_sites;
+  a.n_tips = tree->n_tips;
+  a.n_ops = (int)sch->ops.size();
+  a.depth = std::max(sch->max_depth, 1);
+  const size_t smem = (size_t)a.depth * F64_THREADS * sizeof(uint2);
+  if (smem > (size_t)ctx->smem_optin)
+    return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: tree too deep (%d stack entries)", a.depth);
+  PGPU_CUDA(ctx, cudaFuncSetAttribute(fitch_tree64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+  const unsigned grid = (unsigned)((n_sites + F64_THREADS - 1) / F64_THREADS);
+  fitch_tree64_kernel<<<grid, F64_THREADS, smem, s>>>(a);
+  return pgpu_after_launch(ctx, "fitch_tree64_kernel");
+}
+
 pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips, size_t ld,
                      const uint32_t *weights, size_t n_sites, int lb, uint32_t *node_sets,
                      uint32_t *site_cost, uint64_t *total) {
-  if (!lane_bits_ok(lb)) return pgpu_set_err(ctx, PGPU_ERR_ARG, "lane_bits must be 4, 8, 16 or 32");
+  if (!lane_bits_ok64(lb))
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "lane_bits must be 4, 8, 16, 32 or 64");
   const size_t n_words = words_for(n_sites, lb);
   if (!tips || !node_sets || !total) return pgpu_set_err(ctx, PGPU_ERR_ARG, "fitch_tree: null buffer");
   if (ld % 4 != 0 || ld < n_words)
@@ -836,6 +978,7 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
   if (((uintptr_t)tips | (uintptr_t)node_sets) & 15)
     return pgpu_set_err(ctx, PGPU_ERR_ARG, "fitch_tree: tip and node rows must be 16-byte aligned");
   if (!tree || tree->n_tips < 2) return pgpu_set_err(ctx, PGPU_ERR_ARG, "fitch_tree: need at least 2 tips");
+  if (lb == 64) return tree64_dev(ctx, tree, tips, ld, weights, n_sites, node_sets, site_cost, total);
   FitchSplitArgs a;
   PGPU_TRY(split_device(ctx, tree, &a.ops, &a.seg, &a.top, &a.wseg, &a.tip_seq));
   cudaStream_t s = ctx->stream;
@@ -960,8 +1103,8 @@ pgpu_status pgpu_fitch_tree(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t
   if (!ctx) return PGPU_ERR_ARG;
   if (!tree || !tips || !node_sets || !total)
     return pgpu_set_err(ctx, PGPU_ERR_ARG, "fitch_tree: null argument");
-  if (!lane_bits_ok(lane_bits))
-    return pgpu_set_err(ctx, PGPU_ERR_ARG, "lane_bits must be 4, 8, 16 or 32");
+  if (!lane_bits_ok64(lane_bits))
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "lane_bits must be 4, 8, 16, 32 or 64");
   if (tree->n_tips < 2) return pgpu_set_err(ctx, PGPU_ERR_ARG, "tree: need at least 2 tips");
   PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
   const size_t n_words = words_for(n_sites, lane_bits);

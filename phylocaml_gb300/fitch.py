@@ -22,8 +22,8 @@ def n_words(n_sites: int, lane_bits: int) -> int:
 
 
 def _check_lanes(lane_bits: int) -> None:
-    if lane_bits not in (4, 8, 16, 32):
-        raise ValueError("lane_bits must be 4, 8, 16 or 32")
+    if lane_bits not in (4, 8, 16, 32, 64):
+        raise ValueError("lane_bits must be 4, 8, 16, 32 or 64")
 
 
 @dataclass

@@ -24,9 +24,12 @@ AMBIGUOUS = np.array([A | C, A | G, A | T, G | C, T | C, G | T,
 
 def pack_lanes(states: np.ndarray, lane_bits: int) -> np.ndarray:
     """Packs [rows, n_sites] masks (each < 2**lane_bits) into uint32 words,
-    site s in lane s % (32/lane_bits) of word s // (32/lane_bits)."""
+    site s in lane s % (32/lane_bits) of word s // (32/lane_bits); 64-bit
+    lanes take words 2s (low half) and 2s + 1."""
     states = np.atleast_2d(states)
     rows, n = states.shape
+    if lane_bits == 64:   # one element per word pair, low word first
+        return np.ascontiguousarray(states.astype("<u8")).view("<u4").astype(np.uint32, copy=False)
     per = 32 // lane_bits
     n_words = (n * lane_bits + 31) // 32
     if lane_bits in (4, 8) and states.dtype == np.uint8:
@@ -49,6 +52,8 @@ def pack_lanes(states: np.ndarray, lane_bits: int) -> np.ndarray:
 
 def unpack_lanes(words: np.ndarray, n_sites: int, lane_bits: int) -> np.ndarray:
     words = np.atleast_2d(words).astype(np.uint32)
+    if lane_bits == 64:
+        return np.ascontiguousarray(words.astype("<u4")).view("<u8").astype(np.uint64)[:, :n_sites]
     per = 32 // lane_bits
     mask = np.uint32(0xFFFFFFFF if lane_bits == 32 else (1 << lane_bits) - 1)
     shifts = (np.arange(per, dtype=np.uint32) * lane_bits).astype(np.uint32)

@@ -20,6 +20,10 @@ Fixtures written:
                           over its postorder.
   bvref_w32_pairs.npz     random 32-bit masks and bv_fitch's medians and
                           counts at WIDTH=32.
+  bvref_w64_pairs.npz     the same at WIDTH=64 (BV64).
+  bvref_w64_tree.npz      a seeded 12-tip Yule tree with 300 random 64-bit
+                          masks, and bv_fitch's internal sets and per-node
+                          counts at WIDTH=64.
 """
 from __future__ import annotations
 
@@ -115,6 +119,35 @@ def main() -> None:
     dist = bv32.bvref_distance(x.ctypes.data, y.ctypes.data, n)
     np.savez_compressed(HERE / "bvref_w32_pairs.npz", a=x, b=y, median=out,
                         count=np.uint64(cnt), distance=np.uint64(dist))
+
+    # 64-bit elements (BV64): sparse masks over all 64 bits, so that both
+    # outcomes occur and the high word matters
+    bv64 = oracle.ref_lib(64)
+
+    def sparse64(shape):
+        z = rng.integers(0, 2 ** 64, shape, dtype=np.uint64, endpoint=False)
+        for _ in range(3):
+            z &= rng.integers(0, 2 ** 64, shape, dtype=np.uint64, endpoint=False)
+        return np.where(z == 0, np.uint64(1) << rng.integers(0, 64, shape).astype(np.uint64), z)
+
+    x, y = sparse64(n), sparse64(n)
+    out = np.empty(n, np.uint64)
+    cnt = bv64.bvref_fitch_median2(x.ctypes.data, y.ctypes.data, out.ctypes.data, n)
+    dist = bv64.bvref_distance(x.ctypes.data, y.ctypes.data, n)
+    np.savez_compressed(HERE / "bvref_w64_pairs.npz", a=x, b=y, median=out,
+                        count=np.uint64(cnt), distance=np.uint64(dist))
+    tr = T.yule(12, rng, 0.1)
+    chars = 300
+    tips = np.ascontiguousarray(sparse64((12, chars)))
+    internal = np.zeros((11, chars), np.uint64)
+    counts = np.zeros(11, np.uint64)
+    left = np.ascontiguousarray(tr.left)
+    right = np.ascontiguousarray(tr.right)
+    rc = bv64.bvref_fitch_tree(12, left.ctypes.data, right.ctypes.data, tips.ctypes.data, chars,
+                               internal.ctypes.data, counts.ctypes.data)
+    assert rc == 0
+    np.savez_compressed(HERE / "bvref_w64_tree.npz", left=tr.left, right=tr.right, tips=tips,
+                        internal=internal, node_counts=counts)
     print("golden fixtures written to", HERE)
 
 
