@@ -753,7 +753,13 @@ def bench_batch(args, rank, world, local):
     stream = torch.cuda.Stream(dev)
     torch.cuda.synchronize(dev)
     ctx.set_stream(stream.cuda_stream)
-    b = Batch(variants, ctx)
+    # the launch shape is chosen by the autotuner on a sample of the batch's
+    # variants (outside the timed region, as a library user would at setup)
+    from phylocaml_gb300.batch import autotune
+    t_tune = time.perf_counter()
+    choice, tune_ms = autotune(variants, ctx, sample=min(128, len(variants)), reps=2)
+    t_tune = time.perf_counter() - t_tune
+    b = Batch(variants, ctx, choice)
     n_pat_total = b.patterns
     units = sum((v.tree.n_internal) * v.n_pat for v in variants)
     flops = 0.0   # unpadded tensor-core MACs x 2: internal children only
@@ -836,6 +842,10 @@ def bench_batch(args, rank, world, local):
                                "U{5,000..200,000}; even: 20-state LogNormal/Dirichlet Q + Gamma4; "
                                "odd: 61-state codon Q (kappa ~ U(1,4), omega ~ U(0.1,1))",
                    "patterns": n_pat_total, "work_items": b.work_items,
+                   "autotune": {"choice": {"rate_pairs": choice.rate_pairs, "order": choice.order},
+                                "sample_ms": {f"rate_pairs={o.rate_pairs},order={o.order}": t
+                                              for o, t in tune_ms.items()},
+                                "seconds": t_tune},
                    "graph_captured": graph is not None, "ungraphed_ms_per_step": ungraphed_ms},
         "lnl_error_vs_fp64": {"sample_patterns_per_variant": BATCH_SAMPLE,
                               "max_abs": float(err.max()), "median_abs": float(np.median(err)),

@@ -303,6 +303,24 @@ typedef struct pgpu_batch pgpu_batch;
  * to must outlive the batch. */
 pgpu_status pgpu_batch_create(pgpu_ctx *ctx, const pgpu_variant *variants, int n_variants,
                               pgpu_batch **out);
+
+/* Launch-shape options of a batch, for an autotuner to choose between
+ * (results are the same to rounding, since each variant's sum runs in tile
+ * order whatever the work order):
+ *   rate_pairs  non-zero: two rate classes share a pass where their vectors
+ *               fit in tensor memory together (the default); zero: one
+ *               rate class per pass;
+ *   order       PGPU_BATCH_ORDER_VARIANT: (variant, tile) items in variant
+ *               order, the persistent CTAs striding over them (the default);
+ *               PGPU_BATCH_ORDER_COST: items by estimated cost, largest
+ *               first, dealt back and forth over the CTAs. */
+enum { PGPU_BATCH_ORDER_VARIANT = 0, PGPU_BATCH_ORDER_COST = 1 };
+typedef struct {
+  int rate_pairs;
+  int order;
+} pgpu_batch_options;
+pgpu_status pgpu_batch_create_opts(pgpu_ctx *ctx, const pgpu_variant *variants, int n_variants,
+                                   const pgpu_batch_options *options, pgpu_batch **out);
 void pgpu_batch_destroy(pgpu_batch *batch);
 
 /* Scores every variant, asynchronously on the context's stream and without

@@ -62,6 +62,10 @@ class PgpuTipCodes(C.Structure):
     ]
 
 
+class PgpuBatchOptions(C.Structure):
+    _fields_ = [("rate_pairs", C.c_int), ("order", C.c_int)]
+
+
 class PgpuVariant(C.Structure):
     _fields_ = [
         ("tree", PgpuTree),
@@ -107,6 +111,8 @@ SIGNATURES: dict[str, tuple] = {
     "pgpu_prune_lnl_dev": (_I, [_P, C.POINTER(PgpuTree), C.POINTER(PgpuModel),
                                 C.POINTER(PgpuTipCodes), _P, _SZ, _P, _SZ, _I, _P, _P]),
     "pgpu_batch_create": (_I, [_P, C.POINTER(PgpuVariant), _I, C.POINTER(_P)]),
+    "pgpu_batch_create_opts": (_I, [_P, C.POINTER(PgpuVariant), _I, C.POINTER(PgpuBatchOptions),
+                                    C.POINTER(_P)]),
     "pgpu_batch_destroy": (None, [_P]),
     "pgpu_batch_run": (_I, [_P, _P, _P, _P]),
     "pgpu_batch_run_fp64": (_I, [_P, _P, _SZ, _P]),

@@ -35,9 +35,22 @@ class Variant:
         return max(128, (n_pat + 127) // 128 * 128)
 
 
+@dataclass(frozen=True)
+class Options:
+    """pgpu_batch_options: two rate classes per pass where they fit, and the
+    work order ("variant" or "cost")."""
+    rate_pairs: bool = True
+    order: str = "variant"
+
+
+ORDERS = {"variant": 0, "cost": 1}
+
+
 class Batch:
-    def __init__(self, variants: list[Variant], ctx: _native.Context | None = None):
+    def __init__(self, variants: list[Variant], ctx: _native.Context | None = None,
+                 options: Options | None = None):
         self.ctx = ctx or _native.default_context()
+        self.options = options or Options()
         self.variants = variants
         self._keep = []
         arr = (_native.PgpuVariant * len(variants))()
@@ -60,7 +73,8 @@ class Batch:
             x.n_pat = v.n_pat
             x.ld_pat = v.tip_codes.shape[1]
         h = C.c_void_p()
-        self.ctx.call("pgpu_batch_create", arr, len(variants), C.byref(h))
+        o = _native.PgpuBatchOptions(int(self.options.rate_pairs), ORDERS[self.options.order])
+        self.ctx.call("pgpu_batch_create_opts", arr, len(variants), C.byref(o), C.byref(h))
         self.h = h
         self.n_var = len(variants)
 
@@ -116,3 +130,73 @@ def device_codes(codes: np.ndarray, device) -> object:
     t = torch.zeros((n_tips, Variant.ld_for(n_pat)), dtype=torch.uint8, device=device)
     t[:, :n_pat] = torch.from_numpy(np.ascontiguousarray(codes)).to(device)
     return t
+
+
+# ---- autotuner ---------------------------------------------------------------
+# The launch shape of a batch (rate classes per pass, work order) is chosen
+# by timing every candidate on a sample of the batch's own variants, and the
+# choice is cached under the batch's composition: its state counts, rate
+# classes and pattern-count spread.
+
+CANDIDATES = [Options(rp, order) for rp in (True, False) for order in ("variant", "cost")]
+
+
+def composition_key(variants: list[Variant]) -> str:
+    """(states, rate classes) mix and pattern-count octiles of the batch."""
+    mix: dict[str, int] = {}
+    for v in variants:
+        k = f"{v.q.shape[0]}x{len(v.rates)}"
+        mix[k] = mix.get(k, 0) + 1
+    n_pat = np.array([v.n_pat for v in variants], np.float64)
+    octiles = np.percentile(n_pat, [12.5, 50, 87.5])
+    bucket = "-".join(str(int(2 ** round(np.log2(max(x, 1.0))))) for x in octiles)
+    parts = ",".join(f"{k}:{round(c / len(variants), 2)}" for k, c in sorted(mix.items()))
+    return f"{parts}|{bucket}|{len(variants) >= 1024}"
+
+
+def autotune(variants: list[Variant], ctx: _native.Context | None = None, sample: int = 128,
+             reps: int = 2, cache_path=None, candidates=CANDIDATES):
+    """(best Options, {option: ms per run of the sample}).  ``sample``
+    variants are drawn evenly over the batch; a cache file (JSON), when
+    given, returns an earlier choice for the same composition untimed."""
+    import json
+    import torch
+    from pathlib import Path
+    ctx = ctx or _native.default_context()
+    key = composition_key(variants)
+    cache = {}
+    if cache_path is not None and Path(cache_path).exists():
+        cache = json.loads(Path(cache_path).read_text())
+        if key in cache:
+            c = cache[key]
+            return Options(bool(c["rate_pairs"]), c["order"]), {}
+    step = max(1, len(variants) // sample)
+    sub = variants[::step][:sample]
+    dev = torch.device(f"cuda:{ctx.device}")
+    out = torch.zeros(len(sub), dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    times = {}
+    for opt in candidates:
+        b = Batch(sub, ctx, opt)
+        b.run_dev(out)   # warm-up
+        ctx.synchronize()
+        best = float("inf")
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize(dev)
+            e0.record(stream)
+            ctx.after_torch()
+            b.run_dev(out)
+            ctx.before_torch()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            best = min(best, e0.elapsed_time(e1))
+        times[opt] = best
+        b.close()
+    choice = min(times, key=times.get)
+    if cache_path is not None:
+        cache[key] = {"rate_pairs": choice.rate_pairs, "order": choice.order,
+                      "ms": {f"{o.rate_pairs}/{o.order}": t for o, t in times.items()}}
+        Path(cache_path).write_text(json.dumps(cache, indent=1))
+    return choice, times

@@ -60,6 +60,7 @@ struct BVar {
   const uint8_t *codes;            // [n_tips][ld] device tip codes of this variant
   const double *weights;           // [n_pat] device weights or null
   long long pat_off;               // first pattern of the variant in the site outputs
+  long long tile0;                 // the variant's first partial-sum slot (variant-major)
   long long ops_off;               // int4 entries into the ops array
   long long bmat_off;              // floats into the B array
   long long tip_off;               // floats into the tip-row array
@@ -513,7 +514,8 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
           ss = t;
           cc += e + red[k].y;
         }
-        p.partials[w] = make_double2(ss, cc);
+        // by (variant, tile), whatever order the work list runs in
+        p.partials[v.tile0 + wk.y] = make_double2(ss, cc);
       }
       asm volatile("bar.sync 1, 256;" ::: "memory");
     }
@@ -765,8 +767,17 @@ void free_batch(pgpu_batch *b) {
 extern "C" {
 
 pgpu_status pgpu_batch_create(pgpu_ctx *ctx, const pgpu_variant *vs, int n_var, pgpu_batch **out) {
+  return pgpu_batch_create_opts(ctx, vs, n_var, nullptr, out);
+}
+
+pgpu_status pgpu_batch_create_opts(pgpu_ctx *ctx, const pgpu_variant *vs, int n_var,
+                                   const pgpu_batch_options *opts, pgpu_batch **out) {
   if (!ctx || !out) return PGPU_ERR_ARG;
   *out = nullptr;
+  const int rate_pairs = opts ? opts->rate_pairs : 1;
+  const int order = opts ? opts->order : PGPU_BATCH_ORDER_VARIANT;
+  if (order != PGPU_BATCH_ORDER_VARIANT && order != PGPU_BATCH_ORDER_COST)
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "batch: unknown work order %d", order);
   if (!vs || n_var < 1) return pgpu_set_err(ctx, PGPU_ERR_ARG, "batch: no variants");
   PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
   pgpu_batch *b = new pgpu_batch();
@@ -829,7 +840,9 @@ pgpu_status pgpu_batch_create(pgpu_ctx *ctx, const pgpu_variant *vs, int n_var, 
     if (sch.max_depth > v.n_slots) return fail(PGPU_ERR_LIMIT, "tree too deep for the TMEM stack", vi);
     // two rate classes per pass when their D columns and stacks fit in TMEM
     v.RP = 1;
-    if (R % 2 == 0 && v.Kp <= 32 && (BT_TMEM_COLS - 4 * v.Np) / (2 * v.Kp) >= sch.max_depth) v.RP = 2;
+    if (rate_pairs && R % 2 == 0 && v.Kp <= 32 &&
+        (BT_TMEM_COLS - 4 * v.Np) / (2 * v.Kp) >= sch.max_depth)
+      v.RP = 2;
     b->max_depth = std::max(b->max_depth, sch.max_depth);
     // TMEM stack positions from the stack simulation
     int sp = 0;
@@ -840,6 +853,7 @@ pgpu_status pgpu_batch_create(pgpu_ctx *ctx, const pgpu_variant *vs, int n_var, 
       const int so = sp++;
       ops.push_back(make_int4(o.k, o.a, o.b, sa | (sb << 8) | (so << 16)));
     }
+    v.tile0 = (long long)work.size();
     for (long long t = 0; t < nt; ++t) work.push_back(make_int2(vi, (int)t));
     tile_base.push_back((long long)work.size() - nt);
     ntiles.push_back((int)nt);
@@ -884,6 +898,35 @@ pgpu_status pgpu_batch_create(pgpu_ctx *ctx, const pgpu_variant *vs, int n_var, 
     }
     q_acc += (long long)b->group_members[g].size() * S * S;
     l_acc += (long long)b->group_members[g].size() * S;
+  }
+  if (order == PGPU_BATCH_ORDER_COST && !work.empty()) {
+    // Largest items first, dealt back and forth over the persistent CTAs
+    // (CTA c runs items c, c + G, c + 2G, ...), so every CTA's total is close
+    // to the mean.  An item's cost is its postorder steps times the state
+    // columns each step handles.
+    const long long G = std::min<long long>(ctx->num_sms, (long long)work.size());
+    std::vector<double> cost(work.size());
+    for (size_t i = 0; i < work.size(); ++i) {
+      const BVar &v = b->hvars[work[i].x];
+      cost[i] = (double)(v.R / v.RP) * v.n_ops * (v.RP * v.Kp + 16.0);
+    }
+    std::vector<size_t> idx(work.size());
+    for (size_t i = 0; i < idx.size(); ++i) idx[i] = i;
+    std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t c) { return cost[a] > cost[c]; });
+    std::vector<std::vector<int2>> per(G);
+    for (size_t r = 0; r < idx.size(); ++r) {
+      const long long round = (long long)r / G, pos = (long long)r % G;
+      per[round % 2 == 0 ? pos : G - 1 - pos].push_back(work[idx[r]]);
+    }
+    // CTA c's k-th item goes to position k G + c; the last, partial round
+    // is packed to the front of its row
+    std::vector<int2> compact;
+    compact.reserve(work.size());
+    const size_t rounds = (work.size() + G - 1) / G;
+    for (size_t k = 0; k < rounds; ++k)
+      for (long long c = 0; c < G; ++c)
+        if (k < per[c].size()) compact.push_back(per[c][k]);
+    work.swap(compact);
   }
   b->n_work = (long long)work.size();
   b->total_pat = pat_off;

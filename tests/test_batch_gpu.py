@@ -88,3 +88,47 @@ def test_batch_rejects_trees_deeper_than_the_tmem_stack(ctx):
     with pytest.raises(_native.NativeError) as e:
         Batch([v], ctx)
     assert e.value.status == 10
+
+
+def test_launch_options_give_the_same_scores(ctx):
+    """Work order and rate pairing change only the launch shape: every
+    variant's score is the same (each variant sums its tiles in tile order)."""
+    import torch
+    from phylocaml_gb300.batch import Batch, Options
+    dev = torch.device("cuda:0")
+    rng = np.random.default_rng(5)
+    specs = [("protein", 30, 900), ("codon", 18, 400), ("protein", 12, 2000), ("codon", 25, 130),
+             ("protein", 40, 3000), ("codon", 9, 77), ("protein", 16, 1)] * 3
+    vs = [make_variant(rng, k, n, p, dev)[0] for k, n, p in specs]
+    ref = None
+    for opt in (Options(True, "variant"), Options(True, "cost"), Options(False, "variant"),
+                Options(False, "cost")):
+        b = Batch(vs, ctx, opt)
+        try:
+            got, site = b.run(site_lnl=True)
+        finally:
+            b.close()
+        if ref is None:
+            ref, ref_site = got, site
+            continue
+        if opt.rate_pairs:   # same arithmetic, other order: bit for bit
+            assert np.array_equal(got, ref) and np.array_equal(site, ref_site)
+        else:                # one rate class per pass: the same per-rate arithmetic
+            np.testing.assert_allclose(got, ref, rtol=1e-12)
+            np.testing.assert_allclose(site, ref_site, rtol=1e-12)
+
+
+def test_autotune_and_cache(ctx, tmp_path):
+    import torch
+    from phylocaml_gb300 import batch as B
+    dev = torch.device("cuda:0")
+    rng = np.random.default_rng(6)
+    vs = [make_variant(rng, "protein" if k % 2 == 0 else "codon", 20, int(rng.integers(100, 3000)),
+                       dev)[0] for k in range(16)]
+    path = tmp_path / "tune.json"
+    choice, times = B.autotune(vs, ctx, sample=8, reps=1, cache_path=path)
+    assert choice in B.CANDIDATES and set(times) == set(B.CANDIDATES)
+    assert all(t > 0 for t in times.values())
+    again, t2 = B.autotune(vs, ctx, sample=8, reps=1, cache_path=path)
+    assert again == choice and t2 == {}
+    assert B.composition_key(vs) in path.read_text()
