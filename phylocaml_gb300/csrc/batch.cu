@@ -571,7 +571,7 @@ __global__ void __launch_bounds__(256) batch_setup_kernel(const SetupArgs a) {
   const double *U = a.U + (size_t)g * SS, *Ui = a.Ui + (size_t)g * SS, *lam = a.lam + (size_t)g * S;
   double *e = P + SS;
   const double t = a.brlen[v.brlen_off + c], rate = a.rates[v.rates_off + r];
-  const bool ident = !(t >= 1e-10);
+  const bool ident = !(t * rate >= 1e-10);   // effective time: a rate-0 class gets I exactly
   for (int k = tid; k < S; k += nt) e[k] = exp(lam[k] * rate * t);
   __syncthreads();
   for (int o = tid; o < SS; o += nt) {
@@ -660,7 +660,7 @@ __global__ void __launch_bounds__(F64_NP) batch_fp64_kernel(const F64Args a) {
         const int ch = h == 0 ? op.y : op.z;
         __syncthreads();
         const double t = a.brlen[v.brlen_off + ch], rate = a.rates[v.rates_off + r];
-        const bool ident = !(t >= 1e-10);
+        const bool ident = !(t * rate >= 1e-10);
         for (int k = tid; k < S; k += F64_NP) e[k] = exp(lam[k] * rate * t);
         __syncthreads();
         for (int o = tid; o < SS; o += F64_NP) {

@@ -95,12 +95,13 @@ __device__ __forceinline__ ff ff_mul(ff a, ff b) {
 // 2^k as a float for 0 <= k <= 127
 __device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
 
-// frexp's exponent E of a positive finite v (v = f 2^E, f in [0.5, 1)),
-// read from the bits so the float forms issue no FP64 instruction
+// frexp's exponent E of a finite v >= 0 (v = f 2^E, f in [0.5, 1); 0 for
+// v = 0, as frexp gives), read from the bits so the float forms issue no
+// FP64 instruction
 __device__ __forceinline__ int frexp_exp(float v) {
-  const int b = __float_as_int(v);
-  const int e = (b >> 23) & 0xff;
-  return e ? e - 126 : -126 - __clz(b << 9);
+  const int b = __float_as_int(v) & 0x7fffffff;
+  const int e = b >> 23;
+  return e ? e - 126 : b ? -126 - __clz(b << 9) : 0;
 }
 __device__ __forceinline__ int frexp_exp(double v) {
   int e;

@@ -212,7 +212,6 @@ __global__ void __launch_bounds__(256) compose_kernel(const ComposeArgs p) {
   }
   const double t = p.t[b];
   const bool q_mode = p.allow_q && t == -1.0;
-  const bool ident = !q_mode && !(t >= 1e-10);
   for (int i = tid; i < R * S; i += nt) {
     const int r = i / S, k = i % S;
     const double rate = p.rates ? p.rates[r] : 1.0;
@@ -221,6 +220,9 @@ __global__ void __launch_bounds__(256) compose_kernel(const ComposeArgs p) {
   __syncthreads();
   for (int o = tid; o < R * SS; o += nt) {
     const int r = o / SS, i = (o % SS) / S, j = o % S;
+    // the identity below an effective time of 1e-10 (rate times length):
+    // a rate-0 class (invariant sites) gets I exactly, not U Ui to rounding
+    const bool ident = !q_mode && !(t * (p.rates ? p.rates[r] : 1.0) >= 1e-10);
     double v;
     if (ident) {
       v = (i == j) ? 1.0 : 0.0;
@@ -266,7 +268,7 @@ __global__ void __launch_bounds__(128) tip_table_kernel(const TipTabArgs p) {
   const int tip = blockIdx.x, r = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
   if (p.status && *p.status) return;
   const double tt = p.t[tip], rate = p.rates ? p.rates[r] : 1.0;
-  const bool ident = !(tt >= 1e-10);
+  const bool ident = !(tt * rate >= 1e-10);   // effective time, as in compose_kernel
   for (int o = tid; o < SS; o += nt) {
     const int i = o / S, j = o % S;
     double v = 0.0;

@@ -39,6 +39,7 @@ class Spec:
     substitution: tuple                 # ("JC69",) ("F81",) ("K2P", b) ("F84", k) ("HKY85", k)
                                         # ("TN93", (a, b)) ("GTR", co) ("Const", matrix)
     site_variation: tuple = ("Constant",)   # ("DiscreteGamma", k, alpha) | ("DiscreteCustom", [(r, p)])
+                                            # | ("DiscreteTheta", k, alpha, pinvar)
     base_priors: object = "Equal"           # "Equal" | ("Empirical", freqs)
     alphabet_size: int = 4
 
@@ -195,6 +196,21 @@ def _site_classes(spec: Spec):
     if sv[0] == "DiscreteCustom":
         arr = np.asarray(sv[1], np.float64)
         return arr[:, 0].copy(), arr[:, 1].copy()
+    if sv[0] == "DiscreteTheta":
+        # (GAMMA_SITES, ALPHA, PERCENT_INVAR), lib/mlModel.ml:684-694: w Gamma
+        # classes (one rate-1 class when w = 1) and the proportion of invariant
+        # sites.  The reference's likelihood is a stub, so how that proportion
+        # enters is not fixed there; here it is the usual mixture, an extra
+        # class of rate 0 (P = I) with probability pinvar and the Gamma classes
+        # sharing 1 - pinvar.
+        w, alpha, pinv = int(sv[1]), float(sv[2]), float(sv[3])
+        if w < 1:
+            raise Error("Number of rate categories must be >= 1 (if invar w/out gamma)")
+        if not 0.0 <= pinv < 1.0:
+            raise Error("proportion of invariant sites must lie in [0, 1)")
+        g = np.ones(1) if w == 1 else gamma_rates(alpha, w)
+        return (np.concatenate([[0.0], g]),
+                np.concatenate([[pinv], np.full(w, (1.0 - pinv) / w)]))
     raise Error(f"site variation {sv[0]} is not supported")
 
 
@@ -299,9 +315,19 @@ def gen_subst_opt_func(model: Model, ctx: _native.Context | None = None):
 
 
 def gen_rates_opt_func(model: Model, ctx: _native.Context | None = None):
-    """Site-rate parameters: the shape of DiscreteGamma; Constant and a
-    custom rate list have none."""
+    """Site-rate parameters: the shape of DiscreteGamma; the shape (when more
+    than one class) and the invariant proportion (as a logit) of
+    DiscreteTheta; Constant and a custom rate list have none."""
     sv = model.spec.site_variation
+    if sv[0] == "DiscreteTheta":
+        w, alpha, pinv = int(sv[1]), float(sv[2]), float(sv[3])
+        if w > 1:
+            return (np.array([np.log(alpha), np.log(pinv / (1.0 - pinv))]),
+                    lambda x: _with(model, ctx, site_variation=(
+                        "DiscreteTheta", w, float(np.exp(x[0])), float(1.0 / (1.0 + np.exp(-x[1]))))))
+        return (np.array([np.log(pinv / (1.0 - pinv))]),
+                lambda x: _with(model, ctx, site_variation=(
+                    "DiscreteTheta", w, alpha, float(1.0 / (1.0 + np.exp(-x[0]))))))
     if sv[0] == "DiscreteGamma":
         k = sv[1]
         return np.log([float(sv[2])]), lambda x: _with(model, ctx,

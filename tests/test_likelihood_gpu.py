@@ -212,3 +212,32 @@ def test_full_size_precision_config(ctx, orc):
     assert abs(g64 - exp) <= FP64_REL * abs(exp)
     assert abs(g32 - exp) <= fp32_bound(tr.n_internal, w, pats.shape[1])
     assert abs(g48 - exp) <= FP32X2_ABS
+
+
+@pytest.mark.parametrize("w", [1, 4])
+def test_discrete_theta_gamma_plus_invariant(ctx, orc, w):
+    """+G+I: the invariant class is a rate-0 class (P = I); the GPU forms
+    against the oracle on the same rates and probabilities, and pinvar 0
+    against DiscreteGamma."""
+    from phylocaml_gb300 import likelihood as Lk
+    rng = np.random.default_rng(31 + w)
+    tr = T.yule(40, rng, 0.1)
+    spec = M.Spec(("GTR", rng.uniform(0.5, 2, 5)), ("DiscreteTheta", w, 0.7, 0.25),
+                  ("Empirical", rng.dirichlet([5] * 4)))
+    m = M.create(spec, ctx)
+    assert len(m.rates) == w + 1 and m.rates[0] == 0.0
+    q, pi, rr, pp = synth.host_model(M.Spec(("GTR", spec.substitution[1]), ("DiscreteGamma", 4, 0.7),
+                                            spec.base_priors))
+    states = synth.simulate_sites(tr, q, pi, rr, pp, 2000, rng)
+    codes = (np.uint8(1) << states).astype(np.uint8)
+    exp = oracle_lnl(orc, tr, m, codes, None)
+    g64 = Lk.tree_lnl(tr, m, codes, synth.dna_code_table(), None, 64, ctx)
+    g48 = Lk.tree_lnl(tr, m, codes, synth.dna_code_table(), None, 48, ctx)
+    assert abs(g64 - exp) <= FP64_REL * abs(exp)
+    assert abs(g48 - exp) <= FP32X2_ABS
+    if w == 4:
+        m0 = M.create(M.Spec(spec.substitution, ("DiscreteTheta", 4, 0.7, 0.0), spec.base_priors), ctx)
+        mg = M.create(M.Spec(spec.substitution, ("DiscreteGamma", 4, 0.7), spec.base_priors), ctx)
+        a = Lk.tree_lnl(tr, m0, codes, synth.dna_code_table(), None, 64, ctx)
+        b = Lk.tree_lnl(tr, mg, codes, synth.dna_code_table(), None, 64, ctx)
+        assert abs(a - b) <= 1e-10 * abs(b)

@@ -60,3 +60,17 @@ def test_ml_fit_reaches_the_truth_and_matches_the_oracle(ctx, orc):
     # the estimates are near the simulating values
     assert fit.spec.site_variation[2] == pytest.approx(spec.site_variation[2], rel=0.3)
     np.testing.assert_allclose(fit.priors, truth.priors, atol=0.02)
+
+
+def test_rates_hook_for_gamma_plus_invariant(ctx):
+    m = M.create(M.Spec(("HKY85", 2.0), ("DiscreteTheta", 4, 0.8, 0.15),
+                        ("Empirical", [0.3, 0.2, 0.2, 0.3])), ctx)
+    x0, build = M.gen_rates_opt_func(m, ctx)
+    assert len(x0) == 2
+    back = build(x0)
+    np.testing.assert_allclose(back.rates, m.rates, rtol=1e-12)
+    np.testing.assert_allclose(back.probs, m.probs, rtol=1e-12)
+    moved = build(x0 + np.array([0.0, 1.0]))
+    assert moved.probs[0] > m.probs[0] and moved.rates[0] == 0.0
+    one = M.create(M.Spec(("JC69",), ("DiscreteTheta", 1, 0.8, 0.15)), ctx)
+    assert len(M.gen_rates_opt_func(one, ctx)[0]) == 1

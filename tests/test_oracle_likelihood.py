@@ -137,3 +137,18 @@ def test_prune_oracle_rescaling_on_deep_tree(orc):
                             None, site_lnl=True)
     assert np.isfinite(lnl) and np.isfinite(sl).all() and (sl < -800).all()
     assert abs(lnl - sl.sum()) < 1e-9 * abs(lnl)
+
+
+def test_discrete_theta_classes():
+    """DiscreteTheta (lib/mlModel.ml:684-694): w Gamma classes plus a rate-0
+    class holding the invariant proportion; w = 1 keeps one rate-1 class."""
+    from phylocaml_gb300 import mlmodel as M
+    r, p = M._site_classes(M.Spec(("JC69",), ("DiscreteTheta", 4, 0.5, 0.2)))
+    np.testing.assert_allclose(r[1:], M.gamma_rates(0.5, 4))
+    assert r[0] == 0.0 and p[0] == 0.2
+    np.testing.assert_allclose(p[1:], 0.2)
+    assert abs(p.sum() - 1.0) < 1e-15
+    r1, p1 = M._site_classes(M.Spec(("JC69",), ("DiscreteTheta", 1, 0.5, 0.3)))
+    assert list(r1) == [0.0, 1.0] and list(p1) == [0.3, 0.7]
+    with pytest.raises(M.Error):
+        M._site_classes(M.Spec(("JC69",), ("DiscreteTheta", 0, 0.5, 0.3)))
