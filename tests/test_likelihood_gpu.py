@@ -241,3 +241,24 @@ def test_discrete_theta_gamma_plus_invariant(ctx, orc, w):
         a = Lk.tree_lnl(tr, m0, codes, synth.dna_code_table(), None, 64, ctx)
         b = Lk.tree_lnl(tr, mg, codes, synth.dna_code_table(), None, 64, ctx)
         assert abs(a - b) <= 1e-10 * abs(b)
+
+
+def test_zero_length_branches(ctx, orc):
+    """Branches of length 0 (P = I for every rate class): every form agrees
+    with the oracle, including sites that such a branch makes impossible for
+    one rate class and improbable overall."""
+    from phylocaml_gb300 import likelihood as Lk
+    rng = np.random.default_rng(77)
+    tr = T.yule(30, rng, 0.1)
+    bl = tr.brlen.copy()
+    bl[rng.choice(len(bl), 8, replace=False)] = 0.0
+    tr = T.RootedTree(tr.left, tr.right, bl)
+    spec = M.Spec(("GTR", [1.2, 0.8, 1.5, 0.7, 1.1]), ("DiscreteGamma", 4, 0.6),
+                  ("Empirical", [0.3, 0.2, 0.25, 0.25]))
+    m = M.create(spec, ctx)
+    codes = (np.uint8(1) << rng.integers(0, 4, (30, 1500))).astype(np.uint8)
+    exp = oracle_lnl(orc, tr, m, codes, None)
+    assert np.isfinite(exp)
+    for prec, tol in ((64, FP64_REL * abs(exp)), (48, FP32X2_ABS), (32, fp32_bound(29, None, 1500))):
+        got = Lk.tree_lnl(tr, m, codes, synth.dna_code_table(), None, prec, ctx)
+        assert np.isfinite(got) and abs(got - exp) <= tol, (prec, got, exp)
