@@ -104,7 +104,30 @@ __device__ __forceinline__ uint32_t tf32_bits(float x) {
   return r;
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t ta, float *v) {
+// W consecutive TMEM columns of this thread's lane (32x32b shape)
+template <int W>
+__device__ __forceinline__ void tmem_ld(uint32_t ta, float *v);
+template <>
+__device__ __forceinline__ void tmem_ld<4>(uint32_t ta, float *v) {
+  uint32_t r[4];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(ta));
+#pragma unroll
+  for (int j = 0; j < 4; ++j) v[j] = __uint_as_float(r[j]);
+}
+template <>
+__device__ __forceinline__ void tmem_ld<8>(uint32_t ta, float *v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                 "=r"(r[7])
+               : "r"(ta));
+#pragma unroll
+  for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
+}
+template <>
+__device__ __forceinline__ void tmem_ld<16>(uint32_t ta, float *v) {
   uint32_t r[16];
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
@@ -157,11 +180,13 @@ __device__ __forceinline__ int blk_bytes(const BVar &v) {
 }
 
 
-// What one epilogue step reads.
+// What one epilogue step reads.  Shapes that follow from the padded state
+// count are template parameters of the step; these are the rest, read from
+// the variant once per work item.
 struct EpiIn {
-  int4 op;
   const unsigned char *sl;   // the step's ring slot
   int BB;                    // bytes of one child block in the slot
+  int n_tips, n_codes, S;
   uint32_t tmem, lane_base;
   int m;                     // pattern within the tile (TMEM lane)
   bool active, last;
@@ -172,16 +197,17 @@ struct EpiIn {
 // the RP rate classes of this pass: the product of the two children (tip
 // rows from the slot, or the MMA results from TMEM), rescaled by a power of
 // two agreed with the other half, written into the node's TMEM stack slot.
-// KP and RP are template parameters so that every state index is a
-// compile-time constant and the vectors stay in registers.  TMEM columns:
-// D of child h, rate q at (h*RP + q)*Np; stack slot s, rate q at
-// 2*RP*Np + (s*RP + q)*Kp.
+// KP and RP are template parameters so that every state index and TMEM
+// column is a compile-time constant and the vectors stay in registers.
+// TMEM columns: D of child h, rate q at (h*RP + q)*NP; stack slot s, rate q
+// at 2*RP*NP + (s*RP + q)*KP.
 template <int KP, int RP>
-__device__ __forceinline__ void epi_step(const BVar &v, const BatchArgs &p, const EpiIn &in, int hf,
-                                         int lane, int slot, uint64_t *empty, float (*xch)[RP][BT_M],
+__device__ __forceinline__ void epi_step(const BatchArgs &p, const EpiIn &in, const int4 op, int hf,
+                                         int lane, int slot, uint64_t *empty, float (*xch)[2][BT_M],
                                          int *escale, bool &ok, double *Lp) {
   constexpr int B = KP / 2;
-  const int S = v.S;
+  constexpr int NP = (KP + 15) / 16 * 16;
+  constexpr int SPT = KP | 1;
   float acc[RP][B];
 #pragma unroll
   for (int q = 0; q < RP; ++q)
@@ -193,38 +219,39 @@ __device__ __forceinline__ void epi_step(const BVar &v, const BatchArgs &p, cons
   auto half = [&](auto HFc) {
     constexpr int HF = decltype(HFc)::value;
     constexpr int e0 = HF * B;
-    constexpr int c_first = (e0 / 16) * 16;
-    constexpr int n_chunks = (e0 - c_first + B + 15) / 16;
-    for (int h = 0; h < 2 && ok; ++h) {
-      const int ch = h == 0 ? in.op.y : in.op.z;
-      if (ch < v.n_tips) {
+    // TMEM loads of W columns: the widest of 16, 8, 4 that divides both the
+    // first column and the width of this half
+    constexpr int W = (e0 % 16 == 0 && B % 16 == 0) ? 16 : (e0 % 8 == 0 && B % 8 == 0) ? 8 : 4;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      if (!ok) break;
+      const int ch = h == 0 ? op.y : op.z;
+      if (ch < in.n_tips) {
         int code = in.sl[h * 128 + in.m];
-        if (code >= v.n_codes) {
+        if (code >= in.n_codes) {
           if (in.active && HF == 0) atomicOr(p.flag, PGPU_FLAG_BADCODE);
           code = 0;
         }
 #pragma unroll
         for (int q = 0; q < RP; ++q) {
           const float *row = reinterpret_cast<const float *>(in.sl + 256 + (size_t)(h * RP + q) * in.BB) +
-                             (size_t)code * v.SpT + e0;
+                             code * SPT + e0;
 #pragma unroll
           for (int e = 0; e < B; ++e)
             acc[q][e] *= row[e];
         }
       } else {
+        float d[RP][B];
 #pragma unroll
-        for (int q = 0; q < RP; ++q) {
-          float d[n_chunks][16];
+        for (int q = 0; q < RP; ++q)
 #pragma unroll
-          for (int u = 0; u < n_chunks; ++u)
-            tmem_ld16(in.tmem + in.lane_base + (uint32_t)((h * RP + q) * v.Np + c_first + 16 * u), d[u]);
-          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          for (int c = 0; c < B; c += W)
+            tmem_ld<W>(in.tmem + in.lane_base + (uint32_t)((h * RP + q) * NP + e0 + c), &d[q][c]);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-          for (int e = 0; e < B; ++e) {
-            const int col = e0 + e - c_first;
-            acc[q][e] *= d[col / 16][col % 16];
-          }
-        }
+        for (int q = 0; q < RP; ++q)
+#pragma unroll
+          for (int e = 0; e < B; ++e) acc[q][e] *= d[q][e];
       }
     }
   };
@@ -237,10 +264,15 @@ __device__ __forceinline__ void epi_step(const BVar &v, const BatchArgs &p, cons
   float mx[RP];
 #pragma unroll
   for (int q = 0; q < RP; ++q) {
-    mx[q] = 0.0f;
+    // pairwise maxima: a short dependency chain
+    float t[B];
 #pragma unroll
-    for (int e = 0; e < B; ++e)
-      mx[q] = fmaxf(mx[q], acc[q][e]);
+    for (int e = 0; e < B; ++e) t[e] = acc[q][e];
+#pragma unroll
+    for (int w = 1; w < B; w *= 2)
+#pragma unroll
+      for (int e = 0; e + w < B; e += 2 * w) t[e] = fmaxf(t[e], t[e + w]);
+    mx[q] = t[0];
     xch[hf][q][in.m] = mx[q];
   }
   // the exchange barrier also makes the timeout verdict uniform over the
@@ -255,7 +287,7 @@ __device__ __forceinline__ void epi_step(const BVar &v, const BatchArgs &p, cons
         : "memory");
     ok = all_ok != 0;
   }
-  const int so = (in.op.w >> 16) & 0xff;
+  const int so = (op.w >> 16) & 0xff;
 #pragma unroll
   for (int q = 0; q < RP; ++q) {
     const float m2 = fmaxf(mx[q], xch[hf ^ 1][q][in.m]);
@@ -269,11 +301,10 @@ __device__ __forceinline__ void epi_step(const BVar &v, const BatchArgs &p, cons
       for (int e = 0; e < B; ++e) acc[q][e] = acc[q][e] * f1 * f2;
     }
     // into the TMEM stack slot: my K columns e0 .. e0 + B - 1
-    const uint32_t col = (uint32_t)(2 * RP * v.Np + (so * RP + q) * v.Kp + e0);
+    const uint32_t col = in.tmem + in.lane_base + (uint32_t)(2 * RP * NP + (so * RP + q) * KP + e0);
 #pragma unroll
     for (int c0 = 0; c0 < B; c0 += 4)
-      asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(
-                       in.tmem + in.lane_base + col + (uint32_t)c0),
+      asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(col + (uint32_t)c0),
                    "r"(tf32_bits(acc[q][c0])), "r"(tf32_bits(acc[q][c0 + 1])),
                    "r"(tf32_bits(acc[q][c0 + 2])), "r"(tf32_bits(acc[q][c0 + 3]))
                    : "memory");
@@ -281,33 +312,183 @@ __device__ __forceinline__ void epi_step(const BVar &v, const BatchArgs &p, cons
       double l = 0.0;
 #pragma unroll
       for (int e = 0; e < B; ++e)
-        if (e0 + e < S) l += in.pi[e0 + e] * (double)acc[q][e];
+        if (e0 + e < in.S) l += in.pi[e0 + e] * (double)acc[q][e];
       Lp[q] = l;
     }
   }
 }
 
+// Shared state of the epilogue warps.
+struct EpiShared {
+  uint64_t *full, *empty, *mma_bar;
+  const int4 *slot_op;       // each ring slot's postorder step, written by the producer
+  unsigned char *smem;
+  float (*xch)[2][BT_M];     // per half, rate class of the pass, lane: max entry
+  double (*xchd)[2][BT_M];
+  double2 *red;
+  uint32_t tmem;
+};
+
+// Every pass and postorder step of one work item (variant, tile) with
+// compile-time shapes: thread 0 issues each step's MMAs, then the eight
+// warps run its epilogue.
+template <int KP, int RP>
+__device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh, const BVar &vg, const int2 wk,
+                                      int tid, long long &seq, bool &ok) {
+  constexpr int NP = (KP + 15) / 16 * 16;
+  constexpr uint32_t LBO = 128, SBO = (uint32_t)(KP / 4) * 128;
+  constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NP >> 3) << 17) |
+                             ((uint32_t)(BT_M >> 4) << 24);
+  const int warp = tid >> 5, lane = tid & 31;
+  const int q4 = warp & 3, hf = warp >> 2;
+  const int m = 32 * q4 + lane;   // pattern within the tile
+  // the variant's fields, once per item
+  const int n_ops = vg.n_ops, R = vg.R;
+  EpiIn in;
+  in.BB = blk_bytes(vg);
+  in.n_tips = vg.n_tips;
+  in.n_codes = vg.n_codes;
+  in.S = vg.S;
+  in.tmem = sh.tmem;
+  in.lane_base = (uint32_t)(32 * q4) << 16;
+  in.m = m;
+  const long long pat = (long long)wk.y * BT_M + m;
+  in.active = pat < vg.n_pat;
+  in.pi = p.pis + vg.pi_off;
+  double lnr[4];
+  double Lp[RP];
+#pragma unroll
+  for (int q = 0; q < RP; ++q) Lp[q] = 0.0;
+  for (int r0 = 0; r0 < R && ok; r0 += RP) {
+    int escale[RP];
+#pragma unroll
+    for (int q = 0; q < RP; ++q) escale[q] = 0;
+    for (int i = 0; i < n_ops; ++i, ++seq) {
+      const int slot = (int)(seq & (BT_ST - 1));
+      const uint32_t par = (uint32_t)((seq / BT_ST) & 1);
+      in.sl = sh.smem + (size_t)slot * p.slot_bytes;
+      // ---- issue this step's MMAs (internal children) ----
+      if (tid == 0) {
+        const bool got = mbar_wait_bounded(&sh.full[slot], par, p.flag);
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int4 op = sh.slot_op[slot];
+        bool any = false;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int ch = h == 0 ? op.y : op.z;
+          if (!got || ch < in.n_tips) continue;
+          any = true;
+          const int sa = (op.w >> (8 * h)) & 0xff;
+#pragma unroll
+          for (int q = 0; q < RP; ++q) {
+            const uint32_t d_col = (uint32_t)((h * RP + q) * NP);
+            const uint32_t a_col = (uint32_t)(2 * RP * NP + (sa * RP + q) * KP);
+            const unsigned char *blk = in.sl + 256 + (size_t)(h * RP + q) * in.BB;
+#pragma unroll
+            for (int ks = 0; ks < KP / 8; ++ks) {
+              const uint64_t bd = smem_desc(blk + (size_t)ks * 2 * LBO, LBO, SBO);
+              const uint32_t accf = ks > 0 ? 1u : 0u;
+              asm volatile(
+                  "{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %4, 0;\n\t"
+                  "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, q;\n\t}" ::"r"(sh.tmem + d_col),
+                  "r"(sh.tmem + a_col + (uint32_t)(ks * 8)), "l"(bd), "r"(IDESC), "r"(accf)
+                  : "memory");
+            }
+          }
+        }
+        if (any) {
+          asm volatile(
+              "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                  su32(sh.mma_bar))
+              : "memory");
+          asm volatile(
+              "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                  su32(&sh.empty[slot]))
+              : "memory");
+        } else {
+          mbar_arrive(sh.mma_bar);
+          mbar_arrive(&sh.empty[slot]);
+        }
+      }
+      // ---- epilogue of this step ----
+      bool got = mbar_wait_bounded(&sh.full[slot], par, p.flag);
+      got = got && mbar_wait_bounded(sh.mma_bar, (uint32_t)(seq & 1), p.flag);
+      got = __all_sync(0xffffffffu, got);
+      if (!got) {
+        ok = false;
+        atomicOr(p.flag, PGPU_FLAG_TIMEOUT);
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int4 op = sh.slot_op[slot];
+      in.last = i == n_ops - 1;
+      epi_step<KP, RP>(p, in, op, hf, lane, slot, sh.empty, sh.xch, escale, ok, Lp);
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      // every vector of this step is in TMEM before the next MMA issues
+      asm volatile("bar.sync 1, 256;" ::: "memory");
+      if (!ok) break;
+    }
+    if (!ok) break;
+    // roots of this pass's rate classes (both halves of the row)
+#pragma unroll
+    for (int q = 0; q < RP; ++q) sh.xchd[hf][q][m] = Lp[q];
+    asm volatile("bar.sync 1, 256;" ::: "memory");
+#pragma unroll
+    for (int q = 0; q < RP; ++q) {
+      const double L = Lp[q] + sh.xchd[hf ^ 1][q][m];
+      lnr[r0 + q] = log(L) + (double)escale[q] * 0.69314718055994530942;
+    }
+    asm volatile("bar.sync 1, 256;" ::: "memory");
+  }
+  // join the rate classes: log sum_r probs[r] exp(lnr[r])
+  double s = 0.0, comp = 0.0;
+  if (ok && in.active && hf == 0) {
+    double mxl = -INFINITY;
+    for (int r = 0; r < R; ++r) mxl = fmax(mxl, lnr[r]);
+    double sum = 0.0;
+    for (int r = 0; r < R; ++r) sum += vg.probs[r] * exp(lnr[r] - mxl);
+    const double lnl = mxl + log(sum);
+    if (p.site_lnl) p.site_lnl[vg.pat_off + pat] = lnl;
+    s = vg.weights ? vg.weights[pat] * lnl : lnl;
+  }
+  if (hf == 0) {
+    warp_csum_d(s, comp);
+    if (lane == 0) sh.red[q4] = make_double2(s, comp);
+  }
+  asm volatile("bar.sync 1, 256;" ::: "memory");
+  if (tid == 0) {
+    double ss = 0.0, cc = 0.0;
+    for (int k = 0; k < 4; ++k) {
+      double t, e;
+      two_sum_d(ss, sh.red[k].x, t, e);
+      ss = t;
+      cc += e + sh.red[k].y;
+    }
+    // by (variant, tile), whatever order the work list runs in
+    p.partials[vg.tile0 + wk.y] = make_double2(ss, cc);
+  }
+  asm volatile("bar.sync 1, 256;" ::: "memory");
+}
+
 template <int KP>
-__device__ __forceinline__ void epi_dispatch(const BVar &v, const BatchArgs &p, const EpiIn &in, int hf,
-                                             int lane, int slot, uint64_t *empty, float (*xch1)[1][BT_M],
-                                             float (*xch2)[2][BT_M], int *escale, bool &ok,
-                                             double *Lp) {
+__device__ __forceinline__ void epi_item_rp(const BatchArgs &p, const EpiShared &sh, const BVar &vg,
+                                            const int2 wk, int tid, long long &seq, bool &ok) {
   if constexpr (KP <= 32) {
-    if (v.RP == 2) {
-      epi_step<KP, 2>(v, p, in, hf, lane, slot, empty, xch2, escale, ok, Lp);
+    if (vg.RP == 2) {
+      epi_item<KP, 2>(p, sh, vg, wk, tid, seq, ok);
       return;
     }
   }
-  epi_step<KP, 1>(v, p, in, hf, lane, slot, empty, xch1, escale, ok, Lp);
+  epi_item<KP, 1>(p, sh, vg, wk, tid, seq, ok);
 }
 
 __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs p) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint64_t full[BT_ST], empty[BT_ST], mma_bar;
+  __shared__ int4 slot_op[BT_ST];
   __shared__ uint32_t tmem_base;
-  __shared__ float xch2[2][2][BT_M];   // per half, rate class of the pass, lane: max entry
+  __shared__ float xch[2][2][BT_M];    // per half, rate class of the pass, lane: max entry
   __shared__ double xchd[2][2][BT_M];
-  float(*xch1)[1][BT_M] = reinterpret_cast<float(*)[1][BT_M]>(&xch2[0][0][0]);
   __shared__ double2 red[4];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -341,37 +522,39 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
         const int BB = blk_bytes(v);
         const uint32_t bmat_bytes = (uint32_t)(v.Np * v.Kp * 4);
         const uint32_t tip_bytes = (uint32_t)(v.NCp * v.SpT * 4);
-        const int RP = v.RP;
-        for (int r0 = 0; r0 < v.R && ok; r0 += RP) {
-          for (int i = 0; i < v.n_ops; ++i, ++seq) {
+        const int RP = v.RP, R = v.R, n_ops = v.n_ops, n_tips = v.n_tips;
+        const long long ops_off = v.ops_off, ld = v.ld, tip_off = v.tip_off, bmat_off = v.bmat_off;
+        const uint8_t *codes = v.codes;
+        const long long bstride = (long long)v.Np * v.Kp, tstride = (long long)v.NCp * v.SpT;
+        for (int r0 = 0; r0 < R && ok; r0 += RP) {
+          for (int i = 0; i < n_ops; ++i, ++seq) {
             const int slot = (int)(seq & (BT_ST - 1));
             const long long round = seq / BT_ST;
+            const int4 op = __ldg(p.ops + ops_off + i);
             if (round > 0 && !mbar_wait_bounded(&empty[slot], (uint32_t)((round - 1) & 1), p.flag)) {
               ok = false;
               break;
             }
-            const int4 op = __ldg(p.ops + v.ops_off + i);
             unsigned char *sl = smem + (size_t)slot * p.slot_bytes;
             uint32_t tx = 0;
             for (int h = 0; h < 2; ++h) {
               const int ch = h == 0 ? op.y : op.z;
-              tx += ch < v.n_tips ? 128u + RP * tip_bytes : RP * bmat_bytes;
+              tx += ch < n_tips ? 128u + RP * tip_bytes : RP * bmat_bytes;
             }
+            // the step itself, published by the arrive below (release)
+            slot_op[slot] = op;
             mbar_arrive_expect_tx(&full[slot], tx);
             for (int h = 0; h < 2; ++h) {
               const int ch = h == 0 ? op.y : op.z;
-              if (ch < v.n_tips)
-                bulk_g2s(sl + h * 128, v.codes + (long long)ch * v.ld + (long long)wk.y * 128, 128u,
-                         &full[slot]);
+              if (ch < n_tips)
+                bulk_g2s(sl + h * 128, codes + (long long)ch * ld + (long long)wk.y * 128, 128u, &full[slot]);
               for (int q = 0; q < RP; ++q) {
                 unsigned char *blk = sl + 256 + (size_t)(h * RP + q) * BB;
-                if (ch < v.n_tips)
-                  bulk_g2s(blk, p.tiptab + v.tip_off + ((long long)ch * v.R + r0 + q) * v.NCp * v.SpT,
-                           tip_bytes, &full[slot]);
+                if (ch < n_tips)
+                  bulk_g2s(blk, p.tiptab + tip_off + ((long long)ch * R + r0 + q) * tstride, tip_bytes,
+                           &full[slot]);
                 else
-                  bulk_g2s(blk,
-                           p.bmat + v.bmat_off +
-                               ((long long)(ch - v.n_tips) * v.R + r0 + q) * (long long)v.Np * v.Kp,
+                  bulk_g2s(blk, p.bmat + bmat_off + ((long long)(ch - n_tips) * R + r0 + q) * bstride,
                            bmat_bytes, &full[slot]);
               }
             }
@@ -386,138 +569,22 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
     // warp w: TMEM lanes 32 (w % 4) ..; states [hf B, hf B + B) of the row,
     // B = Kp / 2.  Thread 0 also issues every step's MMAs, right after the
     // previous step's vectors are in TMEM.
-    const int q = warp & 3, hf = warp >> 2;
-    const int m = 32 * q + lane;                          // pattern within the tile
-    const uint32_t lane_base = (uint32_t)(32 * q) << 16;
+    const EpiShared sh{full, empty, &mma_bar, slot_op, smem, xch, xchd, red, tmem};
     long long seq = 0;
     bool ok = true;
     for (long long w = blockIdx.x; w < p.n_work && ok; w += gridDim.x) {
       const int2 wk = __ldg(p.work + w);
       const BVar &v = p.vars[wk.x];
-      const int BB = blk_bytes(v);
-      const long long pat = (long long)wk.y * BT_M + m;
-      const bool active = pat < v.n_pat;
-      const uint32_t LBO = 128, SBO = (uint32_t)(v.Kp / 4) * 128;
-      uint32_t idesc = 0;
-      idesc |= 1u << 4;
-      idesc |= 2u << 7;
-      idesc |= 2u << 10;
-      idesc |= (uint32_t)(v.Np >> 3) << 17;
-      idesc |= (uint32_t)(BT_M >> 4) << 24;
-      double lnr[4];
-      double Lp[2] = {0.0, 0.0};   // this half row's share of the root likelihoods
-      const int RP = v.RP;
-      for (int r0 = 0; r0 < v.R && ok; r0 += RP) {
-        int escale[2] = {0, 0};
-        for (int i = 0; i < v.n_ops; ++i, ++seq) {
-          const int slot = (int)(seq & (BT_ST - 1));
-          const int4 op = __ldg(p.ops + v.ops_off + i);
-          const unsigned char *sl = smem + (size_t)slot * p.slot_bytes;
-          // ---- issue this step's MMAs (internal children) ----
-          if (tid == 0) {
-            bool got = mbar_wait_bounded(&full[slot], (uint32_t)((seq / BT_ST) & 1), p.flag);
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            bool any = false;
-            for (int h = 0; h < 2 && got; ++h) {
-              const int ch = h == 0 ? op.y : op.z;
-              if (ch < v.n_tips) continue;
-              any = true;
-              const int sa = (op.w >> (8 * h)) & 0xff;
-              for (int q = 0; q < RP; ++q) {
-                const uint32_t d_col = (uint32_t)((h * RP + q) * v.Np);
-                const uint32_t a_col = (uint32_t)(2 * RP * v.Np + (sa * RP + q) * v.Kp);
-                const unsigned char *blk = sl + 256 + (size_t)(h * RP + q) * BB;
-                for (int ks = 0; ks < v.Kp / 8; ++ks) {
-                  const uint64_t bd = smem_desc(blk + (size_t)ks * 2 * LBO, LBO, SBO);
-                  const uint32_t accf = ks > 0 ? 1u : 0u;
-                  asm volatile(
-                      "{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %4, 0;\n\t"
-                      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, q;\n\t}" ::"r"(tmem + d_col),
-                      "r"(tmem + a_col + (uint32_t)(ks * 8)), "l"(bd), "r"(idesc), "r"(accf)
-                      : "memory");
-                }
-              }
-            }
-            if (any) {
-              asm volatile(
-                  "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                      su32(&mma_bar))
-                  : "memory");
-              asm volatile(
-                  "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                      su32(&empty[slot]))
-                  : "memory");
-            } else {
-              mbar_arrive(&mma_bar);
-              mbar_arrive(&empty[slot]);
-            }
-          }
-          // ---- epilogue of this step ----
-          bool got = mbar_wait_bounded(&full[slot], (uint32_t)((seq / BT_ST) & 1), p.flag);
-          got = got && mbar_wait_bounded(&mma_bar, (uint32_t)(seq & 1), p.flag);
-          got = __all_sync(0xffffffffu, got);
-          if (!got) {
-            ok = false;
-            atomicOr(p.flag, PGPU_FLAG_TIMEOUT);
-          }
-          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          EpiIn in{op, sl, BB, tmem, lane_base, m, active, i == v.n_ops - 1, p.pis + v.pi_off};
-#define EPI(K) epi_dispatch<K>(v, p, in, hf, lane, slot, empty, xch1, xch2, escale, ok, Lp)
-          switch (v.Kp) {
-            case 8: EPI(8); break;
-            case 16: EPI(16); break;
-            case 24: EPI(24); break;
-            case 32: EPI(32); break;
-            case 40: EPI(40); break;
-            case 48: EPI(48); break;
-            case 56: EPI(56); break;
-            default: EPI(64); break;
-          }
-#undef EPI
-          asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-          // every vector of this step is in TMEM before the next MMA issues
-          asm volatile("bar.sync 1, 256;" ::: "memory");
-          if (!ok) break;
-        }
-        if (!ok) break;
-        // roots of this pass's rate classes (both halves of the row)
-        for (int q = 0; q < RP; ++q) xchd[hf][q][m] = Lp[q];
-        asm volatile("bar.sync 1, 256;" ::: "memory");
-        for (int q = 0; q < RP; ++q) {
-          const double L = Lp[q] + xchd[hf ^ 1][q][m];
-          lnr[r0 + q] = log(L) + (double)escale[q] * 0.69314718055994530942;
-        }
-        asm volatile("bar.sync 1, 256;" ::: "memory");
+      switch (v.Kp) {
+        case 8: epi_item_rp<8>(p, sh, v, wk, tid, seq, ok); break;
+        case 16: epi_item_rp<16>(p, sh, v, wk, tid, seq, ok); break;
+        case 24: epi_item_rp<24>(p, sh, v, wk, tid, seq, ok); break;
+        case 32: epi_item_rp<32>(p, sh, v, wk, tid, seq, ok); break;
+        case 40: epi_item_rp<40>(p, sh, v, wk, tid, seq, ok); break;
+        case 48: epi_item_rp<48>(p, sh, v, wk, tid, seq, ok); break;
+        case 56: epi_item_rp<56>(p, sh, v, wk, tid, seq, ok); break;
+        default: epi_item_rp<64>(p, sh, v, wk, tid, seq, ok); break;
       }
-      // join the rate classes: log sum_r probs[r] exp(lnr[r])
-      double s = 0.0, comp = 0.0;
-      if (ok && active && hf == 0) {
-        double mxl = -INFINITY;
-        for (int r = 0; r < v.R; ++r) mxl = fmax(mxl, lnr[r]);
-        double sum = 0.0;
-        for (int r = 0; r < v.R; ++r) sum += v.probs[r] * exp(lnr[r] - mxl);
-        const double lnl = mxl + log(sum);
-        if (p.site_lnl) p.site_lnl[v.pat_off + pat] = lnl;
-        s = v.weights ? v.weights[pat] * lnl : lnl;
-      }
-      if (hf == 0) {
-        warp_csum_d(s, comp);
-        if (lane == 0) red[q] = make_double2(s, comp);
-      }
-      asm volatile("bar.sync 1, 256;" ::: "memory");
-      if (tid == 0) {
-        double ss = 0.0, cc = 0.0;
-        for (int k = 0; k < 4; ++k) {
-          double t, e;
-          two_sum_d(ss, red[k].x, t, e);
-          ss = t;
-          cc += e + red[k].y;
-        }
-        // by (variant, tile), whatever order the work list runs in
-        p.partials[v.tile0 + wk.y] = make_double2(ss, cc);
-      }
-      asm volatile("bar.sync 1, 256;" ::: "memory");
     }
     // the last MMAs finish before TMEM is released
     if (tid == 0 && seq > 0) (void)mbar_wait_bounded(&mma_bar, (uint32_t)((seq - 1) & 1), p.flag);

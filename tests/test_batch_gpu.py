@@ -132,3 +132,44 @@ def test_autotune_and_cache(ctx, tmp_path):
     again, t2 = B.autotune(vs, ctx, sample=8, reps=1, cache_path=path)
     assert again == choice and t2 == {}
     assert B.composition_key(vs) in path.read_text()
+
+
+def random_model(rng, S):
+    """Random reversible S-state Q (exchangeabilities ~ LogNormal(0, 1),
+    frequencies ~ Dirichlet(1 x S)), mean rate 1."""
+    ex = np.triu(rng.lognormal(0.0, 1.0, (S, S)), 1)
+    ex = ex + ex.T
+    pi = rng.dirichlet(np.ones(S))
+    return synth.normalize_q(ex * pi[None, :], pi), pi
+
+
+@pytest.mark.parametrize("S,R", [(4, 1), (4, 4), (12, 2), (13, 3), (20, 1), (30, 4), (35, 1),
+                                 (45, 2), (50, 1), (64, 1), (33, 4)])
+def test_state_counts_and_rate_classes(ctx, orc, S, R):
+    """Every padded width (Kp = 8 .. 64) and rate-class count: the epilogue
+    warps split each row into shares of states (or rate class and half the
+    states), including the widths whose last shares are empty."""
+    import torch
+    from phylocaml_gb300.batch import Batch, Variant, device_codes
+    dev = torch.device("cuda:0")
+    rng = np.random.default_rng(1000 + 7 * S + R)
+    built = []
+    for n_tips, n_pat in ((11, 300), (17, 129), (6, 1)):
+        tr = T.yule(n_tips, rng, 0.1)
+        q, pi = random_model(rng, S)
+        rates = M.gamma_rates(0.7, R) if R > 1 else np.ones(1)
+        probs = np.full(R, 1.0 / R)
+        table = synth.state_code_table(S)
+        codes = rng.integers(0, S + 1, (n_tips, n_pat)).astype(np.uint8)
+        w = rng.integers(1, 4, n_pat).astype(np.float64)
+        v = Variant(tr, q, pi, rates, probs, table, device_codes(codes, dev),
+                    torch.from_numpy(w).to(dev), n_pat)
+        built.append((v, codes, w))
+    b = Batch([x[0] for x in built], ctx)
+    try:
+        tc = b.run()
+        for k, (v, codes, w) in enumerate(built):
+            exp, _ = oracle_variant(orc, v, codes, w)
+            assert abs(tc[k] - exp) <= TF32_REL * abs(exp), (S, R, k, tc[k], exp)
+    finally:
+        b.close()
