@@ -149,7 +149,7 @@ SIGNATURES: dict[str, tuple] = {
 }
 
 _lib = None
-_lock = threading.Lock()
+_lock = threading.RLock()   # default_context() holds it while load() takes it
 
 
 def load() -> C.CDLL:

@@ -105,3 +105,24 @@ def test_codon_and_protein_models():
     assert qp.shape == (20, 20) and np.allclose(pp[:, None] * qp, (pp[:, None] * qp).T)
     t = synth.state_code_table(20)
     assert t.shape == (21, 20) and (t[20] == 1).all() and (t[:20].sum(1) == 1).all()
+
+
+def test_default_context_returns_instead_of_deadlocking(native_lib):
+    """default_context() takes the module lock and then loads the library,
+    which takes it again; it must come back (with a context, or with the
+    error of a machine without a GPU) rather than wait on itself."""
+    import threading
+    from phylocaml_gb300 import _native
+    res = {}
+
+    def make():
+        try:
+            res["ctx"] = _native.default_context()
+        except _native.NativeError as e:
+            res["err"] = e
+
+    t = threading.Thread(target=make, daemon=True)
+    t.start()
+    t.join(60)
+    assert not t.is_alive()
+    assert res
