@@ -21,17 +21,21 @@
 //                  come from the staged tip table.  Rate classes are separate
 //                  passes with their own power-of-two scalers, joined at the
 //                  root with a log-sum-exp in FP64.
-//     warp 4       producer: per postorder step, bulk-copies the B blocks of
-//                  internal children, the tip-table blocks and tip-code rows
-//                  of tip children into a shared ring slot;
-//     warp 5       MMA issuer (lane 0) and TMEM allocator;
-//     warps 0-3    epilogue: thread = pattern; reads D rows (tcgen05.ld) or
-//                  tip rows, forms the product, rescales, writes the parent's
-//                  vector back into TMEM (tcgen05.st).
-//   Producer, MMA and epilogue move in lockstep per step through mbarriers
-//   (mma_bar: MMA -> epilogue, epi_bar: epilogue -> MMA), so a step's MMA
-//   never reads a vector before it is written and no mbarrier phase can be
-//   skipped.  Every wait is bounded.
+//     warp 16      producer and TMEM allocator: per postorder step,
+//                  bulk-copies the B blocks of internal children, the
+//                  tip-table blocks and tip-code rows of tip children into a
+//                  shared ring slot, and publishes the step itself;
+//     warps 0-15   epilogue: four warps per TMEM lane group of 32 patterns,
+//                  each owning a share of the row (a range of states, or a
+//                  rate class and half the states); a thread reads its D
+//                  columns (tcgen05.ld) or tip rows, forms the product,
+//                  rescales, writes the parent's vector back into TMEM
+//                  (tcgen05.st).  Thread 0 also issues every step's MMAs.
+//   The MMA (tcgen05.commit -> mma_bar) and the epilogue (a named barrier
+//   after its TMEM stores) alternate per step, so a step's MMA never reads a
+//   vector before it is written and no mbarrier phase can be skipped.
+//   Every wait is bounded.  Each work item runs a step loop compiled for its
+//   padded state count and rate classes per pass.
 //   batch_fp64_kernel  the FP64 comparison form on a sample of patterns.
 #include <algorithm>
 #include <cmath>
@@ -46,7 +50,10 @@ namespace {
 
 constexpr int BT_M = 128;          // patterns per tile (TMEM lanes)
 constexpr int BT_ST = 4;           // ring slots (power of two)
-constexpr int BT_THREADS = 288;    // 8 epilogue warps (thread 0 issues MMAs), producer
+constexpr int BT_EPI_WARPS = 16;   // epilogue warps, four per TMEM lane group; thread 0 issues MMAs
+constexpr int BT_PARTS = BT_EPI_WARPS / 4;
+constexpr int BT_EPI = 32 * BT_EPI_WARPS;
+constexpr int BT_THREADS = BT_EPI + 32;   // + the producer warp
 constexpr int BT_TMEM_COLS = 512;
 
 struct BVar {
@@ -193,34 +200,45 @@ struct EpiIn {
   const double *pi;
 };
 
-// One postorder step for the half row of states [hf*KP/2, (hf+1)*KP/2) of
-// the RP rate classes of this pass: the product of the two children (tip
-// rows from the slot, or the MMA results from TMEM), rescaled by a power of
-// two agreed with the other half, written into the node's TMEM stack slot.
-// KP and RP are template parameters so that every state index and TMEM
-// column is a compile-time constant and the vectors stay in registers.
-// TMEM columns: D of child h, rate q at (h*RP + q)*NP; stack slot s, rate q
-// at 2*RP*NP + (s*RP + q)*KP.
-template <int KP, int RP>
-__device__ __forceinline__ void epi_step(const BatchArgs &p, const EpiIn &in, const int4 op, int hf,
-                                         int lane, int slot, uint64_t *empty, float (*xch)[2][BT_M],
-                                         int *escale, bool &ok, double *Lp) {
-  constexpr int B = KP / 2;
+// The share of a row that epilogue warp w owns (PT = w / 4; the four warps
+// of a TMEM lane group own the four shares).  With two rate classes per pass
+// a share is rate class PT / 2 and half PT % 2 of the states; with one, it is
+// the PT-th range of W4 states, W4 = Kp / 4 rounded up to a multiple of 4, so
+// the last ranges of a small Kp may be empty.  Every range starts on a
+// multiple of 4 columns and is a multiple of 4 wide.
+template <int KP, int RP, int PT>
+struct Share {
+  static constexpr int W4 = ((KP / 4) + 3) & ~3;
+  static constexpr int rate = RP == 2 ? PT >> 1 : 0;
+  static constexpr int e0 = RP == 2 ? (PT & 1) * (KP / 2) : PT * W4;
+  static constexpr int B = RP == 2 ? KP / 2 : (KP - e0 <= 0 ? 0 : (KP - e0 < W4 ? KP - e0 : W4));
+};
+
+// One postorder step for this warp's share of the row: the product of the
+// two children (tip rows from the slot, or the MMA results from TMEM),
+// rescaled by a power of two agreed with the other shares of the same rate
+// class, written into the node's TMEM stack slot.  KP, RP and the share are
+// template parameters so that every state index and TMEM column is a
+// compile-time constant and the vectors stay in registers.  TMEM columns: D
+// of child h, rate q at (h*RP + q)*NP; stack slot s, rate q at
+// 2*RP*NP + (s*RP + q)*KP.
+template <int KP, int RP, int PT>
+__device__ __forceinline__ void epi_step(const BatchArgs &p, const EpiIn &in, const int4 op, int lane,
+                                         int slot, uint64_t *empty, float (*xch)[BT_M], int &escale,
+                                         bool &ok, double &Lp) {
+  using SH = Share<KP, RP, PT>;
+  constexpr int B = SH::B, e0 = SH::e0, rate = SH::rate;
+  constexpr int BA = B > 0 ? B : 1;
   constexpr int NP = (KP + 15) / 16 * 16;
   constexpr int SPT = KP | 1;
-  float acc[RP][B];
+  float acc[BA];
 #pragma unroll
-  for (int q = 0; q < RP; ++q)
-#pragma unroll
-    for (int e = 0; e < B; ++e) acc[q][e] = 1.0f;
+  for (int e = 0; e < BA; ++e) acc[e] = 1.0f;
   // states S .. KP-1 need no masks: the tip rows and the B blocks are zero
   // there, so every vector's padding is a product of zeros
-  // both halves are compiled; the warp takes its own (hf is warp-uniform)
-  auto half = [&](auto HFc) {
-    constexpr int HF = decltype(HFc)::value;
-    constexpr int e0 = HF * B;
+  if constexpr (B > 0) {
     // TMEM loads of W columns: the widest of 16, 8, 4 that divides both the
-    // first column and the width of this half
+    // first column and the width of the share
     constexpr int W = (e0 % 16 == 0 && B % 16 == 0) ? 16 : (e0 % 8 == 0 && B % 8 == 0) ? 8 : 4;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -229,92 +247,84 @@ __device__ __forceinline__ void epi_step(const BatchArgs &p, const EpiIn &in, co
       if (ch < in.n_tips) {
         int code = in.sl[h * 128 + in.m];
         if (code >= in.n_codes) {
-          if (in.active && HF == 0) atomicOr(p.flag, PGPU_FLAG_BADCODE);
+          if (in.active && PT == 0) atomicOr(p.flag, PGPU_FLAG_BADCODE);
           code = 0;
         }
+        const float *row = reinterpret_cast<const float *>(in.sl + 256 + (size_t)(h * RP + rate) * in.BB) +
+                           code * SPT + e0;
 #pragma unroll
-        for (int q = 0; q < RP; ++q) {
-          const float *row = reinterpret_cast<const float *>(in.sl + 256 + (size_t)(h * RP + q) * in.BB) +
-                             code * SPT + e0;
-#pragma unroll
-          for (int e = 0; e < B; ++e)
-            acc[q][e] *= row[e];
-        }
+        for (int e = 0; e < B; ++e) acc[e] *= row[e];
       } else {
-        float d[RP][B];
+        float d[B];
 #pragma unroll
-        for (int q = 0; q < RP; ++q)
-#pragma unroll
-          for (int c = 0; c < B; c += W)
-            tmem_ld<W>(in.tmem + in.lane_base + (uint32_t)((h * RP + q) * NP + e0 + c), &d[q][c]);
+        for (int c = 0; c < B; c += W)
+          tmem_ld<W>(in.tmem + in.lane_base + (uint32_t)((h * RP + rate) * NP + e0 + c), &d[c]);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-        for (int q = 0; q < RP; ++q)
-#pragma unroll
-          for (int e = 0; e < B; ++e) acc[q][e] *= d[q][e];
+        for (int e = 0; e < B; ++e) acc[e] *= d[e];
       }
     }
-  };
-  if (hf == 0) half(std::integral_constant<int, 0>{});
-  else half(std::integral_constant<int, 1>{});
+  }
   __syncwarp();
   if (lane == 0) mbar_arrive(&empty[slot]);
-  const int e0 = hf * B;
-  // rescale by an exact power of two per rate class; the two halves agree
-  float mx[RP];
-#pragma unroll
-  for (int q = 0; q < RP; ++q) {
+  // rescale by an exact power of two per rate class; the shares agree
+  float mx = 0.0f;
+  if constexpr (B > 0) {
     // pairwise maxima: a short dependency chain
     float t[B];
 #pragma unroll
-    for (int e = 0; e < B; ++e) t[e] = acc[q][e];
+    for (int e = 0; e < B; ++e) t[e] = acc[e];
 #pragma unroll
     for (int w = 1; w < B; w *= 2)
 #pragma unroll
       for (int e = 0; e + w < B; e += 2 * w) t[e] = fmaxf(t[e], t[e + w]);
-    mx[q] = t[0];
-    xch[hf][q][in.m] = mx[q];
+    mx = t[0];
   }
+  xch[PT][in.m] = mx;
   // the exchange barrier also makes the timeout verdict uniform over the
   // epilogue warps, so none can leave the loop alone
   {
     uint32_t all_ok;
     asm volatile(
         "{\n\t.reg .pred a, b;\n\tsetp.ne.u32 a, %1, 0;\n\t"
-        "bar.red.and.pred b, 1, 256, a;\n\tselp.u32 %0, 1, 0, b;\n\t}"
+        "bar.red.and.pred b, 1, %2, a;\n\tselp.u32 %0, 1, 0, b;\n\t}"
         : "=r"(all_ok)
-        : "r"((uint32_t)ok)
+        : "r"((uint32_t)ok), "n"(BT_EPI)
         : "memory");
     ok = all_ok != 0;
   }
-  const int so = (op.w >> 16) & 0xff;
+  float m2 = 0.0f;
 #pragma unroll
-  for (int q = 0; q < RP; ++q) {
-    const float m2 = fmaxf(mx[q], xch[hf ^ 1][q][in.m]);
-    if (m2 < 0x1p-32f && m2 > 0.0f) {
-      int ex;
-      (void)frexpf(m2, &ex);
-      escale[q] += ex;
-      const int k1 = min(-ex, 120), k2 = -ex - k1;
-      const float f1 = __int_as_float((127 + k1) << 23), f2 = __int_as_float((127 + k2) << 23);
+  for (int pp = 0; pp < BT_PARTS; ++pp)
+    if (RP == 1 || (pp >> 1) == rate) m2 = fmaxf(m2, xch[pp][in.m]);
+  if (m2 < 0x1p-32f && m2 > 0.0f) {
+    int ex;
+    (void)frexpf(m2, &ex);
+    escale += ex;
+    const int k1 = min(-ex, 120), k2 = -ex - k1;
+    const float f1 = __int_as_float((127 + k1) << 23), f2 = __int_as_float((127 + k2) << 23);
 #pragma unroll
-      for (int e = 0; e < B; ++e) acc[q][e] = acc[q][e] * f1 * f2;
-    }
-    // into the TMEM stack slot: my K columns e0 .. e0 + B - 1
-    const uint32_t col = in.tmem + in.lane_base + (uint32_t)(2 * RP * NP + (so * RP + q) * KP + e0);
+    for (int e = 0; e < BA; ++e) acc[e] = acc[e] * f1 * f2;
+  }
+  if constexpr (B > 0) {
+    // into the TMEM stack slot: columns e0 .. e0 + B - 1 of rate class rate
+    const int so = (op.w >> 16) & 0xff;
+    const uint32_t col = in.tmem + in.lane_base + (uint32_t)(2 * RP * NP + (so * RP + rate) * KP + e0);
 #pragma unroll
     for (int c0 = 0; c0 < B; c0 += 4)
       asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(col + (uint32_t)c0),
-                   "r"(tf32_bits(acc[q][c0])), "r"(tf32_bits(acc[q][c0 + 1])),
-                   "r"(tf32_bits(acc[q][c0 + 2])), "r"(tf32_bits(acc[q][c0 + 3]))
+                   "r"(tf32_bits(acc[c0])), "r"(tf32_bits(acc[c0 + 1])), "r"(tf32_bits(acc[c0 + 2])),
+                   "r"(tf32_bits(acc[c0 + 3]))
                    : "memory");
     if (in.last) {
       double l = 0.0;
 #pragma unroll
       for (int e = 0; e < B; ++e)
-        if (e0 + e < in.S) l += in.pi[e0 + e] * (double)acc[q][e];
-      Lp[q] = l;
+        if (e0 + e < in.S) l += in.pi[e0 + e] * (double)acc[e];
+      Lp = l;
     }
+  } else {
+    if (in.last) Lp = 0.0;
   }
 }
 
@@ -323,25 +333,29 @@ struct EpiShared {
   uint64_t *full, *empty, *mma_bar;
   const int4 *slot_op;       // each ring slot's postorder step, written by the producer
   unsigned char *smem;
-  float (*xch)[2][BT_M];     // per half, rate class of the pass, lane: max entry
-  double (*xchd)[2][BT_M];
+  float (*xch)[BT_M];        // per share, lane: max entry
+  double (*xchd)[BT_M];      // per share, lane: root likelihood
+  double (*lnr)[BT_M];       // per rate class, lane: log root likelihood
   double2 *red;
   uint32_t tmem;
 };
 
 // Every pass and postorder step of one work item (variant, tile) with
-// compile-time shapes: thread 0 issues each step's MMAs, then the eight
+// compile-time shapes: thread 0 issues each step's MMAs, then the sixteen
 // warps run its epilogue.
 template <int KP, int RP>
 __device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh, const BVar &vg, const int2 wk,
-                                      int tid, long long &seq, bool &ok) {
+                                         int tid, long long &seq, bool &ok) {
   constexpr int NP = (KP + 15) / 16 * 16;
   constexpr uint32_t LBO = 128, SBO = (uint32_t)(KP / 4) * 128;
   constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NP >> 3) << 17) |
                              ((uint32_t)(BT_M >> 4) << 24);
   const int warp = tid >> 5, lane = tid & 31;
-  const int q4 = warp & 3, hf = warp >> 2;
-  const int m = 32 * q4 + lane;   // pattern within the tile
+  const int lg = warp & 3, pt = warp >> 2;
+  const int m = 32 * lg + lane;   // pattern within the tile
+  const int my_rate = RP == 2 ? pt >> 1 : 0;
+  // the share that combines its rate class's root likelihood
+  const bool lead = RP == 1 ? pt == 0 : (pt & 1) == 0;
   // the variant's fields, once per item
   const int n_ops = vg.n_ops, R = vg.R;
   EpiIn in;
@@ -350,19 +364,14 @@ __device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh
   in.n_codes = vg.n_codes;
   in.S = vg.S;
   in.tmem = sh.tmem;
-  in.lane_base = (uint32_t)(32 * q4) << 16;
+  in.lane_base = (uint32_t)(32 * lg) << 16;
   in.m = m;
   const long long pat = (long long)wk.y * BT_M + m;
   in.active = pat < vg.n_pat;
   in.pi = p.pis + vg.pi_off;
-  double lnr[4];
-  double Lp[RP];
-#pragma unroll
-  for (int q = 0; q < RP; ++q) Lp[q] = 0.0;
+  double Lp = 0.0;
   for (int r0 = 0; r0 < R && ok; r0 += RP) {
-    int escale[RP];
-#pragma unroll
-    for (int q = 0; q < RP; ++q) escale[q] = 0;
+    int escale = 0;
     for (int i = 0; i < n_ops; ++i, ++seq) {
       const int slot = (int)(seq & (BT_ST - 1));
       const uint32_t par = (uint32_t)((seq / BT_ST) & 1);
@@ -421,41 +430,48 @@ __device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const int4 op = sh.slot_op[slot];
       in.last = i == n_ops - 1;
-      epi_step<KP, RP>(p, in, op, hf, lane, slot, sh.empty, sh.xch, escale, ok, Lp);
+      // pt is warp-uniform
+      switch (pt) {
+        case 0: epi_step<KP, RP, 0>(p, in, op, lane, slot, sh.empty, sh.xch, escale, ok, Lp); break;
+        case 1: epi_step<KP, RP, 1>(p, in, op, lane, slot, sh.empty, sh.xch, escale, ok, Lp); break;
+        case 2: epi_step<KP, RP, 2>(p, in, op, lane, slot, sh.empty, sh.xch, escale, ok, Lp); break;
+        default: epi_step<KP, RP, 3>(p, in, op, lane, slot, sh.empty, sh.xch, escale, ok, Lp); break;
+      }
       asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       // every vector of this step is in TMEM before the next MMA issues
-      asm volatile("bar.sync 1, 256;" ::: "memory");
+      asm volatile("bar.sync 1, %0;" ::"n"(BT_EPI) : "memory");
       if (!ok) break;
     }
     if (!ok) break;
-    // roots of this pass's rate classes (both halves of the row)
+    // roots of this pass's rate classes: the shares of each meet
+    sh.xchd[pt][m] = Lp;
+    asm volatile("bar.sync 1, %0;" ::"n"(BT_EPI) : "memory");
+    if (lead) {
+      double L = 0.0;
 #pragma unroll
-    for (int q = 0; q < RP; ++q) sh.xchd[hf][q][m] = Lp[q];
-    asm volatile("bar.sync 1, 256;" ::: "memory");
-#pragma unroll
-    for (int q = 0; q < RP; ++q) {
-      const double L = Lp[q] + sh.xchd[hf ^ 1][q][m];
-      lnr[r0 + q] = log(L) + (double)escale[q] * 0.69314718055994530942;
+      for (int pp = 0; pp < BT_PARTS; ++pp)
+        if (RP == 1 || (pp >> 1) == my_rate) L += sh.xchd[pp][m];
+      sh.lnr[r0 + my_rate][m] = log(L) + (double)escale * 0.69314718055994530942;
     }
-    asm volatile("bar.sync 1, 256;" ::: "memory");
+    asm volatile("bar.sync 1, %0;" ::"n"(BT_EPI) : "memory");
   }
   // join the rate classes: log sum_r probs[r] exp(lnr[r])
   double s = 0.0, comp = 0.0;
-  if (ok && in.active && hf == 0) {
+  if (ok && in.active && pt == 0) {
     double mxl = -INFINITY;
-    for (int r = 0; r < R; ++r) mxl = fmax(mxl, lnr[r]);
+    for (int r = 0; r < R; ++r) mxl = fmax(mxl, sh.lnr[r][m]);
     double sum = 0.0;
-    for (int r = 0; r < R; ++r) sum += vg.probs[r] * exp(lnr[r] - mxl);
+    for (int r = 0; r < R; ++r) sum += vg.probs[r] * exp(sh.lnr[r][m] - mxl);
     const double lnl = mxl + log(sum);
     if (p.site_lnl) p.site_lnl[vg.pat_off + pat] = lnl;
     s = vg.weights ? vg.weights[pat] * lnl : lnl;
   }
-  if (hf == 0) {
+  if (pt == 0) {
     warp_csum_d(s, comp);
-    if (lane == 0) sh.red[q4] = make_double2(s, comp);
+    if (lane == 0) sh.red[lg] = make_double2(s, comp);
   }
-  asm volatile("bar.sync 1, 256;" ::: "memory");
+  asm volatile("bar.sync 1, %0;" ::"n"(BT_EPI) : "memory");
   if (tid == 0) {
     double ss = 0.0, cc = 0.0;
     for (int k = 0; k < 4; ++k) {
@@ -467,7 +483,7 @@ __device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh
     // by (variant, tile), whatever order the work list runs in
     p.partials[vg.tile0 + wk.y] = make_double2(ss, cc);
   }
-  asm volatile("bar.sync 1, 256;" ::: "memory");
+  asm volatile("bar.sync 1, %0;" ::"n"(BT_EPI) : "memory");
 }
 
 template <int KP>
@@ -487,12 +503,13 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
   __shared__ uint64_t full[BT_ST], empty[BT_ST], mma_bar;
   __shared__ int4 slot_op[BT_ST];
   __shared__ uint32_t tmem_base;
-  __shared__ float xch[2][2][BT_M];    // per half, rate class of the pass, lane: max entry
-  __shared__ double xchd[2][2][BT_M];
+  __shared__ float xch[BT_PARTS][BT_M];     // per share, lane: max entry
+  __shared__ double xchd[BT_PARTS][BT_M];   // per share, lane: root likelihood
+  __shared__ double lnr[4][BT_M];           // per rate class, lane: log root likelihood
   __shared__ double2 red[4];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-  if (warp == 8) {
+  if (warp == BT_EPI_WARPS) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      su32(&tmem_base)),
                  "r"(BT_TMEM_COLS));
@@ -501,7 +518,7 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
   if (tid == 0) {
     for (int s = 0; s < BT_ST; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1 + 8);   // the MMA commit + 8 epilogue warps
+      mbar_init(&empty[s], 1 + BT_EPI_WARPS);   // the MMA commit + the epilogue warps
     }
     mbar_init(&mma_bar, 1);
     fence_mbarrier_init();
@@ -511,7 +528,7 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
 
-  if (warp == 8) {
+  if (warp == BT_EPI_WARPS) {
     // ------------------------------------------------------------ producer
     if (lane == 0) {
       long long seq = 0;
@@ -566,10 +583,10 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
     }
   } else {
     // ------------------------------------------------------------ epilogue
-    // warp w: TMEM lanes 32 (w % 4) ..; states [hf B, hf B + B) of the row,
-    // B = Kp / 2.  Thread 0 also issues every step's MMAs, right after the
-    // previous step's vectors are in TMEM.
-    const EpiShared sh{full, empty, &mma_bar, slot_op, smem, xch, xchd, red, tmem};
+    // warp w: TMEM lanes 32 (w % 4) .. 32 (w % 4) + 31, share w / 4 of the
+    // row.  Thread 0 also issues every step's MMAs, right after the previous
+    // step's vectors are in TMEM.
+    const EpiShared sh{full, empty, &mma_bar, slot_op, smem, xch, xchd, lnr, red, tmem};
     long long seq = 0;
     bool ok = true;
     for (long long w = blockIdx.x; w < p.n_work && ok; w += gridDim.x) {
@@ -593,7 +610,7 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (warp == 8)
+  if (warp == BT_EPI_WARPS)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BT_TMEM_COLS));
 }
 
