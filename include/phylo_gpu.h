@@ -370,6 +370,11 @@ pgpu_status pgpu_spr_set_tree(pgpu_spr *spr, const pgpu_tree *tree);
 pgpu_status pgpu_spr_get_tree(pgpu_spr *spr, int32_t *left, int32_t *right, double *brlen);
 /* lnL of the current tree (host scalar) and optionally every pattern's. */
 pgpu_status pgpu_spr_lnl(pgpu_spr *spr, double *lnl, double *site_lnl);
+/* Limits the neighbourhood to regraft edges at most join_distance nodes from
+ * the break (0, the default: every SPR move; 1: the NNI moves, each NNI tree
+ * four times).  It mirrors TreeNeighborhoods.generate_spr ?join_distance and
+ * generate_nni (lib/treeNeighborhoods.ml:71-75) and holds until changed. */
+pgpu_status pgpu_spr_set_join_distance(pgpu_spr *spr, int join_distance);
 pgpu_status pgpu_spr_n_moves(pgpu_spr *spr, size_t *n_moves);
 /* Node ids of every move, in the numbering of pgpu_spr_get_tree. */
 pgpu_status pgpu_spr_moves(pgpu_spr *spr, int32_t *p, int32_t *u, int32_t *c, int32_t *y, size_t cap);

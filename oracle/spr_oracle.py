@@ -53,9 +53,12 @@ def side(adj: dict, x: int, y: int) -> set:
     return seen
 
 
-def moves(adj: dict, n: int):
+def moves(adj: dict, n: int, join_distance: int = 0):
     """Every move (p, u, c, y): u internal, (c, y) an edge on u's side not
-    touching u, y the end nearer to u."""
+    touching u, y the end nearer to u; with join_distance d > 0 only those
+    whose y is at most d edges from u (TreeNeighborhoods.generate_spr
+    ?join_distance, lib/treeNeighborhoods.ml:71-72; d = 1 is generate_nni,
+    :74-75)."""
     out = []
     for u in sorted(adj):
         if u < n:
@@ -75,7 +78,8 @@ def moves(adj: dict, n: int):
                 for b in sorted(adj[a]):
                     if b in keep and a < b:
                         y, c = (a, b) if dist[a] < dist[b] else (b, a)
-                        out.append((p, u, c, y))
+                        if join_distance <= 0 or dist[y] <= join_distance:
+                            out.append((p, u, c, y))
     return out
 
 

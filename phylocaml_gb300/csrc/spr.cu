@@ -938,6 +938,7 @@ struct pgpu_spr {
   SprPlan all, sel;
   SprPlanDev all_d, sel_d;
   bool pool_valid = false, plan_valid = false, fitch_valid = false, summ_valid = false;
+  int join_distance = 0;   // 0: every SPR move; d: regraft edges at most d nodes from the break
   std::vector<void *> owned;
 };
 
@@ -1092,7 +1093,7 @@ pgpu_status upload_plan(pgpu_spr *s, const SprPlan &p, SprPlanDev *d) {
 pgpu_status ensure_plan(pgpu_spr *s) {
   if (s->plan_valid) return PGPU_OK;
   PGPU_TRY(ensure_pool(s));
-  spr_plan_all(s->T, s->pp, &s->all);
+  spr_plan_all(s->T, s->pp, &s->all, s->join_distance);
   PGPU_TRY(upload_plan(s, s->all, &s->all_d));
   s->plan_valid = true;
   return PGPU_OK;
@@ -1569,6 +1570,17 @@ pgpu_status pgpu_spr_features(pgpu_spr *s, float *X_dev) {
   spr_feature_kernel<<<(unsigned)((nm + 255) / 256), 256, 0, s->ctx->stream>>>(f);
   PGPU_TRY(pgpu_after_launch(s->ctx, "spr_feature_kernel"));
   return sync_check(s, "spr_features");
+}
+
+pgpu_status pgpu_spr_set_join_distance(pgpu_spr *s, int join_distance) {
+  if (!s) return PGPU_ERR_ARG;
+  if (join_distance < 0)
+    return pgpu_set_err(s->ctx, PGPU_ERR_ARG, "spr: join distance %d < 0", join_distance);
+  if (join_distance != s->join_distance) {
+    s->join_distance = join_distance;
+    s->plan_valid = false;
+  }
+  return PGPU_OK;
 }
 
 pgpu_status pgpu_spr_apply(pgpu_spr *s, int64_t move_idx) {

@@ -71,7 +71,7 @@ struct SprPrune {
 struct SprMove {
   int32_t prune;     // index into the prune list
   int32_t dc;        // directed edge c->y: regraft onto edge dc >> 1
-  int32_t depth;     // nodes between the merged edge and y
+  int32_t depth;     // y's distance from the merged edge in nodes (1 for s and g)
   int32_t pad;
 };
 
@@ -91,9 +91,10 @@ pgpu_status spr_from_rooted(pgpu_ctx *ctx, const pgpu_tree *t, SprTopo *out);
 void spr_to_rooted(const SprTopo &T, int32_t *left, int32_t *right, double *brlen,
                    int32_t *ids = nullptr);
 void spr_pool_plan(const SprTopo &T, PoolPlan *out);
-// every SPR move of T (selected == nullptr), or only the listed ones
-// (pairs of prune directed edge, regraft directed edge c->y)
-void spr_plan_all(const SprTopo &T, const PoolPlan &pp, SprPlan *out);
+// every SPR move of T whose regraft edge lies at most join_distance nodes
+// from the merged edge (0: no limit; 1: the NNI moves), or only the listed
+// ones (pairs of prune directed edge, regraft directed edge c->y)
+void spr_plan_all(const SprTopo &T, const PoolPlan &pp, SprPlan *out, int join_distance = 0);
 pgpu_status spr_plan_selected(pgpu_ctx *ctx, const SprTopo &T, const PoolPlan &pp,
                               const int32_t *dp, const int32_t *dc, int k, SprPlan *out);
 // apply the move: prune p's side of (p,u), regraft onto the edge of dc

@@ -8,6 +8,7 @@
 // Tree.join (lib/tree.ml:299-494) with the branch-length rule that the
 // reference leaves to its callers.
 #include <algorithm>
+#include <climits>
 #include <cstring>
 
 #include "spr.cuh"
@@ -174,7 +175,7 @@ struct Pending {
 // walk continues into the node across edge e.
 template <typename Want, typename Down>
 void emit_prune(const SprTopo &T, const PoolPlan &pp, int prune_idx, int dp, SprPlan *plan,
-                Want want, Down down) {
+                Want want, Down down, int max_depth = INT_MAX) {
   const int u = T.ddst(dp), e_pu = dp >> 1;
   int es = -1, eg = -1;
   other_two(T, u, e_pu, &es, &eg);
@@ -185,7 +186,9 @@ void emit_prune(const SprTopo &T, const PoolPlan &pp, int prune_idx, int dp, Spr
   pr.move_off = (int)plan->moves.size();
   pr.ds = T.dedge(s, es);
   pr.dg = T.dedge(g, eg);
-  const bool down_s = s >= T.n && down(s, es), down_g = g >= T.n && down(g, eg);
+  // s and g are at depth 1: their other two edges are the NNI regrafts
+  const bool down_s = s >= T.n && max_depth >= 1 && down(s, es);
+  const bool down_g = g >= T.n && max_depth >= 1 && down(g, eg);
   if (!down_s && !down_g) return;   // no regraft edge wanted beyond s or g
   SprStep st{};
   st.d1 = pr.ds;
@@ -234,8 +237,9 @@ void emit_prune(const SprTopo &T, const PoolPlan &pp, int prune_idx, int dp, Spr
         plan->moves.push_back(SprMove{prune_idx, d, cur.depth, 0});
       }
     }
-    const bool d1 = c[0] >= T.n && down(c[0], e[0]);
-    const bool d2 = c[1] >= T.n && down(c[1], e[1]);
+    const bool deeper = cur.depth + 1 <= max_depth;
+    const bool d1 = deeper && c[0] >= T.n && down(c[0], e[0]);
+    const bool d2 = deeper && c[1] >= T.n && down(c[1], e[1]);
     v.flags = (d1 ? SPR_DOWN1 : 0) | (d2 ? SPR_DOWN2 : 0);
     const Pending p1{c[0], e[0], cur.depth + 1}, p2{c[1], e[1], cur.depth + 1};
     if (d1 && d2) {
@@ -276,12 +280,14 @@ void plan_reset(SprPlan *out) {
 
 }  // namespace
 
-void spr_plan_all(const SprTopo &T, const PoolPlan &pp, SprPlan *out) {
+void spr_plan_all(const SprTopo &T, const PoolPlan &pp, SprPlan *out, int join_distance) {
   plan_reset(out);
+  const int max_depth = join_distance > 0 ? join_distance : INT_MAX;
   for (int dp = 0; dp < T.n_dedges(); ++dp) {
     if (T.ddst(dp) < T.n) continue;   // u must be internal
     const int idx = (int)out->prunes.size();
-    emit_prune(T, pp, idx, dp, out, [](int, int) { return true; }, [](int, int) { return true; });
+    emit_prune(T, pp, idx, dp, out, [](int, int) { return true; }, [](int, int) { return true; },
+               max_depth);
   }
 }
 

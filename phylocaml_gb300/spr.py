@@ -5,7 +5,10 @@ and leaves the neighbourhood enumerators as TODOs
 (lib/treeNeighborhoods.ml:27-75).  ``SprEngine`` holds one tree over fixed
 DNA data and scores every subtree-prune-and-regraft neighbour in one pass:
 its log-likelihood (``scan``), its Fitch length (``fitch``) and 64 move
-features for a learned ranking (``features``).  A move (p, u, c, y) cuts
+features for a learned ranking (``features``).  ``join_distance`` limits the
+neighbourhood as TreeNeighborhoods.generate_spr ?join_distance does
+(lib/treeNeighborhoods.ml:71-75); 1 gives the NNI neighbourhood
+(generate_nni).  A move (p, u, c, y) cuts
 edge (p,u), carries p's side away, joins u's other two neighbours into one
 edge (lengths added) and puts u in the middle of edge (c,y); the pruned
 branch keeps its length.
@@ -72,7 +75,8 @@ class SprEngine:
     """One tree, its SPR neighbourhood and its branch lengths, on one GPU."""
 
     def __init__(self, tip_codes_dev, n_pat: int, model: Model, code_table: np.ndarray,
-                 weights_dev=None, precision: int = 48, ctx: _native.Context | None = None):
+                 weights_dev=None, precision: int = 48, ctx: _native.Context | None = None,
+                 join_distance: int = 0):
         import torch
         self.ctx = ctx or _native.default_context()
         self.lib = self.ctx.lib
@@ -93,6 +97,7 @@ class SprEngine:
                                       self.n_pat, precision, C.byref(h))
         self._check(st, "pgpu_spr_create")
         self.h = h
+        self.set_join_distance(join_distance)
 
     def _check(self, st: int, what: str) -> None:
         self.ctx.check(st, what)
@@ -139,6 +144,12 @@ class SprEngine:
         return ln, ea, eb
 
     # -- moves ----------------------------------------------------------------
+    def set_join_distance(self, d: int) -> None:
+        """Regraft edges at most d nodes from the break (0: every SPR move;
+        1: the NNI moves)."""
+        self._check(self.lib.pgpu_spr_set_join_distance(self.h, int(d)), "pgpu_spr_set_join_distance")
+        self.join_distance = int(d)
+
     @property
     def n_moves(self) -> int:
         n = _native._SZ(0)

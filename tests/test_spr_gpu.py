@@ -174,3 +174,45 @@ def test_features_do_not_depend_on_numbering(small, ctx):
     assert worst < 1e-4, worst
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("d", [1, 2])
+def test_join_distance_neighbourhoods(small, ctx, d):
+    """TreeNeighborhoods.generate_nni / generate_spr ?join_distance
+    (lib/treeNeighborhoods.ml:71-75): the engine lists exactly the oracle's
+    moves within the distance, scores them as the full scan does, and
+    applies them."""
+    dd = small
+    n = dd["tr"].n_tips
+    e = engine(dd, ctx, 48)
+    cur = e.get_tree()
+    adj = SO.unroot(cur.left, cur.right, cur.brlen)
+    full_mv = e.moves()
+    full = e.scan().cpu().numpy()
+    full_f, tl = e.fitch()
+    full_f = full_f.cpu().numpy()
+    keys_full = list(zip(full_mv.p, full_mv.u, full_mv.c, full_mv.y))
+    by_move = dict(zip(keys_full, full))
+    fitch_by_move = dict(zip(keys_full, full_f))
+    e.set_join_distance(d)
+    mv = e.moves()
+    keys = list(zip(mv.p, mv.u, mv.c, mv.y))
+    assert sorted(keys) == sorted(SO.moves(adj, n, join_distance=d))
+    if d == 1:
+        assert len(keys) == 8 * (n - 3)
+    got = e.scan().cpu().numpy()
+    np.testing.assert_allclose(got, [by_move[k] for k in keys], rtol=1e-12)
+    f, tl2 = e.fitch()
+    assert tl2 == tl and np.array_equal(f.cpu().numpy(), [fitch_by_move[k] for k in keys])
+    np.testing.assert_allclose(e.score(np.arange(len(keys))), got, rtol=1e-12)
+    best = int(np.argmax(got))
+    e.apply(best)
+    after = e.get_tree()
+    exp = SO.apply_move(adj, *keys[best])
+    assert SO.splits(SO.unroot(after.left, after.right, after.brlen), n) == SO.splits(exp, n)
+    assert abs(e.lnl() - got[best]) <= 1e-9 * abs(got[best])
+    # the limit holds across moves until it is changed
+    assert e.n_moves == len(SO.moves(SO.unroot(after.left, after.right, after.brlen), n, join_distance=d))
+    e.set_join_distance(0)
+    assert e.n_moves == len(SO.moves(SO.unroot(after.left, after.right, after.brlen), n))
+    e.close()

@@ -54,3 +54,20 @@ def test_parsimony_start(seed):
     assert length < SO.fitch_length(adj_r, n, pats, masks, w)
     again, length2 = spr.parsimony_start(pats, table, w, seed=seed, brlen=0.05)
     assert length2 == length and (again.left == start.left).all()
+
+
+@pytest.mark.parametrize("n", [4, 6, 11])
+def test_oracle_nni_neighbourhood(n):
+    """Join distance 1 is the NNI neighbourhood: 2(n-3) distinct trees, each
+    reached by 8(n-3) / 2(n-3) = 4 moves; a larger distance nests."""
+    tr = T.yule(n, np.random.default_rng(40 + n), 0.1)
+    adj = SO.unroot(tr.left, tr.right, tr.brlen)
+    base = SO.splits(adj, n)
+    nni = SO.moves(adj, n, join_distance=1)
+    assert len(nni) == 8 * (n - 3)
+    tops = {SO.splits(SO.apply_move(adj, *m), n) for m in nni}
+    assert base not in tops and len(tops) == 2 * (n - 3)
+    # every NNI tree differs from the tree by exactly one split
+    assert all(len(t - base) == 1 for t in tops)
+    two = set(SO.moves(adj, n, join_distance=2))
+    assert set(nni) <= two <= set(SO.moves(adj, n))
