@@ -391,6 +391,29 @@ pgpu_status pgpu_spr_fitch(pgpu_spr *spr, uint64_t *len_dev, uint64_t *tree_len)
  * change, and pattern-averaged state profiles of the sides involved. */
 pgpu_status pgpu_spr_features(pgpu_spr *spr, float *X_dev);
 pgpu_status pgpu_spr_apply(pgpu_spr *spr, int64_t move_idx);
+
+/* TBR (tree bisection and reconnection), the moves that reroot both sides:
+ * cut an edge (a,b) whose ends are both internal, dissolve a and b (each
+ * one's two other edges become one, lengths added), put a in the middle of
+ * an edge (jc,jy) of its side and b in the middle of an edge (kc,ky) of its
+ * side, and keep the cut edge's length between them.  Rerooting one side
+ * only gives the SPR moves above, so the two lists together are the TBR
+ * neighbourhood.  The reference's TreeNeighborhoods.generate_tbr
+ * ?join_distance ?reroot_distance is a TODO (lib/treeNeighborhoods.ml:27-69);
+ * `distance` limits both attach edges to that many nodes from the cut (0:
+ * no limit).  Moves are listed per cut edge, a's attach edge major. */
+pgpu_status pgpu_spr_set_tbr_distance(pgpu_spr *spr, int distance);
+/* Device bytes for the attach vectors of one batch of cut edges (0: 2 GB);
+ * a scan runs as many batches as it needs, at least one cut each. */
+pgpu_status pgpu_spr_set_tbr_budget(pgpu_spr *spr, size_t bytes);
+pgpu_status pgpu_spr_tbr_n_moves(pgpu_spr *spr, size_t *n_moves);
+/* Node ids of every TBR move (arrays [n_moves]), numbered as by
+ * pgpu_spr_get_tree. */
+pgpu_status pgpu_spr_tbr_moves(pgpu_spr *spr, int32_t *a, int32_t *b, int32_t *jc, int32_t *jy,
+                               int32_t *kc, int32_t *ky, size_t cap);
+/* lnL of the tree after each TBR move into DEVICE lnl_dev[n_moves]. */
+pgpu_status pgpu_spr_tbr_scan(pgpu_spr *spr, double *lnl_dev);
+pgpu_status pgpu_spr_tbr_apply(pgpu_spr *spr, int64_t move_idx);
 /* Newton steps on all branch lengths at once, up to `passes` rounds or until
  * a round gains less than tol; lnl (or NULL) receives the final lnL. */
 pgpu_status pgpu_spr_optimize(pgpu_spr *spr, int passes, double tol, double *lnl);

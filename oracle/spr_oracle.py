@@ -98,6 +98,35 @@ def apply_move(adj: dict, p: int, u: int, c: int, y: int) -> dict:
     return new
 
 
+def tbr_moves(adj: dict, n: int, distance: int = 0):
+    """Every TBR move (a, b, jc, jy, kc, ky) that reroots both sides of an
+    internal edge (a, b): a goes into the middle of edge (jc, jy) of its own
+    side, b into the middle of (kc, ky) of its side, the cut edge keeps its
+    length.  The attach edges are the SPR regraft edges of the prunes that
+    carry the other side away (not touching the cut node; jy, ky the ends
+    nearer to it), at most `distance` edges from the cut when distance > 0.
+    The reference's TBR enumerator is a TODO (lib/treeNeighborhoods.ml:27-69);
+    Tree.break / Tree.join (lib/tree.ml:299-494) are its primitives."""
+    by_prune: dict = {}
+    for p, u, c, y in moves(adj, n, distance):
+        by_prune.setdefault((p, u), []).append((c, y))
+    out = []
+    for a in sorted(adj):
+        for b in sorted(adj[a]):
+            if a < n or b < n or a > b:
+                continue
+            for jc, jy in by_prune.get((b, a), []):
+                for kc, ky in by_prune.get((a, b), []):
+                    out.append((a, b, jc, jy, kc, ky))
+    return out
+
+
+def apply_tbr(adj: dict, a: int, b: int, jc: int, jy: int, kc: int, ky: int) -> dict:
+    """Dissolve a and put it on (jc, jy), then dissolve b and put it on
+    (kc, ky); each half is an SPR move that keeps the cut edge."""
+    return apply_move(apply_move(adj, b, a, jc, jy), a, b, kc, ky)
+
+
 def reroot(adj: dict, n: int):
     """Adjacency -> rooted postorder arrays (root on tip 0's edge, all of the
     edge on the far side)."""

@@ -125,6 +125,12 @@ SIGNATURES: dict[str, tuple] = {
     "pgpu_spr_get_tree": (_I, [_P, _P, _P, _P]),
     "pgpu_spr_lnl": (_I, [_P, _DP, _P]),
     "pgpu_spr_set_join_distance": (_I, [_P, _I]),
+    "pgpu_spr_set_tbr_distance": (_I, [_P, _I]),
+    "pgpu_spr_set_tbr_budget": (_I, [_P, _SZ]),
+    "pgpu_spr_tbr_n_moves": (_I, [_P, C.POINTER(_SZ)]),
+    "pgpu_spr_tbr_moves": (_I, [_P, _P, _P, _P, _P, _P, _P, _SZ]),
+    "pgpu_spr_tbr_scan": (_I, [_P, _P]),
+    "pgpu_spr_tbr_apply": (_I, [_P, C.c_int64]),
     "pgpu_spr_n_moves": (_I, [_P, C.POINTER(_SZ)]),
     "pgpu_spr_moves": (_I, [_P, _P, _P, _P, _P, _SZ]),
     "pgpu_spr_scan": (_I, [_P, _P]),

@@ -210,6 +210,11 @@ struct ScanArgs {
   int *flag;
   size_t np, n_moves;
   int R, NP, G, n_blocks, depth, max_moves;
+  // emit mode (TBR): the attach vector of every wanted edge instead of a score
+  void *xout;                 // [slot][np][R] x 4
+  int32_t *xsc;               // [slot][np]
+  long long slot_base;        // move index of slot 0
+  int prune_base;             // first prune of the launch
 };
 
 template <typename Pol>
@@ -218,13 +223,16 @@ __host__ __device__ size_t scan_smem(int depth, int max_moves) {
          (size_t)depth * 4 * SPR_NT * sizeof(typename Pol::V) + (size_t)depth * SPR_NT * sizeof(int);
 }
 
-template <typename Pol, int RT>
+// EMIT: instead of scoring a regraft, store the walked side's vector at the
+// middle of the edge, [P(t_yc/2) L'[y|c]] (.) H[c->y], with its scaler: the
+// side rerooted there, for TBR.
+template <typename Pol, int RT, bool EMIT = false>
 __global__ void __launch_bounds__(SPR_NT) spr_scan_kernel(const ScanArgs a) {
   using V = typename Pol::V;
   using Coef = typename Pol::Coef;
   constexpr int NT = SPR_NT;
   extern __shared__ __align__(16) unsigned char smem[];
-  const SprPrune pr = a.prunes[blockIdx.x];
+  const SprPrune pr = a.prunes[a.prune_base + blockIdx.x];
   float4 *ltab = reinterpret_cast<float4 *>(smem);
   ff *red = reinterpret_cast<ff *>(smem + 1024);
   V *stk = reinterpret_cast<V *>(smem + 1024 + a16((size_t)SPR_NW * a.max_moves * sizeof(ff)));
@@ -242,7 +250,7 @@ __global__ void __launch_bounds__(SPR_NT) spr_scan_kernel(const ScanArgs a) {
   const bool mine1 = r == 0, mine2 = RT == 1 ? true : r == 1;
   const int lane2 = RT == 1 ? 0 : 1;
   const Coef *Dh = static_cast<const Coef *>(a.Dhalf);
-  const Coef *Dm = static_cast<const Coef *>(a.Dmer) + ((size_t)blockIdx.x * R + (on ? r : 0)) * 16;
+  const Coef *Dm = static_cast<const Coef *>(a.Dmer) + ((size_t)(a.prune_base + blockIdx.x) * R + (on ? r : 0)) * 16;
   bool ok = true;
 
   for (int g = 0; g < a.G && ok; ++g) {
@@ -253,8 +261,8 @@ __global__ void __launch_bounds__(SPR_NT) spr_scan_kernel(const ScanArgs a) {
     auto scv = [&](int d) { return a.sc[(size_t)d * a.np + pat]; };
     const float w = a.wts[pat];
     V vp[4];
-    const int scp = scv(pr.dp);
-    if (on) {
+    const int scp = EMIT ? 0 : scv(pr.dp);
+    if (on && !EMIT) {
       Pol::load_tip(a.M, vi(pr.dp), vp);
 #pragma unroll
       for (int e = 0; e < 4; ++e) vp[e] = Pol::mul(vp[e], piv[e]);
@@ -334,7 +342,22 @@ __global__ void __launch_bounds__(SPR_NT) spr_scan_kernel(const ScanArgs a) {
       V h1[4], h2[4];
       Pol::rows(D1, l1, h1);
       Pol::rows(D2, l2, h2);
-      if (st.out1 >= 0 || st.out2 >= 0) {
+      if (EMIT && (st.out1 >= 0 || st.out2 >= 0)) {
+        if (on) {
+          V hh[4], x[4];
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int out = h == 0 ? st.out1 : st.out2;
+            if (out < 0) continue;
+            Pol::load_tip(a.H, vi(h == 0 ? st.d1 : st.d2), hh);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) x[e] = Pol::mul(h == 0 ? h1[e] : h2[e], hh[e]);
+            const size_t slot = (size_t)(out - a.slot_base);
+            Pol::store4(a.xout, (slot * a.np + pat) * R + r, x);
+            if (r == 0) a.xsc[slot * a.np + pat] = h == 0 ? sc1 + s1 : sc2 + s2;
+          }
+        }
+      } else if (st.out1 >= 0 || st.out2 >= 0) {
         V p1 = Pol::zero(), p2 = Pol::zero();
         if (on) {
           V hh[4];
@@ -399,6 +422,7 @@ __global__ void __launch_bounds__(SPR_NT) spr_scan_kernel(const ScanArgs a) {
     }
   }
   if (!ok && c == 0) atomicOr(a.flag, PGPU_FLAG_EIGEN);   // program and stack disagree
+  if (EMIT) return;
   __syncthreads();
   for (int j = c; j < pr.n_moves; j += NT) {
     ff s = red[j];
@@ -419,6 +443,121 @@ __global__ void spr_reduce_kernel(const double *partials, int n_groups, size_t n
     c += e;
   }
   lnl[m] = s + c;
+}
+
+// ---------------------------------------------------------------------------
+// TBR pairs.  For a cut edge e with attach vectors X_j (a's side rerooted at
+// edge j) and Y_k (b's side rerooted at edge k), both from the emit walks,
+//   site(j, k) = sum_r probs_r sum_i pi_i X_j[r][i] [P(t_e) Y_k][r][i]
+// with the two scalers added.  A CTA takes 16 x 16 (j, k) pairs, one per
+// thread, over a group of pattern blocks; per block of TB_PB patterns the
+// weighted X_j and the P(t_e) Y_k are staged in shared memory, rows padded
+// by one element so that the 16 k rows of a warp fall in distinct banks.
+// ---------------------------------------------------------------------------
+constexpr int TB_T = 16;
+constexpr int TB_PB = 8;
+
+struct TbrCutDev {
+  int edge, nA, nB, pad;
+  long long slotA, slotB;   // first emit slot of each side
+  long long move_off;       // first move of the cut within the launch's range
+};
+
+struct PairArgs {
+  const void *X;            // [slot][np][R] x 4
+  const int32_t *xsc;       // [slot][np]
+  const int4 *tiles;        // {cut, j0, k0, 0}
+  const TbrCutDev *cuts;
+  const void *Dfull;        // [n_edges][R][16]
+  const double *pi, *probs;
+  const float *wts;         // [np], zero beyond n_pat
+  const float4 *logtab;
+  double *partials;         // [n_groups][n_moves]
+  int *flag;
+  size_t np;
+  long long n_moves;
+  int R, G, n_pblocks;
+};
+
+__host__ __device__ inline int tbr_row(int R) { return TB_PB * R * 4 + 1; }
+
+template <typename Pol>
+__host__ __device__ size_t pair_smem(int R) {
+  return 1024 + 2 * (size_t)TB_T * tbr_row(R) * sizeof(typename Pol::V) + 2 * TB_T * TB_PB * sizeof(int);
+}
+
+template <typename Pol>
+__global__ void __launch_bounds__(256) tbr_pair_kernel(const PairArgs a) {
+  using V = typename Pol::V;
+  using Coef = typename Pol::Coef;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int R = a.R, RS = tbr_row(R);
+  float4 *ltab = reinterpret_cast<float4 *>(smem);
+  V *Xs = reinterpret_cast<V *>(smem + 1024);
+  V *Zs = Xs + (size_t)TB_T * RS;
+  int *xs = reinterpret_cast<int *>(Zs + (size_t)TB_T * RS);
+  int *ys = xs + TB_T * TB_PB;
+  const int t = threadIdx.x;
+  for (int i = t; i < 64; i += 256) ltab[i] = a.logtab[i];
+  const int4 tl = a.tiles[blockIdx.x];
+  const TbrCutDev cut = a.cuts[tl.x];
+  const int jj = t / TB_T, kk = t % TB_T;
+  const int j = tl.y + jj, k = tl.z + kk;
+  const bool mine = j < cut.nA && k < cut.nB;
+  const Coef *D = static_cast<const Coef *>(a.Dfull) + (size_t)cut.edge * R * 16;
+  const int per_side = TB_T * TB_PB * R;
+  ff sum{0.0f, 0.0f};
+  for (int g = 0; g < a.G; ++g) {
+    const int blk = blockIdx.y * a.G + g;
+    if (blk >= a.n_pblocks) break;
+    const size_t pat0 = (size_t)blk * TB_PB;
+    __syncthreads();   // the previous block's tiles are consumed
+    for (int it = t; it < 2 * per_side; it += 256) {
+      const int side = it / per_side, rem = it % per_side;
+      const int row = rem / (TB_PB * R), p = (rem / R) % TB_PB, r = rem % R;
+      const int idx = (side == 0 ? tl.y : tl.z) + row;
+      const size_t pat = pat0 + p;
+      V o[4];
+      int sc = 0;
+      if (idx < (side == 0 ? cut.nA : cut.nB)) {
+        const size_t slot = (size_t)((side == 0 ? cut.slotA : cut.slotB) + idx);
+        V v[4];
+        Pol::load_tip(a.X, (slot * a.np + pat) * R + r, v);
+        sc = a.xsc[slot * a.np + pat];
+        if (side == 0) {
+#pragma unroll
+          for (int e = 0; e < 4; ++e) o[e] = Pol::mul(v[e], Pol::from_d(a.probs[r] * a.pi[e]));
+        } else {
+          Pol::rows(D + (size_t)r * 16, v, o);
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) o[e] = Pol::zero();
+      }
+      V *dst = (side == 0 ? Xs : Zs) + (size_t)row * RS + ((size_t)p * R + r) * 4;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) dst[e] = o[e];
+      if (r == 0) (side == 0 ? xs : ys)[row * TB_PB + p] = sc;
+    }
+    __syncthreads();
+    if (!mine) continue;
+    for (int p = 0; p < TB_PB; ++p) {
+      const float w = a.wts[pat0 + p];
+      if (w == 0.0f) continue;
+      const V *xr = Xs + (size_t)jj * RS + (size_t)p * R * 4;
+      const V *zr = Zs + (size_t)kk * RS + (size_t)p * R * 4;
+      V acc = Pol::zero();
+      for (int q = 0; q < R * 4; ++q) acc = Pol::add(acc, Pol::mul(xr[q], zr[q]));
+      if (Pol::positive(acc))
+        sum = ff_add(sum, ff_mul(Pol::site_log(acc, xs[jj * TB_PB + p] + ys[kk * TB_PB + p], ltab),
+                                 ff{w, 0.0f}));
+      else
+        atomicOr(a.flag, PGPU_FLAG_NAN);
+    }
+  }
+  if (mine)
+    a.partials[(size_t)blockIdx.y * a.n_moves + cut.move_off + (long long)j * cut.nB + k] =
+        (double)sum.h + (double)sum.l;
 }
 
 // ---------------------------------------------------------------------------
@@ -939,6 +1078,17 @@ struct pgpu_spr {
   SprPlanDev all_d, sel_d;
   bool pool_valid = false, plan_valid = false, fitch_valid = false, summ_valid = false;
   int join_distance = 0;   // 0: every SPR move; d: regraft edges at most d nodes from the break
+  // TBR: plan, emit walks on the device, attach vectors of a batch of cuts
+  TbrPlan tbr;
+  SprPlanDev tbr_d;
+  bool tbr_valid = false;
+  int tbr_distance = 0;    // 0: no limit; d: attach edges at most d nodes from the cut
+  size_t tbr_budget = size_t(2) << 30;   // attach-vector bytes per batch of cuts
+  char *tbr_x = nullptr;
+  int32_t *tbr_xsc = nullptr;
+  TbrCutDev *tbr_cuts = nullptr;
+  int4 *tbr_tiles = nullptr;
+  size_t tbr_x_cap = 0, tbr_xsc_cap = 0, tbr_cuts_cap = 0, tbr_tiles_cap = 0;
   std::vector<void *> owned;
 };
 
@@ -1125,6 +1275,10 @@ pgpu_status launch_scan_rt(pgpu_spr *s, const SprPlan &p, const SprPlanDev &d, i
   a.n_blocks = n_blocks;
   a.depth = std::max(p.max_depth, 1);
   a.max_moves = std::max(p.max_moves_per_prune, 1);
+  a.xout = nullptr;
+  a.xsc = nullptr;
+  a.slot_base = 0;
+  a.prune_base = 0;
   const size_t smem = scan_smem<Pol>(a.depth, a.max_moves);
   if (smem > s->ctx->smem_optin)
     return pgpu_set_err(s->ctx, PGPU_ERR_LIMIT, "spr: scan needs %zu bytes of shared memory", smem);
@@ -1164,6 +1318,160 @@ pgpu_status run_scan(pgpu_spr *s, const SprPlan &p, const SprPlanDev &d, double 
   spr_reduce_kernel<<<(unsigned)((nm + 255) / 256), 256, 0, s->ctx->stream>>>(s->partials, n_groups, nm,
                                                                               lnl_dev);
   return pgpu_after_launch(s->ctx, "spr_reduce_kernel");
+}
+
+// ---------------------------------------------------------------------------
+// TBR: per batch of cuts, the emit walks store every attach vector, then the
+// pair kernel scores every (j, k) of each cut
+// ---------------------------------------------------------------------------
+pgpu_status ensure_tbr(pgpu_spr *s) {
+  if (s->tbr_valid) return PGPU_OK;
+  PGPU_TRY(ensure_pool(s));
+  tbr_plan(s->T, s->pp, s->tbr_distance, &s->tbr);
+  PGPU_TRY(upload_plan(s, s->tbr.emit, &s->tbr_d));
+  s->tbr_valid = true;
+  return PGPU_OK;
+}
+
+template <typename Pol, int RT>
+pgpu_status launch_emit_rt(pgpu_spr *s, int prune_base, int n_prunes, long long slot_base) {
+  const SprPlan &p = s->tbr.emit;
+  ScanArgs a;
+  a.L = s->L;
+  a.M = s->M;
+  a.H = s->H;
+  a.sc = s->sc;
+  a.Dhalf = static_cast<char *>(s->Dfull) + (size_t)s->T.n_edges() * s->cbytes;
+  a.Dmer = s->tbr_d.Dmer;
+  a.steps = s->tbr_d.steps;
+  a.prunes = s->tbr_d.prunes;
+  a.pi = s->pi;
+  a.probs = s->probs;
+  a.wts = s->wf;
+  a.logtab = s->logtab;
+  a.partials = nullptr;
+  a.flag = s->ctx->d_flag;
+  a.np = s->np;
+  a.n_moves = p.moves.size();
+  a.R = s->R;
+  a.NP = s->NP;
+  a.G = 1;
+  a.n_blocks = (int)(s->np / s->NP);
+  a.depth = std::max(p.max_depth, 1);
+  a.max_moves = std::max(p.max_moves_per_prune, 1);
+  a.xout = s->tbr_x;
+  a.xsc = s->tbr_xsc;
+  a.slot_base = slot_base;
+  a.prune_base = prune_base;
+  if (a.n_blocks > 65535) return pgpu_set_err(s->ctx, PGPU_ERR_LIMIT, "tbr: too many pattern blocks");
+  const size_t smem = scan_smem<Pol>(a.depth, a.max_moves);
+  if (smem > s->ctx->smem_optin)
+    return pgpu_set_err(s->ctx, PGPU_ERR_LIMIT, "tbr: walk needs %zu bytes of shared memory", smem);
+  PGPU_CUDA(s->ctx, cudaFuncSetAttribute(spr_scan_kernel<Pol, RT, true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  spr_scan_kernel<Pol, RT, true><<<dim3((unsigned)n_prunes, (unsigned)a.n_blocks), SPR_NT, smem,
+                                   s->ctx->stream>>>(a);
+  return pgpu_after_launch(s->ctx, "spr_scan_kernel (emit)");
+}
+
+template <typename Pol>
+pgpu_status launch_tbr_batch(pgpu_spr *s, size_t c0, size_t c1, double *lnl_dev) {
+  const TbrPlan &tp = s->tbr;
+  const SprPlan &P = tp.emit;
+  const int pb0 = tp.cuts[c0].pa, n_prunes = tp.cuts[c1 - 1].pb + 1 - pb0;
+  const long long slot_base = P.prunes[pb0].move_off;
+  switch (s->RT) {
+    case 1: PGPU_TRY((launch_emit_rt<Pol, 1>(s, pb0, n_prunes, slot_base))); break;
+    case 2: PGPU_TRY((launch_emit_rt<Pol, 2>(s, pb0, n_prunes, slot_base))); break;
+    case 4: PGPU_TRY((launch_emit_rt<Pol, 4>(s, pb0, n_prunes, slot_base))); break;
+    default: PGPU_TRY((launch_emit_rt<Pol, 8>(s, pb0, n_prunes, slot_base))); break;
+  }
+  // the batch's cuts and tiles
+  const long long move0 = tp.cuts[c0].move_off;
+  const long long nm = tp.cuts[c1 - 1].move_off + (long long)tp.cuts[c1 - 1].nA * tp.cuts[c1 - 1].nB - move0;
+  std::vector<TbrCutDev> cuts;
+  std::vector<int4> tiles;
+  for (size_t c = c0; c < c1; ++c) {
+    const TbrCut &x = tp.cuts[c];
+    TbrCutDev d{};
+    d.edge = x.edge;
+    d.nA = x.nA;
+    d.nB = x.nB;
+    d.slotA = P.prunes[x.pa].move_off - slot_base;
+    d.slotB = P.prunes[x.pb].move_off - slot_base;
+    d.move_off = x.move_off - move0;
+    cuts.push_back(d);
+    for (int j0 = 0; j0 < x.nA; j0 += TB_T)
+      for (int k0 = 0; k0 < x.nB; k0 += TB_T) tiles.push_back(make_int4((int)(c - c0), j0, k0, 0));
+  }
+  PGPU_TRY(grow(s, &s->tbr_cuts, &s->tbr_cuts_cap, cuts.size()));
+  PGPU_TRY(grow(s, &s->tbr_tiles, &s->tbr_tiles_cap, tiles.size()));
+  PGPU_CUDA(s->ctx, cudaMemcpyAsync(s->tbr_cuts, cuts.data(), cuts.size() * sizeof(TbrCutDev),
+                                    cudaMemcpyHostToDevice, s->ctx->stream));
+  PGPU_CUDA(s->ctx, cudaMemcpyAsync(s->tbr_tiles, tiles.data(), tiles.size() * sizeof(int4),
+                                    cudaMemcpyHostToDevice, s->ctx->stream));
+  if (tiles.size() > 0x7fffffffu) return pgpu_set_err(s->ctx, PGPU_ERR_LIMIT, "tbr: too many tiles");
+  // pattern groups: partial sums at most 256 MB
+  const int n_pblocks = (int)(s->np / TB_PB);
+  const size_t budget = size_t(256) << 20;
+  int G = (int)std::max<size_t>(1, ((size_t)n_pblocks * (size_t)nm * 8 + budget - 1) / budget);
+  G = std::min(G, n_pblocks);
+  const int n_groups = (n_pblocks + G - 1) / G;
+  if (n_groups > 65535) return pgpu_set_err(s->ctx, PGPU_ERR_LIMIT, "tbr: too many pattern groups");
+  PGPU_TRY(grow(s, &s->partials, &s->part_cap, (size_t)n_groups * nm));
+  PairArgs a;
+  a.X = s->tbr_x;
+  a.xsc = s->tbr_xsc;
+  a.tiles = s->tbr_tiles;
+  a.cuts = s->tbr_cuts;
+  a.Dfull = s->Dfull;
+  a.pi = s->pi;
+  a.probs = s->probs;
+  a.wts = s->wf;
+  a.logtab = s->logtab;
+  a.partials = s->partials;
+  a.flag = s->ctx->d_flag;
+  a.np = s->np;
+  a.n_moves = nm;
+  a.R = s->R;
+  a.G = G;
+  a.n_pblocks = n_pblocks;
+  const size_t smem = pair_smem<Pol>(s->R);
+  if (smem > s->ctx->smem_optin)
+    return pgpu_set_err(s->ctx, PGPU_ERR_LIMIT, "tbr: pairs need %zu bytes of shared memory", smem);
+  PGPU_CUDA(s->ctx, cudaFuncSetAttribute(tbr_pair_kernel<Pol>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)std::max<size_t>(smem, 48 * 1024)));
+  tbr_pair_kernel<Pol><<<dim3((unsigned)tiles.size(), (unsigned)n_groups), 256, smem, s->ctx->stream>>>(a);
+  PGPU_TRY(pgpu_after_launch(s->ctx, "tbr_pair_kernel"));
+  spr_reduce_kernel<<<(unsigned)((nm + 255) / 256), 256, 0, s->ctx->stream>>>(s->partials, n_groups,
+                                                                              (size_t)nm, lnl_dev + move0);
+  return pgpu_after_launch(s->ctx, "spr_reduce_kernel");
+}
+
+// lnL of every TBR move into lnl_dev, in batches of cuts whose attach
+// vectors fit in the budget (at least one cut per batch)
+pgpu_status run_tbr_scan(pgpu_spr *s, double *lnl_dev) {
+  PGPU_TRY(ensure_tbr(s));
+  const TbrPlan &tp = s->tbr;
+  if (tp.n_moves == 0) return PGPU_OK;
+  const size_t slot_bytes = s->np * s->R * 4 * s->vbytes;
+  const size_t max_slots = std::max<size_t>(1, s->tbr_budget / slot_bytes);
+  for (size_t c0 = 0; c0 < tp.cuts.size();) {
+    size_t c1 = c0, slots = 0;
+    while (c1 < tp.cuts.size()) {
+      const size_t add = (size_t)tp.cuts[c1].nA + tp.cuts[c1].nB;
+      if (c1 > c0 && slots + add > max_slots) break;
+      slots += add;
+      ++c1;
+    }
+    PGPU_TRY(grow(s, &s->tbr_x, &s->tbr_x_cap, slots * slot_bytes));
+    PGPU_TRY(grow(s, &s->tbr_xsc, &s->tbr_xsc_cap, slots * s->np));
+    if (s->precision == 32) PGPU_TRY(launch_tbr_batch<Fp32>(s, c0, c1, lnl_dev));
+    else if (s->precision == 48) PGPU_TRY(launch_tbr_batch<Ff32>(s, c0, c1, lnl_dev));
+    else PGPU_TRY(launch_tbr_batch<Fp64>(s, c0, c1, lnl_dev));
+    c0 = c1;
+  }
+  return PGPU_OK;
 }
 
 pgpu_status ensure_fitch(pgpu_spr *s) {
@@ -1236,7 +1544,7 @@ pgpu_status sync_check(pgpu_spr *s, const char *what) {
 }
 
 void invalidate(pgpu_spr *s) {
-  s->pool_valid = s->plan_valid = s->fitch_valid = s->summ_valid = false;
+  s->pool_valid = s->plan_valid = s->fitch_valid = s->summ_valid = s->tbr_valid = false;
 }
 
 }  // namespace
@@ -1580,6 +1888,89 @@ pgpu_status pgpu_spr_set_join_distance(pgpu_spr *s, int join_distance) {
     s->join_distance = join_distance;
     s->plan_valid = false;
   }
+  return PGPU_OK;
+}
+
+pgpu_status pgpu_spr_set_tbr_distance(pgpu_spr *s, int distance) {
+  if (!s) return PGPU_ERR_ARG;
+  if (distance < 0) return pgpu_set_err(s->ctx, PGPU_ERR_ARG, "tbr: distance %d < 0", distance);
+  if (distance != s->tbr_distance) {
+    s->tbr_distance = distance;
+    s->tbr_valid = false;
+  }
+  return PGPU_OK;
+}
+
+pgpu_status pgpu_spr_set_tbr_budget(pgpu_spr *s, size_t bytes) {
+  if (!s) return PGPU_ERR_ARG;
+  s->tbr_budget = bytes ? bytes : size_t(2) << 30;
+  return PGPU_OK;
+}
+
+pgpu_status pgpu_spr_tbr_n_moves(pgpu_spr *s, size_t *n_moves) {
+  if (!s || !n_moves) return PGPU_ERR_ARG;
+  if (s->T.n == 0) return pgpu_set_err(s->ctx, PGPU_ERR_ARG, "spr: no tree set");
+  PGPU_CUDA(s->ctx, cudaSetDevice(s->ctx->device));
+  PGPU_TRY(ensure_tbr(s));
+  *n_moves = (size_t)s->tbr.n_moves;
+  return PGPU_OK;
+}
+
+pgpu_status pgpu_spr_tbr_moves(pgpu_spr *s, int32_t *a, int32_t *b, int32_t *jc, int32_t *jy, int32_t *kc,
+                               int32_t *ky, size_t cap) {
+  if (!s || !a || !b || !jc || !jy || !kc || !ky) return PGPU_ERR_ARG;
+  size_t nm = 0;
+  PGPU_TRY(pgpu_spr_tbr_n_moves(s, &nm));
+  if (cap < nm) return pgpu_set_err(s->ctx, PGPU_ERR_ARG, "tbr: %zu moves, room for %zu", nm, cap);
+  const int n = s->n;
+  std::vector<int32_t> l(n - 1), r(n - 1), ids(2 * n - 2);
+  std::vector<double> bl(2 * n - 2);
+  spr_to_rooted(s->T, l.data(), r.data(), bl.data(), ids.data());
+  const SprPlan &P = s->tbr.emit;
+  for (const TbrCut &c : s->tbr.cuts) {
+    const int ia = ids[s->T.ea[c.edge]], ib = ids[s->T.eb[c.edge]];
+    for (int j = 0; j < c.nA; ++j) {
+      const int dj = P.moves[P.prunes[c.pa].move_off + j].dc;
+      for (int k = 0; k < c.nB; ++k) {
+        const int dk = P.moves[P.prunes[c.pb].move_off + k].dc;
+        const size_t m = (size_t)(c.move_off + (int64_t)j * c.nB + k);
+        a[m] = ia;
+        b[m] = ib;
+        jc[m] = ids[s->T.dsrc(dj)];
+        jy[m] = ids[s->T.ddst(dj)];
+        kc[m] = ids[s->T.dsrc(dk)];
+        ky[m] = ids[s->T.ddst(dk)];
+      }
+    }
+  }
+  return PGPU_OK;
+}
+
+pgpu_status pgpu_spr_tbr_scan(pgpu_spr *s, double *lnl_dev) {
+  if (!s || !lnl_dev) return PGPU_ERR_ARG;
+  if (s->T.n == 0) return pgpu_set_err(s->ctx, PGPU_ERR_ARG, "spr: no tree set");
+  PGPU_CUDA(s->ctx, cudaSetDevice(s->ctx->device));
+  PGPU_TRY(run_tbr_scan(s, lnl_dev));
+  return sync_check(s, "pgpu_spr_tbr_scan");
+}
+
+pgpu_status pgpu_spr_tbr_apply(pgpu_spr *s, int64_t move_idx) {
+  if (!s) return PGPU_ERR_ARG;
+  size_t nm = 0;
+  PGPU_TRY(pgpu_spr_tbr_n_moves(s, &nm));
+  if (move_idx < 0 || (size_t)move_idx >= nm)
+    return pgpu_set_err(s->ctx, PGPU_ERR_ARG, "tbr: move index %lld out of range", (long long)move_idx);
+  const std::vector<TbrCut> &cuts = s->tbr.cuts;
+  size_t c = std::upper_bound(cuts.begin(), cuts.end(), (int64_t)move_idx,
+                              [](int64_t m, const TbrCut &x) { return m < x.move_off; }) -
+             cuts.begin() - 1;
+  const TbrCut &x = cuts[c];
+  const int64_t rel = move_idx - x.move_off;
+  const SprPlan &P = s->tbr.emit;
+  const int dj = P.moves[P.prunes[x.pa].move_off + (int)(rel / x.nB)].dc;
+  const int dk = P.moves[P.prunes[x.pb].move_off + (int)(rel % x.nB)].dc;
+  PGPU_TRY(tbr_apply(s->ctx, &s->T, x.edge, dj, dk));
+  invalidate(s);
   return PGPU_OK;
 }
 

@@ -84,6 +84,36 @@ struct SprPlan {
   int max_moves_per_prune = 0;
 };
 
+// TBR (tree bisection and reconnection) moves that reroot both sides.  Cut
+// an edge (a,b) whose ends are both internal; a's side with a dissolved (its
+// two other edges joined into one) is A', b's side likewise B'.  A move puts
+// a in the middle of an edge j of A' and b in the middle of an edge k of B',
+// the cut edge keeping its length between them.  j and k exclude the joined
+// edges (putting a back on its joined edge is no reroot: with one side
+// rerooted only, the move is an SPR move).  Per cut, an emit plan walks A'
+// (the SPR prune carrying b's side away) and B' (carrying a's side away);
+// its moves are the attach edges j and k, and TBR move (j, k) of the cut is
+// move_off + j * nB + k.
+struct TbrCut {
+  int32_t edge;          // the cut edge
+  int32_t pa, pb;        // emit prunes walking A' and B'
+  int32_t nA, nB;        // attach edges on each side
+  int64_t move_off;      // first TBR move of the cut
+};
+
+struct TbrPlan {
+  SprPlan emit;
+  std::vector<TbrCut> cuts;
+  int64_t n_moves = 0;
+};
+
+// every TBR move of T whose attach edges lie at most `distance` nodes from
+// the cut (0: no limit)
+void tbr_plan(const SprTopo &T, const PoolPlan &pp, int distance, TbrPlan *out);
+// apply: cut edge `edge` (a = ea, b = eb), a onto the edge of directed edge
+// dj (c->y, y nearer a), b onto that of dk
+pgpu_status tbr_apply(pgpu_ctx *ctx, SprTopo *T, int edge, int32_t dj, int32_t dk);
+
 // rooted postorder tree (pgpu_tree layout) -> unrooted topology
 pgpu_status spr_from_rooted(pgpu_ctx *ctx, const pgpu_tree *t, SprTopo *out);
 // unrooted -> rooted on the edge above tip 0 (half of its length each side);

@@ -291,6 +291,42 @@ void spr_plan_all(const SprTopo &T, const PoolPlan &pp, SprPlan *out, int join_d
   }
 }
 
+void tbr_plan(const SprTopo &T, const PoolPlan &pp, int distance, TbrPlan *out) {
+  SprPlan &P = out->emit;
+  plan_reset(&P);
+  out->cuts.clear();
+  out->n_moves = 0;
+  const int max_depth = distance > 0 ? distance : INT_MAX;
+  auto all = [](int, int) { return true; };
+  for (int e = 0; e < T.n_edges(); ++e) {
+    if (T.ea[e] < T.n || T.eb[e] < T.n) continue;   // both sides rerootable
+    const size_t s0 = P.steps.size(), m0 = P.moves.size(), l0 = P.merged_len.size();
+    const int p0 = (int)P.prunes.size();
+    // directed edge 2e+1 carries b's side away and walks a's (A'), 2e the reverse
+    emit_prune(T, pp, p0, 2 * e + 1, &P, all, all, max_depth);
+    if ((int)P.prunes.size() == p0) continue;
+    emit_prune(T, pp, p0 + 1, 2 * e, &P, all, all, max_depth);
+    if ((int)P.prunes.size() == p0 + 1) {   // no attach edge on b's side: drop a's walk too
+      P.steps.resize(s0);
+      P.moves.resize(m0);
+      P.merged_len.resize(l0);
+      P.prunes.resize(p0);
+      continue;
+    }
+    TbrCut c{e, p0, p0 + 1, P.prunes[p0].n_moves, P.prunes[p0 + 1].n_moves, out->n_moves};
+    out->n_moves += (int64_t)c.nA * c.nB;
+    out->cuts.push_back(c);
+  }
+}
+
+pgpu_status tbr_apply(pgpu_ctx *ctx, SprTopo *T, int edge, int32_t dj, int32_t dk) {
+  if (edge < 0 || edge >= T->n_edges() || T->ea[edge] < T->n || T->eb[edge] < T->n)
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "tbr: edge %d is not an internal edge", edge);
+  // a's side first: spr_apply leaves the cut edge and b's side as they are
+  PGPU_TRY(spr_apply(ctx, T, 2 * edge + 1, dj));
+  return spr_apply(ctx, T, 2 * edge, dk);
+}
+
 pgpu_status spr_plan_selected(pgpu_ctx *ctx, const SprTopo &T, const PoolPlan &pp,
                               const int32_t *dp, const int32_t *dc, int k, SprPlan *out) {
   plan_reset(out);

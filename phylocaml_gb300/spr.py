@@ -8,7 +8,9 @@ its log-likelihood (``scan``), its Fitch length (``fitch``) and 64 move
 features for a learned ranking (``features``).  ``join_distance`` limits the
 neighbourhood as TreeNeighborhoods.generate_spr ?join_distance does
 (lib/treeNeighborhoods.ml:71-75); 1 gives the NNI neighbourhood
-(generate_nni).  A move (p, u, c, y) cuts
+(generate_nni).  ``tbr_scan`` scores the TBR moves that reroot both sides
+of a cut (the rest of the TBR neighbourhood, generate_tbr, are the SPR
+moves).  A move (p, u, c, y) cuts
 edge (p,u), carries p's side away, joins u's other two neighbours into one
 edge (lengths added) and puts u in the middle of edge (c,y); the pruned
 branch keeps its length.
@@ -201,6 +203,43 @@ class SprEngine:
         self._check(self.lib.pgpu_spr_features(self.h, _native.ptr(out)), "pgpu_spr_features")
         self.ctx.before_torch()
         return out[:nm]
+
+    # -- TBR ------------------------------------------------------------------
+    def set_tbr_distance(self, d: int) -> None:
+        """Attach edges at most d nodes from the cut on both sides (0: no limit)."""
+        self._check(self.lib.pgpu_spr_set_tbr_distance(self.h, int(d)), "pgpu_spr_set_tbr_distance")
+
+    def set_tbr_budget(self, nbytes: int) -> None:
+        """Device bytes for the attach vectors of one batch of cut edges (0: 2 GB)."""
+        self._check(self.lib.pgpu_spr_set_tbr_budget(self.h, int(nbytes)), "pgpu_spr_set_tbr_budget")
+
+    @property
+    def n_tbr_moves(self) -> int:
+        n = _native._SZ(0)
+        self._check(self.lib.pgpu_spr_tbr_n_moves(self.h, C.byref(n)), "pgpu_spr_tbr_n_moves")
+        return int(n.value)
+
+    def tbr_moves(self) -> np.ndarray:
+        """[n, 6] node ids (a, b, jc, jy, kc, ky): cut edge (a, b), a onto edge
+        (jc, jy) of its side, b onto (kc, ky) of its side."""
+        nm = self.n_tbr_moves
+        arr = [np.empty(nm, np.int32) for _ in range(6)]
+        self._check(self.lib.pgpu_spr_tbr_moves(self.h, *[x.ctypes.data for x in arr], nm),
+                    "pgpu_spr_tbr_moves")
+        return np.stack(arr, axis=1) if nm else np.empty((0, 6), np.int32)
+
+    def tbr_scan(self, out=None):
+        """lnL after every TBR move (device float64 tensor)."""
+        nm = self.n_tbr_moves
+        if out is None:
+            out = self.torch.empty(max(nm, 1), dtype=self.torch.float64, device=self.device)
+        self.ctx.after_torch()
+        self._check(self.lib.pgpu_spr_tbr_scan(self.h, _native.ptr(out)), "pgpu_spr_tbr_scan")
+        self.ctx.before_torch()
+        return out[:nm]
+
+    def tbr_apply(self, i: int) -> None:
+        self._check(self.lib.pgpu_spr_tbr_apply(self.h, int(i)), "pgpu_spr_tbr_apply")
 
     def apply(self, i: int) -> None:
         self._check(self.lib.pgpu_spr_apply(self.h, int(i)), "pgpu_spr_apply")

@@ -216,3 +216,56 @@ def test_join_distance_neighbourhoods(small, ctx, d):
     e.set_join_distance(0)
     assert e.n_moves == len(SO.moves(SO.unroot(after.left, after.right, after.brlen), n))
     e.close()
+
+
+def canon(m):
+    """A TBR move with its cut edge's ends in increasing order."""
+    a, b, jc, jy, kc, ky = (int(x) for x in m)
+    return (a, b, jc, jy, kc, ky) if a < b else (b, a, kc, ky, jc, jy)
+
+
+@pytest.mark.parametrize("prec", [64, 48, 32])
+def test_tbr_moves_and_scores(small, ctx, prec):
+    """TBR moves that reroot both sides of a cut: the engine lists the
+    oracle's moves, and every score is the lnL of the rebuilt tree scored
+    from scratch by the FP64 oracle."""
+    d = small
+    n = d["tr"].n_tips
+    e = engine(d, ctx, prec)
+    cur = e.get_tree()
+    adj = SO.unroot(cur.left, cur.right, cur.brlen)
+    mv = [tuple(int(x) for x in m) for m in e.tbr_moves()]
+    assert sorted(map(canon, mv)) == sorted(SO.tbr_moves(adj, n))
+    got = e.tbr_scan().cpu().numpy()
+    exp = np.array([oracle_lnl(d, SO.apply_tbr(adj, *m)) for m in mv])
+    ok = close(got, exp, prec, float(d["w"].sum()))
+    assert ok.all(), (np.flatnonzero(~ok)[:5], np.max(np.abs(got - exp)))
+    # one cut per batch: the same scores
+    e.set_tbr_budget(1)
+    np.testing.assert_array_equal(e.tbr_scan().cpu().numpy(), got)
+    e.close()
+
+
+def test_tbr_distance_and_apply(small, ctx):
+    d = small
+    n = d["tr"].n_tips
+    e = engine(d, ctx, 48)
+    cur = e.get_tree()
+    adj = SO.unroot(cur.left, cur.right, cur.brlen)
+    full = dict(zip([tuple(int(x) for x in m) for m in e.tbr_moves()], e.tbr_scan().cpu().numpy()))
+    e.set_tbr_distance(1)
+    mv = [tuple(int(x) for x in m) for m in e.tbr_moves()]
+    assert sorted(map(canon, mv)) == sorted(SO.tbr_moves(adj, n, 1)) and 0 < len(mv) < len(full)
+    got = e.tbr_scan().cpu().numpy()
+    np.testing.assert_allclose(got, [full[m] for m in mv], rtol=1e-12)
+    best = int(np.argmax(got))
+    e.tbr_apply(best)
+    after = e.get_tree()
+    exp = SO.apply_tbr(adj, *mv[best])
+    assert SO.splits(SO.unroot(after.left, after.right, after.brlen), n) == SO.splits(exp, n)
+    assert abs(e.lnl() - got[best]) <= 1e-9 * abs(got[best])
+    # the SPR side of the engine follows the new tree
+    adj2 = SO.unroot(after.left, after.right, after.brlen)
+    smv = e.moves()
+    assert sorted(zip(smv.p, smv.u, smv.c, smv.y)) == sorted(SO.moves(adj2, n))
+    e.close()

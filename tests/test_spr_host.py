@@ -71,3 +71,67 @@ def test_oracle_nni_neighbourhood(n):
     assert all(len(t - base) == 1 for t in tops)
     two = set(SO.moves(adj, n, join_distance=2))
     assert set(nni) <= two <= set(SO.moves(adj, n))
+
+
+def _bisect_reconnect_all(adj, n):
+    """Every tree one bisection and reconnection away, built directly: cut
+    each edge, dissolve the cut node on each side (a lone tip stays as it
+    is), then join a new node on any edge of one side to a new node on any
+    edge of the other."""
+    out = set()
+    for a in adj:
+        for b in adj[a]:
+            if a > b:
+                continue
+            sides = []
+            for x, y in ((a, b), (b, a)):
+                nodes = SO.side(adj, x, y)
+                sub = {v: {w: t for w, t in adj[v].items() if w in nodes} for v in nodes}
+                if x < n:
+                    sides.append((sub, [None]))
+                    continue
+                s_, g_ = list(sub[x])
+                ts, tg = sub[x][s_], sub[x][g_]
+                del sub[x], sub[s_][x], sub[g_][x]
+                sub[s_][g_] = sub[g_][s_] = ts + tg
+                edges = [(v, w) for v in sub for w in sub[v] if v < w]
+                sides.append((sub, edges))
+            (sa, ea), (sb, eb) = sides
+            for ja in ea:
+                for kb in eb:
+                    t = {v: dict(nb) for v, nb in list(sa.items()) + list(sb.items())}
+                    ends = []
+                    for ed, node in ((ja, a), (kb, b)):
+                        if ed is None:
+                            ends.append(node)
+                            continue
+                        v, w = ed
+                        ln = t[v].pop(w)
+                        del t[w][v]
+                        t[node] = {v: ln / 2, w: ln / 2}
+                        t[v][node] = t[w][node] = ln / 2
+                        ends.append(node)
+                    t[ends[0]][ends[1]] = t[ends[1]][ends[0]] = adj[a][b]
+                    out.add(SO.splits(t, n))
+    return out
+
+
+@pytest.mark.parametrize("n", [5, 6, 8, 10])
+def test_oracle_tbr_is_spr_plus_double_reroots(n):
+    """The SPR moves and the TBR moves that reroot both sides reach exactly
+    the trees one bisection and reconnection away (built independently)."""
+    tr = T.yule(n, np.random.default_rng(60 + n), 0.1)
+    adj = SO.unroot(tr.left, tr.right, tr.brlen)
+    base = SO.splits(adj, n)
+    spr_t = {SO.splits(SO.apply_move(adj, *m), n) for m in SO.moves(adj, n)}
+    tbr_t = {SO.splits(SO.apply_tbr(adj, *m), n) for m in SO.tbr_moves(adj, n)}
+    assert base not in tbr_t
+    assert (spr_t | tbr_t) - {base} == _bisect_reconnect_all(adj, n) - {base}
+    # a distance limit nests
+    near = set(SO.tbr_moves(adj, n, 1))
+    assert near <= set(SO.tbr_moves(adj, n, 2)) <= set(SO.tbr_moves(adj, n))
+    # lengths are kept: the cut edge stays, dissolved edges add, split ones halve
+    total = sum(t for x in adj for y, t in adj[x].items() if x < y)
+    for m in SO.tbr_moves(adj, n)[:20]:
+        new = SO.apply_tbr(adj, *m)
+        assert abs(sum(t for x in new for y, t in new[x].items() if x < y) - total) < 1e-12
