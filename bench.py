@@ -956,6 +956,15 @@ def bench_spr(args, rank, world, local):
     for _ in range(reps):
         eng.scan(out)
     scan_ms = (time.perf_counter() - t) / reps * 1e3
+    # the TBR moves that reroot both sides of a cut, on the same tree
+    ntb = eng.n_tbr_moves
+    tb_out = torch.empty(max(ntb, 1), dtype=torch.float64, device=dev)
+    eng.tbr_scan(tb_out)
+    torch.cuda.synchronize(dev)
+    t = time.perf_counter()
+    eng.tbr_scan(tb_out)
+    tbr_s = time.perf_counter() - t
+    tbr_best = float(tb_out[:ntb].max().item()) if ntb else float("nan")
     arms = {}
     for arm in ("exhaustive", "learned"):
         eng.set_tree(start_opt)
@@ -994,6 +1003,11 @@ def bench_spr(args, rank, world, local):
         "same_topology": bool(same),
         "scan": {"ms_per_exhaustive_scan": scan_ms, "moves_per_s": nm / (scan_ms * 1e-3),
                  "full_tree_equivalent_updates_per_s": nm * (n - 2) * n_pat / (scan_ms * 1e-3)},
+        "tbr": {"moves_rerooting_both_sides": ntb, "seconds_per_scan": tbr_s,
+                "moves_per_s": ntb / tbr_s if tbr_s > 0 else None,
+                "move_patterns_per_s": ntb * n_pat / tbr_s if tbr_s > 0 else None,
+                "best_gain_over_start": tbr_best - l0,
+                "note": "on the branch-length-optimised start tree; the other TBR moves are the SPR moves"},
     }
     eng.close()
     ctx.close()
