@@ -966,13 +966,14 @@ def bench_spr(args, rank, world, local):
     tbr_s = time.perf_counter() - t
     tbr_best = float(tb_out[:ntb].max().item()) if ntb else float("nan")
     arms = {}
+    diag = []
     for arm in ("exhaustive", "learned"):
         eng.set_tree(start_opt)
         if arm == "exhaustive":
             r = search.exhaustive_spr(eng)
         else:
             net = mlp.MLP(seed=1, max_batch=1024, ctx=ctx)
-            r = search.learned_spr(eng, net)
+            r = search.learned_spr(eng, net, diag=diag)
             net.close()
         arms[arm] = r
     ex, le = arms["exhaustive"], arms["learned"]
@@ -998,6 +999,8 @@ def bench_spr(args, rank, world, local):
                    "n_patterns": n_pat, "n_moves": nm, "precision": "fp32x2"},
         "start": {"parsimony_length": plen, "seconds": t_start, "lnl_after_brlen": l0},
         "exhaustive": arm_rec(ex), "learned": arm_rec(le),
+        "learned_fallbacks": [{k: (round(v, 3) if isinstance(v, float) else v) for k, v in d.items()}
+                              for d in diag if d.get("fallback")],
         "dlnl_learned_minus_exhaustive": le.lnl - ex.lnl,
         "reaches_exhaustive_optimum": bool(le.lnl >= ex.lnl - 1e-3),
         "same_topology": bool(same),

@@ -211,6 +211,7 @@ struct ScanArgs {
   size_t np, n_moves;
   int R, NP, G, n_blocks, depth, max_moves;
   // emit mode (TBR): the attach vector of every wanted edge instead of a score
+  const void *Dfull;          // [n_edges][R][16]: P(t) of the cut edge (b's side)
   void *xout;                 // [slot][np][R] x 4
   int32_t *xsc;               // [slot][np]
   long long slot_base;        // move index of slot 0
@@ -225,7 +226,10 @@ __host__ __device__ size_t scan_smem(int depth, int max_moves) {
 
 // EMIT: instead of scoring a regraft, store the walked side's vector at the
 // middle of the edge, [P(t_yc/2) L'[y|c]] (.) H[c->y], with its scaler: the
-// side rerooted there, for TBR.
+// side rerooted there, for TBR.  Emit prunes come in pairs per cut edge
+// (a,b): the even one walks a's side and stores X weighted by probs_r pi_i,
+// the odd one walks b's side and stores P(t_ab) Y, carried across the cut,
+// so that a TBR site likelihood is the plain dot product of the two.
 template <typename Pol, int RT, bool EMIT = false>
 __global__ void __launch_bounds__(SPR_NT) spr_scan_kernel(const ScanArgs a) {
   using V = typename Pol::V;
@@ -344,7 +348,8 @@ __global__ void __launch_bounds__(SPR_NT) spr_scan_kernel(const ScanArgs a) {
       Pol::rows(D2, l2, h2);
       if (EMIT && (st.out1 >= 0 || st.out2 >= 0)) {
         if (on) {
-          V hh[4], x[4];
+          const bool side_b = ((a.prune_base + blockIdx.x) & 1) != 0;
+          V hh[4], x[4], y[4];
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
             const int out = h == 0 ? st.out1 : st.out2;
@@ -352,8 +357,14 @@ __global__ void __launch_bounds__(SPR_NT) spr_scan_kernel(const ScanArgs a) {
             Pol::load_tip(a.H, vi(h == 0 ? st.d1 : st.d2), hh);
 #pragma unroll
             for (int e = 0; e < 4; ++e) x[e] = Pol::mul(h == 0 ? h1[e] : h2[e], hh[e]);
+            if (side_b) {
+              Pol::rows(static_cast<const Coef *>(a.Dfull) + ((size_t)(pr.dp >> 1) * R + r) * 16, x, y);
+            } else {
+#pragma unroll
+              for (int e = 0; e < 4; ++e) y[e] = Pol::mul(x[e], Pol::from_d(a.probs[r] * a.pi[e]));
+            }
             const size_t slot = (size_t)(out - a.slot_base);
-            Pol::store4(a.xout, (slot * a.np + pat) * R + r, x);
+            Pol::store4(a.xout, (slot * a.np + pat) * R + r, y);
             if (r == 0) a.xsc[slot * a.np + pat] = h == 0 ? sc1 + s1 : sc2 + s2;
           }
         }
@@ -446,16 +457,17 @@ __global__ void spr_reduce_kernel(const double *partials, int n_groups, size_t n
 }
 
 // ---------------------------------------------------------------------------
-// TBR pairs.  For a cut edge e with attach vectors X_j (a's side rerooted at
-// edge j) and Y_k (b's side rerooted at edge k), both from the emit walks,
-//   site(j, k) = sum_r probs_r sum_i pi_i X_j[r][i] [P(t_e) Y_k][r][i]
+// TBR pairs.  For a cut edge (a,b) with the attach vectors of both sides
+// from the emit walks (a's side weighted, b's side carried across the cut),
+//   site(j, k) = sum_r sum_i X_j[r][i] Z_k[r][i]
+//              = sum_r probs_r sum_i pi_i X_j[r][i] [P(t_ab) Y_k][r][i],
 // with the two scalers added.  A CTA takes 16 x 16 (j, k) pairs, one per
 // thread, over a group of pattern blocks; per block of TB_PB patterns the
-// weighted X_j and the P(t_e) Y_k are staged in shared memory, rows padded
-// by one element so that the 16 k rows of a warp fall in distinct banks.
+// X_j and Z_k are staged in shared memory, rows padded by one element so
+// that the 16 Z rows a warp reads fall in distinct banks.
 // ---------------------------------------------------------------------------
 constexpr int TB_T = 16;
-constexpr int TB_PB = 8;
+constexpr int TB_PB = 16;
 
 struct TbrCutDev {
   int edge, nA, nB, pad;
@@ -468,8 +480,6 @@ struct PairArgs {
   const int32_t *xsc;       // [slot][np]
   const int4 *tiles;        // {cut, j0, k0, 0}
   const TbrCutDev *cuts;
-  const void *Dfull;        // [n_edges][R][16]
-  const double *pi, *probs;
   const float *wts;         // [np], zero beyond n_pat
   const float4 *logtab;
   double *partials;         // [n_groups][n_moves]
@@ -489,7 +499,6 @@ __host__ __device__ size_t pair_smem(int R) {
 template <typename Pol>
 __global__ void __launch_bounds__(256) tbr_pair_kernel(const PairArgs a) {
   using V = typename Pol::V;
-  using Coef = typename Pol::Coef;
   extern __shared__ __align__(16) unsigned char smem[];
   const int R = a.R, RS = tbr_row(R);
   float4 *ltab = reinterpret_cast<float4 *>(smem);
@@ -504,7 +513,6 @@ __global__ void __launch_bounds__(256) tbr_pair_kernel(const PairArgs a) {
   const int jj = t / TB_T, kk = t % TB_T;
   const int j = tl.y + jj, k = tl.z + kk;
   const bool mine = j < cut.nA && k < cut.nB;
-  const Coef *D = static_cast<const Coef *>(a.Dfull) + (size_t)cut.edge * R * 16;
   const int per_side = TB_T * TB_PB * R;
   ff sum{0.0f, 0.0f};
   for (int g = 0; g < a.G; ++g) {
@@ -517,26 +525,19 @@ __global__ void __launch_bounds__(256) tbr_pair_kernel(const PairArgs a) {
       const int row = rem / (TB_PB * R), p = (rem / R) % TB_PB, r = rem % R;
       const int idx = (side == 0 ? tl.y : tl.z) + row;
       const size_t pat = pat0 + p;
-      V o[4];
+      V v[4];
       int sc = 0;
       if (idx < (side == 0 ? cut.nA : cut.nB)) {
         const size_t slot = (size_t)((side == 0 ? cut.slotA : cut.slotB) + idx);
-        V v[4];
         Pol::load_tip(a.X, (slot * a.np + pat) * R + r, v);
         sc = a.xsc[slot * a.np + pat];
-        if (side == 0) {
-#pragma unroll
-          for (int e = 0; e < 4; ++e) o[e] = Pol::mul(v[e], Pol::from_d(a.probs[r] * a.pi[e]));
-        } else {
-          Pol::rows(D + (size_t)r * 16, v, o);
-        }
       } else {
 #pragma unroll
-        for (int e = 0; e < 4; ++e) o[e] = Pol::zero();
+        for (int e = 0; e < 4; ++e) v[e] = Pol::zero();
       }
       V *dst = (side == 0 ? Xs : Zs) + (size_t)row * RS + ((size_t)p * R + r) * 4;
 #pragma unroll
-      for (int e = 0; e < 4; ++e) dst[e] = o[e];
+      for (int e = 0; e < 4; ++e) dst[e] = v[e];
       if (r == 0) (side == 0 ? xs : ys)[row * TB_PB + p] = sc;
     }
     __syncthreads();
@@ -1275,6 +1276,7 @@ pgpu_status launch_scan_rt(pgpu_spr *s, const SprPlan &p, const SprPlanDev &d, i
   a.n_blocks = n_blocks;
   a.depth = std::max(p.max_depth, 1);
   a.max_moves = std::max(p.max_moves_per_prune, 1);
+  a.Dfull = nullptr;
   a.xout = nullptr;
   a.xsc = nullptr;
   a.slot_base = 0;
@@ -1359,6 +1361,7 @@ pgpu_status launch_emit_rt(pgpu_spr *s, int prune_base, int n_prunes, long long 
   a.n_blocks = (int)(s->np / s->NP);
   a.depth = std::max(p.max_depth, 1);
   a.max_moves = std::max(p.max_moves_per_prune, 1);
+  a.Dfull = s->Dfull;
   a.xout = s->tbr_x;
   a.xsc = s->tbr_xsc;
   a.slot_base = slot_base;
@@ -1424,9 +1427,6 @@ pgpu_status launch_tbr_batch(pgpu_spr *s, size_t c0, size_t c1, double *lnl_dev)
   a.xsc = s->tbr_xsc;
   a.tiles = s->tbr_tiles;
   a.cuts = s->tbr_cuts;
-  a.Dfull = s->Dfull;
-  a.pi = s->pi;
-  a.probs = s->probs;
   a.wts = s->wf;
   a.logtab = s->logtab;
   a.partials = s->partials;

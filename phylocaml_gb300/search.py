@@ -219,7 +219,9 @@ def learned_spr(eng: SprEngine, net, k: int = 32, eps: float = 1e-3, smooth_pass
             rec = {"round": rounds, "picked": int(lo), "gain": gain}
             if not gain > eps:
                 # nothing among the network's picks: fall back to every move
+                t = time.perf_counter()
                 scores = exhaustive_round()
+                rec["fallback_s"] = time.perf_counter() - t
                 best = int(np.argmax(scores))
                 gain = float(scores[best]) - lnl
                 rec.update(fallback=True, n_gaining=int(np.sum(scores - lnl > eps)),
