@@ -965,6 +965,13 @@ def bench_spr(args, rank, world, local):
     eng.tbr_scan(tb_out)
     tbr_s = time.perf_counter() - t
     tbr_best = float(tb_out[:ntb].max().item()) if ntb else float("nan")
+    # one-time costs of this process (lazy kernel loading, allocator growth)
+    # are paid before either arm is timed: a two-round learned search with a
+    # throwaway network touches every kernel and tensor op the arms use
+    eng.set_tree(start_opt)
+    warm = mlp.MLP(seed=99, max_batch=1024, ctx=ctx)
+    search.learned_spr(eng, warm, boot_steps=50, max_rounds=2)
+    warm.close()
     arms = {}
     diag = []
     for arm in ("exhaustive", "learned"):
