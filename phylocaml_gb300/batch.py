@@ -136,9 +136,21 @@ def device_codes(codes: np.ndarray, device) -> object:
 # The launch shape of a batch (rate classes per pass, work order) is chosen
 # by timing every candidate on a sample of the batch's own variants, and the
 # choice is cached under the batch's composition: its state counts, rate
-# classes and pattern-count spread.
+# classes and pattern-count spread.  Candidates within TIE of the fastest on
+# the sample count as tied, and the first of them in CANDIDATES order wins:
+# the cost order comes first because a sample does not show what it is worth
+# on a whole batch (2,048 mixed protein and codon variants: 3.32 s against
+# 4.45 s in variant order, while their 128-variant samples time the same).
 
-CANDIDATES = [Options(rp, order) for rp in (True, False) for order in ("variant", "cost")]
+CANDIDATES = [Options(rp, order) for rp in (True, False) for order in ("cost", "variant")]
+TIE = 0.02
+
+
+def pick(times: dict, candidates=CANDIDATES, tie: float = TIE) -> Options:
+    """The first candidate (in ``candidates`` order) within ``tie`` of the
+    fastest time."""
+    fastest = min(times[o] for o in candidates)
+    return next(o for o in candidates if times[o] <= fastest * (1.0 + tie))
 
 
 def composition_key(variants: list[Variant]) -> str:
@@ -194,7 +206,7 @@ def autotune(variants: list[Variant], ctx: _native.Context | None = None, sample
             best = min(best, e0.elapsed_time(e1))
         times[opt] = best
         b.close()
-    choice = min(times, key=times.get)
+    choice = pick(times, candidates)
     if cache_path is not None:
         cache[key] = {"rate_pairs": choice.rate_pairs, "order": choice.order,
                       "ms": {f"{o.rate_pairs}/{o.order}": t for o, t in times.items()}}
