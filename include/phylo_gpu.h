@@ -404,7 +404,12 @@ pgpu_status pgpu_spr_apply(pgpu_spr *spr, int64_t move_idx);
  * no limit).  Moves are listed per cut edge, a's attach edge major. */
 pgpu_status pgpu_spr_set_tbr_distance(pgpu_spr *spr, int distance);
 /* Device bytes for the attach vectors of one batch of cut edges (0: 2 GB);
- * a scan runs as many batches as it needs, at least one cut each. */
+ * a scan runs as many batches as it needs, at least one cut each.  A cut
+ * needs (attach edges on both sides) x n_pat x n_rates x 4 values of the
+ * form (4 bytes for precision 32, 8 otherwise), plus 4 bytes of scaler per
+ * attach edge and pattern, whatever the budget: about 3 GB for the middle
+ * cut of a 256-taxon tree at 45,675 patterns in the float-pair form.  A cut
+ * that does not fit on the device fails with the allocation's error. */
 pgpu_status pgpu_spr_set_tbr_budget(pgpu_spr *spr, size_t bytes);
 pgpu_status pgpu_spr_tbr_n_moves(pgpu_spr *spr, size_t *n_moves);
 /* Node ids of every TBR move (arrays [n_moves]), numbered as by
