@@ -28,6 +28,13 @@
 //
 // The Fitch part (spr_fitch_*_kernel) runs the same programs on packed
 // 4-bit state sets: the parsimony length of every neighbour, exactly.
+//
+// TBR moves that reroot both sides of a cut edge (a,b): the scan program of
+// the prune carrying b's side away walks a's side, and in emit mode stores
+// its vector at the middle of every edge it would regraft onto (a's side
+// rerooted there); the reverse prune does the same for b's side.
+// tbr_pair_kernel then scores every pair of attach edges of the cut as one
+// dot product per pattern.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
