@@ -269,3 +269,34 @@ def test_tbr_distance_and_apply(small, ctx):
     smv = e.moves()
     assert sorted(zip(smv.p, smv.u, smv.c, smv.y)) == sorted(SO.moves(adj2, n))
     e.close()
+
+
+@pytest.mark.parametrize("k,shape", [(1, "balanced"), (3, "yule"), (8, "yule")])
+def test_tbr_rescaling_and_rate_classes(ctx, k, shape):
+    """TBR with 1, 3 and 8 rate classes (thread groups of 1, 4 and 8 lanes
+    per pattern, with idle lanes at 3), and long branches on a balanced tree
+    so that the emit walks and the pairs carry power-of-two scalers."""
+    import torch
+    rng = np.random.default_rng(90 + k)
+    n = 32 if shape == "balanced" else 11
+    tr = T.balanced(n, 1.5) if shape == "balanced" else T.yule(n, rng, 0.2)
+    spec = synth.random_gtr_spec(rng, 0.7, k)
+    q, pi, rates, probs = synth.host_model(spec)
+    pats = rng.choice(np.array([1, 2, 4, 8, 15], np.uint8), size=(n, 257))
+    w = rng.integers(1, 4, size=257).astype(np.float64)
+    dev = torch.device("cuda:0")
+    d = dict(tr=tr, q=q, pi=pi, rates=rates, probs=probs, model=M.create(spec, ctx), pats=pats,
+             w=w, tips=torch.from_numpy(pats).to(dev), wd=torch.from_numpy(w).to(dev),
+             table=synth.dna_code_table())
+    e = engine(d, ctx, 48)
+    cur = e.get_tree()
+    adj = SO.unroot(cur.left, cur.right, cur.brlen)
+    mv = [tuple(int(x) for x in m) for m in e.tbr_moves()]
+    assert sorted(map(canon, mv)) == sorted(SO.tbr_moves(adj, n))
+    got = e.tbr_scan().cpu().numpy()
+    idx = rng.choice(len(mv), size=min(25, len(mv)), replace=False)
+    exp = np.array([oracle_lnl(d, SO.apply_tbr(adj, *mv[i])) for i in idx])
+    assert np.all(np.abs(got[idx] - exp) <= 1e-9 * np.abs(exp)), np.max(np.abs(got[idx] - exp))
+    if shape == "balanced":
+        assert np.min(got) < -2000   # long branches: vectors went through the rescaling
+    e.close()
