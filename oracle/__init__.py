@@ -28,7 +28,9 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIBORACLE = HERE / "_build" / "liboracle.so"
 REF_DIR = HERE / "_ref"
-REFERENCE_TREE = Path(os.environ.get("PHYLOCAML_REF", "/root/reference"))
+# the phylocaml checkout: $PHYLOCAML_REF, else a directory named `reference`
+# beside this repository
+REFERENCE_TREE = Path(os.environ.get("PHYLOCAML_REF", str(HERE.parent.parent / "reference")))
 
 _I32P = C.POINTER(C.c_int32)
 _P = C.c_void_p
