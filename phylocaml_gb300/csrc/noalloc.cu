@@ -3,13 +3,12 @@
 // pgpu_fitch_tree and pgpu_fitch_tree_dev keep their scratch (the stack
 // schedule of the tree and an error word) in buffers the context obtains with
 // cudaMalloc.  Some callers cannot allow that: a host program that hands all
-// of the GPU's memory to its own pool up front, a service that forbids
+// of the GPU's memory to its own pool up front, or a service that forbids
 // allocation once it is serving (cudaMalloc can synchronise the device and
-// stall every other stream), or code that records its work into a CUDA graph
-// and must not allocate while recording.  pgpu_fitch_tree_noalloc serves
-// them: it needs no context and allocates nothing.  Its scratch is the one
-// file-scope device array below, of fixed size, which every GPU that loads
-// this library holds until the process exits.
+// stall every other stream).  pgpu_fitch_tree_noalloc serves them: it needs
+// no context and allocates nothing.  Its scratch is the one file-scope device
+// array below, of fixed size, which every GPU that loads this library holds
+// until the process exits.
 //
 // Limits and sharing:
 //   - trees of at most PGPU_NOALLOC_MAX_TIPS tips (larger ones get
@@ -19,9 +18,13 @@
 //     work overlaps on the GPU (different streams, or different host threads
 //     on one device) race on the array and must be serialised by the caller;
 //     host threads are serialised here while the schedule is written.
-//   - the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (once per device, with that device current), so
-//     make that first call before any stream capture begins.
+//   - the call copies the schedule from host memory, reads the error word
+//     back and waits for the stream before it returns.
+//   - the first call in a device's context looks up the array's device
+//     address with cudaGetSymbolAddress (with that device current) and keeps
+//     it for that context, so make that first call before any stream capture
+//     begins.  A device reset between calls is not supported: a new context
+//     can reuse the old one's handle, and the kept address would be stale.
 #include <algorithm>
 #include <mutex>
 
@@ -49,7 +52,33 @@ static __device__ __align__(256) int4 g_noalloc_scratch[kScratchInt4];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
-void *g_scratch_addr[kMaxDevices] = {};
+// per device: the context the address was looked up in, and the address
+struct ScratchSlot {
+  void *context;
+  void *addr;
+};
+ScratchSlot g_scratch[kMaxDevices] = {};
+
+// The calling thread's current context (a CUcontext), through the driver's
+// cuCtxGetCurrent reached from the runtime, so the library needs no link
+// against the driver library.  Null if there is none yet.
+void *current_context() {
+  using CtxGetCurrent = int (*)(void **);
+  static CtxGetCurrent fn = nullptr;   // guarded by g_mutex
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    void *f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !f) {
+      (void)cudaGetLastError();
+      return nullptr;
+    }
+    fn = reinterpret_cast<CtxGetCurrent>(f);
+  }
+  void *c = nullptr;
+  return fn(&c) == 0 ? c : nullptr;
+}
 
 // host-side schedule workspace, also fixed (no heap), guarded by g_mutex
 int32_t h_uses[2 * kMaxTips], h_need[2 * kMaxTips];
@@ -141,17 +170,21 @@ extern "C" pgpu_status pgpu_fitch_tree_noalloc(const pgpu_tree *tree, const uint
     return PGPU_ERR_CUDA;
   }
   std::lock_guard<std::mutex> lock(g_mutex);
-  // set-up, once per device, with that device current: the array's name is
-  // a host-side stand-in, so the device address must be looked up
-  if (!g_scratch_addr[dev]) {
+  // set-up, once per device and context, with that device current: the
+  // array's name is a host-side stand-in, so the device address must be
+  // looked up (which also creates the device's primary context if needed)
+  ScratchSlot &slot = g_scratch[dev];
+  void *context = current_context();
+  if (!slot.addr || !context || slot.context != context) {
     void *p = nullptr;
     if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
       (void)cudaGetLastError();
       return PGPU_ERR_CUDA;
     }
-    g_scratch_addr[dev] = p;
+    slot.addr = p;
+    slot.context = context ? context : current_context();
   }
-  int4 *scratch = static_cast<int4 *>(g_scratch_addr[dev]);
+  int4 *scratch = static_cast<int4 *>(slot.addr);
   int depth = 0;
   PGPU_TRY(schedule_static(tree, &depth));
   const int n = tree->n_tips;
