@@ -695,6 +695,12 @@ pgpu_status pair_host(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b, const
     return pgpu_set_err(ctx, PGPU_ERR_ARG, "fitch: null buffer");
   PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
   const size_t n_words = words_for(n_sites, lb);
+  // The host buffers hold exactly the sites' bytes, as the reference's
+  // vectors do (bv_malloc allocates chars * sizeof(CTYPE), lib/bitvector/
+  // bv.c:32-42): a BV8 vector of 5 characters is 5 bytes, not two words.
+  // Only those bytes are read and written; the device word they end in is
+  // cleared first, so the lanes past the last site are zero.
+  const size_t n_bytes = (n_sites * (size_t)lb + 7) / 8;
   void *da, *db, *dout, *dw = nullptr, *dc;
   PGPU_TRY(pgpu_buf(ctx, BUF_A, n_words * 4, &da));
   PGPU_TRY(pgpu_buf(ctx, BUF_B, n_words * 4, &db));
@@ -702,8 +708,12 @@ pgpu_status pair_host(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b, const
   PGPU_TRY(pgpu_buf(ctx, BUF_SCALAR, 64, &dc));
   if (mode == 1) PGPU_TRY(pgpu_buf(ctx, BUF_WEIGHTS, n_sites * 4, &dw));
   cudaStream_t s = ctx->stream;
-  PGPU_CUDA(ctx, cudaMemcpyAsync(da, a, n_words * 4, cudaMemcpyHostToDevice, s));
-  PGPU_CUDA(ctx, cudaMemcpyAsync(db, b, n_words * 4, cudaMemcpyHostToDevice, s));
+  if (n_bytes < n_words * 4) {
+    PGPU_CUDA(ctx, cudaMemsetAsync((uint32_t *)da + (n_words - 1), 0, 4, s));
+    PGPU_CUDA(ctx, cudaMemsetAsync((uint32_t *)db + (n_words - 1), 0, 4, s));
+  }
+  PGPU_CUDA(ctx, cudaMemcpyAsync(da, a, n_bytes, cudaMemcpyHostToDevice, s));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(db, b, n_bytes, cudaMemcpyHostToDevice, s));
   if (mode == 1) PGPU_CUDA(ctx, cudaMemcpyAsync(dw, w, n_sites * 4, cudaMemcpyHostToDevice, s));
   PGPU_CUDA(ctx, cudaMemsetAsync(dc, 0, 8, s));
   if (n_words) {
@@ -731,7 +741,7 @@ pgpu_status pair_host(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b, const
       default: PGPU_TRY(launch_pair<32>(ctx, pa, pb, pw, po, n_words, n_sites, cnt, mode)); break;
     }
   }
-  if (mode != 2) PGPU_CUDA(ctx, cudaMemcpyAsync(out, dout, n_words * 4, cudaMemcpyDeviceToHost, s));
+  if (mode != 2) PGPU_CUDA(ctx, cudaMemcpyAsync(out, dout, n_bytes, cudaMemcpyDeviceToHost, s));
   uint64_t *hc = reinterpret_cast<uint64_t *>(ctx->h_pinned);
   PGPU_CUDA(ctx, cudaMemcpyAsync(hc, dc, 8, cudaMemcpyDeviceToHost, s));
   PGPU_CUDA(ctx, cudaStreamSynchronize(s));
