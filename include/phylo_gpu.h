@@ -107,7 +107,11 @@ pgpu_status pgpu_tree_schedule(pgpu_ctx *ctx, const pgpu_tree *tree, int32_t *op
 
 /* Bitvector.BVn.fitch_median_2 (lib/bitvector.mli:94; bv_CAML_fitch_median2,
  * lib/bitvector/bv.c:463-480, and bv_fitch, bv.c:148-160).  out[i] = a&b,
- * or a|b where a&b is empty; *union_count = number of such sites. */
+ * or a|b where a&b is empty; *union_count = number of such sites.
+ * The three pair entry points below read and write exactly
+ * ceil(n_sites * lane_bits / 8) bytes of a, b and out -- the size of the
+ * reference's vectors (bv_malloc, bv.c:32-42) -- so the buffers need no
+ * padding to whole words and need no particular alignment. */
 pgpu_status pgpu_fitch_median2(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b,
                                uint32_t *out, size_t n_sites, int lane_bits,
                                uint64_t *union_count);
@@ -152,11 +156,11 @@ pgpu_status pgpu_fitch_tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree,
 /* No counterpart in the reference (phylocaml allocates a result per call,
  * lib/bitvector/bv.c:163-178).  pgpu_fitch_tree_dev for callers that may not
  * allocate device memory: a program that keeps the GPU's memory in its own
- * pool, a service that forbids cudaMalloc once it is serving (an allocation
- * can synchronise the device), or work being recorded into a CUDA graph.  It
- * takes no context and allocates nothing: its scratch (the tree's schedule
- * and an error word) lives in one fixed device array in the library, about
- * 320 KB, held on every GPU that loads the library until the process exits.
+ * pool, or a service that forbids cudaMalloc once it is serving (an
+ * allocation can synchronise the device).  It takes no context and
+ * allocates nothing: its scratch (the tree's schedule and an error word)
+ * lives in one fixed device array in the library, about 320 KB, held on
+ * every GPU that loads the library until the process exits.
  *   - trees of at most 16,384 tips; larger ones return PGPU_ERR_LIMIT;
  *   - runs on cuda_stream (a cudaStream_t, or NULL for the legacy stream) of
  *     the current device and returns after that stream has finished;
@@ -164,8 +168,9 @@ pgpu_status pgpu_fitch_tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree,
  *   - all calls share the array: calls whose GPU work overlaps (other
  *     streams or host threads on the same device) race and must be
  *     serialised by the caller;
- *   - the first call on each device looks the array up with
- *     cudaGetSymbolAddress; make it before any stream capture starts.
+ *   - the first call in each device's context looks the array up with
+ *     cudaGetSymbolAddress; make it before any stream capture starts.  A
+ *     device reset between calls is not supported.
  * Arguments as for pgpu_fitch_tree_dev. */
 pgpu_status pgpu_fitch_tree_noalloc(const pgpu_tree *tree, const uint32_t *tips_dev,
                                     size_t ld_words, const uint32_t *weights_dev,
@@ -249,6 +254,42 @@ pgpu_status pgpu_model_diagonalize(pgpu_ctx *ctx, const double *Q, const double 
 pgpu_status pgpu_model_compose(pgpu_ctx *ctx, const double *U, const double *lambda,
                                const double *Ui, int S, const double *t, size_t n_t,
                                double *P_out);
+
+/* The reference's own four externals, at their arity (declared at
+ * lib/mlModel.ml:73-90 and called by MlModel.diagonalize / compose,
+ * lib/mlModel.ml:554-587), so an OCaml stub binds them without changing
+ * mlModel.ml.  Matrices are row-major n x n FP64 (C-layout Bigarrays), 1 <= n
+ * <= 64; the work runs on the GPU in FP64.
+ *
+ * likelihood_CAML_diagonalize_gtr (lib/mlmodel.c:208-262, 265-271): U holds
+ * Q on entry and receives the eigenvectors; D (filled with zeros by the
+ * caller in the reference) receives the eigenvalues on its diagonal and
+ * zeros elsewhere; Ui receives U's inverse; Q = U D Ui.  Q must be
+ * reversible: its stationary distribution is found on the GPU (no pi
+ * argument is needed) and used to symmetrise Q for the Jacobi solver.  A Q
+ * without a stationary distribution above zero, or not reversible, returns
+ * PGPU_ERR_NONREVERSIBLE; NaN or Inf returns PGPU_ERR_NAN. */
+pgpu_status pgpu_diagonalize_gtr(pgpu_ctx *ctx, double *U, double *D, double *Ui, int n);
+
+/* likelihood_CAML_diagonalize_sym (lib/mlmodel.c:163-197, 200-205): U holds
+ * a symmetric Q on entry (only its lower triangle is read, the triangle
+ * dsyev('U') reads in column-major order) and receives the orthonormal
+ * eigenvectors as ROWS, in ascending order of eigenvalue; D the eigenvalues
+ * on its diagonal.  Q = U^T D U. */
+pgpu_status pgpu_diagonalize_sym(pgpu_ctx *ctx, double *U, double *D, int n);
+
+/* likelihood_CAML_compose_gtr (lib/mlmodel.c:325-342, 344-365):
+ * P = U exp(D t) Ui (only D's diagonal is read); t == -1 gives Q = U D Ui,
+ * t < 1e-10 the identity. */
+pgpu_status pgpu_compose_gtr(pgpu_ctx *ctx, const double *U, const double *D, const double *Ui,
+                             int n, double t, double *P);
+
+/* likelihood_CAML_compose_sym (lib/mlmodel.c:280-302, 304-323):
+ * P = U^T exp(D t) U for U from pgpu_diagonalize_sym.  t is rounded to
+ * float first, as the reference's `const float t` parameter does; then -1
+ * gives Q and anything below 1e-10 the identity. */
+pgpu_status pgpu_compose_sym(pgpu_ctx *ctx, const double *U, const double *D, int n, double t,
+                             double *P);
 
 /* ---- Felsenstein pruning -------------------------------------------------
  * The tree log-likelihood that Likelihood_c.median_2 / root_cost would

@@ -106,6 +106,10 @@ SIGNATURES: dict[str, tuple] = {
     "pgpu_tcm_tree_dev": (_I, [_P, C.POINTER(PgpuTree), _P, _SZ, _P, _SZ, _P, _P, _P, _P]),
     "pgpu_model_diagonalize": (_I, [_P, _P, _P, _I, _P, _P, _P]),
     "pgpu_model_compose": (_I, [_P, _P, _P, _P, _I, _P, _SZ, _P]),
+    "pgpu_diagonalize_gtr": (_I, [_P, _P, _P, _P, _I]),
+    "pgpu_diagonalize_sym": (_I, [_P, _P, _P, _I]),
+    "pgpu_compose_gtr": (_I, [_P, _P, _P, _P, _I, C.c_double, _P]),
+    "pgpu_compose_sym": (_I, [_P, _P, _P, _I, C.c_double, _P]),
     "pgpu_prune_lnl": (_I, [_P, C.POINTER(PgpuTree), C.POINTER(PgpuModel),
                             C.POINTER(PgpuTipCodes), _P, _P, _SZ, _I, _DP, _P]),
     "pgpu_prune_lnl_dev": (_I, [_P, C.POINTER(PgpuTree), C.POINTER(PgpuModel),

@@ -17,6 +17,7 @@
 // orthogonal V to working precision.
 #include <algorithm>
 #include <cmath>
+#include <vector>
 
 #include "pgpu_internal.cuh"
 #include "pmatrix.cuh"
@@ -26,12 +27,18 @@ namespace {
 constexpr int MAXS = 64;
 constexpr int LDA = MAXS + 1;   // padded rows against bank conflicts
 
+// pi == null selects the symmetric mode of diagonalize_sym
+// (lib/mlmodel.c:163-197): B is Q's lower triangle mirrored (the upper
+// triangle dsyev('U') reads in column-major order), U receives the
+// eigenvectors as rows (the row-major view of dsyev's column-major V), in
+// ascending order of their eigenvalues as dsyev returns them, and Ui is not
+// written.
 struct EigArgs {
   const double *Q;    // [n_models][S][S]
-  const double *pi;   // [n_models][S]
+  const double *pi;   // [n_models][S], or null: symmetric mode
   double *U;          // [n_models][S][S]
   double *lam;        // [n_models][S]
-  double *Ui;         // [n_models][S][S]
+  double *Ui;         // [n_models][S][S] (unused in the symmetric mode)
   int *status;        // [n_models]: 0 ok, PGPU_ERR_* otherwise
   int S;
   int max_sweeps;
@@ -49,15 +56,22 @@ __global__ void __launch_bounds__(256) jacobi_eig_kernel(const EigArgs p) {
   __shared__ int bad;
   const int m = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
   const double *Q = p.Q + (size_t)m * S * S;
-  const double *pi = p.pi + (size_t)m * S;
+  const bool sym = p.pi == nullptr;
+  const double *pi = sym ? nullptr : p.pi + (size_t)m * S;
   if (tid == 0) bad = 0;
   __syncthreads();
 
-  // B = Pi^1/2 Q Pi^-1/2, checked for NaN/Inf and for reversibility
+  // B = Pi^1/2 Q Pi^-1/2, checked for NaN/Inf and for reversibility; in the
+  // symmetric mode B is Q's lower triangle, mirrored
   for (int e = tid; e < N * N; e += nt) {
     const int i = e / N, j = e % N;
     double v = 0.0, vt = 0.0;
-    if (i < S && j < S) {
+    if (sym) {
+      if (i < S && j < S) {
+        v = vt = Q[(i > j ? i : j) * S + (i > j ? j : i)];
+        if (!isfinite(v)) atomicOr(&bad, 1);
+      }
+    } else if (i < S && j < S) {
       const double qi = Q[i * S + j], qt = Q[j * S + i];
       const double pi_i = pi[i], pi_j = pi[j];
       if (!isfinite(qi) || !isfinite(pi_i) || !(pi_i > 0.0)) atomicOr(&bad, 1);
@@ -170,6 +184,28 @@ __global__ void __launch_bounds__(256) jacobi_eig_kernel(const EigArgs p) {
       __syncthreads();
     }
   }
+  if (sym) {
+    // eigenpairs in ascending order (ties by index): order[k] is the
+    // column of V with the k-th smallest eigenvalue
+    __syncthreads();
+    for (int i = tid; i < S; i += nt) {
+      const double li = A[i * LDA + i];
+      int rank = 0;
+      for (int j = 0; j < S; ++j) {
+        const double lj = A[j * LDA + j];
+        rank += (lj < li) || (lj == li && j < i);
+      }
+      order[rank] = i;
+    }
+    __syncthreads();
+    for (int e = tid; e < S * S; e += nt) {
+      const int k = e / S, i = e % S;
+      p.U[(size_t)m * S * S + e] = V[i * LDA + order[k]];
+    }
+    for (int k = tid; k < S; k += nt) p.lam[(size_t)m * S + k] = A[order[k] * LDA + order[k]];
+    if (tid == 0) p.status[m] = converged ? 0 : PGPU_ERR_EIGEN;
+    return;
+  }
   // outputs: lambda, U = Pi^-1/2 V, Ui = V^T Pi^1/2
   for (int e = tid; e < S * S; e += nt) {
     const int i = e / S, j = e % S;
@@ -178,6 +214,101 @@ __global__ void __launch_bounds__(256) jacobi_eig_kernel(const EigArgs p) {
   }
   for (int i = tid; i < S; i += nt) p.lam[(size_t)m * S + i] = A[i * LDA + i];
   if (tid == 0) p.status[m] = converged ? 0 : PGPU_ERR_EIGEN;
+}
+
+// Stationary distribution of one rate matrix: pi Q = 0 with sum(pi) = 1,
+// i.e. Q^T pi = 0 with its last equation replaced by the sum, solved by
+// Gaussian elimination with partial pivoting in FP64 shared memory, one CTA.
+// The reference's diagonalize_gtr (lib/mlmodel.c:208-262) takes Q alone;
+// the Jacobi solver above needs pi to symmetrise Q, so it is recovered here.
+// status: 0, PGPU_ERR_NAN (a NaN or Inf in Q), or PGPU_ERR_NONREVERSIBLE (no
+// stationary vector with every entry above 1e-15 of the total: a singular
+// system or a reducible Q).
+__global__ void __launch_bounds__(256) stationary_kernel(const double *Q, int S, double *pi,
+                                                         int *status) {
+  extern __shared__ __align__(16) double sm[];
+  const int L = S + 1;   // S coefficients and the right-hand side per row
+  double *M = sm;        // [S][L]
+  __shared__ int piv, bad;
+  __shared__ double pval;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  for (int e = tid; e < S * S; e += nt) {
+    const int i = e / S, j = e % S;
+    const double q = Q[j * S + i];   // row i of Q^T
+    if (!isfinite(q)) atomicOr(&bad, 1);
+    M[i * L + j] = (i == S - 1) ? 1.0 : q;
+  }
+  for (int i = tid; i < S; i += nt) M[i * L + S] = (i == S - 1) ? 1.0 : 0.0;
+  __syncthreads();
+  if (bad) {
+    if (tid == 0) *status = PGPU_ERR_NAN;
+    return;
+  }
+  for (int k = 0; k < S; ++k) {
+    if (tid < 32) {
+      double best = -1.0;
+      int row = k;
+      for (int r = k + lane; r < S; r += 32) {
+        const double v = fabs(M[r * L + k]);
+        if (v > best) {
+          best = v;
+          row = r;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int orow = __shfl_xor_sync(0xffffffffu, row, o);
+        if (ob > best || (ob == best && orow < row)) {
+          best = ob;
+          row = orow;
+        }
+      }
+      if (lane == 0) {
+        piv = row;
+        pval = best;
+      }
+    }
+    __syncthreads();
+    if (!(pval > 0.0) || !isfinite(pval)) {
+      if (tid == 0) *status = PGPU_ERR_NONREVERSIBLE;
+      return;
+    }
+    if (piv != k) {
+      for (int c = k + tid; c <= S; c += nt) {
+        const double t = M[k * L + c];
+        M[k * L + c] = M[piv * L + c];
+        M[piv * L + c] = t;
+      }
+      __syncthreads();
+    }
+    const int rows = S - 1 - k, cols = S - k;   // rows below k; columns k+1..S
+    for (int e = tid; e < rows * cols; e += nt) {
+      const int r = k + 1 + e / cols, c = k + 1 + e % cols;
+      M[r * L + c] -= (M[r * L + k] / M[k * L + k]) * M[k * L + c];
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    double sum = 0.0;
+    int ok = 1;
+    for (int i = S - 1; i >= 0; --i) {
+      double x = M[i * L + S];
+      for (int j = i + 1; j < S; ++j) x -= M[i * L + j] * M[j * L + S];
+      x /= M[i * L + i];
+      M[i * L + S] = x;
+      sum += x;
+      ok &= (x > 0.0) && isfinite(x);
+    }
+    // a frequency below 1e-15 of the total is a state the chain never
+    // reaches (rounding leaves it near zero rather than at zero)
+    for (int i = 0; ok && i < S; ++i) ok &= M[i * L + S] > 1e-15 * sum;
+    if (ok)
+      for (int i = 0; i < S; ++i) pi[i] = M[i * L + S] / sum;
+    *status = ok ? 0 : PGPU_ERR_NONREVERSIBLE;
+  }
 }
 
 // P[b][r] = U diag(exp(lambda * rate_r * t_b)) Ui for every branch b and
@@ -421,6 +552,111 @@ pgpu_status pgpu_model_compose(pgpu_ctx *ctx, const double *U, const double *lam
   PGPU_CUDA(ctx, cudaMemcpyAsync(P_out, dp, n_t * SS * 8, cudaMemcpyDeviceToHost, s));
   PGPU_CUDA(ctx, cudaStreamSynchronize(s));
   return PGPU_OK;
+}
+
+// ---- the reference's four externals, at their own arity -------------------
+// likelihood_CAML_diagonalize_gtr / _sym and likelihood_CAML_compose_gtr /
+// _sym (lib/mlmodel.c:200-205, 265-271, 304-323, 344-365; declared at
+// lib/mlModel.ml:73-90).  Matrices are row-major n x n FP64, as the OCaml
+// Bigarrays are; D is a diagonal matrix.
+
+pgpu_status pgpu_diagonalize_gtr(pgpu_ctx *ctx, double *U, double *D, double *Ui, int n) {
+  if (!ctx) return PGPU_ERR_ARG;
+  if (!U || !D || !Ui) return pgpu_set_err(ctx, PGPU_ERR_ARG, "diagonalize_gtr: null buffer");
+  if (n < 1 || n > MAXS) return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "diagonalize_gtr: 1..%d states", MAXS);
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  const size_t SS = (size_t)n * n;
+  void *dq, *dpi, *du, *dl, *dui, *dst;
+  PGPU_TRY(pgpu_buf(ctx, BUF_A, SS * 8, &dq));
+  PGPU_TRY(pgpu_buf(ctx, BUF_B, n * 8, &dpi));
+  PGPU_TRY(pgpu_buf(ctx, BUF_C, SS * 8, &du));
+  PGPU_TRY(pgpu_buf(ctx, BUF_D, n * 8, &dl));
+  PGPU_TRY(pgpu_buf(ctx, BUF_E, SS * 8, &dui));
+  PGPU_TRY(pgpu_buf(ctx, BUF_SCALAR, 64, &dst));
+  cudaStream_t s = ctx->stream;
+  int *st = static_cast<int *>(dst);
+  PGPU_CUDA(ctx, cudaMemcpyAsync(dq, U, SS * 8, cudaMemcpyHostToDevice, s));
+  PGPU_CUDA(ctx, cudaMemsetAsync(dpi, 0, n * 8, s));
+  PGPU_CUDA(ctx, cudaMemsetAsync(dst, 0, 2 * sizeof(int), s));
+  const size_t smem = sizeof(double) * (size_t)n * (n + 1);
+  PGPU_CUDA(ctx, cudaFuncSetAttribute(stationary_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)std::max<size_t>(smem, 1024)));
+  stationary_kernel<<<1, 256, smem, s>>>((const double *)dq, n, (double *)dpi, st + 1);
+  PGPU_TRY(pgpu_after_launch(ctx, "stationary_kernel"));
+  PGPU_TRY(pgpu_launch_eig(ctx, (double *)dq, (double *)dpi, n, 1, (double *)du, (double *)dl,
+                           (double *)dui, st));
+  int *hst = reinterpret_cast<int *>(ctx->h_pinned);
+  std::vector<double> lam(n);
+  PGPU_CUDA(ctx, cudaMemcpyAsync(hst, dst, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(lam.data(), dl, n * 8, cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  if (hst[1] == PGPU_ERR_NAN) return status_to_err(ctx, PGPU_ERR_NAN);
+  if (hst[1])
+    return pgpu_set_err(ctx, PGPU_ERR_NONREVERSIBLE,
+                        "diagonalize_gtr: Q has no stationary distribution with every state above 0");
+  PGPU_TRY(status_to_err(ctx, hst[0]));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(U, du, SS * 8, cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(Ui, dui, SS * 8, cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  for (size_t i = 0; i < SS; ++i) D[i] = 0.0;
+  for (int i = 0; i < n; ++i) D[(size_t)i * n + i] = lam[i];
+  return PGPU_OK;
+}
+
+pgpu_status pgpu_diagonalize_sym(pgpu_ctx *ctx, double *U, double *D, int n) {
+  if (!ctx) return PGPU_ERR_ARG;
+  if (!U || !D) return pgpu_set_err(ctx, PGPU_ERR_ARG, "diagonalize_sym: null buffer");
+  if (n < 1 || n > MAXS) return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "diagonalize_sym: 1..%d states", MAXS);
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  const size_t SS = (size_t)n * n;
+  void *dq, *du, *dl, *dst;
+  PGPU_TRY(pgpu_buf(ctx, BUF_A, SS * 8, &dq));
+  PGPU_TRY(pgpu_buf(ctx, BUF_C, SS * 8, &du));
+  PGPU_TRY(pgpu_buf(ctx, BUF_D, n * 8, &dl));
+  PGPU_TRY(pgpu_buf(ctx, BUF_SCALAR, 64, &dst));
+  cudaStream_t s = ctx->stream;
+  PGPU_CUDA(ctx, cudaMemcpyAsync(dq, U, SS * 8, cudaMemcpyHostToDevice, s));
+  PGPU_TRY(pgpu_launch_eig(ctx, (double *)dq, nullptr, n, 1, (double *)du, (double *)dl, nullptr,
+                           (int *)dst));
+  int *hst = reinterpret_cast<int *>(ctx->h_pinned);
+  std::vector<double> lam(n);
+  PGPU_CUDA(ctx, cudaMemcpyAsync(hst, dst, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(lam.data(), dl, n * 8, cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  if (*hst == PGPU_ERR_NAN) return pgpu_set_err(ctx, PGPU_ERR_NAN, "diagonalize_sym: NaN or Inf in Q");
+  PGPU_TRY(status_to_err(ctx, *hst));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(U, du, SS * 8, cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  for (size_t i = 0; i < SS; ++i) D[i] = 0.0;
+  for (int i = 0; i < n; ++i) D[(size_t)i * n + i] = lam[i];
+  return PGPU_OK;
+}
+
+pgpu_status pgpu_compose_gtr(pgpu_ctx *ctx, const double *U, const double *D, const double *Ui,
+                             int n, double t, double *P) {
+  if (!ctx) return PGPU_ERR_ARG;
+  if (!U || !D || !Ui || !P) return pgpu_set_err(ctx, PGPU_ERR_ARG, "compose_gtr: null buffer");
+  if (n < 1 || n > MAXS) return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "compose_gtr: 1..%d states", MAXS);
+  std::vector<double> lam(n);
+  for (int i = 0; i < n; ++i) lam[i] = D[(size_t)i * n + i];
+  return pgpu_model_compose(ctx, U, lam.data(), Ui, n, &t, 1, P);
+}
+
+pgpu_status pgpu_compose_sym(pgpu_ctx *ctx, const double *U, const double *D, int n, double t,
+                             double *P) {
+  if (!ctx) return PGPU_ERR_ARG;
+  if (!U || !D || !P) return pgpu_set_err(ctx, PGPU_ERR_ARG, "compose_sym: null buffer");
+  if (n < 1 || n > MAXS) return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "compose_sym: 1..%d states", MAXS);
+  // the reference takes t as a float here (`const float t`, lib/mlmodel.c:280)
+  const double t32 = (double)(float)t;
+  // U holds the eigenvectors as rows, so P = U^T exp(D t) U: compose with
+  // U^T in the left factor's place and U in the right one's
+  const size_t SS = (size_t)n * n;
+  std::vector<double> lam(n), ut(SS);
+  for (int i = 0; i < n; ++i) lam[i] = D[(size_t)i * n + i];
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) ut[(size_t)i * n + j] = U[(size_t)j * n + i];
+  return pgpu_model_compose(ctx, ut.data(), lam.data(), U, n, &t32, 1, P);
 }
 
 }  // extern "C"

@@ -256,6 +256,85 @@ def diagonalize(q: np.ndarray, pi: np.ndarray, ctx: _native.Context | None = Non
     return U, lam, Ui
 
 
+# ---- the reference's externals at their own arity (lib/mlModel.ml:73-90) ---
+# Matrices are C-contiguous float64 [n, n] arrays, changed in place as the
+# reference's Bigarrays are.
+
+def _mat(a: np.ndarray, name: str) -> np.ndarray:
+    if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.ndim == 2
+            and a.shape[0] == a.shape[1] and a.flags.c_contiguous):
+        raise Error(f"{name} must be a C-contiguous float64 square matrix")
+    return a
+
+
+def diagonalize_gtr(u: np.ndarray, d: np.ndarray, ui: np.ndarray,
+                    ctx: _native.Context | None = None) -> None:
+    """likelihood_CAML_diagonalize_gtr: ``u`` holds Q and becomes U, ``d``
+    the diagonal matrix of eigenvalues, ``ui`` U's inverse (Q = U D Ui)."""
+    n = _mat(u, "U").shape[0]
+    if _mat(d, "D").shape[0] != n or _mat(ui, "Ui").shape[0] != n:
+        raise Error("U, D and Ui must have the same size")
+    ctx = ctx or _native.default_context()
+    ctx.call("pgpu_diagonalize_gtr", u.ctypes.data, d.ctypes.data, ui.ctypes.data, n)
+
+
+def diagonalize_sym(u: np.ndarray, d: np.ndarray, ctx: _native.Context | None = None) -> None:
+    """likelihood_CAML_diagonalize_sym: ``u`` holds a symmetric Q and becomes
+    the eigenvectors as rows (ascending eigenvalues), ``d`` the diagonal
+    matrix of eigenvalues (Q = U^T D U)."""
+    n = _mat(u, "U").shape[0]
+    if _mat(d, "D").shape[0] != n:
+        raise Error("U and D must have the same size")
+    ctx = ctx or _native.default_context()
+    ctx.call("pgpu_diagonalize_sym", u.ctypes.data, d.ctypes.data, n)
+
+
+def compose_gtr(u: np.ndarray, d: np.ndarray, ui: np.ndarray, t: float,
+                ctx: _native.Context | None = None) -> np.ndarray:
+    """likelihood_CAML_compose_gtr: P = U exp(D t) Ui (Q for t == -1)."""
+    n = _mat(u, "U").shape[0]
+    _mat(d, "D"), _mat(ui, "Ui")
+    ctx = ctx or _native.default_context()
+    out = np.empty((n, n))
+    ctx.call("pgpu_compose_gtr", u.ctypes.data, d.ctypes.data, ui.ctypes.data, n, float(t),
+             out.ctypes.data)
+    return out
+
+
+def compose_sym(u: np.ndarray, d: np.ndarray, t: float,
+                ctx: _native.Context | None = None) -> np.ndarray:
+    """likelihood_CAML_compose_sym: P = U^T exp(D t) U, t rounded to float."""
+    n = _mat(u, "U").shape[0]
+    _mat(d, "D")
+    ctx = ctx or _native.default_context()
+    out = np.empty((n, n))
+    ctx.call("pgpu_compose_sym", u.ctypes.data, d.ctypes.data, n, float(t), out.ctypes.data)
+    return out
+
+
+def diagonalize_matrix(sym: bool, mat: np.ndarray, ctx: _native.Context | None = None):
+    """MlModel.diagonalize (lib/mlModel.ml:554-583) over the externals above:
+    (U, D, Ui or None)."""
+    if np.isnan(mat).any():
+        raise Error("rate matrix contains NaN")
+    n = mat.shape[0]
+    u = np.ascontiguousarray(mat, np.float64).copy()
+    d = np.zeros((n, n))
+    if sym:
+        diagonalize_sym(u, d, ctx)
+        return u, d, None
+    ui = np.zeros((n, n))
+    diagonalize_gtr(u, d, ui, ctx)
+    return u, d, ui
+
+
+def compose_decomposed(decomp, t: float, ctx: _native.Context | None = None) -> np.ndarray:
+    """MlModel.compose (lib/mlModel.ml:585-587) on diagonalize_matrix's
+    result: compose_gtr when Ui is present, else compose_sym."""
+    u, d, ui = decomp
+    return compose_sym(u, d, t, ctx) if ui is None else compose_gtr(u, d, ui, t, ctx)
+
+
 def create(spec: Spec, ctx: _native.Context | None = None) -> Model:
     """MlModel.create (lib/mlModel.ml:664-746)."""
     priors = _priors(spec)
