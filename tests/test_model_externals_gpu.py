@@ -94,8 +94,12 @@ def test_gtr_externals_match_oracle(ctx, S, seed):
 def test_mlmodel_diagonalize_and_compose_over_externals(ctx, name):
     """MlModel.diagonalize false / compose over the externals equal the model
     that MlModel.create builds (which passes pi explicitly)."""
-    from tests.test_likelihood_gpu import SPECS
-    m = M.create(SPECS[name], ctx)
+    pri = ("Empirical", [0.1, 0.2, 0.3, 0.4])
+    specs = {"F81": M.Spec(("F81",), base_priors=pri), "HKY85": M.Spec(("HKY85", 2.0), base_priors=pri),
+             "TN93": M.Spec(("TN93", (2.0, 3.0)), base_priors=pri),
+             "GTR": M.Spec(("GTR", [1.1, 0.7, 1.9, 0.6, 1.4]), ("DiscreteGamma", 4, 0.5),
+                           ("Empirical", [0.3, 0.2, 0.25, 0.25]))}
+    m = M.create(specs[name], ctx)
     dec = M.diagonalize_matrix(False, m.q, ctx)
     for t in (0.0, 0.03, 0.7, -1.0):
         assert np.abs(M.compose_decomposed(dec, t, ctx) - M.compose(m, t, ctx)).max() < 1e-13
