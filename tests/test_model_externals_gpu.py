@@ -67,7 +67,7 @@ def test_compose_sym_rounds_t_to_float(ctx):
     assert np.array_equal(M.compose_sym(u, d, t, ctx), M.compose_sym(u, d, t32, ctx))
     # and that is the float length's matrix, not the double one's
     from scipy.linalg import expm
-    assert np.abs(M.compose_sym(u, d, t, ctx) - expm(q * t32)).max() < 1e-14
+    assert np.abs(M.compose_sym(u, d, t, ctx) - expm(q * t32)).max() < 1e-13
     assert np.abs(expm(q * t32) - expm(q * t)).max() > 1e-10
 
 
