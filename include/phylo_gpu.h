@@ -125,6 +125,19 @@ pgpu_status pgpu_fitch_median2_weighted(pgpu_ctx *ctx, const uint32_t *a,
                                         uint32_t *out, size_t n_sites, int lane_bits,
                                         uint64_t *cost);
 
+/* NonAdditive_c.median_2 (lib/nonAdditive_c.ml:19-35) over the reference's
+ * own record fields: x.states and y.states as OCaml ints (state sets of up
+ * to 63 bits, sign-extended to int64 by Long_val, so land / lor are 64-bit
+ * AND / OR), x.weights as doubles (any value: fractional weights are
+ * legal).  out[i] = x_i & y_i, or x_i | y_i where that is 0;
+ * *cost = sum_i weights[i] * float([x_i & y_i == 0]), each term formed as
+ * the reference forms it and summed with error-free transformations in a
+ * fixed order, so the result is deterministic and within rounding of the
+ * exact sum (the reference's left-to-right sum may differ from it by its
+ * own rounding). */
+pgpu_status pgpu_nonadditive_median2(pgpu_ctx *ctx, const int64_t *x, const int64_t *y,
+                                     const double *weights, int64_t *out, size_t n, double *cost);
+
 /* Bitvector.BVn.distance (lib/bitvector.mli:90; bv_distance, bv.c:46-55). */
 pgpu_status pgpu_fitch_distance(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b,
                                 size_t n_sites, int lane_bits, uint64_t *distance);
@@ -320,6 +333,59 @@ pgpu_status pgpu_prune_lnl_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_
                                const pgpu_tip_codes *codes, const uint8_t *tip_codes_dev,
                                size_t ld_pat, const double *weights_dev, size_t n_pat,
                                int precision, double *lnl_dev, double *site_lnl_dev);
+
+/* ---- Likelihood_c one node at a time (NodeData.S) ------------------------
+ * The operator Node.Make1D applies per node (median_2 : m -> t option -> t
+ * -> t -> t, median_1, median_3, cost, root_cost; lib/nodeData.ml:20-30),
+ * whose Likelihood_c slot is `failwith "TODO"` in the reference
+ * (lib/likelihood_c.ml:14-21).  pgpu_prune_lnl scores a whole tree in one
+ * launch and is the fast path; these calls let a caller fold the postorder
+ * itself, node by node, with the vectors staying on the GPU.
+ *   pgpu_lk   the m: model eigen system (FP64, on the GPU), rate classes,
+ *             tip-code table, and the character block's n_pat patterns and
+ *             weights (host arrays, copied; weights NULL for 1);
+ *   pgpu_clv  a t: one node's conditional likelihoods [n_pat][R][S] on the
+ *             device, stored in float (precision 32) or double (64), each
+ *             pattern normalised by an exact power of two so that its
+ *             largest entry lies in [1/2, 1), plus the length of the branch
+ *             above the node (pgpu_clv_set_brlen) and its P matrices.
+ * The costs: pgpu_clv_cost of an internal node is what its normalisation
+ * moved out of the likelihood, -ln 2 sum_p w_p e_p; pgpu_clv_root_cost is
+ * -sum_p w_p log(sum_r probs_r sum_i pi_i x[p][r][i]).  The costs of all
+ * internal nodes plus the root's root_cost equal -lnL, the sum of node
+ * costs that lib/node.ml:191 forms.  Leaves cost 0.
+ * median calls are asynchronous on the context's stream; cost and
+ * root_cost synchronise.  `reuse` is the reference's `t option`: the node's
+ * previous value, whose device memory the result takes over (the result is
+ * then that same handle); NULL allocates a new handle (stream-ordered).
+ * Destroy every handle of a pgpu_lk before the pgpu_lk itself.  2..64
+ * states, 1..8 rate classes. */
+typedef struct pgpu_lk pgpu_lk;
+typedef struct pgpu_clv pgpu_clv;
+
+pgpu_status pgpu_lk_create(pgpu_ctx *ctx, const pgpu_model *model, const pgpu_tip_codes *codes,
+                           size_t n_pat, const double *weights, int precision, pgpu_lk **out);
+void pgpu_lk_destroy(pgpu_lk *lk);
+/* A leaf: codes is a host array [n_pat] of rows of the tip-code table.
+ * Its branch length is 0 until set. */
+pgpu_status pgpu_clv_leaf(pgpu_lk *lk, pgpu_clv *reuse, const uint8_t *codes, pgpu_clv **out);
+/* Length of the branch above the node (>= 0); builds that branch's P
+ * matrices in FP64 on the GPU.  A node must have one before it is used as
+ * a neighbour. */
+pgpu_status pgpu_clv_set_brlen(pgpu_clv *t, double brlen);
+pgpu_status pgpu_clv_get_brlen(const pgpu_clv *t, double *brlen);
+/* median_1: P(t_a) a.  median_2: (P(t_a) a) * (P(t_b) b).  median_3: the
+ * same over three neighbours (an unrooted tree's node). */
+pgpu_status pgpu_clv_median1(pgpu_lk *lk, pgpu_clv *reuse, const pgpu_clv *a, pgpu_clv **out);
+pgpu_status pgpu_clv_median2(pgpu_lk *lk, pgpu_clv *reuse, const pgpu_clv *a, const pgpu_clv *b,
+                             pgpu_clv **out);
+pgpu_status pgpu_clv_median3(pgpu_lk *lk, pgpu_clv *reuse, const pgpu_clv *a, const pgpu_clv *b,
+                             const pgpu_clv *c, pgpu_clv **out);
+pgpu_status pgpu_clv_cost(pgpu_clv *t, double *cost);
+/* site_lnl (host [n_pat], or NULL) receives each pattern's lnL at this
+ * root. */
+pgpu_status pgpu_clv_root_cost(pgpu_clv *t, double *cost, double *site_lnl);
+void pgpu_clv_destroy(pgpu_clv *t);
 
 /* ---- batched scoring of many trees and models --------------------------
  * One variant = one tree, one model and its own site patterns; the batch

@@ -98,6 +98,7 @@ SIGNATURES: dict[str, tuple] = {
     "pgpu_fitch_median2": (_I, [_P, _P, _P, _P, _SZ, _I, _U64P]),
     "pgpu_fitch_median2_weighted": (_I, [_P, _P, _P, _P, _P, _SZ, _I, _U64P]),
     "pgpu_fitch_distance": (_I, [_P, _P, _P, _SZ, _I, _U64P]),
+    "pgpu_nonadditive_median2": (_I, [_P, _P, _P, _P, _P, _SZ, _DP]),
     "pgpu_fitch_tree": (_I, [_P, C.POINTER(PgpuTree), _P, _P, _SZ, _I, _P, _P, _U64P]),
     "pgpu_fitch_tree_dev": (_I, [_P, C.POINTER(PgpuTree), _P, _SZ, _P, _SZ, _I, _P, _P, _P]),
     "pgpu_fitch_tree_noalloc": (_I, [C.POINTER(PgpuTree), _P, _SZ, _P, _SZ, _I, _P, _P, _P, _P]),
@@ -114,6 +115,18 @@ SIGNATURES: dict[str, tuple] = {
                             C.POINTER(PgpuTipCodes), _P, _P, _SZ, _I, _DP, _P]),
     "pgpu_prune_lnl_dev": (_I, [_P, C.POINTER(PgpuTree), C.POINTER(PgpuModel),
                                 C.POINTER(PgpuTipCodes), _P, _SZ, _P, _SZ, _I, _P, _P]),
+    "pgpu_lk_create": (_I, [_P, C.POINTER(PgpuModel), C.POINTER(PgpuTipCodes), _SZ, _P, _I,
+                            C.POINTER(_P)]),
+    "pgpu_lk_destroy": (None, [_P]),
+    "pgpu_clv_leaf": (_I, [_P, _P, _P, C.POINTER(_P)]),
+    "pgpu_clv_set_brlen": (_I, [_P, C.c_double]),
+    "pgpu_clv_get_brlen": (_I, [_P, _DP]),
+    "pgpu_clv_median1": (_I, [_P, _P, _P, C.POINTER(_P)]),
+    "pgpu_clv_median2": (_I, [_P, _P, _P, _P, C.POINTER(_P)]),
+    "pgpu_clv_median3": (_I, [_P, _P, _P, _P, _P, C.POINTER(_P)]),
+    "pgpu_clv_cost": (_I, [_P, _DP]),
+    "pgpu_clv_root_cost": (_I, [_P, _DP, _P]),
+    "pgpu_clv_destroy": (None, [_P]),
     "pgpu_batch_create": (_I, [_P, C.POINTER(PgpuVariant), _I, C.POINTER(_P)]),
     "pgpu_batch_create_opts": (_I, [_P, C.POINTER(PgpuVariant), _I, C.POINTER(PgpuBatchOptions),
                                     C.POINTER(_P)]),

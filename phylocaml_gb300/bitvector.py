@@ -119,7 +119,7 @@ class BV:
 
     def fitch_median_2(self, a: Vector, b: Vector) -> tuple[Vector, int]:
         self._pair(a, b)
-        out = np.empty_like(a.words)
+        out = np.zeros_like(a.words)   # the call writes only the sites' bytes
         cnt = C.c_uint64(0)
         self.ctx.call("pgpu_fitch_median2", _native.ptr(a.words), _native.ptr(b.words),
                       _native.ptr(out), a.chars, self.lane_bits, C.byref(cnt))

@@ -1,0 +1,594 @@
+// Likelihood_c one node at a time: the NodeData.S operator
+// (lib/nodeData.ml:20-30) whose slot lib/likelihood_c.ml:14-21 leaves as
+// `failwith "TODO"`.
+//
+//   m  (pgpu_lk)   the substitution model's eigen system (FP64, on the GPU),
+//                  its rate classes, the tip-code table and the character
+//                  block's pattern count and weights;
+//   t  (pgpu_clv)  one node's conditional likelihoods on the device,
+//                  [n_pat][R][S] in the storage type (float or double), a
+//                  power-of-two exponent per pattern, the length of the
+//                  branch above the node and that branch's P matrices.
+//
+// median_1/2/3 combine one, two or three neighbours: y = prod_k P(t_k) x_k
+// per pattern and rate class.  Every result is normalised so that each
+// pattern's largest entry lies in [1/2, 1): stored = true * 2^-E with an
+// exact power of two e_p applied at the node and E summed over the subtree.
+// The node's cost is what its own normalisation moved out of the
+// likelihood, -ln 2 sum_p w_p e_p, and root_cost is
+// -sum_p w_p log(sum_r probs_r sum_i pi_i stored).  The costs of all
+// internal nodes plus the root's root_cost are then -lnL, which is how
+// Node.Make1D sums node costs (lib/node.ml:191).
+//
+// One thread per (pattern, rate class): RL = the power of two >= R lanes
+// per pattern, so a pattern's maximum is a shuffle over its lanes.  Loads
+// of a child's vector are contiguous per thread and contiguous across the
+// warp, so the kernel streams at HBM speed; P blocks are read through the
+// read-only cache.  Each CTA writes a compensated partial of its cost, and
+// the last CTA to finish adds the partials in CTA order, so costs are
+// deterministic.
+//
+// Handles are allocated stream-ordered (cudaMallocAsync) on the context's
+// stream; passing the node's previous value (the reference's `t option`)
+// reuses its memory instead.
+#include <algorithm>
+#include <cmath>
+
+#include "pgpu_internal.cuh"
+#include "forms.cuh"
+#include "pmatrix.cuh"
+
+using namespace pgpu_forms;
+
+struct pgpu_lk {
+  pgpu_ctx *ctx = nullptr;
+  int S = 0, R = 0, RL = 1, n_codes = 0, precision = 64;
+  size_t n_pat = 0;
+  double *block = nullptr;   // U, Ui, lam, pi, rates, probs, code table, weights
+  double *U = nullptr, *Ui = nullptr, *lam = nullptr, *pi = nullptr, *rates = nullptr,
+         *probs = nullptr, *tab = nullptr, *weights = nullptr;
+  int *status = nullptr;     // eigendecomposition status
+  double2 *part = nullptr;   // per-CTA partial sums
+  unsigned *counter = nullptr;
+  size_t n_cta = 0;
+  long long live = 0;        // handles not yet destroyed
+};
+
+struct pgpu_clv {
+  pgpu_lk *lk = nullptr;
+  char *mem = nullptr;       // one stream-ordered allocation
+  void *x = nullptr;         // [n_pat][R][S]
+  int32_t *ex = nullptr;     // [n_pat]
+  void *P = nullptr;         // [R][S][S] of the branch above
+  double *scal = nullptr;    // [0] cost, [1] branch length, [2] root cost
+  double brlen = 0.0;
+  bool has_P = false;
+  bool leaf = false;
+};
+
+namespace {
+
+constexpr int CLV_THREADS = 256;
+
+size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+
+size_t vbytes(const pgpu_lk *lk) { return lk->precision == 32 ? 4 : 8; }
+
+template <typename V> __device__ __forceinline__ V scale2(V v, int e);
+template <> __device__ __forceinline__ float scale2<float>(float v, int e) {
+  // v * 2^e, exact; e beyond a float exponent's range (a denormal maximum)
+  // takes two steps
+  if (e > 126) {
+    v *= pow2f(126);
+    e -= 126;
+  } else if (e < -126) {
+    v *= pow2f(-126);
+    e += 126;
+  }
+  return v * pow2f(e);
+}
+template <> __device__ __forceinline__ double scale2<double>(double v, int e) { return ldexp(v, e); }
+
+// Compensated sum of (s, c) over the CTA into part[blockIdx.x]; the last
+// CTA adds all partials in order into *out (times `sign`) and resets the
+// counter.
+template <int NT>
+__device__ __forceinline__ void cta_partial_and_finish(double s, double c, double2 *part,
+                                                       unsigned *counter, double *out,
+                                                       double sign) {
+  __shared__ double2 red[NT / 32];
+  __shared__ bool last;
+  warp_csum(s, c);
+  const int t = threadIdx.x, lane = t & 31;
+  if (lane == 0) red[t >> 5] = make_double2(s, c);
+  __syncthreads();
+  if (t < 32) {
+    double2 v = lane < NT / 32 ? red[lane] : make_double2(0.0, 0.0);
+    double ss = v.x, cc = v.y;
+    warp_csum(ss, cc);
+    if (lane == 0) {
+      part[blockIdx.x] = make_double2(ss, cc);
+      __threadfence();
+      last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const double tot = csum_block<NT>(part, gridDim.x);
+  if (t == 0) {
+    *out = sign * tot;
+    *counter = 0u;
+  }
+}
+
+// Leaf vectors: x[p][r][i] = code_tab[code_p][i] for every rate class.
+template <typename V>
+__global__ void __launch_bounds__(CLV_THREADS) clv_leaf_kernel(const uint8_t *codes,
+                                                               const double *tab, int n_codes,
+                                                               size_t n_pat, int S, int R,
+                                                               V *x, int32_t *ex, int *flag) {
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t row = (size_t)R * S;
+  if (g >= n_pat * row) return;
+  const size_t p = g / row;
+  const int i = (int)(g % row) % S;
+  int c = codes[p];
+  if (c >= n_codes) {
+    atomicOr(flag, PGPU_FLAG_BADCODE);
+    c = 0;
+  }
+  x[g] = (V)tab[c * S + i];
+  if (g % row == 0) ex[p] = 0;
+}
+
+struct MedArgs {
+  const void *x[3];
+  const int32_t *ex[3];
+  const void *P[3];
+  void *y;
+  int32_t *ey;
+  const double *weights;
+  double2 *part;
+  unsigned *counter;
+  double *cost;
+  size_t n_pat;
+  int n_ch, S, R, RL;
+};
+
+// y = prod_k P_k x_k, normalised per pattern.  SC: the state count at
+// compile time (4), or 0 for any S up to 64 read at run time.
+template <typename V, int SC>
+__global__ void __launch_bounds__(CLV_THREADS) clv_median_kernel(const MedArgs a) {
+  const int S = SC ? SC : a.S, R = a.R, RL = a.RL;
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t p = g / RL;
+  const int r = (int)(g % RL);
+  const bool act = p < a.n_pat && r < R;
+  const size_t off = (p * R + r) * (size_t)S;
+  V *y = static_cast<V *>(a.y);
+  V m = (V)0;
+  if (SC == 4) {
+    V acc[4] = {(V)1, (V)1, (V)1, (V)1};
+    if (act) {
+      for (int k = 0; k < a.n_ch; ++k) {
+        const V *xs = static_cast<const V *>(a.x[k]) + off;
+        const V *P = static_cast<const V *>(a.P[k]) + (size_t)r * 16;
+        V xv[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) xv[j] = xs[j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          V s = (V)0;
+#pragma unroll
+          for (int j = 0; j < 4; ++j) s = fma(__ldg(P + i * 4 + j), xv[j], s);
+          acc[i] *= s;
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) m = acc[i] > m ? acc[i] : m;
+    }
+    V mm = m;
+    for (int o = 1; o < RL; o <<= 1) {
+      const V q = __shfl_xor_sync(0xffffffffu, mm, o);
+      mm = q > mm ? q : mm;
+    }
+    const int e = frexp_exp(mm);
+    if (act) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) y[off + i] = scale2<V>(acc[i], -e);
+    }
+    m = (V)e;
+  } else {
+    if (act) {
+      for (int i = 0; i < S; ++i) {
+        V v = (V)1;
+        for (int k = 0; k < a.n_ch; ++k) {
+          const V *xs = static_cast<const V *>(a.x[k]) + off;
+          const V *P = static_cast<const V *>(a.P[k]) + ((size_t)r * S + i) * S;
+          V s = (V)0;
+          for (int j = 0; j < S; ++j) s = fma(__ldg(P + j), xs[j], s);
+          v *= s;
+        }
+        y[off + i] = v;
+        m = v > m ? v : m;
+      }
+    }
+    V mm = m;
+    for (int o = 1; o < RL; o <<= 1) {
+      const V q = __shfl_xor_sync(0xffffffffu, mm, o);
+      mm = q > mm ? q : mm;
+    }
+    const int e = frexp_exp(mm);
+    if (act)
+      for (int i = 0; i < S; ++i) y[off + i] = scale2<V>(y[off + i], -e);
+    m = (V)e;
+  }
+  // exponent bookkeeping and this node's cost, by the pattern's first lane
+  double s = 0.0, c = 0.0;
+  if (act && r == 0) {
+    const int e = (int)m;
+    int E = e;
+    for (int k = 0; k < a.n_ch; ++k) E += a.ex[k][p];
+    a.ey[p] = E;
+    const double w = a.weights ? a.weights[p] : 1.0;
+    s = w * (double)e;
+  }
+  // cost = -ln 2 * sum_p w_p e_p
+  cta_partial_and_finish<CLV_THREADS>(s, c, a.part, a.counter, a.cost, -0.69314718055994530942);
+}
+
+// root_cost: -sum_p w_p [log(sum_r probs_r sum_i pi_i x[p][r][i]) + E_p ln 2]
+// (E counts every normalisation of the subtree, the node costs only their
+// own, so the root's E is dropped here: costs + root_cost = -lnL).
+template <typename V>
+__global__ void __launch_bounds__(CLV_THREADS) clv_root_kernel(
+    const V *x, const int32_t *ex, const double *pi, const double *probs, const double *weights,
+    size_t n_pat, int S, int R, int RL, double *site_lnl, double2 *part, unsigned *counter,
+    double *out) {
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t p = g / RL;
+  const int r = (int)(g % RL);
+  const bool act = p < n_pat && r < R;
+  double v = 0.0;
+  if (act) {
+    const V *xs = x + (p * R + r) * (size_t)S;
+    for (int i = 0; i < S; ++i) v = fma(pi[i], (double)xs[i], v);
+    v *= probs[r];
+  }
+  for (int o = 1; o < RL; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  double s = 0.0, c = 0.0;
+  if (act && r == 0) {
+    const double site = log(v);
+    if (site_lnl) site_lnl[p] = site + (double)ex[p] * 0.69314718055994530942;
+    s = (weights ? weights[p] : 1.0) * site;
+  }
+  cta_partial_and_finish<CLV_THREADS>(s, c, part, counter, out, -1.0);
+}
+
+pgpu_status lk_err(pgpu_lk *lk, pgpu_status st, const char *msg) {
+  return pgpu_set_err(lk->ctx, st, "%s", msg);
+}
+
+// allocation of a handle for lk (or reuse of `reuse`'s memory)
+pgpu_status clv_alloc(pgpu_lk *lk, pgpu_clv *reuse, pgpu_clv **out) {
+  pgpu_ctx *ctx = lk->ctx;
+  if (reuse) {
+    if (reuse->lk != lk)
+      return lk_err(lk, PGPU_ERR_ARG, "likelihood: the reused node belongs to another model");
+    *out = reuse;
+    reuse->has_P = false;
+    reuse->leaf = false;
+    reuse->brlen = 0.0;
+    return PGPU_OK;
+  }
+  const size_t vb = vbytes(lk);
+  const size_t xb = al256(lk->n_pat * lk->R * lk->S * vb), eb = al256(lk->n_pat * 4),
+               pb = al256((size_t)lk->R * lk->S * lk->S * vb), sb = 256;
+  pgpu_clv *t = new (std::nothrow) pgpu_clv();
+  if (!t) return lk_err(lk, PGPU_ERR_OOM, "likelihood: host allocation failed");
+  void *mem = nullptr;
+  cudaError_t e = cudaMallocAsync(&mem, xb + eb + pb + sb, ctx->stream);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    delete t;
+    return pgpu_set_err(ctx, e == cudaErrorMemoryAllocation ? PGPU_ERR_OOM : PGPU_ERR_CUDA,
+                        "likelihood: node allocation of %zu bytes failed: %s", xb + eb + pb + sb,
+                        cudaGetErrorString(e));
+  }
+  t->lk = lk;
+  t->mem = static_cast<char *>(mem);
+  t->x = t->mem;
+  t->ex = reinterpret_cast<int32_t *>(t->mem + xb);
+  t->P = t->mem + xb + eb;
+  t->scal = reinterpret_cast<double *>(t->mem + xb + eb + pb);
+  lk->live++;
+  *out = t;
+  return PGPU_OK;
+}
+
+pgpu_status check_cta(pgpu_lk *lk) {
+  // grid of every per-pattern kernel: n_pat * RL threads
+  const size_t n_cta = std::max<size_t>((lk->n_pat * lk->RL + CLV_THREADS - 1) / CLV_THREADS, 1);
+  if (n_cta > 0x7fffffffu) return lk_err(lk, PGPU_ERR_LIMIT, "likelihood: too many patterns");
+  return PGPU_OK;
+}
+
+pgpu_status median(pgpu_lk *lk, pgpu_clv *reuse, const pgpu_clv *const *ch, int n_ch,
+                   pgpu_clv **out) {
+  if (!lk || !out) return PGPU_ERR_ARG;
+  pgpu_ctx *ctx = lk->ctx;
+  for (int k = 0; k < n_ch; ++k) {
+    if (!ch[k]) return lk_err(lk, PGPU_ERR_ARG, "likelihood: null neighbour");
+    if (ch[k]->lk != lk) return lk_err(lk, PGPU_ERR_ARG, "likelihood: neighbour of another model");
+    if (!ch[k]->has_P)
+      return lk_err(lk, PGPU_ERR_ARG,
+                    "likelihood: a neighbour has no branch length (pgpu_clv_set_brlen)");
+    if (ch[k] == reuse)
+      return lk_err(lk, PGPU_ERR_ARG, "likelihood: the reused node is also a neighbour");
+  }
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  pgpu_clv *t = nullptr;
+  PGPU_TRY(clv_alloc(lk, reuse, &t));
+  MedArgs a{};
+  for (int k = 0; k < n_ch; ++k) {
+    a.x[k] = ch[k]->x;
+    a.ex[k] = ch[k]->ex;
+    a.P[k] = ch[k]->P;
+  }
+  a.y = t->x;
+  a.ey = t->ex;
+  a.weights = lk->weights;
+  a.part = lk->part;
+  a.counter = lk->counter;
+  a.cost = t->scal;
+  a.n_pat = lk->n_pat;
+  a.n_ch = n_ch;
+  a.S = lk->S;
+  a.R = lk->R;
+  a.RL = lk->RL;
+  const unsigned grid = (unsigned)lk->n_cta;
+  if (lk->precision == 32) {
+    if (lk->S == 4) clv_median_kernel<float, 4><<<grid, CLV_THREADS, 0, ctx->stream>>>(a);
+    else clv_median_kernel<float, 0><<<grid, CLV_THREADS, 0, ctx->stream>>>(a);
+  } else {
+    if (lk->S == 4) clv_median_kernel<double, 4><<<grid, CLV_THREADS, 0, ctx->stream>>>(a);
+    else clv_median_kernel<double, 0><<<grid, CLV_THREADS, 0, ctx->stream>>>(a);
+  }
+  PGPU_TRY(pgpu_after_launch(ctx, "clv_median_kernel"));
+  *out = t;
+  return PGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+pgpu_status pgpu_lk_create(pgpu_ctx *ctx, const pgpu_model *m, const pgpu_tip_codes *codes,
+                           size_t n_pat, const double *weights, int precision, pgpu_lk **out) {
+  if (!ctx || !out) return PGPU_ERR_ARG;
+  *out = nullptr;
+  if (!m || !m->Q || !m->pi || !m->rates || !m->probs)
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "likelihood: null model field");
+  if (m->n_states < 2 || m->n_states > 64)
+    return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "likelihood: 2..64 states are supported");
+  if (m->n_rates < 1 || m->n_rates > 8)
+    return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "likelihood: 1..8 rate classes are supported");
+  if (!codes || !codes->table || codes->n_codes < 1 || codes->n_codes > 256)
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "likelihood: tip code table must have 1..256 rows");
+  if (precision != 32 && precision != 64)
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "likelihood: precision must be 32 or 64");
+  if (n_pat == 0) return pgpu_set_err(ctx, PGPU_ERR_ARG, "likelihood: no patterns");
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  pgpu_lk *lk = new (std::nothrow) pgpu_lk();
+  if (!lk) return pgpu_set_err(ctx, PGPU_ERR_OOM, "likelihood: host allocation failed");
+  lk->ctx = ctx;
+  lk->S = m->n_states;
+  lk->R = m->n_rates;
+  lk->RL = lk->R <= 1 ? 1 : lk->R <= 2 ? 2 : lk->R <= 4 ? 4 : 8;
+  lk->n_codes = codes->n_codes;
+  lk->precision = precision;
+  lk->n_pat = n_pat;
+  if (check_cta(lk) != PGPU_OK) {
+    delete lk;
+    return PGPU_ERR_LIMIT;
+  }
+  lk->n_cta = std::max<size_t>((n_pat * lk->RL + CLV_THREADS - 1) / CLV_THREADS, 1);
+  const int S = lk->S, R = lk->R;
+  const size_t SS = (size_t)S * S;
+  const size_t n_dbl = 2 * SS + 2 * S + 2 * R + (size_t)codes->n_codes * S + n_pat + SS;
+  const size_t bytes = n_dbl * 8 + 64 + lk->n_cta * sizeof(double2) + 64;
+  void *blk = nullptr;
+  cudaError_t e = cudaMalloc(&blk, bytes);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    delete lk;
+    return pgpu_set_err(ctx, PGPU_ERR_OOM, "likelihood: model allocation failed");
+  }
+  double *d = static_cast<double *>(blk);
+  lk->block = d;
+  lk->U = d;
+  lk->Ui = lk->U + SS;
+  lk->lam = lk->Ui + SS;
+  lk->pi = lk->lam + S;
+  lk->rates = lk->pi + S;
+  lk->probs = lk->rates + R;
+  lk->tab = lk->probs + R;
+  double *w = lk->tab + (size_t)codes->n_codes * S;
+  double *q = w + n_pat;
+  lk->weights = weights ? w : nullptr;
+  lk->status = reinterpret_cast<int *>(q + SS);
+  lk->counter = reinterpret_cast<unsigned *>(lk->status + 4);
+  lk->part = reinterpret_cast<double2 *>(reinterpret_cast<char *>(lk->status) + 64);
+  cudaStream_t s = ctx->stream;
+  auto fail = [&](pgpu_status st) {
+    cudaFree(blk);
+    delete lk;
+    return st;
+  };
+#define LK_CUDA(call)                                                                   \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      (void)cudaGetLastError();                                                         \
+      return fail(pgpu_set_err(ctx, PGPU_ERR_CUDA, "%s failed: %s", #call,              \
+                               cudaGetErrorString(e_)));                                \
+    }                                                                                   \
+  } while (0)
+  LK_CUDA(cudaMemcpyAsync(q, m->Q, SS * 8, cudaMemcpyHostToDevice, s));
+  LK_CUDA(cudaMemcpyAsync(lk->pi, m->pi, S * 8, cudaMemcpyHostToDevice, s));
+  LK_CUDA(cudaMemcpyAsync(lk->rates, m->rates, R * 8, cudaMemcpyHostToDevice, s));
+  LK_CUDA(cudaMemcpyAsync(lk->probs, m->probs, R * 8, cudaMemcpyHostToDevice, s));
+  LK_CUDA(cudaMemcpyAsync(lk->tab, codes->table, (size_t)codes->n_codes * S * 8,
+                          cudaMemcpyHostToDevice, s));
+  if (weights) LK_CUDA(cudaMemcpyAsync(w, weights, n_pat * 8, cudaMemcpyHostToDevice, s));
+  LK_CUDA(cudaMemsetAsync(lk->status, 0, 64, s));
+  pgpu_status st = pgpu_launch_eig(ctx, q, lk->pi, S, 1, lk->U, lk->lam, lk->Ui, lk->status);
+  if (st != PGPU_OK) return fail(st);
+  int *hst = reinterpret_cast<int *>(ctx->h_pinned);
+  LK_CUDA(cudaMemcpyAsync(hst, lk->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  LK_CUDA(cudaStreamSynchronize(s));
+#undef LK_CUDA
+  if (*hst) {
+    const int code = *hst;
+    return fail(pgpu_set_err(ctx, code,
+                             code == PGPU_ERR_NAN ? "likelihood: NaN or Inf in Q or pi"
+                             : code == PGPU_ERR_NONREVERSIBLE
+                                 ? "likelihood: Q is not reversible with respect to pi"
+                                 : "likelihood: eigendecomposition did not converge"));
+  }
+  *out = lk;
+  return PGPU_OK;
+}
+
+void pgpu_lk_destroy(pgpu_lk *lk) {
+  if (!lk) return;
+  cudaSetDevice(lk->ctx->device);
+  cudaStreamSynchronize(lk->ctx->stream);
+  cudaFree(lk->block);
+  delete lk;
+}
+
+pgpu_status pgpu_clv_leaf(pgpu_lk *lk, pgpu_clv *reuse, const uint8_t *codes, pgpu_clv **out) {
+  if (!lk || !codes || !out) return lk ? lk_err(lk, PGPU_ERR_ARG, "likelihood: null argument")
+                                       : PGPU_ERR_ARG;
+  pgpu_ctx *ctx = lk->ctx;
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  pgpu_clv *t = nullptr;
+  PGPU_TRY(clv_alloc(lk, reuse, &t));
+  // the codes are copied into the context's tip buffer; later calls on the
+  // stream are ordered after this leaf's kernel
+  void *dc;
+  PGPU_TRY(pgpu_buf(ctx, BUF_TIPS, std::max<size_t>(lk->n_pat, 16), &dc));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(dc, codes, lk->n_pat, cudaMemcpyHostToDevice, ctx->stream));
+  const size_t n = lk->n_pat * lk->R * lk->S;
+  const unsigned grid = (unsigned)((n + CLV_THREADS - 1) / CLV_THREADS);
+  if (lk->precision == 32)
+    clv_leaf_kernel<float><<<grid, CLV_THREADS, 0, ctx->stream>>>(
+        (const uint8_t *)dc, lk->tab, lk->n_codes, lk->n_pat, lk->S, lk->R, (float *)t->x, t->ex,
+        ctx->d_flag);
+  else
+    clv_leaf_kernel<double><<<grid, CLV_THREADS, 0, ctx->stream>>>(
+        (const uint8_t *)dc, lk->tab, lk->n_codes, lk->n_pat, lk->S, lk->R, (double *)t->x, t->ex,
+        ctx->d_flag);
+  PGPU_TRY(pgpu_after_launch(ctx, "clv_leaf_kernel"));
+  PGPU_CUDA(ctx, cudaMemsetAsync(t->scal, 0, sizeof(double), ctx->stream));
+  t->leaf = true;
+  *out = t;
+  return PGPU_OK;
+}
+
+pgpu_status pgpu_clv_set_brlen(pgpu_clv *t, double brlen) {
+  if (!t) return PGPU_ERR_ARG;
+  pgpu_lk *lk = t->lk;
+  pgpu_ctx *ctx = lk->ctx;
+  if (!(brlen >= 0.0) || !std::isfinite(brlen))
+    return lk_err(lk, PGPU_ERR_ARG, "likelihood: branch length must be finite and >= 0");
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  void *h, *d;
+  PGPU_TRY(pgpu_stage(ctx, sizeof(double), &h, &d));
+  *static_cast<double *>(h) = brlen;
+  PGPU_TRY(pgpu_stage_commit(ctx, sizeof(double)));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(t->scal + 1, d, sizeof(double), cudaMemcpyDeviceToDevice,
+                                 ctx->stream));
+  PGPU_TRY(pgpu_launch_compose(ctx, lk->U, lk->lam, lk->Ui, lk->S, t->scal + 1, 1, lk->rates, lk->R,
+                               lk->precision == 64 ? (double *)t->P : nullptr,
+                               lk->precision == 64 ? nullptr : (float *)t->P, false, lk->status,
+                               P32_PLAIN));
+  t->brlen = brlen;
+  t->has_P = true;
+  return PGPU_OK;
+}
+
+pgpu_status pgpu_clv_get_brlen(const pgpu_clv *t, double *brlen) {
+  if (!t || !brlen) return PGPU_ERR_ARG;
+  *brlen = t->brlen;
+  return PGPU_OK;
+}
+
+pgpu_status pgpu_clv_median1(pgpu_lk *lk, pgpu_clv *reuse, const pgpu_clv *a, pgpu_clv **out) {
+  const pgpu_clv *ch[1] = {a};
+  return median(lk, reuse, ch, 1, out);
+}
+
+pgpu_status pgpu_clv_median2(pgpu_lk *lk, pgpu_clv *reuse, const pgpu_clv *a, const pgpu_clv *b,
+                             pgpu_clv **out) {
+  const pgpu_clv *ch[2] = {a, b};
+  return median(lk, reuse, ch, 2, out);
+}
+
+pgpu_status pgpu_clv_median3(pgpu_lk *lk, pgpu_clv *reuse, const pgpu_clv *a, const pgpu_clv *b,
+                             const pgpu_clv *c, pgpu_clv **out) {
+  const pgpu_clv *ch[3] = {a, b, c};
+  return median(lk, reuse, ch, 3, out);
+}
+
+pgpu_status pgpu_clv_cost(pgpu_clv *t, double *cost) {
+  if (!t || !cost) return PGPU_ERR_ARG;
+  pgpu_ctx *ctx = t->lk->ctx;
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  double *h = reinterpret_cast<double *>(ctx->h_pinned);
+  PGPU_CUDA(ctx, cudaMemcpyAsync(h, t->scal, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  PGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  PGPU_TRY(pgpu_check_flag(ctx, "likelihood"));
+  *cost = *h;
+  return PGPU_OK;
+}
+
+pgpu_status pgpu_clv_root_cost(pgpu_clv *t, double *cost, double *site_lnl) {
+  if (!t || !cost) return PGPU_ERR_ARG;
+  pgpu_lk *lk = t->lk;
+  pgpu_ctx *ctx = lk->ctx;
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  void *dsl = nullptr;
+  if (site_lnl) PGPU_TRY(pgpu_buf(ctx, BUF_SITECOST, lk->n_pat * 8, &dsl));
+  const unsigned grid = (unsigned)lk->n_cta;
+  if (lk->precision == 32)
+    clv_root_kernel<float><<<grid, CLV_THREADS, 0, ctx->stream>>>(
+        (const float *)t->x, t->ex, lk->pi, lk->probs, lk->weights, lk->n_pat, lk->S, lk->R,
+        lk->RL, (double *)dsl, lk->part, lk->counter, t->scal + 2);
+  else
+    clv_root_kernel<double><<<grid, CLV_THREADS, 0, ctx->stream>>>(
+        (const double *)t->x, t->ex, lk->pi, lk->probs, lk->weights, lk->n_pat, lk->S, lk->R,
+        lk->RL, (double *)dsl, lk->part, lk->counter, t->scal + 2);
+  PGPU_TRY(pgpu_after_launch(ctx, "clv_root_kernel"));
+  double *h = reinterpret_cast<double *>(ctx->h_pinned);
+  PGPU_CUDA(ctx, cudaMemcpyAsync(h, t->scal + 2, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (site_lnl)
+    PGPU_CUDA(ctx, cudaMemcpyAsync(site_lnl, dsl, lk->n_pat * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  PGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  PGPU_TRY(pgpu_check_flag(ctx, "likelihood"));
+  *cost = *h;
+  return PGPU_OK;
+}
+
+void pgpu_clv_destroy(pgpu_clv *t) {
+  if (!t) return;
+  pgpu_ctx *ctx = t->lk->ctx;
+  cudaSetDevice(ctx->device);
+  cudaFreeAsync(t->mem, ctx->stream);
+  t->lk->live--;
+  delete t;
+}
+
+}  // extern "C"

@@ -29,6 +29,7 @@
 #include <cstring>
 
 #include "pgpu_internal.cuh"
+#include "forms.cuh"
 
 namespace {
 
@@ -136,6 +137,54 @@ __global__ void __launch_bounds__(256) fitch_pair64_kernel(const uint2 *__restri
     if (empty) acc += WEIGHTED ? __ldg(weights + i) : 1u;
   }
   block_add_u64(acc, count, red);
+}
+
+// NonAdditive_c.median_2 over the reference's own element types
+// (lib/nonAdditive_c.ml:1-5, 19-35): one OCaml int per character -- a state
+// set of up to 63 bits, passed sign-extended as int64, so 64-bit AND/OR give
+// OCaml's land/lor -- and a float weight per character.  Each term is
+// w_i * float(c_i), c_i = 1 where the intersection is empty, as the
+// reference forms it; the terms are summed with error-free transformations
+// (TwoSum per thread, across the warp and the CTA) into one (sum,
+// compensation) pair per CTA, which nonadd_finalize_kernel adds in CTA
+// order: deterministic, and within rounding of the exact sum whatever the
+// weights.
+constexpr int NA_THREADS = 256;
+
+__global__ void __launch_bounds__(NA_THREADS) nonadd_median_kernel(
+    const unsigned long long *__restrict__ x, const unsigned long long *__restrict__ y,
+    const double *__restrict__ w, unsigned long long *__restrict__ out, size_t n,
+    double2 *partials) {
+  __shared__ double2 red[NA_THREADS / 32];
+  double s = 0.0, c = 0.0;
+  for (size_t i = blockIdx.x * (size_t)NA_THREADS + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * NA_THREADS) {
+    const unsigned long long a = __ldg(x + i), b = __ldg(y + i);
+    const unsigned long long m = a & b;
+    const bool uni = m == 0ull;
+    out[i] = uni ? (a | b) : m;
+    const double term = __ldg(w + i) * (uni ? 1.0 : 0.0);
+    double t, e;
+    pgpu_forms::two_sum(s, term, t, e);
+    s = t;
+    c += e;
+  }
+  pgpu_forms::warp_csum(s, c);
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  if (lane == 0) red[wp] = make_double2(s, c);
+  __syncthreads();
+  if (wp == 0) {
+    double2 v = lane < NA_THREADS / 32 ? red[lane] : make_double2(0.0, 0.0);
+    double ss = v.x, cc = v.y;
+    pgpu_forms::warp_csum(ss, cc);
+    if (lane == 0) partials[blockIdx.x] = make_double2(ss, cc);
+  }
+}
+
+__global__ void __launch_bounds__(1024) nonadd_finalize_kernel(const double2 *partials, int n,
+                                                               double *out) {
+  const double v = pgpu_forms::csum_block<1024>(partials, n);
+  if (threadIdx.x == 0) out[0] = v;
 }
 
 // The whole postorder over 64-bit elements: one thread per element walks
@@ -1084,6 +1133,44 @@ extern "C" {
 pgpu_status pgpu_fitch_median2(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b, uint32_t *out,
                                size_t n_sites, int lane_bits, uint64_t *union_count) {
   return pair_host(ctx, a, b, nullptr, out, n_sites, lane_bits, union_count, 0);
+}
+
+pgpu_status pgpu_nonadditive_median2(pgpu_ctx *ctx, const int64_t *x, const int64_t *y,
+                                     const double *weights, int64_t *out, size_t n, double *cost) {
+  if (!ctx) return PGPU_ERR_ARG;
+  if (!cost || (n && (!x || !y || !weights || !out)))
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "nonadditive: null buffer");
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (n == 0) {
+    *cost = 0.0;
+    return PGPU_OK;
+  }
+  const int sms = ctx->num_sms > 0 ? ctx->num_sms : 1;
+  const size_t blocks =
+      std::min<size_t>((n + NA_THREADS - 1) / NA_THREADS, (size_t)sms * 8);
+  void *dx, *dy, *dw, *dout, *dpart, *dc;
+  PGPU_TRY(pgpu_buf(ctx, BUF_A, n * 8, &dx));
+  PGPU_TRY(pgpu_buf(ctx, BUF_B, n * 8, &dy));
+  PGPU_TRY(pgpu_buf(ctx, BUF_WEIGHTS, n * 8, &dw));
+  PGPU_TRY(pgpu_buf(ctx, BUF_OUT, n * 8, &dout));
+  PGPU_TRY(pgpu_buf(ctx, BUF_C, blocks * sizeof(double2), &dpart));
+  PGPU_TRY(pgpu_buf(ctx, BUF_SCALAR, 64, &dc));
+  cudaStream_t s = ctx->stream;
+  PGPU_CUDA(ctx, cudaMemcpyAsync(dx, x, n * 8, cudaMemcpyHostToDevice, s));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(dy, y, n * 8, cudaMemcpyHostToDevice, s));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(dw, weights, n * 8, cudaMemcpyHostToDevice, s));
+  nonadd_median_kernel<<<(unsigned)blocks, NA_THREADS, 0, s>>>(
+      (const unsigned long long *)dx, (const unsigned long long *)dy, (const double *)dw,
+      (unsigned long long *)dout, n, (double2 *)dpart);
+  PGPU_TRY(pgpu_after_launch(ctx, "nonadd_median_kernel"));
+  nonadd_finalize_kernel<<<1, 1024, 0, s>>>((const double2 *)dpart, (int)blocks, (double *)dc);
+  PGPU_TRY(pgpu_after_launch(ctx, "nonadd_finalize_kernel"));
+  double *hc = reinterpret_cast<double *>(ctx->h_pinned);
+  PGPU_CUDA(ctx, cudaMemcpyAsync(out, dout, n * 8, cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(hc, dc, 8, cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  *cost = *hc;
+  return PGPU_OK;
 }
 
 pgpu_status pgpu_fitch_median2_weighted(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b,

@@ -1,7 +1,7 @@
 """The likelihood character on the GPU: what Likelihood_c
 (lib/likelihood_c.ml:1-33, all `failwith "TODO"` in the reference) stands for.
 
-``tree_lnl`` scores a whole tree: the postorder of conditional likelihood
+``tree_lnl`` scores a whole tree in one launch (the fast path): the postorder of conditional likelihood
 vectors that Likelihood_c.median_2 would compute node by node through
 Node.Make1D.median_2 (lib/node.ml:183-198), the root likelihood that
 root_cost would take, and the weighted sum over site patterns.  ``root_cost``
@@ -64,3 +64,4 @@ def tree_lnl_dev(tree: RootedTree, model: Model, tip_codes_dev, ld_pat: int, n_p
              _native.ptr(tip_codes_dev), ld_pat, _native.ptr(weights_dev), n_pat, precision,
              _native.ptr(lnl_dev), _native.ptr(site_lnl_dev))
     del keep, keep_m, keep_c
+

@@ -61,8 +61,36 @@ def test_nonadditive_median2_weighted(ctx, orc):
     exp_states, exp_cost = orc.nonadditive_median2(x.states, y.states, x.weights)
     assert np.array_equal(r.states, exp_states)
     assert r.cost == exp_cost
-    with pytest.raises(ValueError):
-        NA.median_2(None, NA.NonAdditive([], np.full(n, 0.5), x.states), y, ctx=ctx)
+
+
+@pytest.mark.parametrize("n", [0, 1, 7, 1000, 100_003])
+def test_nonadditive_fractional_weights_and_wide_sets(ctx, orc, n):
+    """The reference's record as it is: float weights of any value and OCaml
+    int state sets up to 63 bits (negative ints included: land / lor act on
+    their bits).  States bit-exact; the cost within rounding of the exact
+    sum (math.fsum), and of the reference's own left-to-right sum."""
+    import math
+    from phylocaml_gb300 import nonadditive as NA
+    rng = np.random.default_rng(100 + n)
+    bits = rng.integers(0, 63, (n, 3))
+    xs = np.zeros(n, np.int64)
+    ys = np.zeros(n, np.int64)
+    for j in range(3):
+        xs |= np.left_shift(np.int64(1), bits[:, j].astype(np.int64))
+        ys |= np.left_shift(np.int64(1), rng.integers(0, 63, n).astype(np.int64))
+    if n > 3:
+        xs[:3] = [-1, -(2 ** 62), 2 ** 62 - 1]          # the 63-bit range's edges
+        ys[:3] = [5, 2 ** 61, -(2 ** 62)]
+    w = rng.random(n) * 10.0 + np.where(rng.random(n) < 0.1, 1e8, 0.0)
+    x = NA.NonAdditive([], w, xs)
+    y = NA.NonAdditive([], w, ys)
+    r = NA.median_2(None, x, y, ctx=ctx)
+    exp_states, seq_cost = orc.nonadditive_median2(xs, ys, w)
+    assert np.array_equal(r.states, exp_states)
+    union = (xs & ys) == 0
+    exact = math.fsum(w[union].tolist())
+    assert abs(r.cost - exact) <= 2 * np.finfo(float).eps * abs(exact)
+    assert abs(r.cost - seq_cost) <= n * np.finfo(float).eps * float(np.sum(np.abs(w)))
 
 
 def test_tree_matches_reference_fixture(ctx):

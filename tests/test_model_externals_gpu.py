@@ -112,9 +112,16 @@ def test_externals_reject_bad_matrices(ctx):
     with pytest.raises(_native.NativeError) as e:
         M.diagonalize_gtr(bad.copy(), np.zeros((4, 4)), np.zeros((4, 4)), ctx)
     assert e.value.status == 4
+    # the symmetric external reads only the lower triangle (dsyev('U') on the
+    # column-major view), so a NaN above the diagonal goes unseen, as there
+    lower = q.copy()
+    lower[2, 1] = np.nan
     with pytest.raises(_native.NativeError) as e:
-        M.diagonalize_sym(bad.copy(), np.zeros((4, 4)), ctx)
+        M.diagonalize_sym(lower, np.zeros((4, 4)), ctx)
     assert e.value.status == 4
+    u = bad.copy()
+    M.diagonalize_sym(u, np.zeros((4, 4)), ctx)
+    assert np.isfinite(u).all()
     # not reversible: a cyclic flow 0 -> 1 -> 2 -> 3 -> 0 on top of JC69
     nr = q.copy()
     for i in range(4):
