@@ -232,6 +232,38 @@ pgpu_status pgpu_tcm_tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32
                               const uint32_t *table, uint32_t *node_sets_dev,
                               uint32_t *site_cost_dev, uint64_t *total_dev);
 
+/* Cost-matrix medians for alphabets of up to 32 atomic states (the
+ * reference's fill_cm takes any BitFlag alphabet, lib/costMatrix.ml:141-166,
+ * e.g. Alphabet.aminoacids' 22 states, lib/alphabet.ml:328-343).  A table
+ * over every pair of codes no longer fits, so each node forms its medians
+ * from the TCM itself with the same rule (mode as for pgpu_tcm_tables;
+ * symmetric != 0 orders each pair's codes first, as the reference's table
+ * for a symmetric TCM is filled for i <= j and mirrored).  Sites are codes
+ * of lane_bits (8, 16 or 32) bits, one site per lane as for pgpu_fitch_tree,
+ * n_states <= lane_bits; tcm is the row-major n_states x n_states cost of
+ * atomic state i to j, each in [0, 2^25].  node_sets, site_cost and total as
+ * for pgpu_tcm_tree; a code of 0 or with bits at or above n_states returns
+ * PGPU_ERR_ARG, and a tree whose per-site cost could exceed 2^32 - 1
+ * PGPU_ERR_OVERFLOW. */
+pgpu_status pgpu_tcm_tree_wide(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
+                               const uint32_t *weights, size_t n_sites, int lane_bits,
+                               const int32_t *tcm, int n_states, int mode, int symmetric,
+                               uint32_t *node_sets, uint32_t *site_cost, uint64_t *total);
+/* Host-only (no context): the median cost and code of one pair of codes
+ * under the rule, as CostMatrix.Make's cost / assign accessors read them
+ * (lib/costMatrix.ml:192-194) for an alphabet of up to 32 states; a code of
+ * 0 or with bits at or above n_states gives INT64_MAX and 0 (the
+ * reference's inf, 0). */
+pgpu_status pgpu_tcm_median(const int32_t *tcm, int n_states, int mode, int symmetric, uint32_t i,
+                            uint32_t j, int64_t *cost, uint32_t *code);
+/* Device-pointer form, asynchronous on the context's stream (rows ld_words
+ * apart; tcm is a host array, staged). */
+pgpu_status pgpu_tcm_tree_wide_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips_dev,
+                                   size_t ld_words, const uint32_t *weights_dev, size_t n_sites,
+                                   int lane_bits, const int32_t *tcm, int n_states, int mode,
+                                   int symmetric, uint32_t *node_sets_dev, uint32_t *site_cost_dev,
+                                   uint64_t *total_dev);
+
 /* ---- substitution models and transition matrices (FP64 on the GPU) ----
  * Q is row-major, rows sum to zero, and reversible with respect to pi
  * (pi_i Q_ij = pi_j Q_ji) -- the models MlModel.create builds

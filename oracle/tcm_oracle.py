@@ -131,3 +131,36 @@ def integerized_model(P, pi, symmetric_model: bool, sigma: int = 4):
             m = P[i, j] if symmetric_model else pi[i] * P[i, j]
             out[i, j] = -int(s * np.log(m))
     return out
+
+
+def tree_cost_direct(left, right, tip_codes, tcm, mode: int, symmetric: bool, weights=None):
+    """The postorder of tree_cost for alphabets too wide for a full table:
+    each pair's median comes from ``median`` (memoised per pair of codes),
+    with a symmetric TCM's pair ordered as its table is filled (i <= j)."""
+    tcm = np.asarray(tcm)
+    S = tcm.shape[0]
+    codes = np.asarray(tip_codes, np.int64)
+    n, n_sites = codes.shape
+    node = np.zeros((n - 1, n_sites), np.int64)
+    site = np.zeros(n_sites, np.int64)
+    memo: dict = {}
+
+    def med(i: int, j: int):
+        if symmetric and i > j:
+            i, j = j, i
+        key = (i, j)
+        if key not in memo:
+            memo[key] = median(tcm, i, j, mode, S)
+        return memo[key]
+
+    def code_of(c):
+        return codes[c] if c < n else node[c - n]
+
+    for k in range(n - 1):
+        a, b = code_of(int(left[k])), code_of(int(right[k]))
+        for s in range(n_sites):
+            c, m = med(int(a[s]), int(b[s]))
+            node[k, s] = m
+            site[s] += c
+    w = np.ones(n_sites, np.int64) if weights is None else np.asarray(weights, np.int64)
+    return node, site, int(np.dot(w, site))

@@ -105,6 +105,11 @@ SIGNATURES: dict[str, tuple] = {
     "pgpu_tcm_tables": (_I, [_P, _P, _I, _I, _I, _P, _P, _P]),
     "pgpu_tcm_tree": (_I, [_P, C.POINTER(PgpuTree), _P, _P, _SZ, _P, _P, _P, _P]),
     "pgpu_tcm_tree_dev": (_I, [_P, C.POINTER(PgpuTree), _P, _SZ, _P, _SZ, _P, _P, _P, _P]),
+    "pgpu_tcm_tree_wide": (_I, [_P, C.POINTER(PgpuTree), _P, _P, _SZ, _I, _P, _I, _I, _I, _P, _P, _P]),
+    "pgpu_tcm_median": (_I, [_P, _I, _I, _I, C.c_uint32, C.c_uint32, C.POINTER(C.c_int64),
+                             C.POINTER(C.c_uint32)]),
+    "pgpu_tcm_tree_wide_dev": (_I, [_P, C.POINTER(PgpuTree), _P, _SZ, _P, _SZ, _I, _P, _I, _I, _I,
+                                    _P, _P, _P]),
     "pgpu_model_diagonalize": (_I, [_P, _P, _P, _I, _P, _P, _P]),
     "pgpu_model_compose": (_I, [_P, _P, _P, _P, _I, _P, _SZ, _P]),
     "pgpu_diagonalize_gtr": (_I, [_P, _P, _P, _P, _I]),
