@@ -366,6 +366,25 @@ pgpu_status pgpu_prune_lnl_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_
                                size_t ld_pat, const double *weights_dev, size_t n_pat,
                                int precision, double *lnl_dev, double *site_lnl_dev);
 
+/* Many models over one tree and one set of patterns in one pruning launch
+ * (lnl[v] for models[v]; every model of S = 4 states and the same number of
+ * rate classes): the 2k + 1 perturbed models of a central-difference
+ * gradient of MlModel's parameters (the hooks gen_subst_opt_func /
+ * gen_rates_opt_func / gen_prior_opt_func are a TODO in the reference,
+ * lib/mlModel.ml:822-829), or any set of candidate models.  The host form
+ * copies tip_codes and weights as pgpu_prune_lnl does and fills the host
+ * array lnl[n_models]; the device form writes lnl_dev[n_models]
+ * asynchronously. */
+pgpu_status pgpu_prune_lnl_models(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *models,
+                                  int n_models, const pgpu_tip_codes *codes,
+                                  const uint8_t *tip_codes, const double *weights, size_t n_pat,
+                                  int precision, double *lnl);
+pgpu_status pgpu_prune_lnl_models_dev(pgpu_ctx *ctx, const pgpu_tree *tree,
+                                      const pgpu_model *models, int n_models,
+                                      const pgpu_tip_codes *codes, const uint8_t *tip_codes_dev,
+                                      size_t ld_pat, const double *weights_dev, size_t n_pat,
+                                      int precision, double *lnl_dev);
+
 /* ---- Likelihood_c one node at a time (NodeData.S) ------------------------
  * The operator Node.Make1D applies per node (median_2 : m -> t option -> t
  * -> t -> t, median_1, median_3, cost, root_cost; lib/nodeData.ml:20-30),

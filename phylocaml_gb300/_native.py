@@ -120,6 +120,10 @@ SIGNATURES: dict[str, tuple] = {
                             C.POINTER(PgpuTipCodes), _P, _P, _SZ, _I, _DP, _P]),
     "pgpu_prune_lnl_dev": (_I, [_P, C.POINTER(PgpuTree), C.POINTER(PgpuModel),
                                 C.POINTER(PgpuTipCodes), _P, _SZ, _P, _SZ, _I, _P, _P]),
+    "pgpu_prune_lnl_models": (_I, [_P, C.POINTER(PgpuTree), C.POINTER(PgpuModel), _I,
+                                   C.POINTER(PgpuTipCodes), _P, _P, _SZ, _I, _P]),
+    "pgpu_prune_lnl_models_dev": (_I, [_P, C.POINTER(PgpuTree), C.POINTER(PgpuModel), _I,
+                                       C.POINTER(PgpuTipCodes), _P, _SZ, _P, _SZ, _I, _P]),
     "pgpu_lk_create": (_I, [_P, C.POINTER(PgpuModel), C.POINTER(PgpuTipCodes), _SZ, _P, _I,
                             C.POINTER(_P)]),
     "pgpu_lk_destroy": (None, [_P]),

@@ -51,6 +51,11 @@ struct PruneArgs {
   const int4 *ops;            // schedule
   const int32_t *tip_seq;
   int *flag;
+  // several models over the same tree and patterns: CTA row blockIdx.y
+  // scores model blockIdx.y, whose P blocks and tip rows lie P_stride and
+  // tab_stride bytes after the previous model's, pi and probs 4 and R
+  // doubles after, and whose partial sums follow the previous model's
+  size_t P_stride, tab_stride;
   size_t ld_pat, n_pat;
   int n_tips, n_ops, n_codes, R, NP, depth;
 };
@@ -145,8 +150,8 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
     // producer: everything step i reads goes into slot i % ST
     if (tid == 0) {
       const uint32_t code_bytes = (uint32_t)min((size_t)NP, p.ld_pat - tile0);
-      const unsigned char *Pg = static_cast<const unsigned char *>(p.P);
-      const unsigned char *Tg = static_cast<const unsigned char *>(p.tiptab);
+      const unsigned char *Pg = static_cast<const unsigned char *>(p.P) + blockIdx.y * p.P_stride;
+      const unsigned char *Tg = static_cast<const unsigned char *>(p.tiptab) + blockIdx.y * p.tab_stride;
       // step i goes into step slot i % ST; group q (steps qG .. qG + G - 1)
       // completes barrier q % NB once per pass over the ring
       int groups = 0;
@@ -316,10 +321,11 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
   // the rate classes of a pattern meet in shared memory
   double part = 0.0;
   if (ok && rate_on) {
+    const double *pi = p.pi + (size_t)blockIdx.y * 4, *probs = p.probs + (size_t)blockIdx.y * R;
     double lr = 0.0;
 #pragma unroll
-    for (int e = 0; e < 4; ++e) lr += p.pi[e] * Pol::to_d(top[e]);
-    part = p.probs[r] * lr;
+    for (int e = 0; e < 4; ++e) lr += pi[e] * Pol::to_d(top[e]);
+    part = probs[r] * lr;
   }
   xch[r][pl] = make_double2(part, (double)escale);
   asm volatile("bar.sync 1, %0;" ::"r"(NT) : "memory");
@@ -346,28 +352,30 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
     double2 v = lane < NT / 32 ? red[lane] : make_double2(0.0, 0.0);
     double ss = v.x, cc = v.y;
     warp_csum(ss, cc);
-    if (lane == 0) p.partials[blockIdx.x] = make_double2(ss, cc);
+    if (lane == 0) p.partials[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = make_double2(ss, cc);
   }
 }
 
-// Neumaier sum of the per-CTA (sum, compensation) pairs in CTA order.
+// Neumaier sum of the per-CTA (sum, compensation) pairs in CTA order, one
+// CTA per model.
 __global__ void __launch_bounds__(1024) prune_finalize_kernel(const double2 *partials, int n,
                                                              double *out) {
-  const double v = csum_block<1024>(partials, n);
-  if (threadIdx.x == 0) out[0] = v;
+  const double v = csum_block<1024>(partials + (size_t)blockIdx.x * n, n);
+  if (threadIdx.x == 0) out[blockIdx.x] = v;
 }
 
 template <typename Pol, int RT>
-pgpu_status launch_prune_rt(pgpu_ctx *ctx, PruneArgs &a, size_t n_tiles, size_t smem) {
+pgpu_status launch_prune_rt(pgpu_ctx *ctx, PruneArgs &a, size_t n_tiles, size_t smem, int n_models) {
   PGPU_CUDA(ctx, cudaFuncSetAttribute(prune_tree_kernel<Pol, RT>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)std::max<size_t>(smem, 48 * 1024)));
-  prune_tree_kernel<Pol, RT><<<(unsigned)n_tiles, 32 + PR_THREADS, smem, ctx->stream>>>(a);
+  prune_tree_kernel<Pol, RT><<<dim3((unsigned)n_tiles, (unsigned)n_models), 32 + PR_THREADS, smem,
+                               ctx->stream>>>(a);
   return pgpu_after_launch(ctx, "prune_tree_kernel");
 }
 
 template <typename Pol>
-pgpu_status launch_prune(pgpu_ctx *ctx, PruneArgs &a, int RT) {
+pgpu_status launch_prune(pgpu_ctx *ctx, PruneArgs &a, int RT, int n_models) {
   a.NP = PR_THREADS / RT;
   const size_t n_tiles = (a.n_pat + a.NP - 1) / a.NP;
   const size_t smem = PruneLayout<Pol>::bytes(a.NP, a.R, a.n_codes, a.depth);
@@ -375,10 +383,10 @@ pgpu_status launch_prune(pgpu_ctx *ctx, PruneArgs &a, int RT) {
     return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "prune: %zu bytes of shared memory needed (tree too deep)",
                         smem);
   switch (RT) {
-    case 1: return launch_prune_rt<Pol, 1>(ctx, a, n_tiles, smem);
-    case 2: return launch_prune_rt<Pol, 2>(ctx, a, n_tiles, smem);
-    case 4: return launch_prune_rt<Pol, 4>(ctx, a, n_tiles, smem);
-    default: return launch_prune_rt<Pol, 8>(ctx, a, n_tiles, smem);
+    case 1: return launch_prune_rt<Pol, 1>(ctx, a, n_tiles, smem, n_models);
+    case 2: return launch_prune_rt<Pol, 2>(ctx, a, n_tiles, smem, n_models);
+    case 4: return launch_prune_rt<Pol, 4>(ctx, a, n_tiles, smem, n_models);
+    default: return launch_prune_rt<Pol, 8>(ctx, a, n_tiles, smem, n_models);
   }
 }
 
@@ -439,7 +447,7 @@ struct Staged {
   size_t bytes;
 };
 
-Staged stage_layout(int S, int R, int n_codes, int n_br) {
+Staged stage_layout(int S, int R, int n_codes, int n_br, int V) {
   Staged s{};
   size_t off = 0;
   auto take = [&](size_t n) {
@@ -447,10 +455,10 @@ Staged stage_layout(int S, int R, int n_codes, int n_br) {
     off += align16(n * sizeof(double));
     return o;
   };
-  s.Q = (double *)take((size_t)S * S);
-  s.pi = (double *)take(S);
-  s.rates = (double *)take(R);
-  s.probs = (double *)take(R);
+  s.Q = (double *)take((size_t)V * S * S);
+  s.pi = (double *)take((size_t)V * S);
+  s.rates = (double *)take((size_t)V * R);
+  s.probs = (double *)take((size_t)V * R);
   s.tab = (double *)take((size_t)n_codes * S);
   s.brlen = (double *)take(n_br);
   s.bytes = off;
@@ -462,11 +470,23 @@ Ptr *rebase(void *base, Ptr *off) {
   return reinterpret_cast<Ptr *>(static_cast<char *>(base) + reinterpret_cast<size_t>(off));
 }
 
-pgpu_status prune_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *m,
+// Scores n_models models (same state and rate-class counts) over one tree
+// and one set of patterns: lnl_dev[v] for model v.  One eigendecomposition
+// launch for all models, a P and a tip-table build per model, then one
+// pruning launch whose CTA rows are the models.
+pgpu_status prune_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *models, int n_models,
                       const pgpu_tip_codes *codes, const uint8_t *tips, size_t ld_pat,
                       const double *weights, size_t n_pat, int precision, double *lnl_dev,
                       double *site_lnl_dev) {
-  PGPU_TRY(check_model(ctx, m, codes));
+  if (!models || n_models < 1) return pgpu_set_err(ctx, PGPU_ERR_ARG, "prune: no model");
+  if (n_models > 65535) return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "prune: at most 65,535 models per call");
+  for (int v = 0; v < n_models; ++v) {
+    PGPU_TRY(check_model(ctx, &models[v], codes));
+    if (models[v].n_rates != models[0].n_rates)
+      return pgpu_set_err(ctx, PGPU_ERR_ARG, "prune: every model needs the same number of rate classes");
+  }
+  if (n_models > 1 && site_lnl_dev)
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "prune: site log-likelihoods are for one model at a time");
   if (precision != 32 && precision != 48 && precision != 64)
     return pgpu_set_err(ctx, PGPU_ERR_ARG, "prune: precision must be 32, 48 or 64");
   if (!tree || !tree->brlen) return pgpu_set_err(ctx, PGPU_ERR_ARG, "prune: tree->brlen is required");
@@ -479,50 +499,61 @@ pgpu_status prune_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *m,
   const int4 *dops;
   const int32_t *dseq;
   PGPU_TRY(pgpu_schedule_device(ctx, tree, &sch, &dops, &dseq));
-  const int S = m->n_states, R = m->n_rates, n = tree->n_tips, n_br = 2 * n - 2;
+  const int V = n_models;
+  const int S = models[0].n_states, R = models[0].n_rates, n = tree->n_tips, n_br = 2 * n - 2;
   for (int i = 0; i < n_br; ++i)
     if (!(tree->brlen[i] >= 0.0) || !std::isfinite(tree->brlen[i]))
       return pgpu_set_err(ctx, PGPU_ERR_ARG, "prune: branch length %d is negative or not finite", i);
 
-  // stage Q, pi, rates, probs, the code table and the branch lengths
-  Staged lay = stage_layout(S, R, codes->n_codes, n_br);
+  // stage every model's Q, pi, rates, probs, then the code table and the
+  // branch lengths
+  Staged lay = stage_layout(S, R, codes->n_codes, n_br, V);
   void *h, *d;
   PGPU_TRY(pgpu_stage(ctx, lay.bytes, &h, &d));
-  std::copy(m->Q, m->Q + S * S, rebase(h, lay.Q));
-  std::copy(m->pi, m->pi + S, rebase(h, lay.pi));
-  std::copy(m->rates, m->rates + R, rebase(h, lay.rates));
-  std::copy(m->probs, m->probs + R, rebase(h, lay.probs));
+  for (int v = 0; v < V; ++v) {
+    const pgpu_model *m = &models[v];
+    std::copy(m->Q, m->Q + S * S, rebase(h, lay.Q) + (size_t)v * S * S);
+    std::copy(m->pi, m->pi + S, rebase(h, lay.pi) + (size_t)v * S);
+    std::copy(m->rates, m->rates + R, rebase(h, lay.rates) + (size_t)v * R);
+    std::copy(m->probs, m->probs + R, rebase(h, lay.probs) + (size_t)v * R);
+  }
   std::copy(codes->table, codes->table + (size_t)codes->n_codes * S, rebase(h, lay.tab));
   std::copy(tree->brlen, tree->brlen + n_br, rebase(h, lay.brlen));
   PGPU_TRY(pgpu_stage_commit(ctx, lay.bytes));
 
-  // device scratch: eigen system, P matrices, per-CTA partial sums
+  // device scratch: eigen systems, P matrices, tip rows, per-CTA partial sums
   const int RT = R <= 1 ? 1 : R <= 2 ? 2 : R <= 4 ? 4 : 8;
   const size_t n_tiles = (n_pat + (PR_THREADS / RT) - 1) / (PR_THREADS / RT);
   const size_t SS = (size_t)S * S;
   const size_t coef = precision == 32 ? 4 : 8;   // float, double, or float pair
-  const size_t p_bytes = (size_t)n_br * R * SS * coef;
-  void *deig, *dP, *dpart;
-  PGPU_TRY(pgpu_buf(ctx, BUF_H, 2 * SS * 8 + S * 8 + 64, &deig));
-  PGPU_TRY(pgpu_buf(ctx, BUF_I, p_bytes, &dP));
-  PGPU_TRY(pgpu_buf(ctx, BUF_G, std::max<size_t>(n_tiles, 1) * sizeof(double2), &dpart));
-  double *dU = (double *)deig, *dUi = dU + SS, *dlam = dUi + SS;
-  int *dst = reinterpret_cast<int *>(dlam + S);
-  PGPU_TRY(pgpu_launch_eig(ctx, rebase(d, lay.Q), rebase(d, lay.pi), S, 1, dU, dlam, dUi, dst));
-  PGPU_TRY(pgpu_launch_compose(ctx, dU, dlam, dUi, S, rebase(d, lay.brlen), n_br,
-                               rebase(d, lay.rates), R, precision == 64 ? (double *)dP : nullptr,
-                               precision == 64 ? nullptr : (float *)dP, false, dst,
-                               precision == 32 ? P32_MINUS_I : precision == 48 ? P32_PAIRS
-                                                                               : P32_PLAIN));
-  // tip rows in FP64, stored in the form's value type
-  const size_t tt_vals = (size_t)n * R * codes->n_codes * S;
-  void *dtt;
-  PGPU_TRY(pgpu_buf(ctx, BUF_J, tt_vals * (precision == 32 ? 4 : 8), &dtt));
-  PGPU_TRY(pgpu_launch_tip_table(ctx, dU, dlam, dUi, S, rebase(d, lay.brlen), n, rebase(d, lay.rates),
-                                 R, rebase(d, lay.tab), codes->n_codes, dtt,
-                                 precision == 32 ? 0 : precision == 48 ? 1 : 2, dst));
+  const size_t p_bytes = align16((size_t)n_br * R * SS * coef);
+  const size_t tt_bytes =
+      align16((size_t)n * R * codes->n_codes * S * (precision == 32 ? 4 : 8));
+  void *deig, *dP, *dpart, *dtt;
+  PGPU_TRY(pgpu_buf(ctx, BUF_H, (size_t)V * (2 * SS + S) * 8 + (size_t)V * sizeof(int) + 64, &deig));
+  PGPU_TRY(pgpu_buf(ctx, BUF_I, (size_t)V * p_bytes, &dP));
+  PGPU_TRY(pgpu_buf(ctx, BUF_G, std::max<size_t>(n_tiles, 1) * V * sizeof(double2), &dpart));
+  PGPU_TRY(pgpu_buf(ctx, BUF_J, (size_t)V * tt_bytes, &dtt));
+  double *dU = (double *)deig, *dUi = dU + V * SS, *dlam = dUi + V * SS;
+  int *dst = reinterpret_cast<int *>(dlam + (size_t)V * S);
+  PGPU_TRY(pgpu_launch_eig(ctx, rebase(d, lay.Q), rebase(d, lay.pi), S, V, dU, dlam, dUi, dst));
+  for (int v = 0; v < V; ++v) {
+    char *Pv = static_cast<char *>(dP) + (size_t)v * p_bytes;
+    PGPU_TRY(pgpu_launch_compose(ctx, dU + v * SS, dlam + (size_t)v * S, dUi + v * SS, S,
+                                 rebase(d, lay.brlen), n_br, rebase(d, lay.rates) + (size_t)v * R, R,
+                                 precision == 64 ? (double *)Pv : nullptr,
+                                 precision == 64 ? nullptr : (float *)Pv, false, dst + v,
+                                 precision == 32 ? P32_MINUS_I : precision == 48 ? P32_PAIRS
+                                                                                 : P32_PLAIN));
+    // tip rows in FP64, stored in the form's value type
+    PGPU_TRY(pgpu_launch_tip_table(ctx, dU + v * SS, dlam + (size_t)v * S, dUi + v * SS, S,
+                                   rebase(d, lay.brlen), n, rebase(d, lay.rates) + (size_t)v * R, R,
+                                   rebase(d, lay.tab), codes->n_codes,
+                                   static_cast<char *>(dtt) + (size_t)v * tt_bytes,
+                                   precision == 32 ? 0 : precision == 48 ? 1 : 2, dst + v));
+  }
   if (n_pat == 0) {
-    PGPU_CUDA(ctx, cudaMemsetAsync(lnl_dev, 0, sizeof(double), ctx->stream));
+    PGPU_CUDA(ctx, cudaMemsetAsync(lnl_dev, 0, (size_t)V * sizeof(double), ctx->stream));
     return PGPU_OK;
   }
   PruneArgs a;
@@ -538,6 +569,8 @@ pgpu_status prune_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *m,
   a.ops = dops;
   a.tip_seq = dseq;
   a.flag = ctx->d_flag;
+  a.P_stride = p_bytes;
+  a.tab_stride = tt_bytes;
   a.ld_pat = ld_pat;
   a.n_pat = n_pat;
   a.n_tips = n;
@@ -546,10 +579,10 @@ pgpu_status prune_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *m,
   a.R = R;
   a.NP = 0;
   a.depth = std::max(sch->max_depth, 1);
-  if (precision == 32) PGPU_TRY(launch_prune<Fp32>(ctx, a, RT));
-  else if (precision == 48) PGPU_TRY(launch_prune<Ff32>(ctx, a, RT));
-  else PGPU_TRY(launch_prune<Fp64>(ctx, a, RT));
-  prune_finalize_kernel<<<1, 1024, 0, ctx->stream>>>((const double2 *)dpart, (int)n_tiles, lnl_dev);
+  if (precision == 32) PGPU_TRY(launch_prune<Fp32>(ctx, a, RT, V));
+  else if (precision == 48) PGPU_TRY(launch_prune<Ff32>(ctx, a, RT, V));
+  else PGPU_TRY(launch_prune<Fp64>(ctx, a, RT, V));
+  prune_finalize_kernel<<<V, 1024, 0, ctx->stream>>>((const double2 *)dpart, (int)n_tiles, lnl_dev);
   return pgpu_after_launch(ctx, "prune_finalize_kernel");
 }
 
@@ -563,8 +596,46 @@ pgpu_status pgpu_prune_lnl_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_
                                int precision, double *lnl_dev, double *site_lnl_dev) {
   if (!ctx) return PGPU_ERR_ARG;
   PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
-  return prune_dev(ctx, tree, model, codes, tip_codes_dev, ld_pat, weights_dev, n_pat, precision,
+  return prune_dev(ctx, tree, model, 1, codes, tip_codes_dev, ld_pat, weights_dev, n_pat, precision,
                    lnl_dev, site_lnl_dev);
+}
+
+pgpu_status pgpu_prune_lnl_models_dev(pgpu_ctx *ctx, const pgpu_tree *tree,
+                                      const pgpu_model *models, int n_models,
+                                      const pgpu_tip_codes *codes, const uint8_t *tip_codes_dev,
+                                      size_t ld_pat, const double *weights_dev, size_t n_pat,
+                                      int precision, double *lnl_dev) {
+  if (!ctx) return PGPU_ERR_ARG;
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  return prune_dev(ctx, tree, models, n_models, codes, tip_codes_dev, ld_pat, weights_dev, n_pat,
+                   precision, lnl_dev, nullptr);
+}
+
+pgpu_status pgpu_prune_lnl_models(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *models,
+                                  int n_models, const pgpu_tip_codes *codes,
+                                  const uint8_t *tip_codes, const double *weights, size_t n_pat,
+                                  int precision, double *lnl) {
+  if (!ctx) return PGPU_ERR_ARG;
+  if (!tree || tree->n_tips < 2 || !tip_codes || !lnl || n_models < 1)
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "prune: null argument, no model or fewer than 2 tips");
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  const size_t n = (size_t)tree->n_tips;
+  const size_t ld = (n_pat + 15) / 16 * 16;
+  void *dt, *dw = nullptr, *dl;
+  PGPU_TRY(pgpu_buf(ctx, BUF_TIPS, std::max<size_t>(n * ld, 16), &dt));
+  PGPU_TRY(pgpu_buf(ctx, BUF_SCALAR, std::max<size_t>((size_t)n_models * 8, 64), &dl));
+  if (weights) PGPU_TRY(pgpu_buf(ctx, BUF_WEIGHTS, n_pat * 8, &dw));
+  cudaStream_t s = ctx->stream;
+  if (n_pat) {
+    PGPU_CUDA(ctx, cudaMemcpy2DAsync(dt, ld, tip_codes, n_pat, n_pat, n, cudaMemcpyHostToDevice, s));
+    if (weights) PGPU_CUDA(ctx, cudaMemcpyAsync(dw, weights, n_pat * 8, cudaMemcpyHostToDevice, s));
+  }
+  PGPU_TRY(prune_dev(ctx, tree, models, n_models, codes, (const uint8_t *)dt, ld,
+                     (const double *)dw, n_pat, precision, (double *)dl, nullptr));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(lnl, dl, (size_t)n_models * 8, cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  PGPU_TRY(pgpu_check_flag(ctx, "prune"));
+  return PGPU_OK;
 }
 
 pgpu_status pgpu_prune_lnl(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *model,
@@ -587,7 +658,7 @@ pgpu_status pgpu_prune_lnl(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_mode
     PGPU_CUDA(ctx, cudaMemcpy2DAsync(dt, ld, tip_codes, n_pat, n_pat, n, cudaMemcpyHostToDevice, s));
     if (weights) PGPU_CUDA(ctx, cudaMemcpyAsync(dw, weights, n_pat * 8, cudaMemcpyHostToDevice, s));
   }
-  PGPU_TRY(prune_dev(ctx, tree, model, codes, (const uint8_t *)dt, ld, (const double *)dw, n_pat,
+  PGPU_TRY(prune_dev(ctx, tree, model, 1, codes, (const uint8_t *)dt, ld, (const double *)dw, n_pat,
                      precision, (double *)dl, (double *)dsl));
   double *hl = reinterpret_cast<double *>(ctx->h_pinned);
   PGPU_CUDA(ctx, cudaMemcpyAsync(hl, dl, 8, cudaMemcpyDeviceToHost, s));

@@ -65,3 +65,31 @@ def tree_lnl_dev(tree: RootedTree, model: Model, tip_codes_dev, ld_pat: int, n_p
              _native.ptr(lnl_dev), _native.ptr(site_lnl_dev))
     del keep, keep_m, keep_c
 
+
+def tree_lnl_models(tree: RootedTree, models: list, tip_codes: np.ndarray, code_table: np.ndarray,
+                    weights: np.ndarray | None = None, precision: int = 64,
+                    ctx: _native.Context | None = None) -> np.ndarray:
+    """lnL of the tree under each of several models (same rate-class count),
+    all in one pruning launch (pgpu_prune_lnl_models)."""
+    ctx = ctx or _native.default_context()
+    tip_codes = np.ascontiguousarray(tip_codes, np.uint8)
+    n_pat = tip_codes.shape[1]
+    if tip_codes.shape[0] != tree.n_tips:
+        raise ValueError("one row of tip codes per tip")
+    if not models:
+        return np.zeros(0)
+    w = None if weights is None else np.ascontiguousarray(weights, np.float64)
+    t, keep = _native.make_tree(tree.left, tree.right, tree.brlen)
+    arr = (_native.PgpuModel * len(models))()
+    keep_m = []
+    for i, m in enumerate(models):
+        st, k = m.to_pgpu()
+        arr[i] = st
+        keep_m.append(k)
+    codes, keep_c = tip_code_table(code_table)
+    out = np.empty(len(models))
+    ctx.call("pgpu_prune_lnl_models", C.byref(t), arr, len(models), C.byref(codes),
+             tip_codes.ctypes.data, _native.ptr(w), n_pat, precision, out.ctypes.data)
+    del keep, keep_m, keep_c
+    return out
+

@@ -335,17 +335,26 @@ def compose_decomposed(decomp, t: float, ctx: _native.Context | None = None) -> 
     return compose_sym(u, d, t, ctx) if ui is None else compose_gtr(u, d, ui, t, ctx)
 
 
-def create(spec: Spec, ctx: _native.Context | None = None) -> Model:
-    """MlModel.create (lib/mlModel.ml:664-746)."""
+def create(spec: Spec, ctx: _native.Context | None = None, eigen: bool = True) -> Model:
+    """MlModel.create (lib/mlModel.ml:664-746).  ``eigen=False`` leaves the
+    eigen system to be solved when ``compose`` first needs it (the pruning
+    entry points solve their own on the GPU)."""
     priors = _priors(spec)
     rates, probs = _site_classes(spec)
     q, sym = substitution_matrix(spec, priors)
+    m = Model(spec, priors, rates, probs, q, None, None, None)
+    if eigen:
+        _solve(m, ctx)
+    return m
+
+
+def _solve(m: Model, ctx) -> None:
     # JC69 and K2P are symmetric (the reference diagonalises them with dsyev,
     # lib/mlmodel.c:163-197): their stationary distribution is uniform
     # whatever the priors field holds
-    eq = np.full(spec.alphabet_size, 1.0 / spec.alphabet_size) if sym else priors
-    U, lam, Ui = diagonalize(q, eq, ctx)
-    return Model(spec, priors, rates, probs, q, U, lam, Ui)
+    sym = m.spec is not None and m.spec.substitution[0] in ("JC69", "K2P")
+    eq = np.full(m.n_states, 1.0 / m.n_states) if sym else m.priors
+    m.u, m.lam, m.ui = diagonalize(m.q, eq, ctx)
 
 
 def compose(model: Model, t, ctx: _native.Context | None = None) -> np.ndarray:
@@ -356,6 +365,8 @@ def compose(model: Model, t, ctx: _native.Context | None = None) -> np.ndarray:
     ts = np.atleast_1d(np.asarray(t, np.float64))
     S = model.n_states
     out = np.empty((len(ts), S, S))
+    if model.u is None:
+        _solve(model, ctx)
     ctx.call("pgpu_model_compose", model.u.ctypes.data, model.lam.ctypes.data,
              model.ui.ctypes.data, S, ts.ctypes.data, len(ts), out.ctypes.data)
     return out[0] if np.ndim(t) == 0 else out
@@ -371,7 +382,7 @@ def compose(model: Model, t, ctx: _native.Context | None = None) -> np.ndarray:
 
 def _with(model: Model, ctx, **changes) -> Model:
     from dataclasses import replace
-    return create(replace(model.spec, **changes), ctx)
+    return create(replace(model.spec, **changes), ctx, eigen=False)
 
 
 def gen_subst_opt_func(model: Model, ctx: _native.Context | None = None):
@@ -432,32 +443,62 @@ def gen_prior_opt_func(model: Model, ctx: _native.Context | None = None):
 HOOKS = {"subst": gen_subst_opt_func, "rates": gen_rates_opt_func, "prior": gen_prior_opt_func}
 
 
-def optimize_model(model: Model, lnl_of, hooks=("subst", "rates", "prior"), rounds: int = 8,
-                   tol: float = 1e-4, ctx: _native.Context | None = None):
-    """Maximise lnl_of(model) over the hooks' parameters, one hook at a time
-    (L-BFGS with forward-difference gradients, each difference one more
-    lnL), until a round gains less than tol.  Returns (model, lnl, calls)."""
+def lnl_and_gradient(x: np.ndarray, build, lnl_many, h: float = 1e-4):
+    """lnL at a hook's parameter vector x and its central-difference gradient,
+    from one batched evaluation of the 2k + 1 models build(x), build(x +- h e_i)
+    (lnl_many: list of models -> array of lnL, e.g. likelihood.tree_lnl_models,
+    which scores them all in one pruning launch)."""
+    x = np.asarray(x, np.float64)
+    k = len(x)
+    pts = [x] + [x + h * e for e in np.eye(k)] + [x - h * e for e in np.eye(k)]
+    vals = np.asarray(lnl_many([build(p) for p in pts]), np.float64)
+    grad = (vals[1:k + 1] - vals[k + 1:]) / (2.0 * h)
+    return float(vals[0]), grad
+
+
+def optimize_model(model: Model, lnl_of=None, hooks=("subst", "rates", "prior"), rounds: int = 8,
+                   tol: float = 1e-4, ctx: _native.Context | None = None, lnl_many=None):
+    """Maximise the tree's lnL over the hooks' parameters, one hook at a time,
+    until a round gains less than tol.  Returns (model, lnl, evaluations).
+
+    With ``lnl_many`` (list of models -> array of lnL) every L-BFGS step takes
+    the lnL and its central-difference gradient from one batched evaluation
+    of 2k + 1 models (``lnl_and_gradient``); otherwise ``lnl_of`` (model ->
+    lnL) is called once per point, L-BFGS forming forward differences itself.
+    ``evaluations`` counts models scored."""
     from scipy.optimize import minimize
+    if lnl_of is None and lnl_many is None:
+        raise ValueError("optimize_model needs lnl_of or lnl_many")
     calls = 0
-    best = lnl_of(model)
+    one = lnl_of if lnl_of is not None else (lambda m: float(lnl_many([m])[0]))
+    best = one(model)
     calls += 1
     for _ in range(rounds):
         start = best
-        for h in hooks:
-            x0, build = HOOKS[h](model, ctx)
+        for hname in hooks:
+            x0, build = HOOKS[hname](model, ctx)
             if len(x0) == 0:
                 continue
-            cache = {}
+            if lnl_many is not None:
+                def fg(x):
+                    nonlocal calls
+                    calls += 2 * len(x) + 1
+                    f, g = lnl_and_gradient(x, build, lnl_many)
+                    return -f, -g
 
-            def neg(x):
-                nonlocal calls
-                key = tuple(np.round(x, 12))
-                if key not in cache:
-                    calls += 1
-                    cache[key] = -lnl_of(build(x))
-                return cache[key]
+                res = minimize(fg, x0, jac=True, method="L-BFGS-B", options={"maxiter": 60})
+            else:
+                cache = {}
 
-            res = minimize(neg, x0, method="L-BFGS-B", options={"eps": 1e-5, "maxiter": 60})
+                def neg(x):
+                    nonlocal calls
+                    key = tuple(np.round(x, 12))
+                    if key not in cache:
+                        calls += 1
+                        cache[key] = -lnl_of(build(x))
+                    return cache[key]
+
+                res = minimize(neg, x0, method="L-BFGS-B", options={"eps": 1e-5, "maxiter": 60})
             if -res.fun > best:
                 model, best = build(res.x), -res.fun
         if best - start < tol:

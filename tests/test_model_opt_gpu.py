@@ -74,3 +74,59 @@ def test_rates_hook_for_gamma_plus_invariant(ctx):
     assert moved.probs[0] > m.probs[0] and moved.rates[0] == 0.0
     one = M.create(M.Spec(("JC69",), ("DiscreteTheta", 1, 0.8, 0.15)), ctx)
     assert len(M.gen_rates_opt_func(one, ctx)[0]) == 1
+
+
+def test_many_models_in_one_launch_equal_single_calls(ctx):
+    """pgpu_prune_lnl_models gives each model exactly what pgpu_prune_lnl gives it."""
+    tr, spec, pats, w = synth.prune_workload(24, 2500, seed=31)
+    table = synth.dna_code_table()
+    base = M.create(M.Spec(spec.substitution, spec.site_variation, spec.base_priors), ctx)
+    models = [base]
+    for h in M.HOOKS.values():
+        x0, build = h(base, ctx)
+        models += [build(x0 + 0.1 * e) for e in np.eye(len(x0))]
+    for prec in (48, 64):
+        many = Lk.tree_lnl_models(tr, models, pats, table, w, prec, ctx)
+        one = np.array([Lk.tree_lnl(tr, m, pats, table, w, prec, ctx) for m in models])
+        assert np.array_equal(many, one)
+
+
+def test_batched_gradient_matches_oracle_differences(ctx, orc):
+    tr, spec, pats, w = synth.prune_workload(32, 4000, seed=32)
+    table = synth.dna_code_table()
+    m = M.create(M.Spec(("GTR", [1.2, 0.5, 1.8, 0.7, 1.3]), ("DiscreteGamma", 4, 0.7),
+                        ("Empirical", [0.28, 0.22, 0.21, 0.29])), ctx)
+
+    def many_gpu(ms):
+        return Lk.tree_lnl_models(tr, ms, pats, table, w, 64, ctx)
+
+    def many_cpu(ms):
+        return np.array([orc.prune_lnl(tr.left, tr.right, O.pmatrices(x.q, x.priors, x.rates, tr.brlen),
+                                       x.priors, x.probs, pats, table, w, n_threads=4) for x in ms])
+
+    for name, hook in M.HOOKS.items():
+        x0, build = hook(m, ctx)
+        f_g, g_g = M.lnl_and_gradient(x0, build, many_gpu)
+        f_c, g_c = M.lnl_and_gradient(x0, build, many_cpu)
+        assert abs(f_g - f_c) <= 1e-9 * abs(f_c)
+        assert np.abs(g_g - g_c).max() <= 1e-4 * max(1.0, np.abs(g_c).max()), name
+
+
+def test_ml_fit_with_batched_gradients(ctx, orc):
+    tr, spec, pats, w = synth.prune_workload(32, 6000, seed=21, mean_brlen=0.1)
+    table = synth.dna_code_table()
+
+    def many_gpu(ms):
+        return Lk.tree_lnl_models(tr, ms, pats, table, w, 48, ctx)
+
+    def cpu_lnl(m):
+        P = O.pmatrices(m.q, m.priors, m.rates, tr.brlen)
+        return orc.prune_lnl(tr.left, tr.right, P, m.priors, m.probs, pats, table, w, n_threads=4)
+
+    start = M.create(M.Spec(("GTR", [1.0] * 5), ("DiscreteGamma", 4, 1.0), "Equal"), ctx)
+    fit, best, evals = M.optimize_model(start, lnl_many=many_gpu, ctx=ctx)
+    fit_cpu, best_cpu, _ = M.optimize_model(start, cpu_lnl, ctx=ctx)
+    assert best >= float(many_gpu([start])[0]) + 10.0
+    assert abs(best - best_cpu) <= 2e-2
+    np.testing.assert_allclose(fit.spec.substitution[1], fit_cpu.spec.substitution[1], rtol=2e-2)
+    np.testing.assert_allclose(fit.priors, fit_cpu.priors, atol=2e-3)
