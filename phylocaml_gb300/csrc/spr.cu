@@ -1097,6 +1097,10 @@ struct pgpu_spr {
   TbrCutDev *tbr_cuts = nullptr;
   int4 *tbr_tiles = nullptr;
   size_t tbr_x_cap = 0, tbr_xsc_cap = 0, tbr_cuts_cap = 0, tbr_tiles_cap = 0;
+  // host copies of a TBR batch's cut and tile lists, owned by the engine so
+  // that they outlive the asynchronous copies to the device
+  std::vector<TbrCutDev> h_tbr_cuts;
+  std::vector<int4> h_tbr_tiles;
   std::vector<void *> owned;
 };
 
@@ -1399,8 +1403,12 @@ pgpu_status launch_tbr_batch(pgpu_spr *s, size_t c0, size_t c1, double *lnl_dev)
   // the batch's cuts and tiles
   const long long move0 = tp.cuts[c0].move_off;
   const long long nm = tp.cuts[c1 - 1].move_off + (long long)tp.cuts[c1 - 1].nA * tp.cuts[c1 - 1].nB - move0;
-  std::vector<TbrCutDev> cuts;
-  std::vector<int4> tiles;
+  // the lists live in the engine; a copy from pageable memory returns once
+  // its source has been staged, so the next batch may rewrite them
+  std::vector<TbrCutDev> &cuts = s->h_tbr_cuts;
+  std::vector<int4> &tiles = s->h_tbr_tiles;
+  cuts.clear();
+  tiles.clear();
   for (size_t c = c0; c < c1; ++c) {
     const TbrCut &x = tp.cuts[c];
     TbrCutDev d{};
@@ -1414,13 +1422,13 @@ pgpu_status launch_tbr_batch(pgpu_spr *s, size_t c0, size_t c1, double *lnl_dev)
     for (int j0 = 0; j0 < x.nA; j0 += TB_T)
       for (int k0 = 0; k0 < x.nB; k0 += TB_T) tiles.push_back(make_int4((int)(c - c0), j0, k0, 0));
   }
+  if (tiles.size() > 0x7fffffffu) return pgpu_set_err(s->ctx, PGPU_ERR_LIMIT, "tbr: too many tiles");
   PGPU_TRY(grow(s, &s->tbr_cuts, &s->tbr_cuts_cap, cuts.size()));
   PGPU_TRY(grow(s, &s->tbr_tiles, &s->tbr_tiles_cap, tiles.size()));
   PGPU_CUDA(s->ctx, cudaMemcpyAsync(s->tbr_cuts, cuts.data(), cuts.size() * sizeof(TbrCutDev),
                                     cudaMemcpyHostToDevice, s->ctx->stream));
   PGPU_CUDA(s->ctx, cudaMemcpyAsync(s->tbr_tiles, tiles.data(), tiles.size() * sizeof(int4),
                                     cudaMemcpyHostToDevice, s->ctx->stream));
-  if (tiles.size() > 0x7fffffffu) return pgpu_set_err(s->ctx, PGPU_ERR_LIMIT, "tbr: too many tiles");
   // pattern groups: partial sums at most 256 MB
   const int n_pblocks = (int)(s->np / TB_PB);
   const size_t budget = size_t(256) << 20;
