@@ -198,6 +198,10 @@ def bench_fitch(args, rank, world, local):
     def step():
         fitch.fitch_tree_dev(tr, tips, ld, n_sites, 4, wd, out, sc, tot, ctx=ctx)
 
+    # the launch shape (words per CTA) picked by timing candidates on these buffers
+    t_tune = time.perf_counter()
+    tile, tile_ms = fitch.autotune_tile(tr, tips, ld, n_sites, 4, wd, out, sc, tot, ctx, reps=10)
+    t_tune = time.perf_counter() - t_tune
     clocks = ClockSampler(local)
     clocks.start()
     for _ in range(args.warmup):
@@ -272,7 +276,8 @@ def bench_fitch(args, rank, world, local):
         "config": {"workload": "fitch: 1,024-taxon Yule tree, 1,000,000 DNA sites, 4-bit masks "
                                "8/word, 3% ambiguity, weights 1..8",
                    "n_tips": tr.n_tips, "n_sites": n_sites, "lane_bits": 4,
-                   "l2": "inputs (512 MB tips) exceed L2; no flush"},
+                   "l2": "inputs (512 MB tips) exceed L2; no flush",
+                   "autotune": {"tile_words": tile, "candidates_ms": tile_ms, "seconds": t_tune}},
         "parity": {"bit_exact_vs_oracle": parity, "checked_sites": check,
                    "e2e_matches_device": bool(e2e_ok)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
@@ -493,9 +498,15 @@ FP32_INSTR_PER_ROW = {32: 5, 48: 37}
 FP32_INSTR_PER_NODE = {32: 4 + 6, 48: 4 * 4 + 6}
 
 
+_PRUNE_DATA: dict = {}
+
+
 def prune_data(rank):
     from phylocaml_gb300 import synth
-    return synth.prune_workload(PRUNE_TAXA, PRUNE_SITES, seed=2 + rank, mean_brlen=PRUNE_BL)
+    if rank not in _PRUNE_DATA:
+        _PRUNE_DATA[rank] = synth.prune_workload(PRUNE_TAXA, PRUNE_SITES, seed=2 + rank,
+                                                 mean_brlen=PRUNE_BL)
+    return _PRUNE_DATA[rank]
 
 
 def prune_oracle_lnl(tr, spec, pats, w, n_threads, limit=None):
@@ -672,6 +683,121 @@ def bench_prune(args, rank, world, local):
                                "all_cores": {"cores": cores, "value": units / oracle_mt_s}}
     ctx.close()
     return rec
+
+
+def bench_clv(args, rank, world, local):
+    """Likelihood_c node by node on the pruning workload (512 taxa x 446k
+    patterns, GTR+Gamma4, float vectors): median_2 folded over the postorder
+    as Node.Make1D drives it, every node's vectors materialised in HBM.  The
+    dominant kernel, clv_median_kernel, is HBM-bound: per launch it reads two
+    children (n_pat x R x S floats and an int exponent each) and the weights
+    and writes the parent."""
+    import torch
+    from phylocaml_gb300 import _native, likelihood_c as LC, mlmodel as M, synth
+
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    tr, spec, pats, w = prune_data(rank)
+    n_pat = pats.shape[1]
+    S, R = 4, 4
+    ctx = _native.Context(local)
+    model = M.create(spec, ctx)
+    table = synth.dna_code_table()
+    lk = LC.LkModel(model, table, n_pat, w, 32, ctx)
+    stream_h = ctx.lib.pgpu_get_stream(ctx.h)
+    stream = torch.cuda.ExternalStream(stream_h, device=dev)
+    nodes, total = LC.fold_postorder(lk, tr, pats)          # warm-up, allocates every node
+    for _ in range(max(args.warmup - 1, 0)):
+        nodes, total = LC.fold_postorder(lk, tr, pats, reuse=nodes)
+    torch.cuda.synchronize(dev)
+    k = max(3, min(args.steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(k):
+        nodes, total = LC.fold_postorder(lk, tr, pats, reuse=nodes)
+    fold_s = (time.perf_counter() - t0) / k
+    # the median kernel alone: repeated median_2 of two fixed internal nodes
+    a, b = nodes[tr.n_tips], nodes[tr.n_tips + 1]
+    out = LC.median_2(lk, None, a, b)
+    launches = 200
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clk = ClockSampler(local)
+    clk.start()
+    e0.record(stream)
+    for _ in range(launches):
+        LC.median_2(lk, out, a, b)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    clocks = clk.stop()
+    per_launch_ms = e0.elapsed_time(e1) / launches
+    vec = n_pat * (R * S * 4 + 4)
+    alg_bytes = 3 * vec + 8 * n_pat
+    peaks, peak_src = load_peaks()
+    achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
+    exp = None
+    if rank == 0:
+        exp, _ = prune_oracle_lnl(tr, spec, pats, w, os.cpu_count() or 1)
+    rec = {
+        "metric": "node-site-pattern updates/s, Likelihood_c median_2 folded over the postorder",
+        "value": tr.n_internal * n_pat / fold_s, "unit": "node-site-pattern updates/s",
+        "ms_per_fold": fold_s * 1e3, "dtype": "f32 vectors, FP64 P matrices and sums",
+        "config": {"workload": "likelihood_c: the pruning workload (512 taxa, GTR+Gamma4) folded "
+                               "node by node with median_2, every node's vectors kept in HBM",
+                   "n_patterns": n_pat, "nodes_reused": True,
+                   "fold": "leaves from host codes, 511 median_2, set_brlen, 511 cost reads, root_cost"},
+        "dlnl_vs_oracle": None if exp is None else -total - exp,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "peak_source": peak_src,
+                     "algorithmic_bytes": alg_bytes,
+                     "bytes_formula": "3 x n_pat x (R*S*4 + 4) + 8 x n_pat (two children read, "
+                                      "parent written, weights)",
+                     "kernel": "clv_median_kernel<float,4>", "per_launch_ms": per_launch_ms,
+                     "traffic": profile_traffic("clv_median_kernel_446k")},
+        "clocks": clocks,
+    }
+    out.close()
+    lk.close()
+    ctx.close()
+    return rec
+
+
+def bench_mlfit(args, rank, world, local):
+    """Maximum-likelihood fit of GTR + Gamma4 + base frequencies through the
+    model hooks on a 64-taxon, 20,000-site alignment, from a JC-like start:
+    central-difference gradients from one batched launch of 2k + 1 models per
+    L-BFGS step, against the same fit with one pruning call per lnL."""
+    import torch
+    from phylocaml_gb300 import _native, likelihood as Lk, mlmodel as M, synth
+
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    tr, spec, pats, w = synth.prune_workload(64, 20000, seed=41, mean_brlen=0.1)
+    ctx = _native.Context(local)
+    table = synth.dna_code_table()
+    start = M.create(M.Spec(("GTR", [1.0] * 5), ("DiscreteGamma", 4, 1.0), "Equal"), ctx)
+
+    def many(ms):
+        return Lk.tree_lnl_models(tr, ms, pats, table, w, 48, ctx)
+
+    def one(m):
+        return Lk.tree_lnl(tr, m, pats, table, w, 48, ctx)
+
+    many([start])
+    one(start)
+    torch.cuda.synchronize(dev)
+    t = time.perf_counter()
+    fit_b, best_b, ev_b = M.optimize_model(start, lnl_many=many, ctx=ctx)
+    batched_s = time.perf_counter() - t
+    t = time.perf_counter()
+    fit_s, best_s, ev_s = M.optimize_model(start, one, ctx=ctx)
+    serial_s = time.perf_counter() - t
+    ctx.close()
+    return {"workload": "ML fit of GTR+Gamma4+frequencies, 64 taxa x 20,000 simulated sites "
+                        f"({pats.shape[1]} patterns), float-pair pruning, from GTR(1,..,1)+G(1)",
+            "batched_gradients": {"seconds": batched_s, "lnl": best_b, "models_scored": ev_b},
+            "serial_calls": {"seconds": serial_s, "lnl": best_s, "models_scored": ev_s},
+            "speedup": serial_s / batched_s if batched_s > 0 else None,
+            "dlnl_batched_minus_serial": best_b - best_s}
 
 
 def bench_prune_reference(args):
@@ -1046,7 +1172,8 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["prune", "fitch", "tcm", "batch", "spr", "all"],
+    ap.add_argument("--workload", choices=["prune", "fitch", "tcm", "batch", "spr", "clv", "mlfit",
+                                           "all"],
                     default="all")
     # smaller runs for profiler captures: a subset of the pruning forms, fewer batch variants
     ap.add_argument("--prune-forms", default="32,48,64")
@@ -1057,7 +1184,7 @@ def main():
     args.warmup = max(args.warmup, 3)
     args.prune_forms = {int(f) for f in args.prune_forms.split(",") if f}
     rank, world, local = dist_info()
-    head = args.workload if args.workload in ("fitch", "tcm", "batch", "spr") else "prune"
+    head = args.workload if args.workload in ("fitch", "tcm", "batch", "spr", "clv", "mlfit") else "prune"
 
     if args.impl == "reference":
         if rank != 0:
@@ -1082,13 +1209,21 @@ def main():
             rec["tcm"] = bench_tcm(args, rank, world, local)
             args.steps = steps_given if steps_given is not None else 3
             rec["batch"] = bench_batch(args, rank, world, local)
+            args.steps = steps_given if steps_given is not None else 10
+            rec["likelihood_c"] = bench_clv(args, rank, world, local)
             if rank == 0:
                 rec["spr"] = bench_spr(args, rank, world, local)
+                rec["ml_fit"] = bench_mlfit(args, rank, world, local)
     elif head == "batch":
         args.steps = steps_given if steps_given is not None else 3
         rec = bench_batch(args, rank, world, local)
     elif head == "spr":
         rec = bench_spr(args, rank, world, local)
+    elif head == "clv":
+        args.steps = steps_given if steps_given is not None else 10
+        rec = bench_clv(args, rank, world, local)
+    elif head == "mlfit":
+        rec = bench_mlfit(args, rank, world, local)
     elif head == "tcm":
         args.steps = steps_given if steps_given is not None else 200
         rec = bench_tcm(args, rank, world, local)

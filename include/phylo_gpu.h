@@ -157,6 +157,14 @@ pgpu_status pgpu_fitch_tree(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t
                             const uint32_t *weights, size_t n_sites, int lane_bits,
                             uint32_t *node_sets, uint32_t *site_cost, uint64_t *total);
 
+/* Launch shape of the Fitch tree kernel on this context: the words of a
+ * state-set row each CTA covers (a multiple of 4 in 32..128; 0 restores the
+ * default, 128).  Results do not depend on it; the time does, through how
+ * evenly the CTAs fall on the SMs, so an autotuner picks it by timing
+ * (fitch.autotune_tile).  No reference counterpart. */
+pgpu_status pgpu_set_fitch_tile_words(pgpu_ctx *ctx, int words);
+int pgpu_get_fitch_tile_words(const pgpu_ctx *ctx);
+
 /* Device-pointer form of pgpu_fitch_tree, asynchronous on the context's
  * stream.  Rows are ld_words apart (ld_words % 4 == 0, every pointer 16-byte
  * aligned); tree arrays are host pointers.  *total_dev is overwritten. */

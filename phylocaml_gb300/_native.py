@@ -98,6 +98,8 @@ SIGNATURES: dict[str, tuple] = {
     "pgpu_fitch_median2": (_I, [_P, _P, _P, _P, _SZ, _I, _U64P]),
     "pgpu_fitch_median2_weighted": (_I, [_P, _P, _P, _P, _P, _SZ, _I, _U64P]),
     "pgpu_fitch_distance": (_I, [_P, _P, _P, _SZ, _I, _U64P]),
+    "pgpu_set_fitch_tile_words": (_I, [_P, _I]),
+    "pgpu_get_fitch_tile_words": (_I, [_P]),
     "pgpu_nonadditive_median2": (_I, [_P, _P, _P, _P, _P, _SZ, _DP]),
     "pgpu_fitch_tree": (_I, [_P, C.POINTER(PgpuTree), _P, _P, _SZ, _I, _P, _P, _U64P]),
     "pgpu_fitch_tree_dev": (_I, [_P, C.POINTER(PgpuTree), _P, _SZ, _P, _SZ, _I, _P, _P, _P]),

@@ -528,6 +528,7 @@ struct FitchSplitArgs {
   size_t ld, n_words, n_sites;
   int32_t n_tips;
   int n_top, rows;                       // rows: ring + stack rows per warp
+  int tile_words;                        // words per CTA: 4 per active lane, <= 128
 };
 
 // one warp's region: ring [FS_P][32] then stack [rows - FS_P][32] uint4
@@ -554,13 +555,17 @@ __global__ void __launch_bounds__(FS_W * 32, 8) fitch_tree_split_kernel(const Fi
   uint32_t *sitecnt = reinterpret_cast<uint32_t *>(region + (size_t)FS_W * rows * 32);
   for (int i = tid; i < 32 * 4 * PER; i += FS_W * 32) sitecnt[i] = 0;
   __syncthreads();
-  const size_t word0 = (size_t)blockIdx.x * 128 + 4 * (size_t)lane;
-  const bool active = word0 < p.ld;
-  uint4 valid;
-  valid.x = valid_lanes<LB>(word0 + 0, p.n_sites);
-  valid.y = valid_lanes<LB>(word0 + 1, p.n_sites);
-  valid.z = valid_lanes<LB>(word0 + 2, p.n_sites);
-  valid.w = valid_lanes<LB>(word0 + 3, p.n_sites);
+  // a tile of tile_words words: lanes past it idle (their loads are
+  // zero-filled, nothing of theirs is counted or stored)
+  const size_t word0 = (size_t)blockIdx.x * p.tile_words + 4 * (size_t)lane;
+  const bool active = 4 * lane < p.tile_words && word0 < p.ld;
+  uint4 valid = make_uint4(0u, 0u, 0u, 0u);
+  if (4 * lane < p.tile_words) {
+    valid.x = valid_lanes<LB>(word0 + 0, p.n_sites);
+    valid.y = valid_lanes<LB>(word0 + 1, p.n_sites);
+    valid.z = valid_lanes<LB>(word0 + 2, p.n_sites);
+    valid.w = valid_lanes<LB>(word0 + 3, p.n_sites);
+  }
   const uint32_t *col = p.tips + (active ? word0 : 0);
   uint4 cnt = make_uint4(0, 0, 0, 0);   // LB-bit lane counters
   uint32_t since = 0;
@@ -1058,7 +1063,9 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
   if (split_smem(a.rows) > ctx->smem_optin)
     return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: tree needs a stack of %d rows; too deep",
                         a.rows);
-  const size_t tiles = (n_words + 127) / 128;
+  a.tile_words = ctx->fitch_tile_words > 0 ? ctx->fitch_tile_words : 128;
+  const size_t tiles = (n_words + a.tile_words - 1) / a.tile_words;
+  if (tiles > 0x7fffffffu) return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: too many tiles");
   cudaError_t e;
   switch (lb) {
     case 4: e = launch_split<4>(s, a, tiles); break;
@@ -1133,6 +1140,19 @@ extern "C" {
 pgpu_status pgpu_fitch_median2(pgpu_ctx *ctx, const uint32_t *a, const uint32_t *b, uint32_t *out,
                                size_t n_sites, int lane_bits, uint64_t *union_count) {
   return pair_host(ctx, a, b, nullptr, out, n_sites, lane_bits, union_count, 0);
+}
+
+pgpu_status pgpu_set_fitch_tile_words(pgpu_ctx *ctx, int words) {
+  if (!ctx) return PGPU_ERR_ARG;
+  if (words != 0 && (words < 32 || words > 128 || words % 4 != 0))
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "fitch tile: 0 or a multiple of 4 in 32..128 words (got %d)",
+                        words);
+  ctx->fitch_tile_words = words;
+  return PGPU_OK;
+}
+
+int pgpu_get_fitch_tile_words(const pgpu_ctx *ctx) {
+  return ctx && ctx->fitch_tile_words > 0 ? ctx->fitch_tile_words : 128;
 }
 
 pgpu_status pgpu_nonadditive_median2(pgpu_ctx *ctx, const int64_t *x, const int64_t *y,

@@ -92,6 +92,8 @@ struct pgpu_ctx {
   size_t stage_cap[2] = {};
   cudaEvent_t stage_ev[2] = {};
   int stage_next = 0, stage_cur = 0;
+  // words of a state-set row per CTA of the Fitch tree kernel (0: 128)
+  int fitch_tile_words = 0;
 };
 
 pgpu_status pgpu_set_err(pgpu_ctx *ctx, pgpu_status st, const char *fmt, ...);

@@ -84,3 +84,55 @@ def fitch_tree_dev(tree: RootedTree, tips_dev, ld_words: int, n_sites: int, lane
              _native.ptr(site_cost_dev), _native.ptr(total_dev))
     if keep is not None:
         keep.append(k)
+
+
+# ---- launch-shape autotuning -------------------------------------------------
+# The tree kernel gives each CTA tile_words words of every row, and all of a
+# launch's CTAs are resident at once, so the SM that holds the most tiles
+# sets the time.  128-word tiles over 125,000 words (1e6 sites at 4-bit
+# lanes) make 977 CTAs: 65 of the 152 SMs hold 7, the rest 6.  Narrower tiles
+# even that out.  Candidates are the widths whose busiest SM handles the
+# fewest words (tiles per SM rounded up, times the width), and each is timed
+# on the caller's own buffers with CUDA events; results do not depend on it.
+
+def tile_candidates(n_words_: int, n_sm: int, keep: int = 6, narrowest: int = 64) -> list[int]:
+    """Tile widths (multiples of 4 from ``narrowest`` to 128; narrower tiles
+    idle most lanes of each warp) ordered by the words the busiest SM
+    handles, the default 128 always included."""
+    cost = {}
+    for w in range(narrowest, 129, 4):
+        tiles = -(-n_words_ // w)
+        cost[w] = (-(-tiles // n_sm)) * w
+    best = sorted(cost, key=lambda w: (cost[w], -w))[:keep]
+    return sorted(set(best) | {128}, key=lambda w: (cost[w], -w))
+
+
+def autotune_tile(tree: RootedTree, tips_dev, ld_words: int, n_sites: int, lane_bits: int,
+                  weights_dev, node_sets_dev, site_cost_dev, total_dev, ctx: _native.Context,
+                  reps: int = 20, candidates=None):
+    """Times pgpu_fitch_tree_dev at each candidate tile width on the given
+    device buffers and leaves the fastest set on ``ctx``.  Returns (width,
+    {width: ms per launch})."""
+    import torch
+    dev = torch.device("cuda", ctx.device)
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    cands = candidates or tile_candidates(n_words(n_sites, lane_bits), n_sm)
+    stream = torch.cuda.ExternalStream(ctx.lib.pgpu_get_stream(ctx.h), device=dev)
+    times = {}
+    keep = []
+    for w in cands:
+        ctx.call("pgpu_set_fitch_tile_words", int(w))
+        for _ in range(3):
+            fitch_tree_dev(tree, tips_dev, ld_words, n_sites, lane_bits, weights_dev, node_sets_dev,
+                           site_cost_dev, total_dev, ctx, keep)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fitch_tree_dev(tree, tips_dev, ld_words, n_sites, lane_bits, weights_dev, node_sets_dev,
+                           site_cost_dev, total_dev, ctx, keep)
+        e1.record(stream)
+        e1.synchronize()
+        times[int(w)] = e0.elapsed_time(e1) / reps
+    best = min(times, key=lambda w: (times[w], -w))
+    ctx.call("pgpu_set_fitch_tile_words", int(best))
+    return best, times
