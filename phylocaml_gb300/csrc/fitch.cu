@@ -529,21 +529,125 @@ struct FitchSplitArgs {
   int32_t n_tips;
   int n_top, rows;                       // rows: ring + stack rows per warp
   int tile_words;                        // words per CTA: 4 per active lane, <= 128
+  const uint32_t *table;                 // cost-matrix pair table (TcmOp), else null
+  int *flag;                             // error word (TcmOp: a pair without median)
+};
+
+// The per-word operation of the segmented tree kernel, with its per-site
+// cost bookkeeping.
+//   FitchOp<LB>  the Fitch rule on LB-bit lanes; union events are counted
+//                in LB-bit lane counters (one add per word) and flushed into
+//                the CTA's per-site counts every 2^LB - 1 steps.
+//   TcmOp        a cost-matrix character on 4-bit codes (csrc/tcm.cu): one
+//                lookup per site in a pair table replicated once per lane in
+//                shared memory (entry e of lane l at [e][l], so a warp's
+//                lookups never share a bank), the cost summed per site in
+//                registers and added to the per-site counts at the end.
+template <int LB>
+struct FitchOp {
+  static constexpr int PER = Lanes<LB>::PER;
+  static constexpr uint32_t FLUSH = Lanes<LB>::FLUSH;
+  static constexpr uint32_t LSB = Lanes<LB>::H >> (LB - 1);
+  static constexpr int MIN_BLOCKS = 8;
+  static constexpr size_t EXTRA_SMEM = 0;
+  uint4 cnt;
+  uint32_t since;
+  __device__ __forceinline__ void init(const FitchSplitArgs &, uint32_t *, int) {
+    cnt = make_uint4(0, 0, 0, 0);
+    since = 0;
+  }
+  // LB-bit lane counters into the shared per-site counts
+  __device__ __forceinline__ void flush(uint32_t *sitecnt, int lane) {
+    const uint32_t c4[4] = {cnt.x, cnt.y, cnt.z, cnt.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int l = 0; l < PER; ++l) {
+        const uint32_t v = LB < 32 ? (c4[q] >> (l * LB)) & FLUSH : c4[q];
+        if (v) atomicAdd(&sitecnt[(q * PER + l) * 32 + lane], v);
+      }
+    cnt = make_uint4(0, 0, 0, 0);
+  }
+  __device__ __forceinline__ uint4 combine(const uint4 &x, const uint4 &y, const uint4 &valid,
+                                           uint32_t *sitecnt, int lane) {
+    uint4 e;
+    const uint4 med = fitch_quad<LB>(x, y, valid, e);
+    cnt.x += e.x & valid.x & LSB;
+    cnt.y += e.y & valid.y & LSB;
+    cnt.z += e.z & valid.z & LSB;
+    cnt.w += e.w & valid.w & LSB;
+    if (LB < 32 && ++since == FLUSH) {
+      flush(sitecnt, lane);
+      since = 0;
+    }
+    return med;
+  }
+  __device__ __forceinline__ void finish(const FitchSplitArgs &, uint32_t *sitecnt, int lane) {
+    flush(sitecnt, lane);
+  }
+};
+
+struct TcmOp {
+  static constexpr int PER = 8;
+  static constexpr int MIN_BLOCKS = 4;
+  static constexpr size_t EXTRA_SMEM = 256 * 32 * 4;
+  static constexpr uint32_t NONE = 0x80000000u;   // pair without a median
+  const uint32_t *tb;
+  uint32_t acc[32];
+  uint32_t none;
+  // every thread of the CTA takes part in filling the table; the kernel's
+  // barrier after init() publishes it
+  __device__ __forceinline__ void init(const FitchSplitArgs &p, uint32_t *extra, int tid) {
+    for (int i = tid; i < 256 * 32; i += FS_W * 32) extra[i] = __ldg(p.table + (i >> 5));
+    tb = extra + (tid & 31);
+#pragma unroll
+    for (int i = 0; i < 32; ++i) acc[i] = 0;
+    none = 0;
+  }
+  __device__ __forceinline__ uint32_t word(uint32_t xa, uint32_t xb, uint32_t valid, int q) {
+    // lanes past the last site read as code 1, which always has a median
+    const uint32_t fill = 0x11111111u & ~valid;
+    xa = (xa & valid) | fill;
+    xb = (xb & valid) | fill;
+    uint32_t out = 0;
+#pragma unroll
+    for (int l = 0; l < 8; ++l) {
+      const uint32_t ia = (xa >> (4 * l)) & 15u, ib = (xb >> (4 * l)) & 15u;
+      const uint32_t e = tb[((ia << 4) | ib) << 5];
+      out |= (e & 15u) << (4 * l);
+      acc[q * 8 + l] += (e >> 4) & 0x07ffffffu;
+      none |= e;
+    }
+    return out & valid;
+  }
+  __device__ __forceinline__ uint4 combine(const uint4 &x, const uint4 &y, const uint4 &valid,
+                                           uint32_t *, int) {
+    uint4 m;
+    m.x = word(x.x, y.x, valid.x, 0);
+    m.y = word(x.y, y.y, valid.y, 1);
+    m.z = word(x.z, y.z, valid.z, 2);
+    m.w = word(x.w, y.w, valid.w, 3);
+    return m;
+  }
+  __device__ __forceinline__ void finish(const FitchSplitArgs &p, uint32_t *sitecnt, int lane) {
+#pragma unroll
+    for (int i = 0; i < 32; ++i)
+      if (acc[i]) atomicAdd(&sitecnt[i * 32 + lane], acc[i]);
+    if (none & NONE) atomicOr(p.flag, PGPU_FLAG_BADCODE);
+  }
 };
 
 // one warp's region: ring [FS_P][32] then stack [rows - FS_P][32] uint4
 // (its finished segments' results at the bottom, the walk above them); after
 // the walks the rings hold the joining nodes' results, FS_W * FS_P >= FS_S
 static_assert(FS_W * FS_P >= FS_S, "joining results overlay the rings");
-__host__ __device__ inline size_t split_smem(int rows) {
-  return (size_t)FS_W * rows * 32 * 16 + 32 * 32 * 4;   // + per-site counts
+__host__ __device__ inline size_t split_smem(int rows, size_t extra = 0) {
+  return (size_t)FS_W * rows * 32 * 16 + 32 * 32 * 4 + extra;   // + per-site counts, op's own
 }
 
-template <int LB>
-__global__ void __launch_bounds__(FS_W * 32, 8) fitch_tree_split_kernel(const FitchSplitArgs p) {
-  constexpr int PER = Lanes<LB>::PER;
-  constexpr uint32_t FLUSH = Lanes<LB>::FLUSH;
-  constexpr uint32_t LSB = Lanes<LB>::H >> (LB - 1);
+template <class Op>
+__global__ void __launch_bounds__(FS_W * 32, Op::MIN_BLOCKS) tree_split_kernel(const FitchSplitArgs p) {
+  constexpr int PER = Op::PER;
   extern __shared__ __align__(128) unsigned char smem[];
   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
   const int rows = p.rows;
@@ -554,6 +658,8 @@ __global__ void __launch_bounds__(FS_W * 32, 8) fitch_tree_split_kernel(const Fi
   // work on the same words): [4 * PER][32 lanes]
   uint32_t *sitecnt = reinterpret_cast<uint32_t *>(region + (size_t)FS_W * rows * 32);
   for (int i = tid; i < 32 * 4 * PER; i += FS_W * 32) sitecnt[i] = 0;
+  Op rule;
+  rule.init(p, sitecnt + 32 * 32, tid);
   __syncthreads();
   // a tile of tile_words words: lanes past it idle (their loads are
   // zero-filled, nothing of theirs is counted or stored)
@@ -561,36 +667,12 @@ __global__ void __launch_bounds__(FS_W * 32, 8) fitch_tree_split_kernel(const Fi
   const bool active = 4 * lane < p.tile_words && word0 < p.ld;
   uint4 valid = make_uint4(0u, 0u, 0u, 0u);
   if (4 * lane < p.tile_words) {
-    valid.x = valid_lanes<LB>(word0 + 0, p.n_sites);
-    valid.y = valid_lanes<LB>(word0 + 1, p.n_sites);
-    valid.z = valid_lanes<LB>(word0 + 2, p.n_sites);
-    valid.w = valid_lanes<LB>(word0 + 3, p.n_sites);
+    valid.x = valid_lanes<32 / PER>(word0 + 0, p.n_sites);
+    valid.y = valid_lanes<32 / PER>(word0 + 1, p.n_sites);
+    valid.z = valid_lanes<32 / PER>(word0 + 2, p.n_sites);
+    valid.w = valid_lanes<32 / PER>(word0 + 3, p.n_sites);
   }
   const uint32_t *col = p.tips + (active ? word0 : 0);
-  uint4 cnt = make_uint4(0, 0, 0, 0);   // LB-bit lane counters
-  uint32_t since = 0;
-  // LB-bit lane counters into the shared per-site counts
-  auto flush = [&]() {
-    const uint32_t c4[4] = {cnt.x, cnt.y, cnt.z, cnt.w};
-#pragma unroll
-    for (int q = 0; q < 4; ++q)
-#pragma unroll
-      for (int l = 0; l < PER; ++l) {
-        const uint32_t v = LB < 32 ? (c4[q] >> (l * LB)) & FLUSH : c4[q];
-        if (v) atomicAdd(&sitecnt[(q * PER + l) * 32 + lane], v);
-      }
-    cnt = make_uint4(0, 0, 0, 0);
-  };
-  auto count = [&](const uint4 &e) {
-    cnt.x += e.x & valid.x & LSB;
-    cnt.y += e.y & valid.y & LSB;
-    cnt.z += e.z & valid.z & LSB;
-    cnt.w += e.w & valid.w & LSB;
-    if (LB < 32 && ++since == FLUSH) {
-      flush();
-      since = 0;
-    }
-  };
   auto store = [&](int k, const uint4 &med) {
     if (active) __stcs(reinterpret_cast<uint4 *>(p.node_sets + (size_t)k * p.ld + word0), med);
   };
@@ -648,9 +730,7 @@ __global__ void __launch_bounds__(FS_W * 32, 8) fitch_tree_split_kernel(const Fi
         y = ring[(consumed % FS_P) * 32 + lane];
         ++consumed;
       }
-      uint4 e;
-      const uint4 med = fitch_quad<LB>(x, y, valid, e);
-      count(e);
+      const uint4 med = rule.combine(x, y, valid, sitecnt, lane);
       // slots read this step are refilled only once their values are in use
       while (issued < consumed + FS_P) issue();
       if (top_valid) stk[(sp++) * 32 + lane] = top;
@@ -684,15 +764,13 @@ __global__ void __launch_bounds__(FS_W * 32, 8) fitch_tree_split_kernel(const Fi
           c[h] = region[((size_t)(t / FS_P) * rows + t % FS_P) * 32 + lane];
         }
       }
-      uint4 e;
-      const uint4 med = fitch_quad<LB>(c[0], c[1], valid, e);
-      count(e);
+      const uint4 med = rule.combine(c[0], c[1], valid, sitecnt, lane);
       region[((size_t)(i / FS_P) * rows + i % FS_P) * 32 + lane] = med;
       store(op.x, med);
     }
   }
   // ---- phase 3: the per-site counts, then the weighted total ----
-  flush();
+  rule.finish(p, sitecnt, lane);
   __syncthreads();
   if (w == 0) {
     unsigned long long wsum = 0;
@@ -985,14 +1063,14 @@ pgpu_status split_device(pgpu_ctx *ctx, const pgpu_tree *tree, const int4 **ops,
   return PGPU_OK;
 }
 
-template <int LB>
+template <class Op>
 cudaError_t launch_split(cudaStream_t stream, const FitchSplitArgs &a, size_t tiles) {
-  const size_t smem = split_smem(a.rows);
-  cudaError_t e = cudaFuncSetAttribute(fitch_tree_split_kernel<LB>,
+  const size_t smem = split_smem(a.rows, Op::EXTRA_SMEM);
+  cudaError_t e = cudaFuncSetAttribute(tree_split_kernel<Op>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)std::max<size_t>(smem, 48 * 1024));
   if (e != cudaSuccess) return e;
-  fitch_tree_split_kernel<LB><<<(unsigned)tiles, FS_W * 32, smem, stream>>>(a);
+  tree_split_kernel<Op><<<(unsigned)tiles, FS_W * 32, smem, stream>>>(a);
   return cudaGetLastError();
 }
 
@@ -1064,18 +1142,20 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
     return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: tree needs a stack of %d rows; too deep",
                         a.rows);
   a.tile_words = ctx->fitch_tile_words > 0 ? ctx->fitch_tile_words : 128;
+  a.table = nullptr;
+  a.flag = ctx->d_flag;
   const size_t tiles = (n_words + a.tile_words - 1) / a.tile_words;
   if (tiles > 0x7fffffffu) return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: too many tiles");
   cudaError_t e;
   switch (lb) {
-    case 4: e = launch_split<4>(s, a, tiles); break;
-    case 8: e = launch_split<8>(s, a, tiles); break;
-    case 16: e = launch_split<16>(s, a, tiles); break;
-    default: e = launch_split<32>(s, a, tiles); break;
+    case 4: e = launch_split<FitchOp<4>>(s, a, tiles); break;
+    case 8: e = launch_split<FitchOp<8>>(s, a, tiles); break;
+    case 16: e = launch_split<FitchOp<16>>(s, a, tiles); break;
+    default: e = launch_split<FitchOp<32>>(s, a, tiles); break;
   }
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
-    return pgpu_set_err(ctx, PGPU_ERR_CUDA, "launch of fitch_tree_split_kernel failed: %s",
+    return pgpu_set_err(ctx, PGPU_ERR_CUDA, "launch of tree_split_kernel failed: %s",
                         cudaGetErrorString(e));
   }
   ctx->launches++;
@@ -1083,6 +1163,48 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
 }
 
 }  // namespace
+
+// The cost-matrix postorder (csrc/tcm.cu) on the segmented schedule: 4-bit
+// codes, the packed pair table already on the device.  *launched is false
+// when the tree's stacks and the lane-replicated table do not fit one CTA's
+// shared memory; the caller then uses its single-walk kernel.
+pgpu_status pgpu_tcm_tree_split(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
+                                size_t ld, const uint32_t *weights, size_t n_sites,
+                                const uint32_t *table_dev, uint32_t *node_sets, uint32_t *site_cost,
+                                unsigned long long *total, bool *launched) {
+  *launched = false;
+  if (((uintptr_t)tips | (uintptr_t)node_sets) & 15) return PGPU_OK;
+  if (ld % 4 != 0) return PGPU_OK;
+  const size_t n_words = (n_sites + 7) / 8;
+  FitchSplitArgs a;
+  PGPU_TRY(split_device(ctx, tree, &a.ops, &a.seg, &a.top, &a.wseg, &a.tip_seq));
+  const SplitSchedule &sp = ctx->split;
+  if (split_smem(sp.rows, TcmOp::EXTRA_SMEM) > ctx->smem_optin) return PGPU_OK;
+  a.tips = tips;
+  a.weights = weights;
+  a.node_sets = node_sets;
+  a.site_cost = site_cost;
+  a.total = total;
+  a.ld = ld;
+  a.n_words = n_words;
+  a.n_sites = n_sites;
+  a.n_tips = tree->n_tips;
+  a.n_top = (int)sp.top.size();
+  a.rows = sp.rows;
+  a.tile_words = 128;
+  a.table = table_dev;
+  a.flag = ctx->d_flag;
+  const size_t tiles = (n_words + 127) / 128;
+  cudaError_t e = launch_split<TcmOp>(ctx->stream, a, tiles);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return pgpu_set_err(ctx, PGPU_ERR_CUDA, "launch of tree_split_kernel<TcmOp> failed: %s",
+                        cudaGetErrorString(e));
+  }
+  ctx->launches++;
+  *launched = true;
+  return PGPU_OK;
+}
 
 // Launches the tree kernel on device arrays the caller manages (schedule ops,
 // tip sequence, error word) on an explicit stream, without a context.  Used

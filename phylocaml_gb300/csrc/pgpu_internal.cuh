@@ -138,6 +138,14 @@ pgpu_status pgpu_build_schedule(pgpu_ctx *ctx, const pgpu_tree *tree, TreeSchedu
 pgpu_status pgpu_schedule_device(pgpu_ctx *ctx, const pgpu_tree *tree, const TreeSchedule **sch,
                                  const int4 **d_ops, const int32_t **d_tip_seq);
 
+// The cost-matrix postorder on the Fitch kernel's segmented schedule
+// (fitch.cu); *launched is false when the tree does not fit its shared
+// memory.
+pgpu_status pgpu_tcm_tree_split(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
+                                size_t ld, const uint32_t *weights, size_t n_sites,
+                                const uint32_t *table_dev, uint32_t *node_sets, uint32_t *site_cost,
+                                unsigned long long *total, bool *launched);
+
 // ---------------------------------------------------------------------------
 // device helpers: mbarrier, bulk copies, bounded waits
 // ---------------------------------------------------------------------------

@@ -376,6 +376,12 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
   PGPU_TRY(pgpu_stage_commit(ctx, 256 * sizeof(uint32_t)));
   PGPU_CUDA(ctx, cudaMemsetAsync(total, 0, sizeof(unsigned long long), ctx->stream));
   if (n_words == 0) return PGPU_OK;
+  // the segmented schedule: subtrees walked by four warps per 128-word slice
+  bool launched = false;
+  PGPU_TRY(pgpu_tcm_tree_split(ctx, tree, tips, ld, weights, n_sites,
+                               static_cast<const uint32_t *>(d), node_sets, site_cost, total,
+                               &launched));
+  if (launched) return PGPU_OK;
   TcmArgs a;
   a.tips = tips;
   a.weights = weights;
