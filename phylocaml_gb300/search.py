@@ -13,10 +13,11 @@ optimisation, so trees of equal topology end at equal lnL.
 * ``exhaustive_spr`` scores every move every round.
 * ``learned_spr`` scores every move once to train the network (the first,
   exhaustive round), then each round ranks all moves with the MLP on their
-  features and scores only the top k exactly (then the next widen*k - k
-  when none of those gains); the network keeps training on every exactly
-  scored move.  When none of them gains, it falls back to an exhaustive
-  round, so it also stops only where no move gains.
+  features and scores only the top k exactly, widening to the next ranks
+  (k, widen k, widen^2 k, ...) up to ``max_ranked`` while none of them
+  gains; the network keeps training on every exactly scored move.  When
+  none of them gains, it falls back to an exhaustive round, so it also
+  stops only where no move gains.
 """
 from __future__ import annotations
 
@@ -45,11 +46,12 @@ class SearchResult:
 
 
 def _target(dl):
-    """Training target: the lnL change, floored at -100 and scaled by 1/10.
-    Only the order of the best few moves matters; moves that lose more
-    than 100 log units are all equally useless, and the floor keeps them from
-    dominating the squared loss."""
-    return np.maximum(dl, -100.0) / 10.0
+    """Training target: asinh of the lnL change.  It keeps the order of every
+    move (no floor), is linear near zero, where the rare gaining moves lie,
+    and logarithmic in the long tail of losing ones, so moves that lose
+    hundreds of log units cannot dominate the squared loss while a gain of a
+    few units still stands well apart from a small loss."""
+    return np.arcsinh(dl)
 
 
 def exhaustive_spr(eng: SprEngine, eps: float = 1e-3, smooth_passes: int = 2,
@@ -120,7 +122,8 @@ class _Replay:
 def learned_spr(eng: SprEngine, net, k: int = 32, eps: float = 1e-3, smooth_passes: int = 2,
                 final_passes: int = 200, boot_steps: int = 1000, round_steps: int = 8, widen: int = 8,
                 batch: int = 1024, lr: float = 2e-3, seed: int = 0,
-                max_rounds: int = 10000, diag: list | None = None) -> SearchResult:
+                max_rounds: int = 10000, diag: list | None = None,
+                max_ranked: int = 4096) -> SearchResult:
     """``net`` is a phylocaml_gb300.mlp.MLP with max_batch >= batch.  With
     ``diag`` a list, one record per round is appended: how many of the
     network's picks gained, and after a fallback the number of gaining moves
@@ -193,8 +196,12 @@ def learned_spr(eng: SprEngine, net, k: int = 32, eps: float = 1e-3, smooth_pass
             order = None
             lo = 0
             gain = -np.inf
-            # the network's top k, then the next (widen - 1) k, exactly scored
-            for kk in (k, k * widen):
+            # the network's top k, then the next ranks up to max_ranked, a
+            # factor widen at a time, exactly scored
+            ladder = [k]
+            while ladder[-1] * widen <= max_ranked:
+                ladder.append(ladder[-1] * widen)
+            for kk in ladder:
                 kk = min(kk, pred.size)
                 if kk <= lo:
                     break

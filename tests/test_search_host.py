@@ -8,9 +8,12 @@ import torch
 from phylocaml_gb300 import search
 
 
-def test_target_floors_and_scales():
-    dl = np.array([-1e6, -100.0, -5.0, 0.0, 12.5])
-    np.testing.assert_allclose(search._target(dl), [-10.0, -10.0, -0.5, 0.0, 1.25])
+def test_target_keeps_order_and_resolution_near_zero():
+    dl = np.array([-1e6, -100.0, -5.0, -0.01, 0.0, 0.01, 12.5, 160.0])
+    t = search._target(dl)
+    assert np.all(np.diff(t) > 0)                       # every move keeps its order
+    np.testing.assert_allclose(t[3:6], [-0.01, 0.0, 0.01], rtol=1e-4)   # linear near 0
+    assert t[0] > -15.0 and t[-1] > 5.0                 # the tails are logarithmic
 
 
 def test_replay_ring_keeps_the_newest_rows():
