@@ -972,6 +972,29 @@ def bench_batch(args, rank, world, local):
     err = np.abs(signed)
     rel = err / np.abs(f64[ok])
     n_nonfinite_sites = int(np.sum(~np.isfinite(site_h)))
+    # the FP64 oracle (CPU) on the same sample of a few variants of each kind
+    vs_oracle = None
+    if rank == 0:
+        import oracle
+        from oracle import mlmodel_oracle as O
+        picks = [i for i in range(len(variants)) if i % 2 == 0][:4] + \
+                [i for i in range(len(variants)) if i % 2 == 1][:4]
+        rows = []
+        for i in picks:
+            v = variants[i]
+            n_use = min(v.n_pat, BATCH_SAMPLE)
+            codes = np.ascontiguousarray(v.codes[:, :n_use].cpu().numpy())
+            P = O.pmatrices(v.q, v.pi, v.rates, v.tree.brlen)
+            ref = oracle.prune_lnl(v.tree.left, v.tree.right, P, v.pi, v.probs, codes,
+                                   v.code_table, None, n_threads=os.cpu_count() or 1)
+            rows.append({"variant": i, "states": int(v.q.shape[0]), "patterns": n_use,
+                         "oracle_lnl": ref, "tf32_abs": abs(tc_sample[i] - ref),
+                         "tf32_rel": abs(tc_sample[i] - ref) / abs(ref),
+                         "fp64_form_abs": abs(f64[i] - ref)})
+        vs_oracle = {"sample_patterns_per_variant": BATCH_SAMPLE, "variants": rows,
+                     "max_tf32_abs": max(r["tf32_abs"] for r in rows),
+                     "max_tf32_rel": max(r["tf32_rel"] for r in rows),
+                     "max_fp64_form_abs": max(r["fp64_form_abs"] for r in rows)}
     peaks, peak_src = load_peaks()
     # a seconds-long step runs under the power cap: the sustained BF16 figure
     tf32_peak = peaks.get("bf16_tflops_sustained", peaks["bf16_tflops"]) / 2.0
@@ -997,6 +1020,7 @@ def bench_batch(args, rank, world, local):
                               "nonfinite_variants_tc": bad_tc[:16].tolist(),
                               "nonfinite_variants_fp64": bad_64[:16].tolist(),
                               "nonfinite_sites_tc": n_nonfinite_sites},
+        "lnl_error_vs_fp64_oracle": vs_oracle,
         "roofline": {"bound": "tensor", "achieved": flops / per_s / 1e12, "peak": tf32_peak,
                      "unit": "TFLOP/s", "frac": flops / per_s / 1e12 / tf32_peak,
                      "peak_source": f"derived: TF32 dense = half the {peak_src} sustained BF16 "
