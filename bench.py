@@ -983,7 +983,7 @@ def bench_batch(args, rank, world, local):
         for i in picks:
             v = variants[i]
             n_use = min(v.n_pat, BATCH_SAMPLE)
-            codes = np.ascontiguousarray(v.codes[:, :n_use].cpu().numpy())
+            codes = np.ascontiguousarray(v.tip_codes[:, :n_use].cpu().numpy())
             P = O.pmatrices(v.q, v.pi, v.rates, v.tree.brlen)
             ref = oracle.prune_lnl(v.tree.left, v.tree.right, P, v.pi, v.probs, codes,
                                    v.code_table, None, n_threads=os.cpu_count() or 1)
