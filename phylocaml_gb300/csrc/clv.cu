@@ -396,8 +396,19 @@ pgpu_status pgpu_lk_create(pgpu_ctx *ctx, const pgpu_model *m, const pgpu_tip_co
   lk->n_cta = std::max<size_t>((n_pat * lk->RL + CLV_THREADS - 1) / CLV_THREADS, 1);
   const int S = lk->S, R = lk->R;
   const size_t SS = (size_t)S * S;
-  const size_t n_dbl = 2 * SS + 2 * S + 2 * R + (size_t)codes->n_codes * S + n_pat + SS;
-  const size_t bytes = n_dbl * 8 + 64 + lk->n_cta * sizeof(double2) + 64;
+  // one block, every part on a 256-byte boundary (the partials are double2
+  // and must be 16-byte aligned whatever the pattern count)
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off += al256(bytes);
+    return o;
+  };
+  const size_t oU = take(SS * 8), oUi = take(SS * 8), olam = take(S * 8), opi = take(S * 8),
+               orates = take(R * 8), oprobs = take(R * 8),
+               otab = take((size_t)codes->n_codes * S * 8), ow = take(n_pat * 8), oq = take(SS * 8),
+               ost = take(64), opart = take(lk->n_cta * sizeof(double2));
+  const size_t bytes = off;
   void *blk = nullptr;
   cudaError_t e = cudaMalloc(&blk, bytes);
   if (e != cudaSuccess) {
@@ -405,21 +416,21 @@ pgpu_status pgpu_lk_create(pgpu_ctx *ctx, const pgpu_model *m, const pgpu_tip_co
     delete lk;
     return pgpu_set_err(ctx, PGPU_ERR_OOM, "likelihood: model allocation failed");
   }
-  double *d = static_cast<double *>(blk);
-  lk->block = d;
-  lk->U = d;
-  lk->Ui = lk->U + SS;
-  lk->lam = lk->Ui + SS;
-  lk->pi = lk->lam + S;
-  lk->rates = lk->pi + S;
-  lk->probs = lk->rates + R;
-  lk->tab = lk->probs + R;
-  double *w = lk->tab + (size_t)codes->n_codes * S;
-  double *q = w + n_pat;
+  char *base = static_cast<char *>(blk);
+  lk->block = reinterpret_cast<double *>(base);
+  lk->U = reinterpret_cast<double *>(base + oU);
+  lk->Ui = reinterpret_cast<double *>(base + oUi);
+  lk->lam = reinterpret_cast<double *>(base + olam);
+  lk->pi = reinterpret_cast<double *>(base + opi);
+  lk->rates = reinterpret_cast<double *>(base + orates);
+  lk->probs = reinterpret_cast<double *>(base + oprobs);
+  lk->tab = reinterpret_cast<double *>(base + otab);
+  double *w = reinterpret_cast<double *>(base + ow);
+  double *q = reinterpret_cast<double *>(base + oq);
   lk->weights = weights ? w : nullptr;
-  lk->status = reinterpret_cast<int *>(q + SS);
+  lk->status = reinterpret_cast<int *>(base + ost);
   lk->counter = reinterpret_cast<unsigned *>(lk->status + 4);
-  lk->part = reinterpret_cast<double2 *>(reinterpret_cast<char *>(lk->status) + 64);
+  lk->part = reinterpret_cast<double2 *>(base + opart);
   cudaStream_t s = ctx->stream;
   auto fail = [&](pgpu_status st) {
     cudaFree(blk);

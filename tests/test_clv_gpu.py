@@ -91,8 +91,9 @@ def test_median1_is_one_transition(ctx):
     model = M.create(spec, ctx)
     q, pi, rates, probs = synth.host_model(spec)
     table = synth.dna_code_table()
-    codes = rng.integers(1, 16, 500).astype(np.uint8)
-    lk = L.LkModel(model, table, 500, None, 64, ctx)
+    # an odd pattern count: the model block's parts stay aligned whatever n_pat is
+    codes = rng.integers(1, 16, 501).astype(np.uint8)
+    lk = L.LkModel(model, table, 501, None, 64, ctx)
     try:
         leaf = lk.leaf(codes, 0.37)
         up = L.median_1(lk, None, leaf)
