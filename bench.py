@@ -417,8 +417,8 @@ def bench_tcm(args, rank, world, local):
                    "e2e_matches_device": bool(e2e_ok)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "peak_source": peak_src,
-                     "algorithmic_bytes": alg_bytes, "traffic": profile_traffic("tcm_tree_kernel_1024x1e6"),
-                     "kernel": "tcm_tree_kernel", "per_launch_ms": per_launch_ms},
+                     "algorithmic_bytes": alg_bytes, "traffic": profile_traffic("tree_split_kernel_tcm_1024x1e6"),
+                     "kernel": "tree_split_kernel<TcmOp>", "per_launch_ms": per_launch_ms},
         "e2e": {"value": units / e2e_s, "unit": "node-site updates/s",
                 "h2d_bytes_per_step": int(words.nbytes + w.nbytes),
                 "d2h_bytes_per_step": int(pin_out.nbytes + pin_sc.nbytes + 8),
@@ -1204,7 +1204,15 @@ def main():
     ap.add_argument("--batch-variants", type=int, default=BATCH_VARIANTS)
     ap.add_argument("--spr-taxa", type=int, default=SPR_TAXA)
     ap.add_argument("--spr-sites", type=int, default=SPR_SITES)
+    # smaller pruning / Fitch workloads for profiler captures (a few GB on the device)
+    ap.add_argument("--prune-taxa", type=int, default=PRUNE_TAXA)
+    ap.add_argument("--prune-sites", type=int, default=PRUNE_SITES)
+    ap.add_argument("--fitch-taxa", type=int, default=FITCH_TAXA)
+    ap.add_argument("--fitch-sites", type=int, default=FITCH_SITES)
     args = ap.parse_args()
+    global PRUNE_TAXA, PRUNE_SITES, FITCH_TAXA, FITCH_SITES
+    PRUNE_TAXA, PRUNE_SITES = args.prune_taxa, args.prune_sites
+    FITCH_TAXA, FITCH_SITES = args.fitch_taxa, args.fitch_sites
     args.warmup = max(args.warmup, 3)
     args.prune_forms = {int(f) for f in args.prune_forms.split(",") if f}
     rank, world, local = dist_info()
