@@ -1191,6 +1191,7 @@ def bench_spr(args, rank, world, local):
     return rec
 
 def main():
+    global PRUNE_TAXA, PRUNE_SITES, FITCH_TAXA, FITCH_SITES
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None)
@@ -1210,7 +1211,6 @@ def main():
     ap.add_argument("--fitch-taxa", type=int, default=FITCH_TAXA)
     ap.add_argument("--fitch-sites", type=int, default=FITCH_SITES)
     args = ap.parse_args()
-    global PRUNE_TAXA, PRUNE_SITES, FITCH_TAXA, FITCH_SITES
     PRUNE_TAXA, PRUNE_SITES = args.prune_taxa, args.prune_sites
     FITCH_TAXA, FITCH_SITES = args.fitch_taxa, args.fitch_sites
     args.warmup = max(args.warmup, 3)
