@@ -53,7 +53,8 @@ constexpr int BT_ST = 4;           // ring slots (power of two)
 constexpr int BT_EPI_WARPS = 16;   // epilogue warps, four per TMEM lane group; thread 0 issues MMAs
 constexpr int BT_PARTS = BT_EPI_WARPS / 4;
 constexpr int BT_EPI = 32 * BT_EPI_WARPS;
-constexpr int BT_THREADS = BT_EPI + 32;   // + the producer warp
+constexpr int BT_THREADS = BT_EPI + 64;   // + the producer warp and the MMA warp
+constexpr int BT_PRODUCER = BT_EPI_WARPS, BT_MMA = BT_EPI_WARPS + 1;   // their warp indices
 constexpr int BT_TMEM_COLS = 512;
 
 struct BVar {
@@ -196,6 +197,7 @@ struct EpiIn {
   int n_tips, n_codes, S;
   uint32_t tmem, lane_base;
   int m;                     // pattern within the tile (TMEM lane)
+  int lg;                    // TMEM lane group (its four warps share a named barrier)
   bool active, last;
   const double *pi;
 };
@@ -281,15 +283,16 @@ __device__ __forceinline__ void epi_step(const BatchArgs &p, const EpiIn &in, co
     mx = t[0];
   }
   xch[PT][in.m] = mx;
-  // the exchange barrier also makes the timeout verdict uniform over the
-  // epilogue warps, so none can leave the loop alone
+  // the exchange joins only the four warps of this TMEM lane group (named
+  // barrier 2 + lg); it also makes the timeout verdict uniform over them, so
+  // the group leaves the step loop together
   {
     uint32_t all_ok;
     asm volatile(
         "{\n\t.reg .pred a, b;\n\tsetp.ne.u32 a, %1, 0;\n\t"
-        "bar.red.and.pred b, 1, %2, a;\n\tselp.u32 %0, 1, 0, b;\n\t}"
+        "bar.red.and.pred b, %2, %3, a;\n\tselp.u32 %0, 1, 0, b;\n\t}"
         : "=r"(all_ok)
-        : "r"((uint32_t)ok), "n"(BT_EPI)
+        : "r"((uint32_t)ok), "r"(2 + in.lg), "n"(4 * 32)
         : "memory");
     ok = all_ok != 0;
   }
@@ -330,10 +333,10 @@ __device__ __forceinline__ void epi_step(const BatchArgs &p, const EpiIn &in, co
 
 // Shared state of the epilogue warps.
 struct EpiShared {
-  uint64_t *full, *empty, *mma_bar;
+  uint64_t *full, *empty, *mma_bar, *stored;
   const int4 *slot_op;       // each ring slot's postorder step, written by the producer
   unsigned char *smem;
-  float (*xch)[BT_M];        // per share, lane: max entry
+  float (*xch)[BT_M];        // [2][BT_PARTS]: per step parity and share, lane: max entry
   double (*xchd)[BT_M];      // per share, lane: root likelihood
   double (*lnr)[BT_M];       // per rate class, lane: log root likelihood
   double2 *red;
@@ -341,15 +344,14 @@ struct EpiShared {
 };
 
 // Every pass and postorder step of one work item (variant, tile) with
-// compile-time shapes: thread 0 issues each step's MMAs, then the sixteen
-// warps run its epilogue.
+// compile-time shapes, for the sixteen epilogue warps: each step waits for
+// its slot and its MMAs, runs the epilogue, and after its TMEM stores every
+// warp arrives on `stored`, which the MMA warp waits for before the next
+// step's MMAs.  A pass ends with the epilogue-wide verdict on timeouts, so
+// the per-pass barriers below are reached by every warp alike.
 template <int KP, int RP>
 __device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh, const BVar &vg, const int2 wk,
                                          int tid, long long &seq, bool &ok) {
-  constexpr int NP = (KP + 15) / 16 * 16;
-  constexpr uint32_t LBO = 128, SBO = (uint32_t)(KP / 4) * 128;
-  constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NP >> 3) << 17) |
-                             ((uint32_t)(BT_M >> 4) << 24);
   const int warp = tid >> 5, lane = tid & 31;
   const int lg = warp & 3, pt = warp >> 2;
   const int m = 32 * lg + lane;   // pattern within the tile
@@ -366,6 +368,7 @@ __device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh
   in.tmem = sh.tmem;
   in.lane_base = (uint32_t)(32 * lg) << 16;
   in.m = m;
+  in.lg = lg;
   const long long pat = (long long)wk.y * BT_M + m;
   in.active = pat < vg.n_pat;
   in.pi = p.pis + vg.pi_off;
@@ -376,50 +379,6 @@ __device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh
       const int slot = (int)(seq & (BT_ST - 1));
       const uint32_t par = (uint32_t)((seq / BT_ST) & 1);
       in.sl = sh.smem + (size_t)slot * p.slot_bytes;
-      // ---- issue this step's MMAs (internal children) ----
-      if (tid == 0) {
-        const bool got = mbar_wait_bounded(&sh.full[slot], par, p.flag);
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const int4 op = sh.slot_op[slot];
-        bool any = false;
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int ch = h == 0 ? op.y : op.z;
-          if (!got || ch < in.n_tips) continue;
-          any = true;
-          const int sa = (op.w >> (8 * h)) & 0xff;
-#pragma unroll
-          for (int q = 0; q < RP; ++q) {
-            const uint32_t d_col = (uint32_t)((h * RP + q) * NP);
-            const uint32_t a_col = (uint32_t)(2 * RP * NP + (sa * RP + q) * KP);
-            const unsigned char *blk = in.sl + 256 + (size_t)(h * RP + q) * in.BB;
-#pragma unroll
-            for (int ks = 0; ks < KP / 8; ++ks) {
-              const uint64_t bd = smem_desc(blk + (size_t)ks * 2 * LBO, LBO, SBO);
-              const uint32_t accf = ks > 0 ? 1u : 0u;
-              asm volatile(
-                  "{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %4, 0;\n\t"
-                  "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, q;\n\t}" ::"r"(sh.tmem + d_col),
-                  "r"(sh.tmem + a_col + (uint32_t)(ks * 8)), "l"(bd), "r"(IDESC), "r"(accf)
-                  : "memory");
-            }
-          }
-        }
-        if (any) {
-          asm volatile(
-              "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                  su32(sh.mma_bar))
-              : "memory");
-          asm volatile(
-              "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                  su32(&sh.empty[slot]))
-              : "memory");
-        } else {
-          mbar_arrive(sh.mma_bar);
-          mbar_arrive(&sh.empty[slot]);
-        }
-      }
-      // ---- epilogue of this step ----
       bool got = mbar_wait_bounded(&sh.full[slot], par, p.flag);
       got = got && mbar_wait_bounded(sh.mma_bar, (uint32_t)(seq & 1), p.flag);
       got = __all_sync(0xffffffffu, got);
@@ -430,18 +389,33 @@ __device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const int4 op = sh.slot_op[slot];
       in.last = i == n_ops - 1;
+      // the max exchange is double-buffered by step parity: a group's next
+      // write cannot meet a read of the previous step's values
+      float(*xch)[BT_M] = sh.xch + (seq & 1) * BT_PARTS;
       // pt is warp-uniform
       switch (pt) {
-        case 0: epi_step<KP, RP, 0>(p, in, op, lane, slot, sh.empty, sh.xch, escale, ok, Lp); break;
-        case 1: epi_step<KP, RP, 1>(p, in, op, lane, slot, sh.empty, sh.xch, escale, ok, Lp); break;
-        case 2: epi_step<KP, RP, 2>(p, in, op, lane, slot, sh.empty, sh.xch, escale, ok, Lp); break;
-        default: epi_step<KP, RP, 3>(p, in, op, lane, slot, sh.empty, sh.xch, escale, ok, Lp); break;
+        case 0: epi_step<KP, RP, 0>(p, in, op, lane, slot, sh.empty, xch, escale, ok, Lp); break;
+        case 1: epi_step<KP, RP, 1>(p, in, op, lane, slot, sh.empty, xch, escale, ok, Lp); break;
+        case 2: epi_step<KP, RP, 2>(p, in, op, lane, slot, sh.empty, xch, escale, ok, Lp); break;
+        default: epi_step<KP, RP, 3>(p, in, op, lane, slot, sh.empty, xch, escale, ok, Lp); break;
       }
       asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      // every vector of this step is in TMEM before the next MMA issues
-      asm volatile("bar.sync 1, %0;" ::"n"(BT_EPI) : "memory");
+      // this warp's vectors of the step are in TMEM and its D columns read
+      __syncwarp();
+      if (lane == 0) mbar_arrive(sh.stored);
       if (!ok) break;
+    }
+    // one verdict for every epilogue warp before the barriers below
+    {
+      uint32_t all_ok;
+      asm volatile(
+          "{\n\t.reg .pred a, b;\n\tsetp.ne.u32 a, %1, 0;\n\t"
+          "bar.red.and.pred b, 1, %2, a;\n\tselp.u32 %0, 1, 0, b;\n\t}"
+          : "=r"(all_ok)
+          : "r"((uint32_t)ok), "n"(BT_EPI)
+          : "memory");
+      ok = all_ok != 0;
     }
     if (!ok) break;
     // roots of this pass's rate classes: the shares of each meet
@@ -486,6 +460,85 @@ __device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh
   asm volatile("bar.sync 1, %0;" ::"n"(BT_EPI) : "memory");
 }
 
+// The MMA warp's side of one work item: per step, once the slot is loaded
+// and the epilogue warps have stored the previous step's vectors (and read
+// its D columns), one thread issues the step's tcgen05.mma for the internal
+// children and commits them to mma_bar and the slot's empty barrier.
+template <int KP, int RP>
+__device__ __forceinline__ void mma_item(const BatchArgs &p, const EpiShared &sh, const BVar &vg,
+                                         long long &seq, bool &ok) {
+  constexpr int NP = (KP + 15) / 16 * 16;
+  constexpr uint32_t LBO = 128, SBO = (uint32_t)(KP / 4) * 128;
+  constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NP >> 3) << 17) |
+                             ((uint32_t)(BT_M >> 4) << 24);
+  const int n_ops = vg.n_ops, R = vg.R, n_tips = vg.n_tips, BB = blk_bytes(vg);
+  for (int r0 = 0; r0 < R && ok; r0 += RP) {
+    for (int i = 0; i < n_ops; ++i, ++seq) {
+      const int slot = (int)(seq & (BT_ST - 1));
+      const uint32_t par = (uint32_t)((seq / BT_ST) & 1);
+      bool got = mbar_wait_bounded(&sh.full[slot], par, p.flag);
+      if (seq > 0) got = got && mbar_wait_bounded(sh.stored, (uint32_t)((seq - 1) & 1), p.flag);
+      if (!got) {
+        ok = false;
+        atomicOr(p.flag, PGPU_FLAG_TIMEOUT);
+        return;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int4 op = sh.slot_op[slot];
+      const unsigned char *sl = sh.smem + (size_t)slot * p.slot_bytes;
+      bool any = false;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int ch = h == 0 ? op.y : op.z;
+        if (ch < n_tips) continue;
+        any = true;
+        const int sa = (op.w >> (8 * h)) & 0xff;
+#pragma unroll
+        for (int q = 0; q < RP; ++q) {
+          const uint32_t d_col = (uint32_t)((h * RP + q) * NP);
+          const uint32_t a_col = (uint32_t)(2 * RP * NP + (sa * RP + q) * KP);
+          const unsigned char *blk = sl + 256 + (size_t)(h * RP + q) * BB;
+#pragma unroll
+          for (int ks = 0; ks < KP / 8; ++ks) {
+            const uint64_t bd = smem_desc(blk + (size_t)ks * 2 * LBO, LBO, SBO);
+            const uint32_t accf = ks > 0 ? 1u : 0u;
+            asm volatile(
+                "{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %4, 0;\n\t"
+                "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, q;\n\t}" ::"r"(sh.tmem + d_col),
+                "r"(sh.tmem + a_col + (uint32_t)(ks * 8)), "l"(bd), "r"(IDESC), "r"(accf)
+                : "memory");
+          }
+        }
+      }
+      if (any) {
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                su32(sh.mma_bar))
+            : "memory");
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                su32(&sh.empty[slot]))
+            : "memory");
+      } else {
+        mbar_arrive(sh.mma_bar);
+        mbar_arrive(&sh.empty[slot]);
+      }
+    }
+  }
+}
+
+template <int KP>
+__device__ __forceinline__ void mma_item_rp(const BatchArgs &p, const EpiShared &sh, const BVar &vg,
+                                            long long &seq, bool &ok) {
+  if constexpr (KP <= 32) {
+    if (vg.RP == 2) {
+      mma_item<KP, 2>(p, sh, vg, seq, ok);
+      return;
+    }
+  }
+  mma_item<KP, 1>(p, sh, vg, seq, ok);
+}
+
 template <int KP>
 __device__ __forceinline__ void epi_item_rp(const BatchArgs &p, const EpiShared &sh, const BVar &vg,
                                             const int2 wk, int tid, long long &seq, bool &ok) {
@@ -500,10 +553,10 @@ __device__ __forceinline__ void epi_item_rp(const BatchArgs &p, const EpiShared 
 
 __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs p) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ uint64_t full[BT_ST], empty[BT_ST], mma_bar;
+  __shared__ uint64_t full[BT_ST], empty[BT_ST], mma_bar, stored;
   __shared__ int4 slot_op[BT_ST];
   __shared__ uint32_t tmem_base;
-  __shared__ float xch[BT_PARTS][BT_M];     // per share, lane: max entry
+  __shared__ float xch[2 * BT_PARTS][BT_M];   // per step parity and share, lane: max entry
   __shared__ double xchd[BT_PARTS][BT_M];   // per share, lane: root likelihood
   __shared__ double lnr[4][BT_M];           // per rate class, lane: log root likelihood
   __shared__ double2 red[4];
@@ -521,6 +574,7 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
       mbar_init(&empty[s], 1 + BT_EPI_WARPS);   // the MMA commit + the epilogue warps
     }
     mbar_init(&mma_bar, 1);
+    mbar_init(&stored, BT_EPI_WARPS);   // each epilogue warp, after a step's TMEM stores
     fence_mbarrier_init();
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -528,7 +582,8 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
 
-  if (warp == BT_EPI_WARPS) {
+  const EpiShared sh{full, empty, &mma_bar, &stored, slot_op, smem, xch, xchd, lnr, red, tmem};
+  if (warp == BT_PRODUCER) {
     // ------------------------------------------------------------ producer
     if (lane == 0) {
       long long seq = 0;
@@ -581,12 +636,32 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
       for (long long s = seq - BT_ST; s < seq; ++s)
         if (s >= 0) (void)mbar_wait_bounded(&full[s & (BT_ST - 1)], (uint32_t)((s / BT_ST) & 1), p.flag);
     }
+  } else if (warp == BT_MMA) {
+    // ------------------------------------------------------------ MMA issue
+    if (lane == 0) {
+      long long seq = 0;
+      bool ok = true;
+      for (long long w = blockIdx.x; w < p.n_work && ok; w += gridDim.x) {
+        const int2 wk = __ldg(p.work + w);
+        const BVar &v = p.vars[wk.x];
+        switch (v.Kp) {
+          case 8: mma_item_rp<8>(p, sh, v, seq, ok); break;
+          case 16: mma_item_rp<16>(p, sh, v, seq, ok); break;
+          case 24: mma_item_rp<24>(p, sh, v, seq, ok); break;
+          case 32: mma_item_rp<32>(p, sh, v, seq, ok); break;
+          case 40: mma_item_rp<40>(p, sh, v, seq, ok); break;
+          case 48: mma_item_rp<48>(p, sh, v, seq, ok); break;
+          case 56: mma_item_rp<56>(p, sh, v, seq, ok); break;
+          default: mma_item_rp<64>(p, sh, v, seq, ok); break;
+        }
+      }
+      // the last MMAs finish before TMEM is released
+      if (seq > 0) (void)mbar_wait_bounded(&mma_bar, (uint32_t)((seq - 1) & 1), p.flag);
+    }
   } else {
     // ------------------------------------------------------------ epilogue
     // warp w: TMEM lanes 32 (w % 4) .. 32 (w % 4) + 31, share w / 4 of the
-    // row.  Thread 0 also issues every step's MMAs, right after the previous
-    // step's vectors are in TMEM.
-    const EpiShared sh{full, empty, &mma_bar, slot_op, smem, xch, xchd, lnr, red, tmem};
+    // row.
     long long seq = 0;
     bool ok = true;
     for (long long w = blockIdx.x; w < p.n_work && ok; w += gridDim.x) {
@@ -603,8 +678,6 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
         default: epi_item_rp<64>(p, sh, v, wk, tid, seq, ok); break;
       }
     }
-    // the last MMAs finish before TMEM is released
-    if (tid == 0 && seq > 0) (void)mbar_wait_bounded(&mma_bar, (uint32_t)((seq - 1) & 1), p.flag);
   }
 
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
