@@ -441,6 +441,10 @@ pgpu_status pgpu_clv_median2(pgpu_lk *lk, pgpu_clv *reuse, const pgpu_clv *a, co
 pgpu_status pgpu_clv_median3(pgpu_lk *lk, pgpu_clv *reuse, const pgpu_clv *a, const pgpu_clv *b,
                              const pgpu_clv *c, pgpu_clv **out);
 pgpu_status pgpu_clv_cost(pgpu_clv *t, double *cost);
+/* The costs of n nodes of one pgpu_lk at once (costs[i] of nodes[i]), with
+ * one synchronisation: what Node.Make1D's sum over a tree's nodes needs
+ * (lib/node.ml:191). */
+pgpu_status pgpu_clv_costs(pgpu_lk *lk, const pgpu_clv *const *nodes, size_t n, double *costs);
 /* site_lnl (host [n_pat], or NULL) receives each pattern's lnL at this
  * root. */
 pgpu_status pgpu_clv_root_cost(pgpu_clv *t, double *cost, double *site_lnl);

@@ -136,6 +136,7 @@ SIGNATURES: dict[str, tuple] = {
     "pgpu_clv_median2": (_I, [_P, _P, _P, _P, C.POINTER(_P)]),
     "pgpu_clv_median3": (_I, [_P, _P, _P, _P, _P, C.POINTER(_P)]),
     "pgpu_clv_cost": (_I, [_P, _DP]),
+    "pgpu_clv_costs": (_I, [_P, _P, _SZ, _P]),
     "pgpu_clv_root_cost": (_I, [_P, _DP, _P]),
     "pgpu_clv_destroy": (None, [_P]),
     "pgpu_batch_create": (_I, [_P, C.POINTER(PgpuVariant), _I, C.POINTER(_P)]),

@@ -156,114 +156,167 @@ struct MedArgs {
   int n_ch, S, R, RL;
 };
 
+// 16-byte vector access to one (pattern, rate class) row of 4 states
+template <typename V> struct Row4;
+template <> struct Row4<float> {
+  __device__ __forceinline__ static void load(const float *p, float *v) {
+    const float4 q = __ldg(reinterpret_cast<const float4 *>(p));
+    v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+  }
+  __device__ __forceinline__ static void store(float *p, const float *v) {
+    *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  }
+};
+template <> struct Row4<double> {
+  __device__ __forceinline__ static void load(const double *p, double *v) {
+    const double2 a = __ldg(reinterpret_cast<const double2 *>(p));
+    const double2 b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+    v[0] = a.x, v[1] = a.y, v[2] = b.x, v[3] = b.y;
+  }
+  __device__ __forceinline__ static void store(double *p, const double *v) {
+    reinterpret_cast<double2 *>(p)[0] = make_double2(v[0], v[1]);
+    reinterpret_cast<double2 *>(p)[1] = make_double2(v[2], v[3]);
+  }
+};
+
 // y = prod_k P_k x_k, normalised per pattern.  SC: the state count at
-// compile time (4), or 0 for any S up to 64 read at run time.
+// compile time (4), or 0 for any S up to 64 read at run time.  A grid of a
+// few CTAs per SM strides over the (pattern, rate class) items, a warp at a
+// time (the stride is a multiple of 32, so a pattern's RL lanes stay in one
+// warp and one iteration); each thread keeps one compensated cost sum and
+// the CTA reduces it once at the end.
 template <typename V, int SC>
 __global__ void __launch_bounds__(CLV_THREADS) clv_median_kernel(const MedArgs a) {
   const int S = SC ? SC : a.S, R = a.R, RL = a.RL;
-  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const size_t p = g / RL;
-  const int r = (int)(g % RL);
-  const bool act = p < a.n_pat && r < R;
-  const size_t off = (p * R + r) * (size_t)S;
+  const int lane = threadIdx.x & 31;
+  const size_t n_items = a.n_pat * (size_t)RL;
+  const size_t stride = (size_t)gridDim.x * CLV_THREADS;
   V *y = static_cast<V *>(a.y);
-  V m = (V)0;
-  if (SC == 4) {
-    V acc[4] = {(V)1, (V)1, (V)1, (V)1};
-    if (act) {
-      for (int k = 0; k < a.n_ch; ++k) {
-        const V *xs = static_cast<const V *>(a.x[k]) + off;
-        const V *P = static_cast<const V *>(a.P[k]) + (size_t)r * 16;
-        V xv[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) xv[j] = xs[j];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          V s = (V)0;
-#pragma unroll
-          for (int j = 0; j < 4; ++j) s = fma(__ldg(P + i * 4 + j), xv[j], s);
-          acc[i] *= s;
-        }
-      }
-#pragma unroll
-      for (int i = 0; i < 4; ++i) m = acc[i] > m ? acc[i] : m;
-    }
-    V mm = m;
-    for (int o = 1; o < RL; o <<= 1) {
-      const V q = __shfl_xor_sync(0xffffffffu, mm, o);
-      mm = q > mm ? q : mm;
-    }
-    const int e = frexp_exp(mm);
-    if (act) {
-#pragma unroll
-      for (int i = 0; i < 4; ++i) y[off + i] = scale2<V>(acc[i], -e);
-    }
-    m = (V)e;
-  } else {
-    if (act) {
-      for (int i = 0; i < S; ++i) {
-        V v = (V)1;
-        for (int k = 0; k < a.n_ch; ++k) {
-          const V *xs = static_cast<const V *>(a.x[k]) + off;
-          const V *P = static_cast<const V *>(a.P[k]) + ((size_t)r * S + i) * S;
-          V s = (V)0;
-          for (int j = 0; j < S; ++j) s = fma(__ldg(P + j), xs[j], s);
-          v *= s;
-        }
-        y[off + i] = v;
-        m = v > m ? v : m;
-      }
-    }
-    V mm = m;
-    for (int o = 1; o < RL; o <<= 1) {
-      const V q = __shfl_xor_sync(0xffffffffu, mm, o);
-      mm = q > mm ? q : mm;
-    }
-    const int e = frexp_exp(mm);
-    if (act)
-      for (int i = 0; i < S; ++i) y[off + i] = scale2<V>(y[off + i], -e);
-    m = (V)e;
-  }
-  // exponent bookkeeping and this node's cost, by the pattern's first lane
   double s = 0.0, c = 0.0;
-  if (act && r == 0) {
-    const int e = (int)m;
-    int E = e;
-    for (int k = 0; k < a.n_ch; ++k) E += a.ex[k][p];
-    a.ey[p] = E;
-    const double w = a.weights ? a.weights[p] : 1.0;
-    s = w * (double)e;
+  for (size_t base = (size_t)blockIdx.x * CLV_THREADS + (threadIdx.x & ~31); base < n_items;
+       base += stride) {
+    const size_t g = base + lane;
+    const size_t p = g / RL;
+    const int r = (int)(g % RL);
+    const bool act = g < n_items && r < R;
+    const size_t off = (p * R + r) * (size_t)S;
+    V m = (V)0;
+    int e;
+    if (SC == 4) {
+      V acc[4] = {(V)1, (V)1, (V)1, (V)1};
+      if (act) {
+        for (int k = 0; k < a.n_ch; ++k) {
+          V xv[4], Pr[16];
+          Row4<V>::load(static_cast<const V *>(a.x[k]) + off, xv);
+          const V *P = static_cast<const V *>(a.P[k]) + (size_t)r * 16;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) Row4<V>::load(P + 4 * i, Pr + 4 * i);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            V t = (V)0;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) t = fma(Pr[4 * i + j], xv[j], t);
+            acc[i] *= t;
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) m = acc[i] > m ? acc[i] : m;
+      }
+      V mm = m;
+      for (int o = 1; o < RL; o <<= 1) {
+        const V q = __shfl_xor_sync(0xffffffffu, mm, o);
+        mm = q > mm ? q : mm;
+      }
+      e = frexp_exp(mm);
+      if (act) {
+        V out[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) out[i] = scale2<V>(acc[i], -e);
+        Row4<V>::store(y + off, out);
+      }
+    } else {
+      if (act) {
+        for (int i = 0; i < S; ++i) {
+          V v = (V)1;
+          for (int k = 0; k < a.n_ch; ++k) {
+            const V *xs = static_cast<const V *>(a.x[k]) + off;
+            const V *P = static_cast<const V *>(a.P[k]) + ((size_t)r * S + i) * S;
+            V t = (V)0;
+            for (int j = 0; j < S; ++j) t = fma(__ldg(P + j), xs[j], t);
+            v *= t;
+          }
+          y[off + i] = v;
+          m = v > m ? v : m;
+        }
+      }
+      V mm = m;
+      for (int o = 1; o < RL; o <<= 1) {
+        const V q = __shfl_xor_sync(0xffffffffu, mm, o);
+        mm = q > mm ? q : mm;
+      }
+      e = frexp_exp(mm);
+      if (act)
+        for (int i = 0; i < S; ++i) y[off + i] = scale2<V>(y[off + i], -e);
+    }
+    // exponent bookkeeping and this node's cost, by the pattern's first lane
+    if (act && r == 0) {
+      int E = e;
+      for (int k = 0; k < a.n_ch; ++k) E += a.ex[k][p];
+      a.ey[p] = E;
+      const double w = a.weights ? a.weights[p] : 1.0;
+      double t, err;
+      two_sum(s, w * (double)e, t, err);
+      s = t;
+      c += err;
+    }
   }
   // cost = -ln 2 * sum_p w_p e_p
   cta_partial_and_finish<CLV_THREADS>(s, c, a.part, a.counter, a.cost, -0.69314718055994530942);
 }
 
-// root_cost: -sum_p w_p [log(sum_r probs_r sum_i pi_i x[p][r][i]) + E_p ln 2]
-// (E counts every normalisation of the subtree, the node costs only their
-// own, so the root's E is dropped here: costs + root_cost = -lnL).
+// root_cost: -sum_p w_p log(sum_r probs_r sum_i pi_i x[p][r][i]); the
+// node costs carry every normalisation, so the root's own exponent E is
+// left out (costs + root_cost = -lnL).  Grid-stride as the median kernel.
 template <typename V>
 __global__ void __launch_bounds__(CLV_THREADS) clv_root_kernel(
     const V *x, const int32_t *ex, const double *pi, const double *probs, const double *weights,
     size_t n_pat, int S, int R, int RL, double *site_lnl, double2 *part, unsigned *counter,
     double *out) {
-  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const size_t p = g / RL;
-  const int r = (int)(g % RL);
-  const bool act = p < n_pat && r < R;
-  double v = 0.0;
-  if (act) {
-    const V *xs = x + (p * R + r) * (size_t)S;
-    for (int i = 0; i < S; ++i) v = fma(pi[i], (double)xs[i], v);
-    v *= probs[r];
-  }
-  for (int o = 1; o < RL; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31;
+  const size_t n_items = n_pat * (size_t)RL;
+  const size_t stride = (size_t)gridDim.x * CLV_THREADS;
   double s = 0.0, c = 0.0;
-  if (act && r == 0) {
-    const double site = log(v);
-    if (site_lnl) site_lnl[p] = site + (double)ex[p] * 0.69314718055994530942;
-    s = (weights ? weights[p] : 1.0) * site;
+  for (size_t base = (size_t)blockIdx.x * CLV_THREADS + (threadIdx.x & ~31); base < n_items;
+       base += stride) {
+    const size_t g = base + lane;
+    const size_t p = g / RL;
+    const int r = (int)(g % RL);
+    const bool act = g < n_items && r < R;
+    double v = 0.0;
+    if (act) {
+      const V *xs = x + (p * R + r) * (size_t)S;
+      for (int i = 0; i < S; ++i) v = fma(pi[i], (double)xs[i], v);
+      v *= probs[r];
+    }
+    for (int o = 1; o < RL; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (act && r == 0) {
+      const double site = log(v);
+      if (site_lnl) site_lnl[p] = site + (double)ex[p] * 0.69314718055994530942;
+      double t, err;
+      two_sum(s, weights ? weights[p] * site : site, t, err);
+      s = t;
+      c += err;
+    }
   }
   cta_partial_and_finish<CLV_THREADS>(s, c, part, counter, out, -1.0);
+}
+
+// costs of many nodes: out[i] = *src[i]
+__global__ void __launch_bounds__(256) clv_gather_kernel(const double *const *src, size_t n,
+                                                        double *out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    out[i] = *src[i];
 }
 
 pgpu_status lk_err(pgpu_lk *lk, pgpu_status st, const char *msg) {
@@ -393,7 +446,9 @@ pgpu_status pgpu_lk_create(pgpu_ctx *ctx, const pgpu_model *m, const pgpu_tip_co
     delete lk;
     return PGPU_ERR_LIMIT;
   }
-  lk->n_cta = std::max<size_t>((n_pat * lk->RL + CLV_THREADS - 1) / CLV_THREADS, 1);
+  // the per-pattern kernels stride over the patterns with a few CTAs per SM
+  const size_t want = (n_pat * lk->RL + CLV_THREADS - 1) / CLV_THREADS;
+  lk->n_cta = std::max<size_t>(std::min<size_t>(want, (size_t)std::max(ctx->num_sms, 1) * 8), 1);
   const int S = lk->S, R = lk->R;
   const size_t SS = (size_t)S * S;
   // one block, every part on a 256-byte boundary (the partials are double2
@@ -564,6 +619,29 @@ pgpu_status pgpu_clv_cost(pgpu_clv *t, double *cost) {
   PGPU_TRY(pgpu_check_flag(ctx, "likelihood"));
   *cost = *h;
   return PGPU_OK;
+}
+
+pgpu_status pgpu_clv_costs(pgpu_lk *lk, const pgpu_clv *const *nodes, size_t n, double *costs) {
+  if (!lk || (n && (!nodes || !costs))) return PGPU_ERR_ARG;
+  if (n == 0) return PGPU_OK;
+  pgpu_ctx *ctx = lk->ctx;
+  for (size_t i = 0; i < n; ++i)
+    if (!nodes[i] || nodes[i]->lk != lk)
+      return lk_err(lk, PGPU_ERR_ARG, "likelihood: a node is null or belongs to another model");
+  PGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+  void *h, *d, *dout;
+  PGPU_TRY(pgpu_stage(ctx, n * sizeof(double *), &h, &d));
+  const double **src = static_cast<const double **>(h);
+  for (size_t i = 0; i < n; ++i) src[i] = nodes[i]->scal;
+  PGPU_TRY(pgpu_stage_commit(ctx, n * sizeof(double *)));
+  PGPU_TRY(pgpu_buf(ctx, BUF_F, n * sizeof(double), &dout));
+  const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 1024);
+  clv_gather_kernel<<<grid, 256, 0, ctx->stream>>>(static_cast<const double *const *>(d), n,
+                                                   static_cast<double *>(dout));
+  PGPU_TRY(pgpu_after_launch(ctx, "clv_gather_kernel"));
+  PGPU_CUDA(ctx, cudaMemcpyAsync(costs, dout, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  PGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return pgpu_check_flag(ctx, "likelihood");
 }
 
 pgpu_status pgpu_clv_root_cost(pgpu_clv *t, double *cost, double *site_lnl) {

@@ -79,6 +79,14 @@ class LkModel:
         return self._new(getattr(self.lib, fn)(self.h, self._reuse(o), *[n.h for n in nbrs],
                                                C.byref(out)), out, fn, o)
 
+    def costs(self, nodes) -> np.ndarray:
+        """cost of each node, read with one synchronisation (pgpu_clv_costs)."""
+        arr = (C.c_void_p * len(nodes))(*[t.h for t in nodes])
+        out = np.empty(len(nodes))
+        self.ctx.check(self.lib.pgpu_clv_costs(self.h, arr, len(nodes), out.ctypes.data),
+                       "pgpu_clv_costs")
+        return out
+
     def close(self) -> None:
         for t in list(self.live):
             t.close()
@@ -177,7 +185,6 @@ def fold_postorder(m: LkModel, tree: RootedTree, tip_codes: np.ndarray, reuse=No
                             nodes[tree.right[k]])
         if v < 2 * n - 2:
             nodes[v].set_brlen(float(tree.brlen[v]))
-    for k in range(n - 1):
-        total += cost(nodes[n + k])
+    total += float(np.sum(m.costs(nodes[n:])))
     total += root_cost(nodes[2 * n - 2])
     return nodes, total
