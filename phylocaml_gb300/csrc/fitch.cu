@@ -609,15 +609,26 @@ struct TcmOp {
     const uint32_t fill = 0x11111111u & ~valid;
     xa = (xa & valid) | fill;
     xb = (xb & valid) | fill;
-    uint32_t out = 0;
+    // the table index (a_l << 4) | b_l of every site, as bytes: even sites
+    // 2k in byte k of ev, odd sites 2k + 1 in byte k of od
+    const uint32_t ev = ((xa << 4) & 0xF0F0F0F0u) | (xb & 0x0F0F0F0Fu);
+    const uint32_t od = (xa & 0xF0F0F0F0u) | ((xb >> 4) & 0x0F0F0F0Fu);
+    uint32_t e[8];
 #pragma unroll
-    for (int l = 0; l < 8; ++l) {
-      const uint32_t ia = (xa >> (4 * l)) & 15u, ib = (xb >> (4 * l)) & 15u;
-      const uint32_t e = tb[((ia << 4) | ib) << 5];
-      out |= (e & 15u) << (4 * l);
-      acc[q * 8 + l] += (e >> 4) & 0x07ffffffu;
-      none |= e;
+    for (int k = 0; k < 4; ++k) {
+      e[2 * k] = tb[__byte_perm(ev, 0u, 0x4440u + k) << 5];
+      e[2 * k + 1] = tb[__byte_perm(od, 0u, 0x4440u + k) << 5];
     }
+#pragma unroll
+    for (int l = 0; l < 8; ++l) acc[q * 8 + l] += e[l] >> 4;
+    none |= e[0] | e[1] | e[2] | e[3] | e[4] | e[5] | e[6] | e[7];
+    // the median codes are the entries' low nibbles: gather the low bytes of
+    // the even and the odd sites' entries, then interleave their nibbles
+    const uint32_t ce = __byte_perm(__byte_perm(e[0], e[2], 0x0040u), __byte_perm(e[4], e[6], 0x0040u),
+                                    0x5410u);
+    const uint32_t co = __byte_perm(__byte_perm(e[1], e[3], 0x0040u), __byte_perm(e[5], e[7], 0x0040u),
+                                    0x5410u);
+    const uint32_t out = (ce & 0x0F0F0F0Fu) | ((co << 4) & 0xF0F0F0F0u);
     return out & valid;
   }
   __device__ __forceinline__ uint4 combine(const uint4 &x, const uint4 &y, const uint4 &valid,
