@@ -573,6 +573,13 @@ pgpu_status pgpu_spr_apply(pgpu_spr *spr, int64_t move_idx);
  * `distance` limits both attach edges to that many nodes from the cut (0:
  * no limit).  Moves are listed per cut edge, a's attach edge major. */
 pgpu_status pgpu_spr_set_tbr_distance(pgpu_spr *spr, int distance);
+/* The two limits of generate_tbr ?join_distance ?reroot_distance
+ * (lib/treeNeighborhoods.ml:27-75): a cut leaves two sides, either of which
+ * may be the one moved, so a move is listed when one side's attach edge lies
+ * within join_distance of the cut and the other's within reroot_distance (0:
+ * no limit).  pgpu_spr_set_tbr_distance(d) is (d, d).  Moves stay in the same
+ * order, those outside the limits left out. */
+pgpu_status pgpu_spr_set_tbr_limits(pgpu_spr *spr, int join_distance, int reroot_distance);
 /* Device bytes for the attach vectors of one batch of cut edges (0: 2 GB);
  * a scan runs as many batches as it needs, at least one cut each.  A cut
  * needs (attach edges on both sides) x n_pat x n_rates x 4 values of the

@@ -121,6 +121,28 @@ def tbr_moves(adj: dict, n: int, distance: int = 0):
     return out
 
 
+def tbr_moves_limits(adj: dict, n: int, join_distance: int = 0, reroot_distance: int = 0):
+    """The TBR moves of tbr_moves with generate_tbr's two limits
+    (lib/treeNeighborhoods.ml:27-75): a cut leaves two sides and either may be
+    the one moved, so a move is kept when one attach edge lies within
+    join_distance of the cut and the other within reroot_distance (0: no
+    limit).  An attach edge's distance is the smallest limit under which
+    `moves` lists it."""
+    inf = 1 << 30
+    J = join_distance if join_distance > 0 else inf
+    Rr = reroot_distance if reroot_distance > 0 else inf
+    depth: dict = {}
+    for d in range(1, 2 * n + 1):
+        for mv in moves(adj, n, d):
+            depth.setdefault(mv, d)
+    out = []
+    for (a, b, jc, jy, kc, ky) in tbr_moves(adj, n, 0):
+        dj, dk = depth[(b, a, jc, jy)], depth[(a, b, kc, ky)]
+        if (dj <= J and dk <= Rr) or (dj <= Rr and dk <= J):
+            out.append((a, b, jc, jy, kc, ky))
+    return out
+
+
 def apply_tbr(adj: dict, a: int, b: int, jc: int, jy: int, kc: int, ky: int) -> dict:
     """Dissolve a and put it on (jc, jy), then dissolve b and put it on
     (kc, ky); each half is an SPR move that keeps the cut edge."""

@@ -155,6 +155,7 @@ SIGNATURES: dict[str, tuple] = {
     "pgpu_spr_lnl": (_I, [_P, _DP, _P]),
     "pgpu_spr_set_join_distance": (_I, [_P, _I]),
     "pgpu_spr_set_tbr_distance": (_I, [_P, _I]),
+    "pgpu_spr_set_tbr_limits": (_I, [_P, _I, _I]),
     "pgpu_spr_set_tbr_budget": (_I, [_P, _SZ]),
     "pgpu_spr_tbr_n_moves": (_I, [_P, C.POINTER(_SZ)]),
     "pgpu_spr_tbr_moves": (_I, [_P, _P, _P, _P, _P, _P, _P, _SZ]),

@@ -1090,13 +1090,17 @@ struct pgpu_spr {
   TbrPlan tbr;
   SprPlanDev tbr_d;
   bool tbr_valid = false;
-  int tbr_distance = 0;    // 0: no limit; d: attach edges at most d nodes from the cut
+  int tbr_join = 0, tbr_reroot = 0;   // attach-edge limits in nodes from the cut (0: none)
   size_t tbr_budget = size_t(2) << 30;   // attach-vector bytes per batch of cuts
   char *tbr_x = nullptr;
   int32_t *tbr_xsc = nullptr;
   TbrCutDev *tbr_cuts = nullptr;
   int4 *tbr_tiles = nullptr;
   size_t tbr_x_cap = 0, tbr_xsc_cap = 0, tbr_cuts_cap = 0, tbr_tiles_cap = 0;
+  // with two different limits: every pair's lnL, and the listed pairs' grid indices
+  double *tbr_grid = nullptr;
+  int64_t *tbr_keep = nullptr;
+  size_t tbr_grid_cap = 0, tbr_keep_cap = 0;
   // host copies of a TBR batch's cut and tile lists, owned by the engine so
   // that they outlive the asynchronous copies to the device
   std::vector<TbrCutDev> h_tbr_cuts;
@@ -1340,8 +1344,12 @@ pgpu_status run_scan(pgpu_spr *s, const SprPlan &p, const SprPlanDev &d, double 
 pgpu_status ensure_tbr(pgpu_spr *s) {
   if (s->tbr_valid) return PGPU_OK;
   PGPU_TRY(ensure_pool(s));
-  tbr_plan(s->T, s->pp, s->tbr_distance, &s->tbr);
+  tbr_plan(s->T, s->pp, s->tbr_join, s->tbr_reroot, &s->tbr);
   PGPU_TRY(upload_plan(s, s->tbr.emit, &s->tbr_d));
+  if (!s->tbr.keep.empty()) {
+    PGPU_TRY(grow(s, &s->tbr_keep, &s->tbr_keep_cap, s->tbr.keep.size()));
+    PGPU_TRY(upload(s, s->tbr_keep, s->tbr.keep.data(), s->tbr.keep.size()));
+  }
   s->tbr_valid = true;
   return PGPU_OK;
 }
@@ -1400,9 +1408,9 @@ pgpu_status launch_tbr_batch(pgpu_spr *s, size_t c0, size_t c1, double *lnl_dev)
     case 4: PGPU_TRY((launch_emit_rt<Pol, 4>(s, pb0, n_prunes, slot_base))); break;
     default: PGPU_TRY((launch_emit_rt<Pol, 8>(s, pb0, n_prunes, slot_base))); break;
   }
-  // the batch's cuts and tiles
-  const long long move0 = tp.cuts[c0].move_off;
-  const long long nm = tp.cuts[c1 - 1].move_off + (long long)tp.cuts[c1 - 1].nA * tp.cuts[c1 - 1].nB - move0;
+  // the batch's cuts and tiles, numbered by their pairs in the grid
+  const long long move0 = tp.cuts[c0].grid_off;
+  const long long nm = tp.cuts[c1 - 1].grid_off + (long long)tp.cuts[c1 - 1].nA * tp.cuts[c1 - 1].nB - move0;
   // the lists live in the engine; a copy from pageable memory returns once
   // its source has been staged, so the next batch may rewrite them
   std::vector<TbrCutDev> &cuts = s->h_tbr_cuts;
@@ -1417,7 +1425,7 @@ pgpu_status launch_tbr_batch(pgpu_spr *s, size_t c0, size_t c1, double *lnl_dev)
     d.nB = x.nB;
     d.slotA = P.prunes[x.pa].move_off - slot_base;
     d.slotB = P.prunes[x.pb].move_off - slot_base;
-    d.move_off = x.move_off - move0;
+    d.move_off = x.grid_off - move0;
     cuts.push_back(d);
     for (int j0 = 0; j0 < x.nA; j0 += TB_T)
       for (int k0 = 0; k0 < x.nB; k0 += TB_T) tiles.push_back(make_int4((int)(c - c0), j0, k0, 0));
@@ -1463,12 +1471,25 @@ pgpu_status launch_tbr_batch(pgpu_spr *s, size_t c0, size_t c1, double *lnl_dev)
   return pgpu_after_launch(s->ctx, "spr_reduce_kernel");
 }
 
+// out[m] = grid[keep[m]]: the listed moves' lnL out of every pair's
+__global__ void __launch_bounds__(256) tbr_gather_kernel(const double *grid, const int64_t *keep,
+                                                        size_t n, double *out) {
+  for (size_t m = blockIdx.x * (size_t)blockDim.x + threadIdx.x; m < n;
+       m += (size_t)gridDim.x * blockDim.x)
+    out[m] = grid[keep[m]];
+}
+
 // lnL of every TBR move into lnl_dev, in batches of cuts whose attach
-// vectors fit in the budget (at least one cut per batch)
+// vectors fit in the budget (at least one cut per batch); with two
+// different limits every pair goes into the grid buffer first and the
+// listed moves are gathered from it
 pgpu_status run_tbr_scan(pgpu_spr *s, double *lnl_dev) {
   PGPU_TRY(ensure_tbr(s));
   const TbrPlan &tp = s->tbr;
   if (tp.n_moves == 0) return PGPU_OK;
+  const bool filter = !tp.keep.empty();
+  if (filter) PGPU_TRY(grow(s, &s->tbr_grid, &s->tbr_grid_cap, (size_t)tp.n_grid));
+  double *out = filter ? s->tbr_grid : lnl_dev;
   const size_t slot_bytes = s->np * s->R * 4 * s->vbytes;
   const size_t max_slots = std::max<size_t>(1, s->tbr_budget / slot_bytes);
   for (size_t c0 = 0; c0 < tp.cuts.size();) {
@@ -1481,10 +1502,16 @@ pgpu_status run_tbr_scan(pgpu_spr *s, double *lnl_dev) {
     }
     PGPU_TRY(grow(s, &s->tbr_x, &s->tbr_x_cap, slots * slot_bytes));
     PGPU_TRY(grow(s, &s->tbr_xsc, &s->tbr_xsc_cap, slots * s->np));
-    if (s->precision == 32) PGPU_TRY(launch_tbr_batch<Fp32>(s, c0, c1, lnl_dev));
-    else if (s->precision == 48) PGPU_TRY(launch_tbr_batch<Ff32>(s, c0, c1, lnl_dev));
-    else PGPU_TRY(launch_tbr_batch<Fp64>(s, c0, c1, lnl_dev));
+    if (s->precision == 32) PGPU_TRY(launch_tbr_batch<Fp32>(s, c0, c1, out));
+    else if (s->precision == 48) PGPU_TRY(launch_tbr_batch<Ff32>(s, c0, c1, out));
+    else PGPU_TRY(launch_tbr_batch<Fp64>(s, c0, c1, out));
     c0 = c1;
+  }
+  if (filter) {
+    const size_t n = (size_t)tp.n_moves;
+    tbr_gather_kernel<<<(unsigned)std::min<size_t>((n + 255) / 256, 65535), 256, 0, s->ctx->stream>>>(
+        s->tbr_grid, s->tbr_keep, n, lnl_dev);
+    PGPU_TRY(pgpu_after_launch(s->ctx, "tbr_gather_kernel"));
   }
   return PGPU_OK;
 }
@@ -1906,14 +1933,23 @@ pgpu_status pgpu_spr_set_join_distance(pgpu_spr *s, int join_distance) {
   return PGPU_OK;
 }
 
-pgpu_status pgpu_spr_set_tbr_distance(pgpu_spr *s, int distance) {
+pgpu_status pgpu_spr_set_tbr_limits(pgpu_spr *s, int join_distance, int reroot_distance) {
   if (!s) return PGPU_ERR_ARG;
-  if (distance < 0) return pgpu_set_err(s->ctx, PGPU_ERR_ARG, "tbr: distance %d < 0", distance);
-  if (distance != s->tbr_distance) {
-    s->tbr_distance = distance;
+  if (join_distance < 0 || reroot_distance < 0)
+    return pgpu_set_err(s->ctx, PGPU_ERR_ARG, "tbr: limits %d, %d must be >= 0", join_distance,
+                        reroot_distance);
+  if (join_distance != s->tbr_join || reroot_distance != s->tbr_reroot) {
+    s->tbr_join = join_distance;
+    s->tbr_reroot = reroot_distance;
     s->tbr_valid = false;
   }
   return PGPU_OK;
+}
+
+pgpu_status pgpu_spr_set_tbr_distance(pgpu_spr *s, int distance) {
+  if (!s) return PGPU_ERR_ARG;
+  if (distance < 0) return pgpu_set_err(s->ctx, PGPU_ERR_ARG, "tbr: distance %d < 0", distance);
+  return pgpu_spr_set_tbr_limits(s, distance, distance);
 }
 
 pgpu_status pgpu_spr_set_tbr_budget(pgpu_spr *s, size_t bytes) {
@@ -1942,19 +1978,23 @@ pgpu_status pgpu_spr_tbr_moves(pgpu_spr *s, int32_t *a, int32_t *b, int32_t *jc,
   std::vector<double> bl(2 * n - 2);
   spr_to_rooted(s->T, l.data(), r.data(), bl.data(), ids.data());
   const SprPlan &P = s->tbr.emit;
+  const std::vector<int64_t> &keep = s->tbr.keep;
+  size_t m = 0;   // listed moves, in grid order
   for (const TbrCut &c : s->tbr.cuts) {
     const int ia = ids[s->T.ea[c.edge]], ib = ids[s->T.eb[c.edge]];
     for (int j = 0; j < c.nA; ++j) {
       const int dj = P.moves[P.prunes[c.pa].move_off + j].dc;
       for (int k = 0; k < c.nB; ++k) {
+        if (!keep.empty() && (m >= keep.size() || keep[m] != c.grid_off + (int64_t)j * c.nB + k))
+          continue;
         const int dk = P.moves[P.prunes[c.pb].move_off + k].dc;
-        const size_t m = (size_t)(c.move_off + (int64_t)j * c.nB + k);
         a[m] = ia;
         b[m] = ib;
         jc[m] = ids[s->T.dsrc(dj)];
         jy[m] = ids[s->T.ddst(dj)];
         kc[m] = ids[s->T.dsrc(dk)];
         ky[m] = ids[s->T.ddst(dk)];
+        ++m;
       }
     }
   }
@@ -1976,11 +2016,12 @@ pgpu_status pgpu_spr_tbr_apply(pgpu_spr *s, int64_t move_idx) {
   if (move_idx < 0 || (size_t)move_idx >= nm)
     return pgpu_set_err(s->ctx, PGPU_ERR_ARG, "tbr: move index %lld out of range", (long long)move_idx);
   const std::vector<TbrCut> &cuts = s->tbr.cuts;
-  size_t c = std::upper_bound(cuts.begin(), cuts.end(), (int64_t)move_idx,
-                              [](int64_t m, const TbrCut &x) { return m < x.move_off; }) -
+  const int64_t g = s->tbr.keep.empty() ? move_idx : s->tbr.keep[(size_t)move_idx];
+  size_t c = std::upper_bound(cuts.begin(), cuts.end(), g,
+                              [](int64_t v, const TbrCut &x) { return v < x.grid_off; }) -
              cuts.begin() - 1;
   const TbrCut &x = cuts[c];
-  const int64_t rel = move_idx - x.move_off;
+  const int64_t rel = g - x.grid_off;
   const SprPlan &P = s->tbr.emit;
   const int dj = P.moves[P.prunes[x.pa].move_off + (int)(rel / x.nB)].dc;
   const int dk = P.moves[P.prunes[x.pb].move_off + (int)(rel % x.nB)].dc;

@@ -92,24 +92,33 @@ struct SprPlan {
 // edges (putting a back on its joined edge is no reroot: with one side
 // rerooted only, the move is an SPR move).  Per cut, an emit plan walks A'
 // (the SPR prune carrying b's side away) and B' (carrying a's side away);
-// its moves are the attach edges j and k, and TBR move (j, k) of the cut is
-// move_off + j * nB + k.
+// its moves are the attach edges j and k, and pair (j, k) of the cut is
+// grid_off + j * nB + k of the grid of all pairs.  With one distance limit
+// (or none) every pair of the grid is a move; with a join and a reroot limit
+// that differ, the listed moves are the pairs whose one attach edge lies
+// within the join limit and whose other lies within the reroot limit (either
+// side may be the one moved), in grid order: keep[m] is the grid index of
+// move m, and move_off the first listed move of a cut.
 struct TbrCut {
   int32_t edge;          // the cut edge
   int32_t pa, pb;        // emit prunes walking A' and B'
   int32_t nA, nB;        // attach edges on each side
-  int64_t move_off;      // first TBR move of the cut
+  int64_t move_off;      // first listed TBR move of the cut
+  int64_t grid_off;      // first pair of the cut in the grid
 };
 
 struct TbrPlan {
   SprPlan emit;
   std::vector<TbrCut> cuts;
-  int64_t n_moves = 0;
+  int64_t n_moves = 0;   // listed moves
+  int64_t n_grid = 0;    // pairs of every cut
+  std::vector<int64_t> keep;   // grid index per listed move; empty when every pair is listed
 };
 
-// every TBR move of T whose attach edges lie at most `distance` nodes from
-// the cut (0: no limit)
-void tbr_plan(const SprTopo &T, const PoolPlan &pp, int distance, TbrPlan *out);
+// the TBR moves of T: attach edges j (on a's side) and k (on b's side) at
+// depths dj and dk nodes from the cut, listed when dj <= join and dk <=
+// reroot, or dk <= join and dj <= reroot (0: no limit)
+void tbr_plan(const SprTopo &T, const PoolPlan &pp, int join, int reroot, TbrPlan *out);
 // apply: cut edge `edge` (a = ea, b = eb), a onto the edge of directed edge
 // dj (c->y, y nearer a), b onto that of dk
 pgpu_status tbr_apply(pgpu_ctx *ctx, SprTopo *T, int edge, int32_t dj, int32_t dk);

@@ -291,12 +291,16 @@ void spr_plan_all(const SprTopo &T, const PoolPlan &pp, SprPlan *out, int join_d
   }
 }
 
-void tbr_plan(const SprTopo &T, const PoolPlan &pp, int distance, TbrPlan *out) {
+void tbr_plan(const SprTopo &T, const PoolPlan &pp, int join, int reroot, TbrPlan *out) {
   SprPlan &P = out->emit;
   plan_reset(&P);
   out->cuts.clear();
+  out->keep.clear();
   out->n_moves = 0;
-  const int max_depth = distance > 0 ? distance : INT_MAX;
+  out->n_grid = 0;
+  const int J = join > 0 ? join : INT_MAX, Rr = reroot > 0 ? reroot : INT_MAX;
+  const int max_depth = std::max(J, Rr);
+  const bool filter = J != Rr;
   auto all = [](int, int) { return true; };
   for (int e = 0; e < T.n_edges(); ++e) {
     if (T.ea[e] < T.n || T.eb[e] < T.n) continue;   // both sides rerootable
@@ -313,8 +317,22 @@ void tbr_plan(const SprTopo &T, const PoolPlan &pp, int distance, TbrPlan *out) 
       P.prunes.resize(p0);
       continue;
     }
-    TbrCut c{e, p0, p0 + 1, P.prunes[p0].n_moves, P.prunes[p0 + 1].n_moves, out->n_moves};
-    out->n_moves += (int64_t)c.nA * c.nB;
+    TbrCut c{e, p0, p0 + 1, P.prunes[p0].n_moves, P.prunes[p0 + 1].n_moves, out->n_moves,
+             out->n_grid};
+    if (filter) {
+      const SprMove *ma = P.moves.data() + P.prunes[p0].move_off;
+      const SprMove *mb = P.moves.data() + P.prunes[p0 + 1].move_off;
+      for (int j = 0; j < c.nA; ++j)
+        for (int k = 0; k < c.nB; ++k) {
+          const int dj = ma[j].depth, dk = mb[k].depth;
+          if ((dj <= J && dk <= Rr) || (dj <= Rr && dk <= J))
+            out->keep.push_back(c.grid_off + (int64_t)j * c.nB + k);
+        }
+      out->n_moves = (int64_t)out->keep.size();
+    } else {
+      out->n_moves += (int64_t)c.nA * c.nB;
+    }
+    out->n_grid += (int64_t)c.nA * c.nB;
     out->cuts.push_back(c);
   }
 }

@@ -209,6 +209,13 @@ class SprEngine:
         """Attach edges at most d nodes from the cut on both sides (0: no limit)."""
         self._check(self.lib.pgpu_spr_set_tbr_distance(self.h, int(d)), "pgpu_spr_set_tbr_distance")
 
+    def set_tbr_limits(self, join_distance: int, reroot_distance: int) -> None:
+        """generate_tbr ?join_distance ?reroot_distance: a move is listed when
+        one side's attach edge lies within join_distance of the cut and the
+        other's within reroot_distance (0: no limit)."""
+        self._check(self.lib.pgpu_spr_set_tbr_limits(self.h, int(join_distance), int(reroot_distance)),
+                    "pgpu_spr_set_tbr_limits")
+
     def set_tbr_budget(self, nbytes: int) -> None:
         """Device bytes for the attach vectors of one batch of cut edges (0: 2 GB)."""
         self._check(self.lib.pgpu_spr_set_tbr_budget(self.h, int(nbytes)), "pgpu_spr_set_tbr_budget")

@@ -271,6 +271,33 @@ def test_tbr_distance_and_apply(small, ctx):
     e.close()
 
 
+@pytest.mark.parametrize("join,reroot", [(2, 1), (1, 3), (0, 1), (2, 2)])
+def test_tbr_join_and_reroot_limits(small, ctx, join, reroot):
+    """generate_tbr's two limits: the engine lists exactly the oracle's moves
+    (one attach edge within the join limit, the other within the reroot
+    limit, either side moved), each scored as the unlimited scan scores it,
+    and applying one gives the oracle's tree."""
+    d = small
+    n = d["tr"].n_tips
+    e = engine(d, ctx, 64)
+    cur = e.get_tree()
+    adj = SO.unroot(cur.left, cur.right, cur.brlen)
+    full = dict(zip([canon(m) for m in e.tbr_moves()], e.tbr_scan().cpu().numpy()))
+    e.set_tbr_limits(join, reroot)
+    mv = [tuple(int(x) for x in m) for m in e.tbr_moves()]
+    exp = SO.tbr_moves_limits(adj, n, join, reroot)
+    assert sorted(map(canon, mv)) == sorted(exp)
+    assert e.n_tbr_moves == len(mv) and 0 < len(mv) <= len(full)
+    got = e.tbr_scan().cpu().numpy()
+    np.testing.assert_allclose(got, [full[canon(m)] for m in mv], rtol=1e-12)
+    best = int(np.argmax(got))
+    e.tbr_apply(best)
+    after = e.get_tree()
+    assert SO.splits(SO.unroot(after.left, after.right, after.brlen), n) == \
+        SO.splits(SO.apply_tbr(adj, *mv[best]), n)
+    e.close()
+
+
 @pytest.mark.parametrize("k,shape", [(1, "balanced"), (3, "yule"), (8, "yule")])
 def test_tbr_rescaling_and_rate_classes(ctx, k, shape):
     """TBR with 1, 3 and 8 rate classes (thread groups of 1, 4 and 8 lanes

@@ -135,3 +135,22 @@ def test_oracle_tbr_is_spr_plus_double_reroots(n):
     for m in SO.tbr_moves(adj, n)[:20]:
         new = SO.apply_tbr(adj, *m)
         assert abs(sum(t for x in new for y, t in new[x].items() if x < y) - total) < 1e-12
+
+
+def test_tbr_limits_oracle_consistency():
+    """generate_tbr's two limits in the oracle: equal limits give the
+    single-distance list, the rule is symmetric in the two limits, and a
+    tighter limit keeps a subset."""
+    import numpy as np
+    from oracle import spr_oracle as SO
+    from phylocaml_gb300 import tree as T
+    rng = np.random.default_rng(3)
+    tr = T.yule(11, rng, 0.1)
+    adj = SO.unroot(tr.left, tr.right, tr.brlen)
+    n = tr.n_tips
+    for d in (1, 2, 3):
+        assert sorted(SO.tbr_moves_limits(adj, n, d, d)) == sorted(SO.tbr_moves(adj, n, d))
+    assert sorted(SO.tbr_moves_limits(adj, n, 2, 1)) == sorted(SO.tbr_moves_limits(adj, n, 1, 2))
+    wide = set(SO.tbr_moves_limits(adj, n, 0, 2))
+    assert set(SO.tbr_moves_limits(adj, n, 3, 2)) <= wide <= set(SO.tbr_moves(adj, n, 0))
+    assert set(SO.tbr_moves(adj, n, 1)) <= set(SO.tbr_moves_limits(adj, n, 2, 1))
