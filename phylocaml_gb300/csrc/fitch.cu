@@ -42,15 +42,22 @@ struct Lanes {
   static constexpr uint32_t FLUSH = LB >= 32 ? 0xffffffffu : ((1u << (LB >= 32 ? 0 : LB)) - 1u);
 };
 
+// Per LB-bit lane: the intersection, or the union where the intersection is
+// empty; e_lsb gets a 1 in the lowest bit of every empty lane.  x has a
+// lane's top bit set when the lane's other bits of a & b are not all zero,
+// so ~(x | m) & H marks the empty lanes; spreading that mark over the lane
+// is a multiply by the lane mask (no carries cross lanes), and
+// (a & b) | ((a | b) & fill) is one three-input logic operation.
 template <int LB>
 __device__ __forceinline__ uint32_t fitch_word(uint32_t a, uint32_t b, uint32_t &e_lsb) {
   constexpr uint32_t H = Lanes<LB>::H;
+  constexpr uint32_t LMASK = LB >= 32 ? 0xffffffffu : ((1u << (LB >= 32 ? 0 : LB)) - 1u);
   const uint32_t m = a & b;
-  const uint32_t nz = (((m & ~H) + ~H) | m) & H;
-  const uint32_t e = nz ^ H;
-  const uint32_t fill = e | (e - (e >> (LB - 1)));
+  const uint32_t x = (m & ~H) + ~H;
+  const uint32_t e = ~(x | m) & H;
   e_lsb = e >> (LB - 1);
-  return m | ((a | b) & fill);
+  const uint32_t fill = e_lsb * LMASK;
+  return (a & b) | ((a | b) & fill);
 }
 
 // mask of the valid lanes of word w (all lanes except in the last word)
