@@ -33,6 +33,7 @@
 // reuses its memory instead.
 #include <algorithm>
 #include <cmath>
+#include <vector>
 
 #include "pgpu_internal.cuh"
 #include "forms.cuh"
@@ -49,6 +50,11 @@ struct pgpu_lk {
          *probs = nullptr, *tab = nullptr, *weights = nullptr;
   int *status = nullptr;     // eigendecomposition status
   double2 *part = nullptr;   // per-CTA partial sums
+  // integer weights (pattern counts): the node costs are summed exactly as
+  // sum_p w_p e_p in int64 on the integer units, the FP64 units being slow
+  bool int_w = false;
+  int32_t *wint = nullptr;   // [n_pat] or null (all 1)
+  long long *ipart = nullptr;   // per-CTA integer partial sums
   unsigned *counter = nullptr;
   size_t n_cta = 0;
   long long live = 0;        // handles not yet destroyed
@@ -122,6 +128,46 @@ __device__ __forceinline__ void cta_partial_and_finish(double s, double c, doubl
   }
 }
 
+// The same for an exact integer sum v: the last CTA adds the per-CTA
+// partials in int64 and writes scale * total.
+template <int NT>
+__device__ __forceinline__ void cta_i64_and_finish(long long v, long long *part, unsigned *counter,
+                                                   double *out, double scale) {
+  __shared__ long long red[NT / 32];
+  __shared__ bool last;
+  const int t = threadIdx.x, lane = t & 31;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) red[t >> 5] = v;
+  __syncthreads();
+  if (t < 32) {
+    long long x = lane < NT / 32 ? red[lane] : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) {
+      part[blockIdx.x] = x;
+      __threadfence();
+      last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  long long sum = 0;
+  for (unsigned i = t; i < gridDim.x; i += NT) sum += __ldcg(part + i);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  __syncthreads();
+  if (lane == 0) red[t >> 5] = sum;
+  __syncthreads();
+  if (t == 0) {
+    long long tot = 0;
+    for (int k = 0; k < NT / 32; ++k) tot += red[k];
+    *out = scale * (double)tot;
+    *counter = 0u;
+  }
+}
+
 // Leaf vectors: x[p][r][i] = code_tab[code_p][i] for every rate class.
 template <typename V>
 __global__ void __launch_bounds__(CLV_THREADS) clv_leaf_kernel(const uint8_t *codes,
@@ -154,6 +200,9 @@ struct MedArgs {
   double *cost;
   size_t n_pat;
   int n_ch, S, R, RL;
+  int int_w;                 // integer weights: exact int64 cost sums
+  const int32_t *wint;
+  long long *ipart;
 };
 
 // 16-byte vector access to one (pattern, rate class) row of 4 states
@@ -193,6 +242,7 @@ __global__ void __launch_bounds__(CLV_THREADS) clv_median_kernel(const MedArgs a
   const size_t stride = (size_t)gridDim.x * CLV_THREADS;
   V *y = static_cast<V *>(a.y);
   double s = 0.0, c = 0.0;
+  long long iacc = 0;
   for (size_t base = (size_t)blockIdx.x * CLV_THREADS + (threadIdx.x & ~31); base < n_items;
        base += stride) {
     const size_t g = base + lane;
@@ -263,15 +313,22 @@ __global__ void __launch_bounds__(CLV_THREADS) clv_median_kernel(const MedArgs a
       int E = e;
       for (int k = 0; k < a.n_ch; ++k) E += a.ex[k][p];
       a.ey[p] = E;
-      const double w = a.weights ? a.weights[p] : 1.0;
-      double t, err;
-      two_sum(s, w * (double)e, t, err);
-      s = t;
-      c += err;
+      if (a.int_w) {
+        iacc += (long long)(a.wint ? a.wint[p] : 1) * e;
+      } else {
+        const double w = a.weights ? a.weights[p] : 1.0;
+        double t, err;
+        two_sum(s, w * (double)e, t, err);
+        s = t;
+        c += err;
+      }
     }
   }
   // cost = -ln 2 * sum_p w_p e_p
-  cta_partial_and_finish<CLV_THREADS>(s, c, a.part, a.counter, a.cost, -0.69314718055994530942);
+  if (a.int_w)
+    cta_i64_and_finish<CLV_THREADS>(iacc, a.ipart, a.counter, a.cost, -0.69314718055994530942);
+  else
+    cta_partial_and_finish<CLV_THREADS>(s, c, a.part, a.counter, a.cost, -0.69314718055994530942);
 }
 
 // root_cost: -sum_p w_p log(sum_r probs_r sum_i pi_i x[p][r][i]); the
@@ -392,6 +449,9 @@ pgpu_status median(pgpu_lk *lk, pgpu_clv *reuse, const pgpu_clv *const *ch, int 
   a.y = t->x;
   a.ey = t->ex;
   a.weights = lk->weights;
+  a.int_w = lk->int_w ? 1 : 0;
+  a.wint = lk->wint;
+  a.ipart = lk->ipart;
   a.part = lk->part;
   a.counter = lk->counter;
   a.cost = t->scal;
@@ -462,7 +522,8 @@ pgpu_status pgpu_lk_create(pgpu_ctx *ctx, const pgpu_model *m, const pgpu_tip_co
   const size_t oU = take(SS * 8), oUi = take(SS * 8), olam = take(S * 8), opi = take(S * 8),
                orates = take(R * 8), oprobs = take(R * 8),
                otab = take((size_t)codes->n_codes * S * 8), ow = take(n_pat * 8), oq = take(SS * 8),
-               ost = take(64), opart = take(lk->n_cta * sizeof(double2));
+               ost = take(64), opart = take(lk->n_cta * sizeof(double2)),
+               owi = take(n_pat * 4), oipart = take(lk->n_cta * sizeof(long long));
   const size_t bytes = off;
   void *blk = nullptr;
   cudaError_t e = cudaMalloc(&blk, bytes);
@@ -486,6 +547,21 @@ pgpu_status pgpu_lk_create(pgpu_ctx *ctx, const pgpu_model *m, const pgpu_tip_co
   lk->status = reinterpret_cast<int *>(base + ost);
   lk->counter = reinterpret_cast<unsigned *>(lk->status + 4);
   lk->part = reinterpret_cast<double2 *>(base + opart);
+  lk->ipart = reinterpret_cast<long long *>(base + oipart);
+  // integer weights, small enough that sum_p w_p e_p fits int64 (|e_p| <= 1074)
+  std::vector<int32_t> wi;
+  lk->int_w = true;
+  if (weights) {
+    wi.resize(n_pat);
+    double wmax = 0.0;
+    for (size_t i = 0; i < n_pat && lk->int_w; ++i) {
+      const double v = weights[i];
+      if (!(v >= 0.0) || v >= 2147483647.0 || v != std::floor(v)) lk->int_w = false;
+      else wi[i] = (int32_t)v, wmax = std::max(wmax, v);
+    }
+    if (lk->int_w && (double)n_pat * std::max(wmax, 1.0) * 1100.0 >= 4.0e18) lk->int_w = false;
+  }
+  lk->wint = lk->int_w && weights ? reinterpret_cast<int32_t *>(base + owi) : nullptr;
   cudaStream_t s = ctx->stream;
   auto fail = [&](pgpu_status st) {
     cudaFree(blk);
@@ -508,6 +584,7 @@ pgpu_status pgpu_lk_create(pgpu_ctx *ctx, const pgpu_model *m, const pgpu_tip_co
   LK_CUDA(cudaMemcpyAsync(lk->tab, codes->table, (size_t)codes->n_codes * S * 8,
                           cudaMemcpyHostToDevice, s));
   if (weights) LK_CUDA(cudaMemcpyAsync(w, weights, n_pat * 8, cudaMemcpyHostToDevice, s));
+  if (lk->wint) LK_CUDA(cudaMemcpyAsync(lk->wint, wi.data(), n_pat * 4, cudaMemcpyHostToDevice, s));
   LK_CUDA(cudaMemsetAsync(lk->status, 0, 64, s));
   pgpu_status st = pgpu_launch_eig(ctx, q, lk->pi, S, 1, lk->U, lk->lam, lk->Ui, lk->status);
   if (st != PGPU_OK) return fail(st);

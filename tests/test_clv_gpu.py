@@ -61,6 +61,23 @@ def test_fold_matches_oracle_and_whole_tree(ctx, dna):
         lk.close()
 
 
+def test_fractional_weights(ctx, dna):
+    """Integer weights sum the node costs exactly in int64; fractional ones
+    take the compensated FP64 sum.  Both agree with the oracle."""
+    tr, spec, pats, w = dna
+    model = M.create(spec, ctx)
+    q, pi, rates, probs = synth.host_model(spec)
+    table = synth.dna_code_table()
+    wf = w * 0.37 + 0.125
+    exp = _oracle_lnl(tr, q, pi, rates, probs, pats, table, wf)
+    lk = L.LkModel(model, table, pats.shape[1], wf, 64, ctx)
+    try:
+        _, total = L.fold_postorder(lk, tr, pats)
+        assert abs(-total - exp) <= FP64_REL * abs(exp)
+    finally:
+        lk.close()
+
+
 def test_median3_reroots_the_unrooted_tree(ctx, dna):
     tr, spec, pats, w = dna
     model = M.create(spec, ctx)
