@@ -198,9 +198,14 @@ def bench_fitch(args, rank, world, local):
     def step():
         fitch.fitch_tree_dev(tr, tips, ld, n_sites, 4, wd, out, sc, tot, ctx=ctx)
 
-    # the launch shape (words per CTA) picked by timing candidates on these buffers
+    # the launch shape (words per CTA) picked by timing candidates on these
+    # buffers, unless given (profiling captures want a fixed launch list)
     t_tune = time.perf_counter()
-    tile, tile_ms = fitch.autotune_tile(tr, tips, ld, n_sites, 4, wd, out, sc, tot, ctx, reps=10)
+    if args.fitch_tile:
+        ctx.call("pgpu_set_fitch_tile_words", args.fitch_tile)
+        tile, tile_ms = args.fitch_tile, None
+    else:
+        tile, tile_ms = fitch.autotune_tile(tr, tips, ld, n_sites, 4, wd, out, sc, tot, ctx, reps=10)
     t_tune = time.perf_counter() - t_tune
     clocks = ClockSampler(local)
     clocks.start()
@@ -284,7 +289,8 @@ def bench_fitch(args, rank, world, local):
                      "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                      "peak_source": peak_src, "algorithmic_bytes": alg_bytes,
                      "traffic": profile_traffic("fitch_tree_split_kernel_1024x1e6"),
-                     "kernel": "fitch_tree_split_kernel<4>", "per_launch_ms": per_launch_ms},
+                     "kernel": f"tree_split_kernel<FitchOp<4, {2 if tile > 128 else 1}>>",
+                     "per_launch_ms": per_launch_ms},
         "e2e": {"value": units / e2e_s, "unit": "node-site updates/s",
                 "h2d_bytes_per_step": int(words.nbytes + w.nbytes),
                 "d2h_bytes_per_step": int(pin_out.nbytes + pin_sc.nbytes + 8),
@@ -1212,6 +1218,8 @@ def main():
     ap.add_argument("--prune-sites", type=int, default=PRUNE_SITES)
     ap.add_argument("--fitch-taxa", type=int, default=FITCH_TAXA)
     ap.add_argument("--fitch-sites", type=int, default=FITCH_SITES)
+    ap.add_argument("--fitch-tile", type=int, default=0,
+                    help="Fitch tile width in words (0: picked by the autotuner)")
     args = ap.parse_args()
     PRUNE_TAXA, PRUNE_SITES = args.prune_taxa, args.prune_sites
     FITCH_TAXA, FITCH_SITES = args.fitch_taxa, args.fitch_sites

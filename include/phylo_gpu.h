@@ -158,10 +158,14 @@ pgpu_status pgpu_fitch_tree(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t
                             uint32_t *node_sets, uint32_t *site_cost, uint64_t *total);
 
 /* Launch shape of the Fitch tree kernel on this context: the words of a
- * state-set row each CTA covers (a multiple of 4 in 32..128; 0 restores the
- * default, 128).  Results do not depend on it; the time does, through how
- * evenly the CTAs fall on the SMs, so an autotuner picks it by timing
- * (fitch.autotune_tile).  No reference counterpart. */
+ * state-set row each CTA covers (a multiple of 4 in 32..256; above 128 each
+ * lane carries two groups of 4 words).  0, the default, picks the width per
+ * launch: of 128..256, the one that gives the busiest SM the fewest words.
+ * A width whose stacks do not fit shared memory falls back to 128.  Results
+ * do not depend on it; the time does, through how evenly the CTAs fall on
+ * the SMs and how many words each step covers, so an autotuner picks it by
+ * timing (fitch.autotune_tile).  pgpu_get_fitch_tile_words returns the width
+ * set, 0 for the default.  No reference counterpart. */
 pgpu_status pgpu_set_fitch_tile_words(pgpu_ctx *ctx, int words);
 int pgpu_get_fitch_tile_words(const pgpu_ctx *ctx);
 

@@ -535,87 +535,170 @@ struct FitchSplitArgs {
   size_t ld, n_words, n_sites;
   int32_t n_tips;
   int n_top, rows;                       // rows: ring + stack rows per warp
-  int tile_words;                        // words per CTA: 4 per active lane, <= 128
+  int tile_words;                        // words per CTA: 4 per active lane and part
+  int count16;                           // per-site counts fit 16 bits (< 65,536 internal nodes)
+  int tcm_period;                        // TcmOp<true>: steps between flushes of the packed sums
   const uint32_t *table;                 // cost-matrix pair table (TcmOp), else null
   int *flag;                             // error word (TcmOp: a pair without median)
 };
 
 // The per-word operation of the segmented tree kernel, with its per-site
-// cost bookkeeping.
-//   FitchOp<LB>  the Fitch rule on LB-bit lanes; union events are counted
-//                in LB-bit lane counters (one add per word) and flushed into
-//                the CTA's per-site counts every 2^LB - 1 steps.
+// cost bookkeeping.  A lane covers NV parts of 4 words (part j of lane l
+// holds words 128 j + 4 l .. + 3 of the CTA's tile, so every part's loads
+// and stores are coalesced), PER sites per word; the CTA's per-site counts
+// are SITES = NV * 4 * PER 32-bit words per lane, [site][lane].
+//   FitchOp<LB, NV>  the Fitch rule on LB-bit lanes; union events are
+//                counted in LB-bit lane counters (one add per word) and
+//                flushed into the per-site counts every 2^LB - 1 steps.
+//                While a site's count fits 16 bits, one flush add carries
+//                two sites' counts (sites 0/4, 2/6, 1/5, 3/7 of a 4-bit
+//                word; 0/2, 1/3 of an 8-bit word; 0/1 of a 16-bit word).
 //   TcmOp        a cost-matrix character on 4-bit codes (csrc/tcm.cu): one
 //                lookup per site in a pair table replicated once per lane in
 //                shared memory (entry e of lane l at [e][l], so a warp's
 //                lookups never share a bank), the cost summed per site in
 //                registers and added to the per-site counts at the end.
-template <int LB>
+// combine<FULL>: FULL is set for CTAs whose words all lie inside the
+// alignment, so no lane of theirs needs the valid-lane mask.
+template <int LB, int NV_>
 struct FitchOp {
+  static constexpr int NV = NV_;
   static constexpr int PER = Lanes<LB>::PER;
+  static constexpr int SITES = NV * 4 * PER;
   static constexpr uint32_t FLUSH = Lanes<LB>::FLUSH;
-  static constexpr uint32_t LSB = Lanes<LB>::H >> (LB - 1);
-  static constexpr int MIN_BLOCKS = 8;
+  static constexpr int MIN_BLOCKS = NV == 1 ? 8 : 4;
   static constexpr size_t EXTRA_SMEM = 0;
-  uint4 cnt;
+  static constexpr bool FULL_ANY_WIDTH = true;   // idle lanes' counts are never read
+  uint32_t cnt[NV][4];
   uint32_t since;
   __device__ __forceinline__ void init(const FitchSplitArgs &, uint32_t *, int) {
-    cnt = make_uint4(0, 0, 0, 0);
+#pragma unroll
+    for (int j = 0; j < NV; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) cnt[j][q] = 0;
     since = 0;
   }
-  // LB-bit lane counters into the shared per-site counts
-  __device__ __forceinline__ void flush(uint32_t *sitecnt, int lane) {
-    const uint32_t c4[4] = {cnt.x, cnt.y, cnt.z, cnt.w};
+  // the LB-bit lane counters into the shared per-site counts
+  __device__ __forceinline__ void flush(const FitchSplitArgs &p, uint32_t *sitecnt, int lane) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
+    for (int j = 0; j < NV; ++j)
 #pragma unroll
-      for (int l = 0; l < PER; ++l) {
-        const uint32_t v = LB < 32 ? (c4[q] >> (l * LB)) & FLUSH : c4[q];
-        if (v) atomicAdd(&sitecnt[(q * PER + l) * 32 + lane], v);
+      for (int q = 0; q < 4; ++q) {
+        const uint32_t c = cnt[j][q];
+        uint32_t *s = sitecnt + (size_t)((j * 4 + q) * PER) * 32 + lane;
+        if (LB == 32) {
+          atomicAdd(s, c);
+        } else if (p.count16) {
+          if (LB == 4) {
+            const uint32_t t = c & 0x0F0F0F0Fu, u = (c >> 4) & 0x0F0F0F0Fu;
+            atomicAdd(s, t & 0x00FF00FFu);
+            atomicAdd(s + 32, (t >> 8) & 0x00FF00FFu);
+            atomicAdd(s + 64, u & 0x00FF00FFu);
+            atomicAdd(s + 96, (u >> 8) & 0x00FF00FFu);
+          } else if (LB == 8) {
+            atomicAdd(s, c & 0x00FF00FFu);
+            atomicAdd(s + 32, (c >> 8) & 0x00FF00FFu);
+          } else {
+            atomicAdd(s, c);
+          }
+        } else {
+#pragma unroll
+          for (int l = 0; l < PER; ++l) atomicAdd(s + l * 32, (c >> (l * LB)) & FLUSH);
+        }
+        cnt[j][q] = 0;
       }
-    cnt = make_uint4(0, 0, 0, 0);
   }
-  __device__ __forceinline__ uint4 combine(const uint4 &x, const uint4 &y, const uint4 &valid,
-                                           uint32_t *sitecnt, int lane) {
-    uint4 e;
-    const uint4 med = fitch_quad<LB>(x, y, valid, e);
-    cnt.x += e.x & valid.x & LSB;
-    cnt.y += e.y & valid.y & LSB;
-    cnt.z += e.z & valid.z & LSB;
-    cnt.w += e.w & valid.w & LSB;
+  template <bool FULL>
+  __device__ __forceinline__ uint4 combine(const uint4 &x, const uint4 &y, const uint4 &valid, int j) {
+    uint32_t e0, e1, e2, e3;
+    uint4 m;
+    m.x = fitch_word<LB>(x.x, y.x, e0);
+    m.y = fitch_word<LB>(x.y, y.y, e1);
+    m.z = fitch_word<LB>(x.z, y.z, e2);
+    m.w = fitch_word<LB>(x.w, y.w, e3);
+    if (!FULL) {
+      m.x &= valid.x, m.y &= valid.y, m.z &= valid.z, m.w &= valid.w;
+      e0 &= valid.x, e1 &= valid.y, e2 &= valid.z, e3 &= valid.w;
+    }
+    cnt[j][0] += e0;
+    cnt[j][1] += e1;
+    cnt[j][2] += e2;
+    cnt[j][3] += e3;
+    return m;
+  }
+  // once per step, after its parts
+  __device__ __forceinline__ void step(const FitchSplitArgs &p, uint32_t *sitecnt, int lane) {
     if (LB < 32 && ++since == FLUSH) {
-      flush(sitecnt, lane);
+      flush(p, sitecnt, lane);
       since = 0;
     }
-    return med;
   }
-  __device__ __forceinline__ void finish(const FitchSplitArgs &, uint32_t *sitecnt, int lane) {
-    flush(sitecnt, lane);
+  __device__ __forceinline__ void finish(const FitchSplitArgs &p, uint32_t *sitecnt, int lane) {
+    flush(p, sitecnt, lane);
+  }
+  __device__ __forceinline__ void check_root(const FitchSplitArgs &, const uint4 (&)[NV],
+                                             const bool (&)[NV], const size_t (&)[NV]) const {}
+  // the count of site l of word q of part j
+  __device__ __forceinline__ uint32_t count(const FitchSplitArgs &p, const uint32_t *sitecnt, int j,
+                                            int q, int l, int lane) const {
+    const uint32_t *s = sitecnt + (size_t)((j * 4 + q) * PER) * 32 + lane;
+    if (LB == 32 || !p.count16) return s[l * 32];
+    int e, h;
+    if (LB == 4) {
+      const int b = l >> 1;
+      e = 2 * (l & 1) + (b & 1);
+      h = b >> 1;
+    } else if (LB == 8) {
+      e = l & 1;
+      h = l >> 1;
+    } else {
+      e = 0;
+      h = l;
+    }
+    return (s[e * 32] >> (16 * h)) & 0xFFFFu;
   }
 };
 
+// TcmOp<PACKED>: the pair table arrives as cost << 4 | code (bit 31: no
+// median).  PACKED (every cost below 4,096) re-packs it in shared memory as
+// cost << 16 | code, so one add per site sums the cost in the high half of a
+// register (the codes pile up in the low half and are dropped); the sums go
+// to the per-site counts every tcm_period steps, before either half can
+// carry.  A pair without a median yields code 0, and code 0 has no median
+// with anything, so such a pair leaves code 0 at the root: the root's row
+// is checked once instead of every entry.
+template <bool PACKED>
 struct TcmOp {
+  static constexpr int NV = 1;
   static constexpr int PER = 8;
+  static constexpr int SITES = 32;
   static constexpr int MIN_BLOCKS = 4;
   static constexpr size_t EXTRA_SMEM = 256 * 32 * 4;
-  static constexpr uint32_t NONE = 0x80000000u;   // pair without a median
+  static constexpr bool FULL_ANY_WIDTH = false;  // an idle lane's code 0 would raise the flag
   const uint32_t *tb;
   uint32_t acc[32];
-  uint32_t none;
+  int since;
   // every thread of the CTA takes part in filling the table; the kernel's
   // barrier after init() publishes it
   __device__ __forceinline__ void init(const FitchSplitArgs &p, uint32_t *extra, int tid) {
-    for (int i = tid; i < 256 * 32; i += FS_W * 32) extra[i] = __ldg(p.table + (i >> 5));
+    for (int i = tid; i < 256 * 32; i += FS_W * 32) {
+      uint32_t e = __ldg(p.table + (i >> 5));
+      if (PACKED) e = (e >> 31) ? 0u : ((e >> 4) << 16) | (e & 15u);
+      extra[i] = e;
+    }
     tb = extra + (tid & 31);
 #pragma unroll
     for (int i = 0; i < 32; ++i) acc[i] = 0;
-    none = 0;
+    since = 0;
   }
+  template <bool FULL>
   __device__ __forceinline__ uint32_t word(uint32_t xa, uint32_t xb, uint32_t valid, int q) {
-    // lanes past the last site read as code 1, which always has a median
-    const uint32_t fill = 0x11111111u & ~valid;
-    xa = (xa & valid) | fill;
-    xb = (xb & valid) | fill;
+    if (!FULL) {
+      // lanes past the last site read as code 1, which always has a median
+      const uint32_t fill = 0x11111111u & ~valid;
+      xa = (xa & valid) | fill;
+      xb = (xb & valid) | fill;
+    }
     // the table index (a_l << 4) | b_l of every site, as bytes: even sites
     // 2k in byte k of ev, odd sites 2k + 1 in byte k of od
     const uint32_t ev = ((xa << 4) & 0xF0F0F0F0u) | (xb & 0x0F0F0F0Fu);
@@ -627,8 +710,7 @@ struct TcmOp {
       e[2 * k + 1] = tb[__byte_perm(od, 0u, 0x4440u + k) << 5];
     }
 #pragma unroll
-    for (int l = 0; l < 8; ++l) acc[q * 8 + l] += e[l] >> 4;
-    none |= e[0] | e[1] | e[2] | e[3] | e[4] | e[5] | e[6] | e[7];
+    for (int l = 0; l < 8; ++l) acc[q * 8 + l] += PACKED ? e[l] : e[l] >> 4;
     // the median codes are the entries' low nibbles: gather the low bytes of
     // the even and the odd sites' entries, then interleave their nibbles
     const uint32_t ce = __byte_perm(__byte_perm(e[0], e[2], 0x0040u), __byte_perm(e[4], e[6], 0x0040u),
@@ -636,70 +718,78 @@ struct TcmOp {
     const uint32_t co = __byte_perm(__byte_perm(e[1], e[3], 0x0040u), __byte_perm(e[5], e[7], 0x0040u),
                                     0x5410u);
     const uint32_t out = (ce & 0x0F0F0F0Fu) | ((co << 4) & 0xF0F0F0F0u);
-    return out & valid;
+    return FULL ? out : out & valid;
   }
-  __device__ __forceinline__ uint4 combine(const uint4 &x, const uint4 &y, const uint4 &valid,
-                                           uint32_t *, int) {
+  template <bool FULL>
+  __device__ __forceinline__ uint4 combine(const uint4 &x, const uint4 &y, const uint4 &valid, int) {
     uint4 m;
-    m.x = word(x.x, y.x, valid.x, 0);
-    m.y = word(x.y, y.y, valid.y, 1);
-    m.z = word(x.z, y.z, valid.z, 2);
-    m.w = word(x.w, y.w, valid.w, 3);
+    m.x = word<FULL>(x.x, y.x, valid.x, 0);
+    m.y = word<FULL>(x.y, y.y, valid.y, 1);
+    m.z = word<FULL>(x.z, y.z, valid.z, 2);
+    m.w = word<FULL>(x.w, y.w, valid.w, 3);
     return m;
   }
-  __device__ __forceinline__ void finish(const FitchSplitArgs &p, uint32_t *sitecnt, int lane) {
+  __device__ __forceinline__ void flush(uint32_t *sitecnt, int lane) {
 #pragma unroll
-    for (int i = 0; i < 32; ++i)
-      if (acc[i]) atomicAdd(&sitecnt[i * 32 + lane], acc[i]);
-    if (none & NONE) atomicOr(p.flag, PGPU_FLAG_BADCODE);
+    for (int i = 0; i < 32; ++i) {
+      const uint32_t v = PACKED ? acc[i] >> 16 : acc[i];
+      if (v) atomicAdd(&sitecnt[i * 32 + lane], v);
+      acc[i] = 0;
+    }
+  }
+  __device__ __forceinline__ void step(const FitchSplitArgs &p, uint32_t *sitecnt, int lane) {
+    if (PACKED && ++since == p.tcm_period) {
+      flush(sitecnt, lane);
+      since = 0;
+    }
+  }
+  __device__ __forceinline__ void finish(const FitchSplitArgs &, uint32_t *sitecnt, int lane) {
+    flush(sitecnt, lane);
+  }
+  // warp 0, after the CTA's last barrier: a valid site whose root code is 0
+  // met a pair without a median
+  __device__ __forceinline__ void check_root(const FitchSplitArgs &p, const uint4 (&valid)[1],
+                                             const bool (&act)[1], const size_t (&word)[1]) const {
+    if (!act[0]) return;
+    const uint4 r = __ldcg(reinterpret_cast<const uint4 *>(p.node_sets + (size_t)(p.n_tips - 2) * p.ld +
+                                                           word[0]));
+    const uint32_t rw[4] = {r.x, r.y, r.z, r.w}, vw[4] = {valid[0].x, valid[0].y, valid[0].z, valid[0].w};
+    uint32_t zero = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t y = rw[q] | ~vw[q];   // lanes past the sites read as 0xF
+      zero |= (y - 0x11111111u) & ~y & 0x88888888u;
+    }
+    if (zero) atomicOr(p.flag, PGPU_FLAG_BADCODE);
+  }
+  __device__ __forceinline__ uint32_t count(const FitchSplitArgs &, const uint32_t *sitecnt, int,
+                                            int q, int l, int lane) const {
+    return sitecnt[(q * 8 + l) * 32 + lane];
   }
 };
 
-// one warp's region: ring [FS_P][32] then stack [rows - FS_P][32] uint4
-// (its finished segments' results at the bottom, the walk above them); after
-// the walks the rings hold the joining nodes' results, FS_W * FS_P >= FS_S
+// one warp's region: ring [FS_P] rows then stack [rows - FS_P] rows, a row
+// being NV parts x 32 lanes of uint4 (its finished segments' results at the
+// bottom of the stack, the walk above them); after the walks the rings hold
+// the joining nodes' results, FS_W * FS_P >= FS_S
 static_assert(FS_W * FS_P >= FS_S, "joining results overlay the rings");
-__host__ __device__ inline size_t split_smem(int rows, size_t extra = 0) {
-  return (size_t)FS_W * rows * 32 * 16 + 32 * 32 * 4 + extra;   // + per-site counts, op's own
+template <class Op>
+__host__ __device__ inline size_t split_smem(int rows) {
+  return (size_t)FS_W * rows * Op::NV * 32 * 16 + (size_t)Op::SITES * 32 * 4 + Op::EXTRA_SMEM;
 }
 
-template <class Op>
-__global__ void __launch_bounds__(FS_W * 32, Op::MIN_BLOCKS) tree_split_kernel(const FitchSplitArgs p) {
-  constexpr int PER = Op::PER;
-  extern __shared__ __align__(128) unsigned char smem[];
-  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-  const int rows = p.rows;
-  uint4 *region = reinterpret_cast<uint4 *>(smem);
-  uint4 *ring = region + (size_t)w * rows * 32;
-  uint4 *stk0 = ring + FS_P * 32;
-  // per-site counts of the CTA's 128 words, shared by its warps (they all
-  // work on the same words): [4 * PER][32 lanes]
-  uint32_t *sitecnt = reinterpret_cast<uint32_t *>(region + (size_t)FS_W * rows * 32);
-  for (int i = tid; i < 32 * 4 * PER; i += FS_W * 32) sitecnt[i] = 0;
-  Op rule;
-  rule.init(p, sitecnt + 32 * 32, tid);
-  __syncthreads();
-  // a tile of tile_words words: lanes past it idle (their loads are
-  // zero-filled, nothing of theirs is counted or stored)
-  const size_t word0 = (size_t)blockIdx.x * p.tile_words + 4 * (size_t)lane;
-  const bool active = 4 * lane < p.tile_words && word0 < p.ld;
-  uint4 valid = make_uint4(0u, 0u, 0u, 0u);
-  if (4 * lane < p.tile_words) {
-    valid.x = valid_lanes<32 / PER>(word0 + 0, p.n_sites);
-    valid.y = valid_lanes<32 / PER>(word0 + 1, p.n_sites);
-    valid.z = valid_lanes<32 / PER>(word0 + 2, p.n_sites);
-    valid.w = valid_lanes<32 / PER>(word0 + 3, p.n_sites);
-  }
-  const uint32_t *col = p.tips + (active ? word0 : 0);
-  auto store = [&](int k, const uint4 &med) {
-    if (active) __stcs(reinterpret_cast<uint4 *>(p.node_sets + (size_t)k * p.ld + word0), med);
-  };
-
-  // ---- phase 1: warp w walks its segments ----
+// Phase 1 of tree_split_kernel: warp w walks its segments.  word[j] is the
+// first of part j's 4 words, act[j] whether the lane has them.
+template <class Op, bool FULL>
+__device__ __forceinline__ void split_walk(const FitchSplitArgs &p, Op &rule, uint4 *ring, uint4 *stk0,
+                                           const uint4 (&valid)[Op::NV], const bool (&act)[Op::NV],
+                                           const size_t (&word)[Op::NV], uint32_t *sitecnt, int w,
+                                           int lane) {
+  constexpr int NV = Op::NV;
   const int4 ws = p.wseg[w];
   for (int q = 0; q < ws.y; ++q) {
     const int4 sg = p.seg[ws.x + q];   // {op_off, n_ops, tip_off, n_tips}
-    uint4 *stk = stk0 + (q + 1) * 32;  // rows below hold earlier results
+    uint4 *stk = stk0 + (q + 1) * NV * 32;   // rows below hold earlier results
     const int32_t *tseq = p.tip_seq + sg.z;
     int issued = 0, consumed = 0;
     int32_t next_tip = sg.w > 0 ? __ldg(tseq) : 0;
@@ -707,7 +797,10 @@ __global__ void __launch_bounds__(FS_W * 32, Op::MIN_BLOCKS) tree_split_kernel(c
       if (issued < sg.w) {
         const int32_t tip = next_tip;
         if (issued + 1 < sg.w) next_tip = __ldg(tseq + issued + 1);
-        cp_async16(&ring[(issued % FS_P) * 32 + lane], col + (size_t)tip * p.ld, active);
+        const uint32_t *row = p.tips + (size_t)tip * p.ld;
+#pragma unroll
+        for (int j = 0; j < NV; ++j)
+          cp_async16(&ring[((issued % FS_P) * NV + j) * 32 + lane], row + (act[j] ? word[j] : 0), act[j]);
       }
       cp_async_commit();   // empty groups keep the count in step
       ++issued;
@@ -715,51 +808,115 @@ __global__ void __launch_bounds__(FS_W * 32, Op::MIN_BLOCKS) tree_split_kernel(c
 #pragma unroll
     for (int j = 0; j < FS_P; ++j) issue();
     int sp = 0;
-    uint4 top = make_uint4(0, 0, 0, 0);
+    uint4 top[NV];
     bool top_valid = false;
-    auto pop = [&]() -> uint4 {
+    auto pop = [&](uint4 (&dst)[NV]) {
       if (top_valid) {
         top_valid = false;
-        return top;
+#pragma unroll
+        for (int j = 0; j < NV; ++j) dst[j] = top[j];
+        return;
       }
-      return stk[(--sp) * 32 + lane];
+      --sp;
+#pragma unroll
+      for (int j = 0; j < NV; ++j) dst[j] = stk[(sp * NV + j) * 32 + lane];
+    };
+    auto from_ring = [&](uint4 (&dst)[NV]) {
+#pragma unroll
+      for (int j = 0; j < NV; ++j) dst[j] = ring[((consumed % FS_P) * NV + j) * 32 + lane];
+      ++consumed;
     };
     const int4 *ops = p.ops + sg.x;
     int4 op = __ldg(ops);
     for (int i = 0; i < sg.y; ++i) {
       const int4 next = i + 1 < sg.y ? __ldg(ops + i + 1) : op;
       const bool ta = op.y < p.n_tips, tb = op.z < p.n_tips;
-      uint4 x = make_uint4(0, 0, 0, 0), y = make_uint4(0, 0, 0, 0);
-      if (!tb) y = pop();
-      if (!ta) x = pop();
+      uint4 x[NV], y[NV];
+      if (!tb) pop(y);
+      if (!ta) pop(x);
       // a step's tips are the next ones of the sequence: the first needs all
       // copy groups but the FS_P-1 newest, the second all but the FS_P-2 newest
       if (ta) {
         cp_async_wait<FS_P - 1>();
-        x = ring[(consumed % FS_P) * 32 + lane];
-        ++consumed;
+        from_ring(x);
         if (tb) {
           cp_async_wait<FS_P - 2>();
-          y = ring[(consumed % FS_P) * 32 + lane];
-          ++consumed;
+          from_ring(y);
         }
       } else if (tb) {
         cp_async_wait<FS_P - 1>();
-        y = ring[(consumed % FS_P) * 32 + lane];
-        ++consumed;
+        from_ring(y);
       }
-      const uint4 med = rule.combine(x, y, valid, sitecnt, lane);
+      uint4 med[NV];
+#pragma unroll
+      for (int j = 0; j < NV; ++j) med[j] = rule.template combine<FULL>(x[j], y[j], valid[j], j);
+      rule.step(p, sitecnt, lane);
       // slots read this step are refilled only once their values are in use
       while (issued < consumed + FS_P) issue();
-      if (top_valid) stk[(sp++) * 32 + lane] = top;
-      top = med;
+      if (top_valid) {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) stk[(sp * NV + j) * 32 + lane] = top[j];
+        ++sp;
+      }
+      uint32_t *dst = p.node_sets + (size_t)op.x * p.ld;
+#pragma unroll
+      for (int j = 0; j < NV; ++j) {
+        top[j] = med[j];
+        if (act[j]) __stcs(reinterpret_cast<uint4 *>(dst + word[j]), med[j]);
+      }
       top_valid = true;
-      store(op.x, med);
       op = next;
     }
     cp_async_wait<0>();
-    stk0[q * 32 + lane] = top;   // this segment's result
+#pragma unroll
+    for (int j = 0; j < NV; ++j) stk0[(q * NV + j) * 32 + lane] = top[j];   // this segment's result
   }
+}
+
+template <class Op>
+__global__ void __launch_bounds__(FS_W * 32, Op::MIN_BLOCKS) tree_split_kernel(const FitchSplitArgs p) {
+  constexpr int NV = Op::NV;
+  constexpr int PER = Op::PER;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  const int rows = p.rows;
+  uint4 *region = reinterpret_cast<uint4 *>(smem);
+  uint4 *ring = region + (size_t)w * rows * NV * 32;
+  uint4 *stk0 = ring + FS_P * NV * 32;
+  // per-site counts of the CTA's words, shared by its warps (they all work
+  // on the same words): [SITES][32 lanes]
+  uint32_t *sitecnt = reinterpret_cast<uint32_t *>(region + (size_t)FS_W * rows * NV * 32);
+  for (int i = tid; i < 32 * Op::SITES; i += FS_W * 32) sitecnt[i] = 0;
+  Op rule;
+  rule.init(p, sitecnt + 32 * Op::SITES, tid);
+  __syncthreads();
+  // a tile of tile_words words: lanes past it idle (their loads are
+  // zero-filled, nothing of theirs is counted or stored)
+  const size_t tile0 = (size_t)blockIdx.x * p.tile_words;
+  size_t word[NV];
+  bool act[NV];
+  uint4 valid[NV];
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    const bool in_tile = 128 * j + 4 * lane < p.tile_words;
+    word[j] = tile0 + 128 * j + 4 * lane;
+    act[j] = in_tile && word[j] < p.ld;
+    valid[j] = make_uint4(0u, 0u, 0u, 0u);
+    if (in_tile) {
+      valid[j].x = valid_lanes<32 / PER>(word[j] + 0, p.n_sites);
+      valid[j].y = valid_lanes<32 / PER>(word[j] + 1, p.n_sites);
+      valid[j].z = valid_lanes<32 / PER>(word[j] + 2, p.n_sites);
+      valid[j].w = valid_lanes<32 / PER>(word[j] + 3, p.n_sites);
+    }
+  }
+  const bool full = (tile0 + p.tile_words) * PER <= p.n_sites &&
+                    (Op::FULL_ANY_WIDTH || p.tile_words == 128 * NV);
+
+  // ---- phase 1: warp w walks its segments ----
+  if (full)
+    split_walk<Op, true>(p, rule, ring, stk0, valid, act, word, sitecnt, w, lane);
+  else
+    split_walk<Op, false>(p, rule, ring, stk0, valid, act, word, sitecnt, w, lane);
   __syncthreads();
   // ---- phase 2: warp 0 joins the segments ----
   // reference of a child: tip id (>= 0), segment result -1 - (warp * 32 +
@@ -767,45 +924,60 @@ __global__ void __launch_bounds__(FS_W * 32, Op::MIN_BLOCKS) tree_split_kernel(c
   if (w == 0) {
     for (int i = 0; i < p.n_top; ++i) {
       const int4 op = __ldg(p.top + i);
-      uint4 c[2];
+      uint4 c[2][NV];
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int ref = h == 0 ? op.y : op.z;
-        if (ref >= 0) {
-          c[h] = active ? __ldcs(reinterpret_cast<const uint4 *>(col + (size_t)ref * p.ld))
-                        : make_uint4(0, 0, 0, 0);
-        } else if (ref > -1000) {
+        size_t at_row = 0;
+        if (ref > -1000 && ref < 0) {
           const int at = -1 - ref;
-          c[h] = region[((size_t)(at >> 5) * rows + FS_P + (at & 31)) * 32 + lane];
-        } else {
+          at_row = (size_t)(at >> 5) * rows + FS_P + (at & 31);
+        } else if (ref <= -1000) {
           const int t = -1000 - ref;
-          c[h] = region[((size_t)(t / FS_P) * rows + t % FS_P) * 32 + lane];
+          at_row = (size_t)(t / FS_P) * rows + t % FS_P;
+        }
+#pragma unroll
+        for (int j = 0; j < NV; ++j) {
+          if (ref >= 0)
+            c[h][j] = act[j] ? __ldcs(reinterpret_cast<const uint4 *>(p.tips + (size_t)ref * p.ld + word[j]))
+                             : make_uint4(0, 0, 0, 0);
+          else
+            c[h][j] = region[(at_row * NV + j) * 32 + lane];
         }
       }
-      const uint4 med = rule.combine(c[0], c[1], valid, sitecnt, lane);
-      region[((size_t)(i / FS_P) * rows + i % FS_P) * 32 + lane] = med;
-      store(op.x, med);
+      const size_t out_row = (size_t)(i / FS_P) * rows + i % FS_P;
+      uint32_t *dst = p.node_sets + (size_t)op.x * p.ld;
+#pragma unroll
+      for (int j = 0; j < NV; ++j) {
+        const uint4 med = rule.template combine<false>(c[0][j], c[1][j], valid[j], j);
+        region[(out_row * NV + j) * 32 + lane] = med;
+        if (act[j]) __stcs(reinterpret_cast<uint4 *>(dst + word[j]), med);
+      }
+      rule.step(p, sitecnt, lane);
     }
   }
   // ---- phase 3: the per-site counts, then the weighted total ----
   rule.finish(p, sitecnt, lane);
   __syncthreads();
   if (w == 0) {
+    rule.check_root(p, valid, act, word);
     unsigned long long wsum = 0;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const size_t s0 = (word0 + q) * PER;
+    for (int j = 0; j < NV; ++j)
 #pragma unroll
-      for (int l = 0; l < PER; ++l) {
-        const size_t s = s0 + l;
-        if (active && s < p.n_sites) {
-          const uint32_t v = sitecnt[(q * PER + l) * 32 + lane];
-          if (p.site_cost) p.site_cost[s] = v;
-          const uint32_t wt = p.weights ? __ldg(p.weights + s) : 1u;
-          wsum += (unsigned long long)wt * v;
+      for (int q = 0; q < 4; ++q) {
+        const size_t s0 = (word[j] + q) * PER;
+#pragma unroll
+        for (int l = 0; l < PER; ++l) {
+          const size_t s = s0 + l;
+          if (act[j] && s < p.n_sites) {
+            const uint32_t v = rule.count(p, sitecnt, j, q, l, lane);
+            if (p.site_cost) p.site_cost[s] = v;
+            const uint32_t wt = p.weights ? __ldg(p.weights + s) : 1u;
+            wsum += (unsigned long long)wt * v;
+          }
         }
       }
-    }
     wsum = warp_sum_u64(wsum);
     if (lane == 0 && wsum) atomicAdd(p.total, wsum);
   }
@@ -1083,13 +1255,36 @@ pgpu_status split_device(pgpu_ctx *ctx, const pgpu_tree *tree, const int4 **ops,
 
 template <class Op>
 cudaError_t launch_split(cudaStream_t stream, const FitchSplitArgs &a, size_t tiles) {
-  const size_t smem = split_smem(a.rows, Op::EXTRA_SMEM);
+  const size_t smem = split_smem<Op>(a.rows);
   cudaError_t e = cudaFuncSetAttribute(tree_split_kernel<Op>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)std::max<size_t>(smem, 48 * 1024));
   if (e != cudaSuccess) return e;
   tree_split_kernel<Op><<<(unsigned)tiles, FS_W * 32, smem, stream>>>(a);
   return cudaGetLastError();
+}
+
+template <int LB>
+cudaError_t launch_fitch_split(cudaStream_t stream, const FitchSplitArgs &a, size_t tiles) {
+  return a.tile_words > 128 ? launch_split<FitchOp<LB, 2>>(stream, a, tiles)
+                            : launch_split<FitchOp<LB, 1>>(stream, a, tiles);
+}
+
+// The default tile width of the Fitch tree kernel: of the widths 128..256
+// (multiples of 4), the one that gives the busiest SM the fewest words when
+// all CTAs are resident at once; ties keep the narrower width.
+int default_tile_words(size_t n_words, int n_sm) {
+  int best = 128;
+  size_t best_cost = SIZE_MAX;
+  for (int w = 128; w <= 256; w += 4) {
+    const size_t tiles = (n_words + w - 1) / w;
+    const size_t cost = ((tiles + n_sm - 1) / n_sm) * (size_t)w;
+    if (cost < best_cost) {
+      best = w;
+      best_cost = cost;
+    }
+  }
+  return best;
 }
 
 // 64-bit elements: the element kernel over the plain schedule
@@ -1156,20 +1351,27 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
   a.n_tips = tree->n_tips;
   a.n_top = (int)sp.top.size();
   a.rows = sp.rows;
-  if (split_smem(a.rows) > ctx->smem_optin)
+  // LB = 4 has the most per-site counters, so it bounds every width's need
+  if (split_smem<FitchOp<4, 1>>(a.rows) > ctx->smem_optin)
     return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: tree needs a stack of %d rows; too deep",
                         a.rows);
-  a.tile_words = ctx->fitch_tile_words > 0 ? ctx->fitch_tile_words : 128;
+  a.tile_words = ctx->fitch_tile_words > 0 ? ctx->fitch_tile_words
+                                           : default_tile_words(n_words, ctx->num_sms);
+  // two parts per lane only where their stacks fit; the width only shapes
+  // the launch, so a narrower one gives the same results
+  if (a.tile_words > 128 && split_smem<FitchOp<4, 2>>(a.rows) > ctx->smem_optin) a.tile_words = 128;
+  a.count16 = tree->n_tips - 1 <= 65535;
+  a.tcm_period = 0;
   a.table = nullptr;
   a.flag = ctx->d_flag;
   const size_t tiles = (n_words + a.tile_words - 1) / a.tile_words;
   if (tiles > 0x7fffffffu) return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: too many tiles");
   cudaError_t e;
   switch (lb) {
-    case 4: e = launch_split<FitchOp<4>>(s, a, tiles); break;
-    case 8: e = launch_split<FitchOp<8>>(s, a, tiles); break;
-    case 16: e = launch_split<FitchOp<16>>(s, a, tiles); break;
-    default: e = launch_split<FitchOp<32>>(s, a, tiles); break;
+    case 4: e = launch_fitch_split<4>(s, a, tiles); break;
+    case 8: e = launch_fitch_split<8>(s, a, tiles); break;
+    case 16: e = launch_fitch_split<16>(s, a, tiles); break;
+    default: e = launch_fitch_split<32>(s, a, tiles); break;
   }
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
@@ -1183,13 +1385,15 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
 }  // namespace
 
 // The cost-matrix postorder (csrc/tcm.cu) on the segmented schedule: 4-bit
-// codes, the packed pair table already on the device.  *launched is false
-// when the tree's stacks and the lane-replicated table do not fit one CTA's
-// shared memory; the caller then uses its single-walk kernel.
+// codes, the packed pair table already on the device.  flush_period > 0
+// (every cost small enough) selects the re-packed table with one add per
+// site.  *launched is false when the tree's stacks and the lane-replicated
+// table do not fit one CTA's shared memory; the caller then uses its
+// single-walk kernel.
 pgpu_status pgpu_tcm_tree_split(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
                                 size_t ld, const uint32_t *weights, size_t n_sites,
-                                const uint32_t *table_dev, uint32_t *node_sets, uint32_t *site_cost,
-                                unsigned long long *total, bool *launched) {
+                                const uint32_t *table_dev, int flush_period, uint32_t *node_sets,
+                                uint32_t *site_cost, unsigned long long *total, bool *launched) {
   *launched = false;
   if (((uintptr_t)tips | (uintptr_t)node_sets) & 15) return PGPU_OK;
   if (ld % 4 != 0) return PGPU_OK;
@@ -1197,7 +1401,7 @@ pgpu_status pgpu_tcm_tree_split(pgpu_ctx *ctx, const pgpu_tree *tree, const uint
   FitchSplitArgs a;
   PGPU_TRY(split_device(ctx, tree, &a.ops, &a.seg, &a.top, &a.wseg, &a.tip_seq));
   const SplitSchedule &sp = ctx->split;
-  if (split_smem(sp.rows, TcmOp::EXTRA_SMEM) > ctx->smem_optin) return PGPU_OK;
+  if (split_smem<TcmOp<false>>(sp.rows) > ctx->smem_optin) return PGPU_OK;
   a.tips = tips;
   a.weights = weights;
   a.node_sets = node_sets;
@@ -1210,10 +1414,13 @@ pgpu_status pgpu_tcm_tree_split(pgpu_ctx *ctx, const pgpu_tree *tree, const uint
   a.n_top = (int)sp.top.size();
   a.rows = sp.rows;
   a.tile_words = 128;
+  a.count16 = 0;
+  a.tcm_period = flush_period;
   a.table = table_dev;
   a.flag = ctx->d_flag;
   const size_t tiles = (n_words + 127) / 128;
-  cudaError_t e = launch_split<TcmOp>(ctx->stream, a, tiles);
+  cudaError_t e = flush_period > 0 ? launch_split<TcmOp<true>>(ctx->stream, a, tiles)
+                                   : launch_split<TcmOp<false>>(ctx->stream, a, tiles);
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
     return pgpu_set_err(ctx, PGPU_ERR_CUDA, "launch of tree_split_kernel<TcmOp> failed: %s",
@@ -1284,15 +1491,15 @@ pgpu_status pgpu_fitch_median2(pgpu_ctx *ctx, const uint32_t *a, const uint32_t 
 
 pgpu_status pgpu_set_fitch_tile_words(pgpu_ctx *ctx, int words) {
   if (!ctx) return PGPU_ERR_ARG;
-  if (words != 0 && (words < 32 || words > 128 || words % 4 != 0))
-    return pgpu_set_err(ctx, PGPU_ERR_ARG, "fitch tile: 0 or a multiple of 4 in 32..128 words (got %d)",
+  if (words != 0 && (words < 32 || words > 256 || words % 4 != 0))
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "fitch tile: 0 or a multiple of 4 in 32..256 words (got %d)",
                         words);
   ctx->fitch_tile_words = words;
   return PGPU_OK;
 }
 
 int pgpu_get_fitch_tile_words(const pgpu_ctx *ctx) {
-  return ctx && ctx->fitch_tile_words > 0 ? ctx->fitch_tile_words : 128;
+  return ctx ? ctx->fitch_tile_words : 0;
 }
 
 pgpu_status pgpu_nonadditive_median2(pgpu_ctx *ctx, const int64_t *x, const int64_t *y,

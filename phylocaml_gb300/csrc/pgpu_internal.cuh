@@ -143,8 +143,8 @@ pgpu_status pgpu_schedule_device(pgpu_ctx *ctx, const pgpu_tree *tree, const Tre
 // memory.
 pgpu_status pgpu_tcm_tree_split(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
                                 size_t ld, const uint32_t *weights, size_t n_sites,
-                                const uint32_t *table_dev, uint32_t *node_sets, uint32_t *site_cost,
-                                unsigned long long *total, bool *launched);
+                                const uint32_t *table_dev, int flush_period, uint32_t *node_sets,
+                                uint32_t *site_cost, unsigned long long *total, bool *launched);
 
 // ---------------------------------------------------------------------------
 // device helpers: mbarrier, bulk copies, bounded waits

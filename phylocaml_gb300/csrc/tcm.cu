@@ -376,10 +376,15 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
   PGPU_TRY(pgpu_stage_commit(ctx, 256 * sizeof(uint32_t)));
   PGPU_CUDA(ctx, cudaMemsetAsync(total, 0, sizeof(unsigned long long), ctx->stream));
   if (n_words == 0) return PGPU_OK;
-  // the segmented schedule: subtrees walked by four warps per 128-word slice
+  // the segmented schedule: subtrees walked by four warps per 128-word slice.
+  // With every cost below 4,096 it sums costs in the high 16 bits of a
+  // register next to the codes' low 16 bits, flushing before either carries:
+  // after p steps a site's sum is at most p * emax and its codes 15 p.
+  const int period = emax < 4096 ? (int)std::min<uint64_t>(65535 / 15, 65535 / std::max<uint64_t>(emax, 1))
+                                  : 0;
   bool launched = false;
   PGPU_TRY(pgpu_tcm_tree_split(ctx, tree, tips, ld, weights, n_sites,
-                               static_cast<const uint32_t *>(d), node_sets, site_cost, total,
+                               static_cast<const uint32_t *>(d), period, node_sets, site_cost, total,
                                &launched));
   if (launched) return PGPU_OK;
   TcmArgs a;

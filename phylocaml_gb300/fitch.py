@@ -89,22 +89,36 @@ def fitch_tree_dev(tree: RootedTree, tips_dev, ld_words: int, n_sites: int, lane
 # ---- launch-shape autotuning -------------------------------------------------
 # The tree kernel gives each CTA tile_words words of every row, and all of a
 # launch's CTAs are resident at once, so the SM that holds the most tiles
-# sets the time.  128-word tiles over 125,000 words (1e6 sites at 4-bit
-# lanes) make 977 CTAs: 65 of the 152 SMs hold 7, the rest 6.  Narrower tiles
-# even that out.  Candidates are the widths whose busiest SM handles the
-# fewest words (tiles per SM rounded up, times the width), and each is timed
-# on the caller's own buffers with CUDA events; results do not depend on it.
+# sets the time.  Up to 128 words a lane carries 4 words; wider tiles (up to
+# 256) give each lane two groups of 4, which spreads every step's fixed
+# work (schedule, stack, copies) over twice the words.  128-word tiles over
+# 125,000 words (1e6 sites at 4-bit lanes) make 977 CTAs, 7 on the busiest
+# SMs (896 words); 208-word tiles make 601, 4 on the busiest (832 words).
+# Candidates are the widths whose busiest SM handles the fewest words (tiles
+# per SM rounded up, times the width), and each is timed on the caller's own
+# buffers with CUDA events; results do not depend on it.
 
 def tile_candidates(n_words_: int, n_sm: int, keep: int = 6, narrowest: int = 64) -> list[int]:
-    """Tile widths (multiples of 4 from ``narrowest`` to 128; narrower tiles
+    """Tile widths (multiples of 4 from ``narrowest`` to 256; narrower tiles
     idle most lanes of each warp) ordered by the words the busiest SM
-    handles, the default 128 always included."""
+    handles, 128 and the widest-part default always included."""
     cost = {}
-    for w in range(narrowest, 129, 4):
+    for w in range(narrowest, 257, 4):
         tiles = -(-n_words_ // w)
         cost[w] = (-(-tiles // n_sm)) * w
     best = sorted(cost, key=lambda w: (cost[w], -w))[:keep]
-    return sorted(set(best) | {128}, key=lambda w: (cost[w], -w))
+    return sorted(set(best) | {128, default_tile(n_words_, n_sm)}, key=lambda w: (cost[w], -w))
+
+
+def default_tile(n_words_: int, n_sm: int) -> int:
+    """The width the library takes when none is set: of 128..256, the one
+    whose busiest SM handles the fewest words (ties to the narrower)."""
+    best, best_cost = 128, None
+    for w in range(128, 257, 4):
+        c = (-(-(-(-n_words_ // w)) // n_sm)) * w
+        if best_cost is None or c < best_cost:
+            best, best_cost = w, c
+    return best
 
 
 def autotune_tile(tree: RootedTree, tips_dev, ld_words: int, n_sites: int, lane_bits: int,

@@ -132,6 +132,32 @@ def test_tree_vs_oracle(ctx, orc, shape, lb, n_sites):
     assert r1.total == int(sc.sum())
 
 
+@pytest.mark.parametrize("lb,n_tips,n_sites,width", [(4, 90_001, 1_100, 0), (4, 90_001, 1_100, 256),
+                                                     (8, 80_001, 600, 200), (16, 80_001, 300, 0)])
+def test_tree_site_counts_above_16_bits(ctx, orc, lb, n_tips, n_sites, width):
+    """Trees of more than 65,536 internal nodes keep one 32-bit counter per
+    site (below that a flush adds two sites' 16-bit counts at once).  On a
+    caterpillar whose tips cycle through single states, most nodes are
+    union events, so per-site counts pass 2^16."""
+    from phylocaml_gb300 import fitch
+    rng = np.random.default_rng(n_tips + lb)
+    tr = T.caterpillar(n_tips)
+    n_states = min(lb, 8)
+    phase = rng.integers(0, n_states, n_sites)
+    tips = (1 << ((np.arange(n_tips)[:, None] + phase[None, :]) % n_states)).astype(np.uint8)
+    w = rng.integers(1, 9, n_sites).astype(np.uint32)
+    words = synth.pack_lanes(tips, lb)
+    ns, sc, tot, _ = orc.fitch_tree_packed(tr.left, tr.right, words, n_sites, lb, w)
+    assert sc.max() > 0xFFFF
+    try:
+        ctx.call("pgpu_set_fitch_tile_words", width)
+        r = fitch.fitch_tree(tr, words, n_sites, lb, w, ctx=ctx)
+    finally:
+        ctx.call("pgpu_set_fitch_tile_words", 0)
+    assert np.array_equal(r.node_sets, ns)
+    assert np.array_equal(r.site_cost, sc) and r.total == tot
+
+
 def test_tree_two_tips_and_zero_sites(ctx, orc):
     from phylocaml_gb300 import fitch
     tr = T.RootedTree(np.array([0], np.int32), np.array([1], np.int32), np.array([0.1, 0.1]))

@@ -20,7 +20,7 @@ def test_every_tile_width_is_bit_exact(ctx, orc, lb):
     n_sites = masks.shape[1]
     ns, sc, tot, _ = orc.fitch_tree_packed(tr.left, tr.right, words, n_sites, lb, w)
     try:
-        for width in (32, 60, 100, 104, 120, 128):
+        for width in (32, 60, 100, 104, 120, 128, 132, 168, 208, 256):
             ctx.call("pgpu_set_fitch_tile_words", width)
             assert ctx.lib.pgpu_get_fitch_tile_words(ctx.h) == width
             r = fitch.fitch_tree(tr, words, n_sites, lb, w, ctx=ctx)
@@ -28,8 +28,13 @@ def test_every_tile_width_is_bit_exact(ctx, orc, lb):
             assert np.array_equal(r.site_cost, sc) and r.total == tot, width
     finally:
         ctx.call("pgpu_set_fitch_tile_words", 0)
-    with pytest.raises(_native.NativeError):
-        ctx.call("pgpu_set_fitch_tile_words", 30)
+    assert ctx.lib.pgpu_get_fitch_tile_words(ctx.h) == 0
+    # the default width (picked per launch) gives the same results
+    r = fitch.fitch_tree(tr, words, n_sites, lb, w, ctx=ctx)
+    assert np.array_equal(r.node_sets, ns) and np.array_equal(r.site_cost, sc) and r.total == tot
+    for bad in (30, 258, 260):
+        with pytest.raises(_native.NativeError):
+            ctx.call("pgpu_set_fitch_tile_words", bad)
 
 
 def test_autotuner_picks_a_candidate(ctx):
