@@ -31,9 +31,13 @@
 //                  columns (tcgen05.ld) or tip rows, forms the product,
 //                  rescales, writes the parent's vector back into TMEM
 //                  (tcgen05.st).  Thread 0 also issues every step's MMAs.
-//   The MMA (tcgen05.commit -> mma_bar) and the epilogue (a named barrier
-//   after its TMEM stores) alternate per step, so a step's MMA never reads a
-//   vector before it is written and no mbarrier phase can be skipped.
+//   The MMA (tcgen05.commit -> mma_bar) and the epilogue (an mbarrier,
+//   `stored`, after its TMEM stores) alternate per step, so a step's MMA
+//   never reads a vector before it is written and no mbarrier phase can be
+//   skipped.  With two rate classes per pass the two classes are separate
+//   chains, each with its own mma_bar and stored barrier and its own eight
+//   epilogue warps: the MMAs of one class's next step run while the other
+//   class's epilogue runs.
 //   Every wait is bounded.  Each work item runs a step loop compiled for its
 //   padded state count and rate classes per pass.
 //   batch_fp64_kernel  the FP64 comparison form on a sample of patterns.
@@ -283,16 +287,17 @@ __device__ __forceinline__ void epi_step(const BatchArgs &p, const EpiIn &in, co
     mx = t[0];
   }
   xch[PT][in.m] = mx;
-  // the exchange joins only the four warps of this TMEM lane group (named
-  // barrier 2 + lg); it also makes the timeout verdict uniform over them, so
-  // the group leaves the step loop together
+  // the exchange joins only the warps of this TMEM lane group that share
+  // the rate class (named barrier 2 + lg, or 2 + lg + 4 rate with two rate
+  // classes per pass); it also makes the timeout verdict uniform over them,
+  // so they leave the step loop together
   {
     uint32_t all_ok;
     asm volatile(
         "{\n\t.reg .pred a, b;\n\tsetp.ne.u32 a, %1, 0;\n\t"
         "bar.red.and.pred b, %2, %3, a;\n\tselp.u32 %0, 1, 0, b;\n\t}"
         : "=r"(all_ok)
-        : "r"((uint32_t)ok), "r"(2 + in.lg), "n"(4 * 32)
+        : "r"((uint32_t)ok), "r"(2 + in.lg + (RP == 2 ? 4 * rate : 0)), "n"(RP == 2 ? 2 * 32 : 4 * 32)
         : "memory");
     ok = all_ok != 0;
   }
@@ -333,7 +338,9 @@ __device__ __forceinline__ void epi_step(const BatchArgs &p, const EpiIn &in, co
 
 // Shared state of the epilogue warps.
 struct EpiShared {
-  uint64_t *full, *empty, *mma_bar, *stored;
+  uint64_t *full, *empty;
+  uint64_t *mma_bar;         // [2]: per rate class of the pass (both complete once per step)
+  uint64_t *stored;          // [2]: the eight epilogue warps of shares 2q, 2q + 1 arrive on q
   const int4 *slot_op;       // each ring slot's postorder step, written by the producer
   unsigned char *smem;
   float (*xch)[BT_M];        // [2][BT_PARTS]: per step parity and share, lane: max entry
@@ -380,7 +387,7 @@ __device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh
       const uint32_t par = (uint32_t)((seq / BT_ST) & 1);
       in.sl = sh.smem + (size_t)slot * p.slot_bytes;
       bool got = mbar_wait_bounded(&sh.full[slot], par, p.flag);
-      got = got && mbar_wait_bounded(sh.mma_bar, (uint32_t)(seq & 1), p.flag);
+      got = got && mbar_wait_bounded(&sh.mma_bar[my_rate], (uint32_t)(seq & 1), p.flag);
       got = __all_sync(0xffffffffu, got);
       if (!got) {
         ok = false;
@@ -403,7 +410,7 @@ __device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       // this warp's vectors of the step are in TMEM and its D columns read
       __syncwarp();
-      if (lane == 0) mbar_arrive(sh.stored);
+      if (lane == 0) mbar_arrive(&sh.stored[pt >> 1]);
       if (!ok) break;
     }
     // one verdict for every epilogue warp before the barriers below
@@ -460,10 +467,14 @@ __device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh
   asm volatile("bar.sync 1, %0;" ::"n"(BT_EPI) : "memory");
 }
 
-// The MMA warp's side of one work item: per step, once the slot is loaded
-// and the epilogue warps have stored the previous step's vectors (and read
-// its D columns), one thread issues the step's tcgen05.mma for the internal
-// children and commits them to mma_bar and the slot's empty barrier.
+// The MMA warp's side of one work item: per step, once the slot is loaded,
+// one thread issues the step's tcgen05.mma for the internal children, rate
+// class by rate class.  A class's MMAs wait until its epilogue warps have
+// stored the previous step's vectors (and read its D columns), and are
+// committed to that class's mma_bar; the last commit also goes to the
+// slot's empty barrier.  With one rate class per pass the MMAs wait for
+// both halves of the epilogue and are committed to both mma_bar barriers,
+// so each barrier completes once per step either way.
 template <int KP, int RP>
 __device__ __forceinline__ void mma_item(const BatchArgs &p, const EpiShared &sh, const BVar &vg,
                                          long long &seq, bool &ok) {
@@ -472,29 +483,44 @@ __device__ __forceinline__ void mma_item(const BatchArgs &p, const EpiShared &sh
   constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NP >> 3) << 17) |
                              ((uint32_t)(BT_M >> 4) << 24);
   const int n_ops = vg.n_ops, R = vg.R, n_tips = vg.n_tips, BB = blk_bytes(vg);
+  auto commit = [&](uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     su32(bar))
+                 : "memory");
+  };
   for (int r0 = 0; r0 < R && ok; r0 += RP) {
     for (int i = 0; i < n_ops; ++i, ++seq) {
       const int slot = (int)(seq & (BT_ST - 1));
       const uint32_t par = (uint32_t)((seq / BT_ST) & 1);
-      bool got = mbar_wait_bounded(&sh.full[slot], par, p.flag);
-      if (seq > 0) got = got && mbar_wait_bounded(sh.stored, (uint32_t)((seq - 1) & 1), p.flag);
-      if (!got) {
+      if (!mbar_wait_bounded(&sh.full[slot], par, p.flag)) {
         ok = false;
         atomicOr(p.flag, PGPU_FLAG_TIMEOUT);
         return;
       }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const int4 op = sh.slot_op[slot];
       const unsigned char *sl = sh.smem + (size_t)slot * p.slot_bytes;
-      bool any = false;
+      const bool any = op.y >= n_tips || op.z >= n_tips;
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int ch = h == 0 ? op.y : op.z;
-        if (ch < n_tips) continue;
-        any = true;
-        const int sa = (op.w >> (8 * h)) & 0xff;
+      for (int q = 0; q < RP; ++q) {
+        // this class's epilogue warps are done with the previous step (with
+        // one class per pass, all sixteen)
+        bool got = true;
+        if (seq > 0) {
+          const uint32_t prev = (uint32_t)((seq - 1) & 1);
+          got = mbar_wait_bounded(&sh.stored[q], prev, p.flag);
+          if (RP == 1) got = got && mbar_wait_bounded(&sh.stored[1], prev, p.flag);
+        }
+        if (!got) {
+          ok = false;
+          atomicOr(p.flag, PGPU_FLAG_TIMEOUT);
+          return;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-        for (int q = 0; q < RP; ++q) {
+        for (int h = 0; h < 2; ++h) {
+          const int ch = h == 0 ? op.y : op.z;
+          if (ch < n_tips) continue;
+          const int sa = (op.w >> (8 * h)) & 0xff;
           const uint32_t d_col = (uint32_t)((h * RP + q) * NP);
           const uint32_t a_col = (uint32_t)(2 * RP * NP + (sa * RP + q) * KP);
           const unsigned char *blk = sl + 256 + (size_t)(h * RP + q) * BB;
@@ -509,18 +535,16 @@ __device__ __forceinline__ void mma_item(const BatchArgs &p, const EpiShared &sh
                 : "memory");
           }
         }
+        if (any)
+          commit(&sh.mma_bar[q]);
+        else
+          mbar_arrive(&sh.mma_bar[q]);
       }
       if (any) {
-        asm volatile(
-            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                su32(sh.mma_bar))
-            : "memory");
-        asm volatile(
-            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                su32(&sh.empty[slot]))
-            : "memory");
+        if (RP == 1) commit(&sh.mma_bar[1]);
+        commit(&sh.empty[slot]);
       } else {
-        mbar_arrive(sh.mma_bar);
+        if (RP == 1) mbar_arrive(&sh.mma_bar[1]);
         mbar_arrive(&sh.empty[slot]);
       }
     }
@@ -553,7 +577,7 @@ __device__ __forceinline__ void epi_item_rp(const BatchArgs &p, const EpiShared 
 
 __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs p) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ uint64_t full[BT_ST], empty[BT_ST], mma_bar, stored;
+  __shared__ uint64_t full[BT_ST], empty[BT_ST], mma_bar[2], stored[2];
   __shared__ int4 slot_op[BT_ST];
   __shared__ uint32_t tmem_base;
   __shared__ float xch[2 * BT_PARTS][BT_M];   // per step parity and share, lane: max entry
@@ -573,8 +597,10 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1 + BT_EPI_WARPS);   // the MMA commit + the epilogue warps
     }
-    mbar_init(&mma_bar, 1);
-    mbar_init(&stored, BT_EPI_WARPS);   // each epilogue warp, after a step's TMEM stores
+    for (int q = 0; q < 2; ++q) {
+      mbar_init(&mma_bar[q], 1);
+      mbar_init(&stored[q], BT_EPI_WARPS / 2);   // eight epilogue warps, after a step's TMEM stores
+    }
     fence_mbarrier_init();
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -582,7 +608,7 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
 
-  const EpiShared sh{full, empty, &mma_bar, &stored, slot_op, smem, xch, xchd, lnr, red, tmem};
+  const EpiShared sh{full, empty, mma_bar, stored, slot_op, smem, xch, xchd, lnr, red, tmem};
   if (warp == BT_PRODUCER) {
     // ------------------------------------------------------------ producer
     if (lane == 0) {
@@ -656,7 +682,7 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
         }
       }
       // the last MMAs finish before TMEM is released
-      if (seq > 0) (void)mbar_wait_bounded(&mma_bar, (uint32_t)((seq - 1) & 1), p.flag);
+      if (seq > 0) (void)mbar_wait_bounded(&mma_bar[1], (uint32_t)((seq - 1) & 1), p.flag);
     }
   } else {
     // ------------------------------------------------------------ epilogue

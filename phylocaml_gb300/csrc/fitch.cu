@@ -660,13 +660,13 @@ struct FitchOp {
 };
 
 // TcmOp<PACKED>: the pair table arrives as cost << 4 | code (bit 31: no
-// median).  PACKED (every cost below 4,096) re-packs it in shared memory as
-// cost << 16 | code, so one add per site sums the cost in the high half of a
-// register (the codes pile up in the low half and are dropped); the sums go
-// to the per-site counts every tcm_period steps, before either half can
-// carry.  A pair without a median yields code 0, and code 0 has no median
-// with anything, so such a pair leaves code 0 at the root: the root's row
-// is checked once instead of every entry.
+// median).  PACKED re-packs it in shared memory as code << 28 | cost, so one
+// add per site sums the cost in the low 28 bits of a register while the
+// codes pile up in the top 4 bits and wrap away; the sums go to the per-site
+// counts every tcm_period steps, before the cost can reach bit 28.  A pair
+// without a median yields code 0, and code 0 has no median with anything,
+// so such a pair leaves code 0 at the root: the root's row is checked once
+// instead of every entry.
 template <bool PACKED>
 struct TcmOp {
   static constexpr int NV = 1;
@@ -675,6 +675,7 @@ struct TcmOp {
   static constexpr int MIN_BLOCKS = 4;
   static constexpr size_t EXTRA_SMEM = 256 * 32 * 4;
   static constexpr bool FULL_ANY_WIDTH = false;  // an idle lane's code 0 would raise the flag
+  static constexpr uint32_t COST = 0x0FFFFFFFu;
   const uint32_t *tb;
   uint32_t acc[32];
   int since;
@@ -683,7 +684,7 @@ struct TcmOp {
   __device__ __forceinline__ void init(const FitchSplitArgs &p, uint32_t *extra, int tid) {
     for (int i = tid; i < 256 * 32; i += FS_W * 32) {
       uint32_t e = __ldg(p.table + (i >> 5));
-      if (PACKED) e = (e >> 31) ? 0u : ((e >> 4) << 16) | (e & 15u);
+      if (PACKED) e = (e >> 31) ? 0u : (e << 28) | ((e >> 4) & COST);
       extra[i] = e;
     }
     tb = extra + (tid & 31);
@@ -711,13 +712,23 @@ struct TcmOp {
     }
 #pragma unroll
     for (int l = 0; l < 8; ++l) acc[q * 8 + l] += PACKED ? e[l] : e[l] >> 4;
-    // the median codes are the entries' low nibbles: gather the low bytes of
-    // the even and the odd sites' entries, then interleave their nibbles
-    const uint32_t ce = __byte_perm(__byte_perm(e[0], e[2], 0x0040u), __byte_perm(e[4], e[6], 0x0040u),
-                                    0x5410u);
-    const uint32_t co = __byte_perm(__byte_perm(e[1], e[3], 0x0040u), __byte_perm(e[5], e[7], 0x0040u),
-                                    0x5410u);
-    const uint32_t out = (ce & 0x0F0F0F0Fu) | ((co << 4) & 0xF0F0F0F0u);
+    uint32_t out;
+    if (PACKED) {
+      // the median codes are the entries' top nibbles: gather the top bytes
+      // of the even and the odd sites' entries, then interleave their nibbles
+      const uint32_t ce = __byte_perm(__byte_perm(e[0], e[2], 0x0073u), __byte_perm(e[4], e[6], 0x0073u),
+                                      0x5410u);
+      const uint32_t co = __byte_perm(__byte_perm(e[1], e[3], 0x0073u), __byte_perm(e[5], e[7], 0x0073u),
+                                      0x5410u);
+      out = ((ce >> 4) & 0x0F0F0F0Fu) | (co & 0xF0F0F0F0u);
+    } else {
+      // the median codes are the entries' low nibbles
+      const uint32_t ce = __byte_perm(__byte_perm(e[0], e[2], 0x0040u), __byte_perm(e[4], e[6], 0x0040u),
+                                      0x5410u);
+      const uint32_t co = __byte_perm(__byte_perm(e[1], e[3], 0x0040u), __byte_perm(e[5], e[7], 0x0040u),
+                                      0x5410u);
+      out = (ce & 0x0F0F0F0Fu) | ((co << 4) & 0xF0F0F0F0u);
+    }
     return FULL ? out : out & valid;
   }
   template <bool FULL>
@@ -732,7 +743,7 @@ struct TcmOp {
   __device__ __forceinline__ void flush(uint32_t *sitecnt, int lane) {
 #pragma unroll
     for (int i = 0; i < 32; ++i) {
-      const uint32_t v = PACKED ? acc[i] >> 16 : acc[i];
+      const uint32_t v = PACKED ? acc[i] & COST : acc[i];
       if (v) atomicAdd(&sitecnt[i * 32 + lane], v);
       acc[i] = 0;
     }

@@ -377,11 +377,11 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
   PGPU_CUDA(ctx, cudaMemsetAsync(total, 0, sizeof(unsigned long long), ctx->stream));
   if (n_words == 0) return PGPU_OK;
   // the segmented schedule: subtrees walked by four warps per 128-word slice.
-  // With every cost below 4,096 it sums costs in the high 16 bits of a
-  // register next to the codes' low 16 bits, flushing before either carries:
-  // after p steps a site's sum is at most p * emax and its codes 15 p.
-  const int period = emax < 4096 ? (int)std::min<uint64_t>(65535 / 15, 65535 / std::max<uint64_t>(emax, 1))
-                                  : 0;
+  // It sums costs in the low 28 bits of a register under the codes' top 4,
+  // flushing every p steps so that a site's sum, at most p * emax, stays
+  // below 2^28; below 16 steps between flushes it keeps one sum per register.
+  const uint64_t per = ((1ull << 28) - 1) / std::max<uint64_t>(emax, 1);
+  const int period = per >= 16 ? (int)std::min<uint64_t>(per, 1u << 30) : 0;
   bool launched = false;
   PGPU_TRY(pgpu_tcm_tree_split(ctx, tree, tips, ld, weights, n_sites,
                                static_cast<const uint32_t *>(d), period, node_sets, site_cost, total,

@@ -112,33 +112,28 @@ def test_edge_cases(ctx):
         big.tree_cost(wide, _codes(rng, 300, 8), None, ctx)
 
 
-@pytest.mark.parametrize("scale,packed", [(1, True), (500, True), (1300, True), (5000, False),
-                                          (1 << 20, False)])
+@pytest.mark.parametrize("scale,packed", [(1, True), (5000, True), (1 << 20, True), (1 << 21, True),
+                                          (1 << 23, False)])
 def test_cost_magnitudes(ctx, scale, packed):
-    """Median costs below 4,096 are summed next to the codes in one register
-    and flushed every 65,535 / max cost steps (about every 20 steps at scale
-    500, far less often at 1); larger costs take one register per site.
-    Both give the restatement's sums, and a pair without a median anywhere
-    in the tree is an error in both."""
+    """Median costs up to (2^28 - 1) / 16 are summed under the codes in one
+    register and flushed every (2^28 - 1) / max cost steps (every 85 steps
+    at scale 2^20, 42 at 2^21, once at the end for small costs); larger
+    costs take one register per site.  Both give the restatement's sums, and
+    a pair without a median anywhere in the tree is an error in both."""
     rng = np.random.default_rng(scale)
-    tr = T.yule(300, rng, 0.1)
+    # the largest costs need a smaller tree to keep a site's sum below 2^32
+    tr = T.yule(300 if packed else 40, rng, 0.1)
     base = rng.integers(1, 5, (4, 4)).astype(np.int32)
-    tcm = np.minimum(base, base.T) * scale
-    tcm = np.minimum(tcm, (1 << 25) // 2)
+    tcm = np.minimum(np.minimum(base, base.T).astype(np.int64) * scale, 1 << 25).astype(np.int32)
     np.fill_diagonal(tcm, 0)
     cm = CM.CostMatrix(tcm, mode="general")
     cost, _ = TO.fill_tables(cm.tcm, CM.MODES[cm.mode], cm.symmetric)
     cost = np.asarray(cost)
     emax = int(cost[cost < TO.INF].max())
-    assert (emax < 4096) == packed, emax
+    assert (((1 << 28) - 1) // emax >= 16) == packed, emax
     n_sites = 5_001
     codes = _codes(rng, tr.n_tips, n_sites, 0.1)
     w = rng.integers(1, 9, n_sites).astype(np.uint32)
-    if scale >= 1 << 20:
-        # 300 nodes of costs up to 2^22 would pass 2^32 per site: refused
-        with pytest.raises(_native.NativeError):
-            cm.tree_cost(tr, codes, w, ctx)
-        return
     _check(ctx, tr, codes, cm, w)
     bad = codes.copy()
     bad[rng.integers(0, tr.n_tips), rng.integers(0, n_sites)] = 0
