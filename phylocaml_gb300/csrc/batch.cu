@@ -246,9 +246,23 @@ __device__ __forceinline__ void epi_step(const BatchArgs &p, const EpiIn &in, co
     // TMEM loads of W columns: the widest of 16, 8, 4 that divides both the
     // first column and the width of the share
     constexpr int W = (e0 % 16 == 0 && B % 16 == 0) ? 16 : (e0 % 8 == 0 && B % 8 == 0) ? 8 : 4;
+    const bool both = op.y >= in.n_tips && op.z >= in.n_tips;
+    if (ok && both) {
+      // two internal children: both children's columns in flight, one wait
+      float d0[B], d1[B];
+#pragma unroll
+      for (int c = 0; c < B; c += W)
+        tmem_ld<W>(in.tmem + in.lane_base + (uint32_t)(rate * NP + e0 + c), &d0[c]);
+#pragma unroll
+      for (int c = 0; c < B; c += W)
+        tmem_ld<W>(in.tmem + in.lane_base + (uint32_t)((RP + rate) * NP + e0 + c), &d1[c]);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+      for (int e = 0; e < B; ++e) acc[e] = d0[e] * d1[e];
+    }
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      if (!ok) break;
+      if (!ok || both) break;
       const int ch = h == 0 ? op.y : op.z;
       if (ch < in.n_tips) {
         int code = in.sl[h * 128 + in.m];

@@ -250,6 +250,18 @@ __global__ void __launch_bounds__(CLV_THREADS) clv_median_kernel(const MedArgs a
     const int r = (int)(g % RL);
     const bool act = g < n_items && r < R;
     const size_t off = (p * R + r) * (size_t)S;
+    // the pattern's first lane reads the children's exponents and its
+    // weight up front, so their latency overlaps the rows' (loaded after the
+    // vector stores below, they would wait on a second round trip)
+    const bool lead = act && r == 0;
+    int ex_sum = 0;
+    long long wi = 0;
+    double wd = 0.0;
+    if (lead) {
+      for (int k = 0; k < a.n_ch; ++k) ex_sum += __ldg(a.ex[k] + p);
+      if (a.int_w) wi = a.wint ? (long long)__ldg(a.wint + p) : 1;
+      else wd = a.weights ? __ldg(a.weights + p) : 1.0;
+    }
     V m = (V)0;
     int e;
     if (SC == 4) {
@@ -309,16 +321,13 @@ __global__ void __launch_bounds__(CLV_THREADS) clv_median_kernel(const MedArgs a
         for (int i = 0; i < S; ++i) y[off + i] = scale2<V>(y[off + i], -e);
     }
     // exponent bookkeeping and this node's cost, by the pattern's first lane
-    if (act && r == 0) {
-      int E = e;
-      for (int k = 0; k < a.n_ch; ++k) E += a.ex[k][p];
-      a.ey[p] = E;
+    if (lead) {
+      a.ey[p] = e + ex_sum;
       if (a.int_w) {
-        iacc += (long long)(a.wint ? a.wint[p] : 1) * e;
+        iacc += wi * e;
       } else {
-        const double w = a.weights ? a.weights[p] : 1.0;
         double t, err;
-        two_sum(s, w * (double)e, t, err);
+        two_sum(s, wd * (double)e, t, err);
         s = t;
         c += err;
       }
