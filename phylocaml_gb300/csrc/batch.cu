@@ -21,23 +21,25 @@
 //                  come from the staged tip table.  Rate classes are separate
 //                  passes with their own power-of-two scalers, joined at the
 //                  root with a log-sum-exp in FP64.
-//     warp 16      producer and TMEM allocator: per postorder step,
+//     warp 8       producer and TMEM allocator: per postorder step,
 //                  bulk-copies the B blocks of internal children, the
 //                  tip-table blocks and tip-code rows of tip children into a
 //                  shared ring slot, and publishes the step itself;
-//     warps 0-15   epilogue: four warps per TMEM lane group of 32 patterns,
-//                  each owning a share of the row (a range of states, or a
-//                  rate class and half the states); a thread reads its D
-//                  columns (tcgen05.ld) or tip rows, forms the product,
+//     warp 9       MMA issue (one thread);
+//     warps 0-7    epilogue: two warps per TMEM lane group of 32 patterns,
+//                  each owning a share of the row (half the states, or a
+//                  whole rate class when two share a pass); a thread reads
+//                  its D columns (tcgen05.ld) or tip rows, forms the product,
 //                  rescales, writes the parent's vector back into TMEM
-//                  (tcgen05.st).  Thread 0 also issues every step's MMAs.
+//                  (tcgen05.st).
 //   The MMA (tcgen05.commit -> mma_bar) and the epilogue (an mbarrier,
 //   `stored`, after its TMEM stores) alternate per step, so a step's MMA
 //   never reads a vector before it is written and no mbarrier phase can be
 //   skipped.  With two rate classes per pass the two classes are separate
-//   chains, each with its own mma_bar and stored barrier and its own eight
+//   chains, each with its own mma_bar and stored barrier and its own four
 //   epilogue warps: the MMAs of one class's next step run while the other
-//   class's epilogue runs.
+//   class's epilogue runs, and no warp waits for another to agree on a
+//   rescaling exponent.
 //   Every wait is bounded.  Each work item runs a step loop compiled for its
 //   padded state count and rate classes per pass.
 //   batch_fp64_kernel  the FP64 comparison form on a sample of patterns.
@@ -54,8 +56,8 @@ namespace {
 
 constexpr int BT_M = 128;          // patterns per tile (TMEM lanes)
 constexpr int BT_ST = 4;           // ring slots (power of two)
-constexpr int BT_EPI_WARPS = 16;   // epilogue warps, four per TMEM lane group; thread 0 issues MMAs
-constexpr int BT_PARTS = BT_EPI_WARPS / 4;
+constexpr int BT_EPI_WARPS = 8;    // epilogue warps, two per TMEM lane group
+constexpr int BT_PARTS = BT_EPI_WARPS / 4;   // shares of a row (one per warp of a lane group)
 constexpr int BT_EPI = 32 * BT_EPI_WARPS;
 constexpr int BT_THREADS = BT_EPI + 64;   // + the producer warp and the MMA warp
 constexpr int BT_PRODUCER = BT_EPI_WARPS, BT_MMA = BT_EPI_WARPS + 1;   // their warp indices
@@ -201,23 +203,26 @@ struct EpiIn {
   int n_tips, n_codes, S;
   uint32_t tmem, lane_base;
   int m;                     // pattern within the tile (TMEM lane)
-  int lg;                    // TMEM lane group (its four warps share a named barrier)
+  int lg;                    // TMEM lane group (its warps of one rate class share a named barrier)
   bool active, last;
   const double *pi;
 };
 
-// The share of a row that epilogue warp w owns (PT = w / 4; the four warps
-// of a TMEM lane group own the four shares).  With two rate classes per pass
-// a share is rate class PT / 2 and half PT % 2 of the states; with one, it is
-// the PT-th range of W4 states, W4 = Kp / 4 rounded up to a multiple of 4, so
-// the last ranges of a small Kp may be empty.  Every range starts on a
-// multiple of 4 columns and is a multiple of 4 wide.
+// The share of a row that epilogue warp w owns (PT = w / 4; the warps of a
+// TMEM lane group own the BT_PARTS shares).  A rate class of the pass has
+// PPR = BT_PARTS / RP shares: share PT is rate class PT / PPR and the
+// (PT % PPR)-th range of WD states, WD = Kp / PPR rounded up to a multiple
+// of 4, so the last range of a small Kp may be short or empty.  Every range
+// starts on a multiple of 4 columns and is a multiple of 4 wide.  With two
+// shares per lane group and two rate classes per pass, a warp owns a whole
+// rate class's row and needs no exchange with another warp.
 template <int KP, int RP, int PT>
 struct Share {
-  static constexpr int W4 = ((KP / 4) + 3) & ~3;
-  static constexpr int rate = RP == 2 ? PT >> 1 : 0;
-  static constexpr int e0 = RP == 2 ? (PT & 1) * (KP / 2) : PT * W4;
-  static constexpr int B = RP == 2 ? KP / 2 : (KP - e0 <= 0 ? 0 : (KP - e0 < W4 ? KP - e0 : W4));
+  static constexpr int PPR = BT_PARTS / RP;
+  static constexpr int WD = ((KP / PPR) + 3) & ~3;
+  static constexpr int rate = PT / PPR;
+  static constexpr int e0 = (PT % PPR) * WD;
+  static constexpr int B = KP - e0 <= 0 ? 0 : (KP - e0 < WD ? KP - e0 : WD);
 };
 
 // One postorder step for this warp's share of the row: the product of the
@@ -246,23 +251,9 @@ __device__ __forceinline__ void epi_step(const BatchArgs &p, const EpiIn &in, co
     // TMEM loads of W columns: the widest of 16, 8, 4 that divides both the
     // first column and the width of the share
     constexpr int W = (e0 % 16 == 0 && B % 16 == 0) ? 16 : (e0 % 8 == 0 && B % 8 == 0) ? 8 : 4;
-    const bool both = op.y >= in.n_tips && op.z >= in.n_tips;
-    if (ok && both) {
-      // two internal children: both children's columns in flight, one wait
-      float d0[B], d1[B];
-#pragma unroll
-      for (int c = 0; c < B; c += W)
-        tmem_ld<W>(in.tmem + in.lane_base + (uint32_t)(rate * NP + e0 + c), &d0[c]);
-#pragma unroll
-      for (int c = 0; c < B; c += W)
-        tmem_ld<W>(in.tmem + in.lane_base + (uint32_t)((RP + rate) * NP + e0 + c), &d1[c]);
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-      for (int e = 0; e < B; ++e) acc[e] = d0[e] * d1[e];
-    }
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      if (!ok || both) break;
+      if (!ok) break;
       const int ch = h == 0 ? op.y : op.z;
       if (ch < in.n_tips) {
         int code = in.sl[h * 128 + in.m];
@@ -300,25 +291,28 @@ __device__ __forceinline__ void epi_step(const BatchArgs &p, const EpiIn &in, co
       for (int e = 0; e + w < B; e += 2 * w) t[e] = fmaxf(t[e], t[e + w]);
     mx = t[0];
   }
-  xch[PT][in.m] = mx;
-  // the exchange joins only the warps of this TMEM lane group that share
-  // the rate class (named barrier 2 + lg, or 2 + lg + 4 rate with two rate
-  // classes per pass); it also makes the timeout verdict uniform over them,
-  // so they leave the step loop together
-  {
+  constexpr int PPR = SH::PPR;
+  float m2 = mx;
+  if constexpr (PPR > 1) {
+    xch[PT][in.m] = mx;
+    // the exchange joins only the warps of this TMEM lane group that share
+    // the rate class (named barrier 2 + lg + 4 rate); it also makes the
+    // timeout verdict uniform over them, so they leave the step loop
+    // together
     uint32_t all_ok;
     asm volatile(
         "{\n\t.reg .pred a, b;\n\tsetp.ne.u32 a, %1, 0;\n\t"
         "bar.red.and.pred b, %2, %3, a;\n\tselp.u32 %0, 1, 0, b;\n\t}"
         : "=r"(all_ok)
-        : "r"((uint32_t)ok), "r"(2 + in.lg + (RP == 2 ? 4 * rate : 0)), "n"(RP == 2 ? 2 * 32 : 4 * 32)
+        : "r"((uint32_t)ok), "r"(2 + in.lg + 4 * rate), "n"(PPR * 32)
         : "memory");
     ok = all_ok != 0;
-  }
-  float m2 = 0.0f;
 #pragma unroll
-  for (int pp = 0; pp < BT_PARTS; ++pp)
-    if (RP == 1 || (pp >> 1) == rate) m2 = fmaxf(m2, xch[pp][in.m]);
+    for (int pp = rate * PPR; pp < rate * PPR + PPR; ++pp) m2 = fmaxf(m2, xch[pp][in.m]);
+  } else {
+    // this warp holds the whole row of its rate class
+    ok = __all_sync(0xffffffffu, ok);
+  }
   if (m2 < 0x1p-32f && m2 > 0.0f) {
     int ex;
     (void)frexpf(m2, &ex);
@@ -354,7 +348,7 @@ __device__ __forceinline__ void epi_step(const BatchArgs &p, const EpiIn &in, co
 struct EpiShared {
   uint64_t *full, *empty;
   uint64_t *mma_bar;         // [2]: per rate class of the pass (both complete once per step)
-  uint64_t *stored;          // [2]: the eight epilogue warps of shares 2q, 2q + 1 arrive on q
+  uint64_t *stored;          // [2]: the epilogue warps of the first and second half of the shares
   const int4 *slot_op;       // each ring slot's postorder step, written by the producer
   unsigned char *smem;
   float (*xch)[BT_M];        // [2][BT_PARTS]: per step parity and share, lane: max entry
@@ -365,7 +359,7 @@ struct EpiShared {
 };
 
 // Every pass and postorder step of one work item (variant, tile) with
-// compile-time shapes, for the sixteen epilogue warps: each step waits for
+// compile-time shapes, for the epilogue warps: each step waits for
 // its slot and its MMAs, runs the epilogue, and after its TMEM stores every
 // warp arrives on `stored`, which the MMA warp waits for before the next
 // step's MMAs.  A pass ends with the epilogue-wide verdict on timeouts, so
@@ -376,9 +370,10 @@ __device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh
   const int warp = tid >> 5, lane = tid & 31;
   const int lg = warp & 3, pt = warp >> 2;
   const int m = 32 * lg + lane;   // pattern within the tile
-  const int my_rate = RP == 2 ? pt >> 1 : 0;
+  constexpr int PPR = BT_PARTS / RP;
+  const int my_rate = pt / PPR;
   // the share that combines its rate class's root likelihood
-  const bool lead = RP == 1 ? pt == 0 : (pt & 1) == 0;
+  const bool lead = pt % PPR == 0;
   // the variant's fields, once per item
   const int n_ops = vg.n_ops, R = vg.R;
   EpiIn in;
@@ -424,7 +419,7 @@ __device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       // this warp's vectors of the step are in TMEM and its D columns read
       __syncwarp();
-      if (lane == 0) mbar_arrive(&sh.stored[pt >> 1]);
+      if (lane == 0) mbar_arrive(&sh.stored[pt / (BT_PARTS / 2)]);
       if (!ok) break;
     }
     // one verdict for every epilogue warp before the barriers below
@@ -445,8 +440,7 @@ __device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh
     if (lead) {
       double L = 0.0;
 #pragma unroll
-      for (int pp = 0; pp < BT_PARTS; ++pp)
-        if (RP == 1 || (pp >> 1) == my_rate) L += sh.xchd[pp][m];
+      for (int pp = my_rate * PPR; pp < my_rate * PPR + PPR; ++pp) L += sh.xchd[pp][m];
       sh.lnr[r0 + my_rate][m] = log(L) + (double)escale * 0.69314718055994530942;
     }
     asm volatile("bar.sync 1, %0;" ::"n"(BT_EPI) : "memory");
@@ -517,7 +511,7 @@ __device__ __forceinline__ void mma_item(const BatchArgs &p, const EpiShared &sh
 #pragma unroll
       for (int q = 0; q < RP; ++q) {
         // this class's epilogue warps are done with the previous step (with
-        // one class per pass, all sixteen)
+        // one class per pass, all of them)
         bool got = true;
         if (seq > 0) {
           const uint32_t prev = (uint32_t)((seq - 1) & 1);
@@ -613,7 +607,7 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
     }
     for (int q = 0; q < 2; ++q) {
       mbar_init(&mma_bar[q], 1);
-      mbar_init(&stored[q], BT_EPI_WARPS / 2);   // eight epilogue warps, after a step's TMEM stores
+      mbar_init(&stored[q], BT_EPI_WARPS / 2);   // half the epilogue warps, after a step's TMEM stores
     }
     fence_mbarrier_init();
   }
