@@ -154,6 +154,35 @@ __device__ __forceinline__ void tmem_ld<16>(uint32_t ta, float *v) {
   for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
+// W consecutive TMEM columns of this thread's lane, each value rounded to
+// the nearest TF32 value (32x32b shape)
+template <int W>
+__device__ __forceinline__ void tmem_st(uint32_t ta, const float *v);
+template <>
+__device__ __forceinline__ void tmem_st<4>(uint32_t ta, const float *v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(ta), "r"(tf32_bits(v[0])),
+               "r"(tf32_bits(v[1])), "r"(tf32_bits(v[2])), "r"(tf32_bits(v[3]))
+               : "memory");
+}
+template <>
+__device__ __forceinline__ void tmem_st<8>(uint32_t ta, const float *v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(ta),
+               "r"(tf32_bits(v[0])), "r"(tf32_bits(v[1])), "r"(tf32_bits(v[2])), "r"(tf32_bits(v[3])),
+               "r"(tf32_bits(v[4])), "r"(tf32_bits(v[5])), "r"(tf32_bits(v[6])), "r"(tf32_bits(v[7]))
+               : "memory");
+}
+template <>
+__device__ __forceinline__ void tmem_st<16>(uint32_t ta, const float *v) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+          ta),
+      "r"(tf32_bits(v[0])), "r"(tf32_bits(v[1])), "r"(tf32_bits(v[2])), "r"(tf32_bits(v[3])), "r"(tf32_bits(v[4])),
+      "r"(tf32_bits(v[5])), "r"(tf32_bits(v[6])), "r"(tf32_bits(v[7])), "r"(tf32_bits(v[8])), "r"(tf32_bits(v[9])),
+      "r"(tf32_bits(v[10])), "r"(tf32_bits(v[11])), "r"(tf32_bits(v[12])), "r"(tf32_bits(v[13])),
+      "r"(tf32_bits(v[14])), "r"(tf32_bits(v[15]))
+      : "memory");
+}
+
 __device__ __forceinline__ void two_sum_d(double a, double b, double &s, double &e) {
   s = a + b;
   const double bb = s - a;
@@ -326,12 +355,9 @@ __device__ __forceinline__ void epi_step(const BatchArgs &p, const EpiIn &in, co
     // into the TMEM stack slot: columns e0 .. e0 + B - 1 of rate class rate
     const int so = (op.w >> 16) & 0xff;
     const uint32_t col = in.tmem + in.lane_base + (uint32_t)(2 * RP * NP + (so * RP + rate) * KP + e0);
+    constexpr int WS = (e0 % 16 == 0 && B % 16 == 0) ? 16 : (e0 % 8 == 0 && B % 8 == 0) ? 8 : 4;
 #pragma unroll
-    for (int c0 = 0; c0 < B; c0 += 4)
-      asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(col + (uint32_t)c0),
-                   "r"(tf32_bits(acc[c0])), "r"(tf32_bits(acc[c0 + 1])), "r"(tf32_bits(acc[c0 + 2])),
-                   "r"(tf32_bits(acc[c0 + 3]))
-                   : "memory");
+    for (int c0 = 0; c0 < B; c0 += WS) tmem_st<WS>(col + (uint32_t)c0, &acc[c0]);
     if (in.last) {
       double l = 0.0;
 #pragma unroll
@@ -395,8 +421,8 @@ __device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh
       const int slot = (int)(seq & (BT_ST - 1));
       const uint32_t par = (uint32_t)((seq / BT_ST) & 1);
       in.sl = sh.smem + (size_t)slot * p.slot_bytes;
-      bool got = mbar_wait_bounded(&sh.full[slot], par, p.flag);
-      got = got && mbar_wait_bounded(&sh.mma_bar[my_rate], (uint32_t)(seq & 1), p.flag);
+      bool got = mbar_wait_bounded_for(&sh.full[slot], par, p.flag);
+      got = got && mbar_wait_bounded_for(&sh.mma_bar[my_rate], (uint32_t)(seq & 1), p.flag);
       got = __all_sync(0xffffffffu, got);
       if (!got) {
         ok = false;
@@ -500,7 +526,7 @@ __device__ __forceinline__ void mma_item(const BatchArgs &p, const EpiShared &sh
     for (int i = 0; i < n_ops; ++i, ++seq) {
       const int slot = (int)(seq & (BT_ST - 1));
       const uint32_t par = (uint32_t)((seq / BT_ST) & 1);
-      if (!mbar_wait_bounded(&sh.full[slot], par, p.flag)) {
+      if (!mbar_wait_bounded_for(&sh.full[slot], par, p.flag)) {
         ok = false;
         atomicOr(p.flag, PGPU_FLAG_TIMEOUT);
         return;
@@ -515,8 +541,8 @@ __device__ __forceinline__ void mma_item(const BatchArgs &p, const EpiShared &sh
         bool got = true;
         if (seq > 0) {
           const uint32_t prev = (uint32_t)((seq - 1) & 1);
-          got = mbar_wait_bounded(&sh.stored[q], prev, p.flag);
-          if (RP == 1) got = got && mbar_wait_bounded(&sh.stored[1], prev, p.flag);
+          got = mbar_wait_bounded_for(&sh.stored[q], prev, p.flag);
+          if (RP == 1) got = got && mbar_wait_bounded_for(&sh.stored[1], prev, p.flag);
         }
         if (!got) {
           ok = false;
@@ -637,7 +663,7 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
             const int slot = (int)(seq & (BT_ST - 1));
             const long long round = seq / BT_ST;
             const int4 op = __ldg(p.ops + ops_off + i);
-            if (round > 0 && !mbar_wait_bounded(&empty[slot], (uint32_t)((round - 1) & 1), p.flag)) {
+            if (round > 0 && !mbar_wait_bounded_for(&empty[slot], (uint32_t)((round - 1) & 1), p.flag)) {
               ok = false;
               break;
             }
@@ -668,7 +694,7 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
         }
       }
       for (long long s = seq - BT_ST; s < seq; ++s)
-        if (s >= 0) (void)mbar_wait_bounded(&full[s & (BT_ST - 1)], (uint32_t)((s / BT_ST) & 1), p.flag);
+        if (s >= 0) (void)mbar_wait_bounded_for(&full[s & (BT_ST - 1)], (uint32_t)((s / BT_ST) & 1), p.flag);
     }
   } else if (warp == BT_MMA) {
     // ------------------------------------------------------------ MMA issue
@@ -690,7 +716,7 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
         }
       }
       // the last MMAs finish before TMEM is released
-      if (seq > 0) (void)mbar_wait_bounded(&mma_bar[1], (uint32_t)((seq - 1) & 1), p.flag);
+      if (seq > 0) (void)mbar_wait_bounded_for(&mma_bar[1], (uint32_t)((seq - 1) & 1), p.flag);
     }
   } else {
     // ------------------------------------------------------------ epilogue

@@ -515,7 +515,8 @@ __global__ void __launch_bounds__(160) fitch_tree_kernel(const FitchTreeArgs p) 
 // ---------------------------------------------------------------------------
 constexpr int FS_W = 4;   // warps per CTA
 constexpr int FS_S = 8;   // segments at most
-constexpr int FS_P = 4;   // tip slices in flight per thread
+constexpr int FS_P = 4;   // tip slices in flight per thread (a power of two)
+static_assert((FS_P & (FS_P - 1)) == 0, "the copy ring is indexed by a mask");
 
 __device__ __forceinline__ void cp_async16(void *dst, const void *src, bool valid) {
   const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
@@ -802,16 +803,19 @@ __device__ __forceinline__ void split_walk(const FitchSplitArgs &p, Op &rule, ui
     const int4 sg = p.seg[ws.x + q];   // {op_off, n_ops, tip_off, n_tips}
     uint4 *stk = stk0 + (q + 1) * NV * 32;   // rows below hold earlier results
     const int32_t *tseq = p.tip_seq + sg.z;
-    int issued = 0, consumed = 0;
+    // copy counts are unsigned so that the ring slot is a mask, not a
+    // signed remainder
+    const uint32_t n_seg_tips = (uint32_t)sg.w;
+    uint32_t issued = 0, consumed = 0;
     int32_t next_tip = sg.w > 0 ? __ldg(tseq) : 0;
     auto issue = [&]() {
-      if (issued < sg.w) {
+      if (issued < n_seg_tips) {
         const int32_t tip = next_tip;
-        if (issued + 1 < sg.w) next_tip = __ldg(tseq + issued + 1);
+        if (issued + 1 < n_seg_tips) next_tip = __ldg(tseq + issued + 1);
         const uint32_t *row = p.tips + (size_t)tip * p.ld;
 #pragma unroll
         for (int j = 0; j < NV; ++j)
-          cp_async16(&ring[((issued % FS_P) * NV + j) * 32 + lane], row + (act[j] ? word[j] : 0), act[j]);
+          cp_async16(&ring[((issued & (FS_P - 1)) * NV + j) * 32 + lane], row + (act[j] ? word[j] : 0), act[j]);
       }
       cp_async_commit();   // empty groups keep the count in step
       ++issued;
@@ -834,7 +838,7 @@ __device__ __forceinline__ void split_walk(const FitchSplitArgs &p, Op &rule, ui
     };
     auto from_ring = [&](uint4 (&dst)[NV]) {
 #pragma unroll
-      for (int j = 0; j < NV; ++j) dst[j] = ring[((consumed % FS_P) * NV + j) * 32 + lane];
+      for (int j = 0; j < NV; ++j) dst[j] = ring[((consumed & (FS_P - 1)) * NV + j) * 32 + lane];
       ++consumed;
     };
     const int4 *ops = p.ops + sg.x;

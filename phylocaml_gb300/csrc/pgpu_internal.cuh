@@ -232,6 +232,40 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
   return true;
 }
 
+// As mbar_try_wait, but a thread whose phase is not complete may stay
+// suspended for up to `ns` nanoseconds (it resumes as soon as the phase
+// completes), so a long wait costs few retries.
+__device__ __forceinline__ bool mbar_try_wait_for(uint64_t *bar, uint32_t parity, uint32_t ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
+      : "memory");
+  return ok != 0;
+}
+
+// mbar_wait_bounded with suspended retries: the same PGPU_WAIT_NS budget,
+// the clock read every 16 retries.
+__device__ __forceinline__ bool mbar_wait_bounded_for(uint64_t *bar, uint32_t parity, int *flag,
+                                                      uint32_t ns = 20000u) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = pgpu_globaltimer();
+  uint32_t it = 0;
+  while (!mbar_try_wait_for(bar, parity, ns)) {
+    if ((++it & 15u) == 0u) {
+      if (pgpu_globaltimer() - t0 > PGPU_WAIT_NS) {
+        atomicOr(flag, PGPU_FLAG_TIMEOUT);
+        return false;
+      }
+      if (*(volatile int *)flag & PGPU_FLAG_TIMEOUT) return false;
+    }
+  }
+  return true;
+}
+
 // 1-D bulk copy global -> shared, completion signalled on *bar.
 // dst, src and bytes must be multiples of 16.
 __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
