@@ -822,20 +822,13 @@ __device__ __forceinline__ void split_walk(const FitchSplitArgs &p, Op &rule, ui
     };
 #pragma unroll
     for (int j = 0; j < FS_P; ++j) issue();
+    // The stack discipline is fixed by the postorder: the previous step's
+    // result is this step's second child when that is internal, else its
+    // first; a step with two tip children sets it aside (push), one with two
+    // internal children takes its first child back (pop).  A segment's
+    // first step has two tip children and nothing to set aside.
     int sp = 0;
     uint4 top[NV];
-    bool top_valid = false;
-    auto pop = [&](uint4 (&dst)[NV]) {
-      if (top_valid) {
-        top_valid = false;
-#pragma unroll
-        for (int j = 0; j < NV; ++j) dst[j] = top[j];
-        return;
-      }
-      --sp;
-#pragma unroll
-      for (int j = 0; j < NV; ++j) dst[j] = stk[(sp * NV + j) * 32 + lane];
-    };
     auto from_ring = [&](uint4 (&dst)[NV]) {
 #pragma unroll
       for (int j = 0; j < NV; ++j) dst[j] = ring[((consumed & (FS_P - 1)) * NV + j) * 32 + lane];
@@ -847,20 +840,35 @@ __device__ __forceinline__ void split_walk(const FitchSplitArgs &p, Op &rule, ui
       const int4 next = i + 1 < sg.y ? __ldg(ops + i + 1) : op;
       const bool ta = op.y < p.n_tips, tb = op.z < p.n_tips;
       uint4 x[NV], y[NV];
-      if (!tb) pop(y);
-      if (!ta) pop(x);
       // a step's tips are the next ones of the sequence: the first needs all
       // copy groups but the FS_P-1 newest, the second all but the FS_P-2 newest
-      if (ta) {
+      if (ta && tb) {
+        if (i > 0) {
+#pragma unroll
+          for (int j = 0; j < NV; ++j) stk[(sp * NV + j) * 32 + lane] = top[j];
+          ++sp;
+        }
         cp_async_wait<FS_P - 1>();
         from_ring(x);
-        if (tb) {
-          cp_async_wait<FS_P - 2>();
-          from_ring(y);
-        }
+        cp_async_wait<FS_P - 2>();
+        from_ring(y);
+      } else if (ta) {
+        cp_async_wait<FS_P - 1>();
+        from_ring(x);
+#pragma unroll
+        for (int j = 0; j < NV; ++j) y[j] = top[j];
       } else if (tb) {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) x[j] = top[j];
         cp_async_wait<FS_P - 1>();
         from_ring(y);
+      } else {
+        --sp;
+#pragma unroll
+        for (int j = 0; j < NV; ++j) {
+          x[j] = stk[(sp * NV + j) * 32 + lane];
+          y[j] = top[j];
+        }
       }
       uint4 med[NV];
 #pragma unroll
@@ -868,18 +876,12 @@ __device__ __forceinline__ void split_walk(const FitchSplitArgs &p, Op &rule, ui
       rule.step(p, sitecnt, lane);
       // slots read this step are refilled only once their values are in use
       while (issued < consumed + FS_P) issue();
-      if (top_valid) {
-#pragma unroll
-        for (int j = 0; j < NV; ++j) stk[(sp * NV + j) * 32 + lane] = top[j];
-        ++sp;
-      }
       uint32_t *dst = p.node_sets + (size_t)op.x * p.ld;
 #pragma unroll
       for (int j = 0; j < NV; ++j) {
         top[j] = med[j];
         if (act[j]) __stcs(reinterpret_cast<uint4 *>(dst + word[j]), med[j]);
       }
-      top_valid = true;
       op = next;
     }
     cp_async_wait<0>();
