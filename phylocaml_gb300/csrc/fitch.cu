@@ -547,7 +547,8 @@ struct FitchSplitArgs {
 // cost bookkeeping.  A lane covers NV parts of 4 words (part j of lane l
 // holds words 128 j + 4 l .. + 3 of the CTA's tile, so every part's loads
 // and stores are coalesced), PER sites per word; the CTA's per-site counts
-// are SITES = NV * 4 * PER 32-bit words per lane, [site][lane].
+// are NV * 4 * PER 32-bit words per lane, [entry][lane]: one per site, or,
+// for FitchOp with two 16-bit counts to a word, the first half of them.
 //   FitchOp<LB, NV>  the Fitch rule on LB-bit lanes; union events are
 //                counted in LB-bit lane counters (one add per word) and
 //                flushed into the per-site counts every 2^LB - 1 steps.
@@ -565,7 +566,10 @@ template <int LB, int NV_>
 struct FitchOp {
   static constexpr int NV = NV_;
   static constexpr int PER = Lanes<LB>::PER;
-  static constexpr int SITES = NV * 4 * PER;
+  // per-site count words of a lane (the packed counts use half of them; a
+  // layout that freed the other half let a fifth CTA onto each SM and made
+  // the 208-word-tile launch slower, 0.224 against 0.201 ms)
+  __host__ __device__ static constexpr int sites(bool) { return NV * 4 * PER; }
   static constexpr uint32_t FLUSH = Lanes<LB>::FLUSH;
   static constexpr int MIN_BLOCKS = NV == 1 ? 8 : 4;
   static constexpr size_t EXTRA_SMEM = 0;
@@ -672,7 +676,7 @@ template <bool PACKED>
 struct TcmOp {
   static constexpr int NV = 1;
   static constexpr int PER = 8;
-  static constexpr int SITES = 32;
+  __host__ __device__ static constexpr int sites(bool) { return 32; }
   static constexpr int MIN_BLOCKS = 4;
   static constexpr size_t EXTRA_SMEM = 256 * 32 * 4;
   static constexpr bool FULL_ANY_WIDTH = false;  // an idle lane's code 0 would raise the flag
@@ -786,8 +790,8 @@ struct TcmOp {
 // the joining nodes' results, FS_W * FS_P >= FS_S
 static_assert(FS_W * FS_P >= FS_S, "joining results overlay the rings");
 template <class Op>
-__host__ __device__ inline size_t split_smem(int rows) {
-  return (size_t)FS_W * rows * Op::NV * 32 * 16 + (size_t)Op::SITES * 32 * 4 + Op::EXTRA_SMEM;
+__host__ __device__ inline size_t split_smem(int rows, bool count16) {
+  return (size_t)FS_W * rows * Op::NV * 32 * 16 + (size_t)Op::sites(count16) * 32 * 4 + Op::EXTRA_SMEM;
 }
 
 // Phase 1 of tree_split_kernel: warp w walks its segments.  word[j] is the
@@ -798,6 +802,16 @@ __device__ __forceinline__ void split_walk(const FitchSplitArgs &p, Op &rule, ui
                                            const size_t (&word)[Op::NV], uint32_t *sitecnt, int w,
                                            int lane) {
   constexpr int NV = Op::NV;
+  // row r of part j: col[j] + r ld (tips) and ncol[j] + r ld (node sets),
+  // a 32-bit row stride so that each is one wide multiply-add
+  const uint32_t ld32 = (uint32_t)p.ld;
+  const uint32_t *col[NV];
+  uint32_t *ncol[NV];
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    col[j] = p.tips + (act[j] ? word[j] : 0);
+    ncol[j] = p.node_sets + word[j];
+  }
   const int4 ws = p.wseg[w];
   for (int q = 0; q < ws.y; ++q) {
     const int4 sg = p.seg[ws.x + q];   // {op_off, n_ops, tip_off, n_tips}
@@ -812,10 +826,10 @@ __device__ __forceinline__ void split_walk(const FitchSplitArgs &p, Op &rule, ui
       if (issued < n_seg_tips) {
         const int32_t tip = next_tip;
         if (issued + 1 < n_seg_tips) next_tip = __ldg(tseq + issued + 1);
-        const uint32_t *row = p.tips + (size_t)tip * p.ld;
+        const uint64_t roff = (uint64_t)(uint32_t)tip * ld32;
 #pragma unroll
         for (int j = 0; j < NV; ++j)
-          cp_async16(&ring[((issued & (FS_P - 1)) * NV + j) * 32 + lane], row + (act[j] ? word[j] : 0), act[j]);
+          cp_async16(&ring[((issued & (FS_P - 1)) * NV + j) * 32 + lane], col[j] + roff, act[j]);
       }
       cp_async_commit();   // empty groups keep the count in step
       ++issued;
@@ -876,11 +890,11 @@ __device__ __forceinline__ void split_walk(const FitchSplitArgs &p, Op &rule, ui
       rule.step(p, sitecnt, lane);
       // slots read this step are refilled only once their values are in use
       while (issued < consumed + FS_P) issue();
-      uint32_t *dst = p.node_sets + (size_t)op.x * p.ld;
+      const uint64_t noff = (uint64_t)(uint32_t)op.x * ld32;
 #pragma unroll
       for (int j = 0; j < NV; ++j) {
         top[j] = med[j];
-        if (act[j]) __stcs(reinterpret_cast<uint4 *>(dst + word[j]), med[j]);
+        if (act[j]) __stcs(reinterpret_cast<uint4 *>(ncol[j] + noff), med[j]);
       }
       op = next;
     }
@@ -901,11 +915,12 @@ __global__ void __launch_bounds__(FS_W * 32, Op::MIN_BLOCKS) tree_split_kernel(c
   uint4 *ring = region + (size_t)w * rows * NV * 32;
   uint4 *stk0 = ring + FS_P * NV * 32;
   // per-site counts of the CTA's words, shared by its warps (they all work
-  // on the same words): [SITES][32 lanes]
+  // on the same words): [entry][32 lanes]
   uint32_t *sitecnt = reinterpret_cast<uint32_t *>(region + (size_t)FS_W * rows * NV * 32);
-  for (int i = tid; i < 32 * Op::SITES; i += FS_W * 32) sitecnt[i] = 0;
+  const int n_entries = Op::sites(p.count16 != 0);
+  for (int i = tid; i < 32 * n_entries; i += FS_W * 32) sitecnt[i] = 0;
   Op rule;
-  rule.init(p, sitecnt + 32 * Op::SITES, tid);
+  rule.init(p, sitecnt + 32 * n_entries, tid);
   __syncthreads();
   // a tile of tile_words words: lanes past it idle (their loads are
   // zero-filled, nothing of theirs is counted or stored)
@@ -1272,7 +1287,7 @@ pgpu_status split_device(pgpu_ctx *ctx, const pgpu_tree *tree, const int4 **ops,
 
 template <class Op>
 cudaError_t launch_split(cudaStream_t stream, const FitchSplitArgs &a, size_t tiles) {
-  const size_t smem = split_smem<Op>(a.rows);
+  const size_t smem = split_smem<Op>(a.rows, a.count16 != 0);
   cudaError_t e = cudaFuncSetAttribute(tree_split_kernel<Op>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)std::max<size_t>(smem, 48 * 1024));
@@ -1369,15 +1384,16 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
   a.n_top = (int)sp.top.size();
   a.rows = sp.rows;
   // LB = 4 has the most per-site counters, so it bounds every width's need
-  if (split_smem<FitchOp<4, 1>>(a.rows) > ctx->smem_optin)
+  if (split_smem<FitchOp<4, 1>>(a.rows, false) > ctx->smem_optin)
     return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: tree needs a stack of %d rows; too deep",
                         a.rows);
   a.tile_words = ctx->fitch_tile_words > 0 ? ctx->fitch_tile_words
                                            : default_tile_words(n_words, ctx->num_sms);
   // two parts per lane only where their stacks fit; the width only shapes
   // the launch, so a narrower one gives the same results
-  if (a.tile_words > 128 && split_smem<FitchOp<4, 2>>(a.rows) > ctx->smem_optin) a.tile_words = 128;
   a.count16 = tree->n_tips - 1 <= 65535;
+  if (ld > 0xffffffffull) return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: rows of 2^32 words or more");
+  if (a.tile_words > 128 && split_smem<FitchOp<4, 2>>(a.rows, a.count16) > ctx->smem_optin) a.tile_words = 128;
   a.tcm_period = 0;
   a.table = nullptr;
   a.flag = ctx->d_flag;
@@ -1413,12 +1429,12 @@ pgpu_status pgpu_tcm_tree_split(pgpu_ctx *ctx, const pgpu_tree *tree, const uint
                                 uint32_t *site_cost, unsigned long long *total, bool *launched) {
   *launched = false;
   if (((uintptr_t)tips | (uintptr_t)node_sets) & 15) return PGPU_OK;
-  if (ld % 4 != 0) return PGPU_OK;
+  if (ld % 4 != 0 || ld > 0xffffffffull) return PGPU_OK;
   const size_t n_words = (n_sites + 7) / 8;
   FitchSplitArgs a;
   PGPU_TRY(split_device(ctx, tree, &a.ops, &a.seg, &a.top, &a.wseg, &a.tip_seq));
   const SplitSchedule &sp = ctx->split;
-  if (split_smem<TcmOp<false>>(sp.rows) > ctx->smem_optin) return PGPU_OK;
+  if (split_smem<TcmOp<false>>(sp.rows, false) > ctx->smem_optin) return PGPU_OK;
   a.tips = tips;
   a.weights = weights;
   a.node_sets = node_sets;
