@@ -518,6 +518,24 @@ constexpr int FS_S = 8;   // segments at most
 constexpr int FS_P = 4;   // tip slices in flight per thread (a power of two)
 static_assert((FS_P & (FS_P - 1)) == 0, "the copy ring is indexed by a mask");
 
+// Shared-memory accesses through 32-bit shared-window addresses.
+__device__ __forceinline__ uint32_t lds_u32(uint32_t a) {
+  uint32_t v;
+  asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ uint4 lds_v4(uint32_t a) {
+  uint4 v;
+  asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(a)
+               : "memory");
+  return v;
+}
+__device__ __forceinline__ void sts_v4(uint32_t a, const uint4 &v) {
+  asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(a), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
+               : "memory");
+}
+
 __device__ __forceinline__ void cp_async16(void *dst, const void *src, bool valid) {
   const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(valid ? 16 : 0)
@@ -681,7 +699,7 @@ struct TcmOp {
   static constexpr size_t EXTRA_SMEM = 256 * 32 * 4;
   static constexpr bool FULL_ANY_WIDTH = false;  // an idle lane's code 0 would raise the flag
   static constexpr uint32_t COST = 0x0FFFFFFFu;
-  const uint32_t *tb;
+  uint32_t tb;   // shared address of this lane's copy of entry 0
   uint32_t acc[32];
   int since;
   // every thread of the CTA takes part in filling the table; the kernel's
@@ -692,7 +710,7 @@ struct TcmOp {
       if (PACKED) e = (e >> 31) ? 0u : (e << 28) | ((e >> 4) & COST);
       extra[i] = e;
     }
-    tb = extra + (tid & 31);
+    tb = static_cast<uint32_t>(__cvta_generic_to_shared(extra + (tid & 31)));
 #pragma unroll
     for (int i = 0; i < 32; ++i) acc[i] = 0;
     since = 0;
@@ -712,8 +730,9 @@ struct TcmOp {
     uint32_t e[8];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      e[2 * k] = tb[__byte_perm(ev, 0u, 0x4440u + k) << 5];
-      e[2 * k + 1] = tb[__byte_perm(od, 0u, 0x4440u + k) << 5];
+      // entry i of this lane's copy lies 128 i bytes after entry 0
+      e[2 * k] = lds_u32(tb + (__byte_perm(ev, 0u, 0x4440u + k) << 7));
+      e[2 * k + 1] = lds_u32(tb + (__byte_perm(od, 0u, 0x4440u + k) << 7));
     }
 #pragma unroll
     for (int l = 0; l < 8; ++l) acc[q * 8 + l] += PACKED ? e[l] : e[l] >> 4;
@@ -812,10 +831,14 @@ __device__ __forceinline__ void split_walk(const FitchSplitArgs &p, Op &rule, ui
     col[j] = p.tips + (act[j] ? word[j] : 0);
     ncol[j] = p.node_sets + word[j];
   }
+  // this lane's element of ring row r, part j: ring_s + (r NV + j) 512
+  // bytes (and likewise for the stack), as 32-bit shared-window addresses
+  const uint32_t ring_s = static_cast<uint32_t>(__cvta_generic_to_shared(ring)) + 16u * lane;
   const int4 ws = p.wseg[w];
   for (int q = 0; q < ws.y; ++q) {
     const int4 sg = p.seg[ws.x + q];   // {op_off, n_ops, tip_off, n_tips}
     uint4 *stk = stk0 + (q + 1) * NV * 32;   // rows below hold earlier results
+    const uint32_t stk_s = static_cast<uint32_t>(__cvta_generic_to_shared(stk)) + 16u * lane;
     const int32_t *tseq = p.tip_seq + sg.z;
     // copy counts are unsigned so that the ring slot is a mask, not a
     // signed remainder
@@ -845,7 +868,7 @@ __device__ __forceinline__ void split_walk(const FitchSplitArgs &p, Op &rule, ui
     uint4 top[NV];
     auto from_ring = [&](uint4 (&dst)[NV]) {
 #pragma unroll
-      for (int j = 0; j < NV; ++j) dst[j] = ring[((consumed & (FS_P - 1)) * NV + j) * 32 + lane];
+      for (int j = 0; j < NV; ++j) dst[j] = lds_v4(ring_s + (((consumed & (FS_P - 1)) * NV + j) << 9));
       ++consumed;
     };
     const int4 *ops = p.ops + sg.x;
@@ -859,7 +882,7 @@ __device__ __forceinline__ void split_walk(const FitchSplitArgs &p, Op &rule, ui
       if (ta && tb) {
         if (i > 0) {
 #pragma unroll
-          for (int j = 0; j < NV; ++j) stk[(sp * NV + j) * 32 + lane] = top[j];
+          for (int j = 0; j < NV; ++j) sts_v4(stk_s + ((sp * NV + j) << 9), top[j]);
           ++sp;
         }
         cp_async_wait<FS_P - 1>();
@@ -880,7 +903,7 @@ __device__ __forceinline__ void split_walk(const FitchSplitArgs &p, Op &rule, ui
         --sp;
 #pragma unroll
         for (int j = 0; j < NV; ++j) {
-          x[j] = stk[(sp * NV + j) * 32 + lane];
+          x[j] = lds_v4(stk_s + ((sp * NV + j) << 9));
           y[j] = top[j];
         }
       }
