@@ -36,6 +36,7 @@
 // tbr_pair_kernel then scores every pair of attach edges of the cut as one
 // dot product per pattern.
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <cstring>
 
@@ -503,6 +504,36 @@ __host__ __device__ size_t pair_smem(int R) {
   return 1024 + 2 * (size_t)TB_T * tbr_row(R) * sizeof(typename Pol::V) + 2 * TB_T * TB_PB * sizeof(int);
 }
 
+// sum_q x_q z_q of one site.  In the float-pair form the terms are
+// non-negative, so they are summed as the pruning rows sum: exact products
+// (TwoProduct and the two cross terms), the high parts added exactly by a
+// Fast2Sum of the larger and the smaller, everything else gathered in one
+// float; the pair is normalised once at the end.  About 11 instructions a
+// term against 15 for a pair add per term.
+template <typename Pol>
+__device__ __forceinline__ typename Pol::V pair_dot(const typename Pol::V *x, const typename Pol::V *z, int n) {
+  if constexpr (std::is_same<Pol, Ff32>::value) {
+    float sh = __fmul_rn(x[0].h, z[0].h);
+    float lo = __fmaf_rn(x[0].h, z[0].h, -sh);
+    lo = __fmaf_rn(x[0].h, z[0].l, lo);
+    lo = __fmaf_rn(x[0].l, z[0].h, lo);
+    for (int q = 1; q < n; ++q) {
+      const float p = __fmul_rn(x[q].h, z[q].h);
+      float e = __fmaf_rn(x[q].h, z[q].h, -p);
+      e = __fmaf_rn(x[q].h, z[q].l, e);
+      e = __fmaf_rn(x[q].l, z[q].h, e);
+      const ff t = fast_two_sum(fmaxf(sh, p), fminf(sh, p));
+      sh = t.h;
+      lo = __fadd_rn(lo, __fadd_rn(t.l, e));
+    }
+    return fast_two_sum(sh, lo);
+  } else {
+    typename Pol::V acc = Pol::zero();
+    for (int q = 0; q < n; ++q) acc = Pol::add(acc, Pol::mul(x[q], z[q]));
+    return acc;
+  }
+}
+
 template <typename Pol>
 __global__ void __launch_bounds__(256) tbr_pair_kernel(const PairArgs a) {
   using V = typename Pol::V;
@@ -554,8 +585,7 @@ __global__ void __launch_bounds__(256) tbr_pair_kernel(const PairArgs a) {
       if (w == 0.0f) continue;
       const V *xr = Xs + (size_t)jj * RS + (size_t)p * R * 4;
       const V *zr = Zs + (size_t)kk * RS + (size_t)p * R * 4;
-      V acc = Pol::zero();
-      for (int q = 0; q < R * 4; ++q) acc = Pol::add(acc, Pol::mul(xr[q], zr[q]));
+      const V acc = pair_dot<Pol>(xr, zr, R * 4);
       if (Pol::positive(acc))
         sum = ff_add(sum, ff_mul(Pol::site_log(acc, xs[jj * TB_PB + p] + ys[kk * TB_PB + p], ltab),
                                  ff{w, 0.0f}));
