@@ -126,9 +126,18 @@ __device__ __forceinline__ ff ff_shfl_xor(ff v, int o) {
 constexpr float LN2_HI = 0.693145751953125f;
 constexpr float LN2_LO = 1.42860682030941723212e-6f;
 
+// an integer |E| < 2^22 as a float, through the bits of 2^23 + 2^22 + E
+// instead of a conversion instruction
+__device__ __forceinline__ float small_int_to_float(int E) {
+  return __int_as_float(0x4B400000 + E) - 12582912.0f;
+}
+
 // E * ln 2 as a float pair (exact high part for |E| < 4096)
 __device__ __forceinline__ ff ff_exp2_log(int E) {
-  if (E > -4096 && E < 4096) return fast_two_sum((float)E * LN2_HI, (float)E * LN2_LO);
+  if (E > -4096 && E < 4096) {
+    const float e = small_int_to_float(E);
+    return fast_two_sum(e * LN2_HI, e * LN2_LO);
+  }
   return ff_from_d((double)E * 0.69314718055994530942);
 }
 
@@ -147,10 +156,14 @@ __device__ __forceinline__ ff ff_log(ff x, int e2, const float4 *tab) {
   const int bits = __float_as_int(x.h);
   const int ex = ((bits >> 23) & 0xff) - 127;
   const float m = __int_as_float((bits & 0x007fffff) | 0x3f800000);
-  const float ml = ldexpf(x.l, -ex);
+  // x.l 2^-ex by two exact power-of-two factors (each exponent within
+  // [-64, 64]), so no library scaling routine is called
+  const int k1 = -ex / 2, k2 = -ex - k1;
+  const float ml = x.l * __int_as_float((127 + k1) << 23) * __int_as_float((127 + k2) << 23);
   const int k = (bits >> 17) & 63;
   const float4 t = tab[k];
-  const float c = 1.0f + (float)(2 * k + 1) * 0.0078125f;
+  // c = 1 + (2k + 1) / 128, written into the mantissa bits directly
+  const float c = __int_as_float(0x3f800000 | ((2 * k + 1) << 16));
   const ff d = two_sum(__fsub_rn(m, c), ml);          // m - c is exact
   const ff r = ff_mul(d, ff{t.z, t.w});
   const ff r2 = ff_mul(r, r);
