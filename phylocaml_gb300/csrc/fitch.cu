@@ -503,8 +503,9 @@ __global__ void __launch_bounds__(160) fitch_tree_kernel(const FitchTreeArgs p) 
 }
 
 // ---------------------------------------------------------------------------
-// tree kernel, segmented form.  One CTA of FS_W warps per 128-word slice
-// (4 words per thread): the postorder is cut into up to FS_S disjoint
+// tree kernel, segmented form.  One CTA of FS_W warps per slice of up to
+// 256 words (one or two groups of 4 words per thread, 128 words apart): the
+// postorder is cut into up to FS_S disjoint
 // subtrees (segments), dealt to the warps longest first; each warp walks its
 // segments one after another with its own stack, and each thread keeps its
 // next FS_P tip slices in flight with cp.async (LDGSTS) into a per-warp ring.
