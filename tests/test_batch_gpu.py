@@ -75,6 +75,35 @@ def test_mixed_batch_matches_fp64_and_oracle(ctx, orc):
         b.close()
 
 
+def test_full_shape_variants_within_tf32_error(ctx, orc):
+    """Variants of the batch workload's own shapes (128 taxa; 20-state
+    GTR-like models with four Gamma rate classes, two to a pass, and 61-state
+    codon models) against the CPU FP64 oracle, at the per-variant relative
+    error the TF32 operands leave (about 5e-7 measured; bound 1e-5 here) and
+    at FP64 for the comparison form."""
+    import os
+    import torch
+    from phylocaml_gb300.batch import Batch
+    dev = torch.device("cuda:0")
+    rng = np.random.default_rng(2048)
+    built = [make_variant(rng, "protein" if k % 2 == 0 else "codon", 128, 3_000, dev) for k in range(8)]
+    b = Batch([x[0] for x in built], ctx)
+    try:
+        tc = b.run()
+        f64 = b.run_fp64(sample=3_000)
+        for k, (v, codes, w) in enumerate(built):
+            P = np.empty((2 * v.tree.n_tips - 2, len(v.rates), v.q.shape[0], v.q.shape[0]))
+            for c in range(2 * v.tree.n_tips - 2):
+                for r, rate in enumerate(v.rates):
+                    P[c, r] = expm(v.q * rate * v.tree.brlen[c])
+            exp = orc.prune_lnl(v.tree.left, v.tree.right, P, v.pi, v.probs, codes, v.code_table, w,
+                                n_threads=os.cpu_count() or 4)
+            assert abs(f64[k] - exp) <= FP64_REL * abs(exp), (k, f64[k], exp)
+            assert abs(tc[k] - exp) <= 1e-5 * abs(exp), (k, tc[k], exp, (tc[k] - exp) / abs(exp))
+    finally:
+        b.close()
+
+
 def test_batch_rejects_trees_deeper_than_the_tmem_stack(ctx):
     import torch
     from phylocaml_gb300 import _native
