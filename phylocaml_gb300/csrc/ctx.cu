@@ -66,6 +66,14 @@ pgpu_status pgpu_check_flag(pgpu_ctx *ctx, const char *what) {
   return PGPU_OK;
 }
 
+pgpu_status pgpu_copy_stream(pgpu_ctx *ctx) {
+  if (ctx->copy_stream) return PGPU_OK;
+  PGPU_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+  for (cudaEvent_t &e : ctx->copy_ev)
+    PGPU_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  return PGPU_OK;
+}
+
 extern "C" {
 
 int pgpu_version(void) { return 100; }
@@ -122,12 +130,19 @@ void pgpu_destroy(pgpu_ctx *ctx) {
     if (ctx->stage_ev[k]) cudaEventDestroy(ctx->stage_ev[k]);
   }
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  if (ctx->copy_stream) {
+    cudaStreamSynchronize(ctx->copy_stream);
+    cudaStreamDestroy(ctx->copy_stream);
+  }
+  for (cudaEvent_t &e : ctx->copy_ev)
+    if (e) cudaEventDestroy(e);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   (void)cudaGetLastError();
   delete ctx;
 }
 
 const char *pgpu_last_error(const pgpu_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
 
 pgpu_status pgpu_set_stream(pgpu_ctx *ctx, void *cuda_stream) {
   if (!ctx) return PGPU_ERR_ARG;

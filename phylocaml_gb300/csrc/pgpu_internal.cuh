@@ -64,6 +64,9 @@ struct SplitSchedule {
   std::vector<int4> top;       // {k, ref_a, ref_b, 0} in postorder
 };
 
+// column chunks of the host-buffer pruning call's tip-code copy
+constexpr int PGPU_COPY_CHUNKS = 4;
+
 struct pgpu_ctx {
   int device = 0;
   int num_sms = 0;
@@ -92,9 +95,17 @@ struct pgpu_ctx {
   size_t stage_cap[2] = {};
   cudaEvent_t stage_ev[2] = {};
   int stage_next = 0, stage_cur = 0;
-  // words of a state-set row per CTA of the Fitch tree kernel (0: 128)
+  // words of a state-set row per CTA of the Fitch tree kernel (0: picked
+  // per launch)
   int fitch_tile_words = 0;
+  // a second stream for host-to-device copies that overlap the scoring,
+  // with one event per copied chunk and one for the start of a call
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_ev[PGPU_COPY_CHUNKS + 1] = {};
 };
+
+// Creates the copy stream and its events on first use.
+pgpu_status pgpu_copy_stream(pgpu_ctx *ctx);
 
 pgpu_status pgpu_set_err(pgpu_ctx *ctx, pgpu_status st, const char *fmt, ...);
 

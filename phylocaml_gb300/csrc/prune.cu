@@ -47,7 +47,7 @@ struct PruneArgs {
   const double *probs;        // [R]
   const double *weights;      // [n_pat] or null
   double *site_lnl;           // [n_pat] or null
-  double2 *partials;          // [gridDim.x]
+  double2 *partials;          // [n_models][n_tiles_total], by tile
   const int4 *ops;            // schedule
   const int32_t *tip_seq;
   int *flag;
@@ -56,6 +56,9 @@ struct PruneArgs {
   // tab_stride bytes after the previous model's, pi and probs 4 and R
   // doubles after, and whose partial sums follow the previous model's
   size_t P_stride, tab_stride;
+  // a launch may cover tiles tile_base .. tile_base + gridDim.x - 1 of
+  // n_tiles_total (the host-buffer entry point launches one per copied chunk)
+  size_t tile_base, n_tiles_total;
   size_t ld_pat, n_pat;
   int n_tips, n_ops, n_codes, R, NP, depth;
 };
@@ -133,7 +136,8 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
   const size_t SB = L::slot_bytes(NP, R, NC);
   unsigned char *ring = smem + L::ring_off();               // [ST][SB]
   V *stk = reinterpret_cast<V *>(smem + L::stk_off(NP, R, NC));   // [depth][4][NT]
-  const size_t tile0 = (size_t)blockIdx.x * NP;
+  const size_t tile = p.tile_base + blockIdx.x;
+  const size_t tile0 = tile * NP;
   const int tid = threadIdx.x;
   const size_t CB = L::coef_bytes(R), TB = L::tip_bytes(R, NC);
 
@@ -352,7 +356,7 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
     double2 v = lane < NT / 32 ? red[lane] : make_double2(0.0, 0.0);
     double ss = v.x, cc = v.y;
     warp_csum(ss, cc);
-    if (lane == 0) p.partials[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = make_double2(ss, cc);
+    if (lane == 0) p.partials[(size_t)blockIdx.y * p.n_tiles_total + tile] = make_double2(ss, cc);
   }
 }
 
@@ -374,19 +378,53 @@ pgpu_status launch_prune_rt(pgpu_ctx *ctx, PruneArgs &a, size_t n_tiles, size_t 
   return pgpu_after_launch(ctx, "prune_tree_kernel");
 }
 
+// Tip codes still in host memory: copied column chunk by column chunk on
+// the context's copy stream, each chunk's launch waiting only for its own
+// columns, so the copy of chunk k + 1 overlaps the scoring of chunk k.
+struct HostTips {
+  const uint8_t *host;   // [n_tips][n_pat]
+  uint8_t *dev;          // [n_tips][ld_pat]
+  size_t n_tips;
+};
+
+pgpu_status copy_chunk(pgpu_ctx *ctx, const HostTips &ht, const PruneArgs &a, size_t c0, size_t c1, int k) {
+  if (c1 > c0)
+    PGPU_CUDA(ctx, cudaMemcpy2DAsync(ht.dev + c0, a.ld_pat, ht.host + c0, a.n_pat, c1 - c0, ht.n_tips,
+                                     cudaMemcpyHostToDevice, ctx->copy_stream));
+  PGPU_CUDA(ctx, cudaEventRecord(ctx->copy_ev[k], ctx->copy_stream));
+  PGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[k], 0));
+  return PGPU_OK;
+}
+
+template <typename Pol, int RT>
+pgpu_status launch_prune_chunks(pgpu_ctx *ctx, PruneArgs &a, size_t n_tiles, size_t smem, int n_models,
+                                const HostTips *ht) {
+  const int K = ht ? (int)std::min<size_t>(PGPU_COPY_CHUNKS, n_tiles) : 1;
+  for (int k = 0; k < K; ++k) {
+    const size_t t0 = n_tiles * k / K, t1 = n_tiles * (k + 1) / K;
+    if (ht) PGPU_TRY(copy_chunk(ctx, *ht, a, t0 * a.NP, std::min(t1 * a.NP, a.n_pat), k));
+    a.tile_base = t0;
+    PGPU_TRY((launch_prune_rt<Pol, RT>(ctx, a, t1 - t0, smem, n_models)));
+  }
+  a.tile_base = 0;
+  return PGPU_OK;
+}
+
 template <typename Pol>
-pgpu_status launch_prune(pgpu_ctx *ctx, PruneArgs &a, int RT, int n_models) {
+pgpu_status launch_prune(pgpu_ctx *ctx, PruneArgs &a, int RT, int n_models, const HostTips *ht) {
   a.NP = PR_THREADS / RT;
   const size_t n_tiles = (a.n_pat + a.NP - 1) / a.NP;
+  a.n_tiles_total = n_tiles;
+  a.tile_base = 0;
   const size_t smem = PruneLayout<Pol>::bytes(a.NP, a.R, a.n_codes, a.depth);
   if (smem > ctx->smem_optin)
     return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "prune: %zu bytes of shared memory needed (tree too deep)",
                         smem);
   switch (RT) {
-    case 1: return launch_prune_rt<Pol, 1>(ctx, a, n_tiles, smem, n_models);
-    case 2: return launch_prune_rt<Pol, 2>(ctx, a, n_tiles, smem, n_models);
-    case 4: return launch_prune_rt<Pol, 4>(ctx, a, n_tiles, smem, n_models);
-    default: return launch_prune_rt<Pol, 8>(ctx, a, n_tiles, smem, n_models);
+    case 1: return launch_prune_chunks<Pol, 1>(ctx, a, n_tiles, smem, n_models, ht);
+    case 2: return launch_prune_chunks<Pol, 2>(ctx, a, n_tiles, smem, n_models, ht);
+    case 4: return launch_prune_chunks<Pol, 4>(ctx, a, n_tiles, smem, n_models, ht);
+    default: return launch_prune_chunks<Pol, 8>(ctx, a, n_tiles, smem, n_models, ht);
   }
 }
 
@@ -474,10 +512,13 @@ Ptr *rebase(void *base, Ptr *off) {
 // and one set of patterns: lnl_dev[v] for model v.  One eigendecomposition
 // launch for all models, a P and a tip-table build per model, then one
 // pruning launch whose CTA rows are the models.
+// host_tips: the codes are still in host memory (n_pat bytes per row) and
+// tips is the device buffer they go to; they are copied in chunks that
+// overlap the scoring.
 pgpu_status prune_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *models, int n_models,
                       const pgpu_tip_codes *codes, const uint8_t *tips, size_t ld_pat,
                       const double *weights, size_t n_pat, int precision, double *lnl_dev,
-                      double *site_lnl_dev) {
+                      double *site_lnl_dev, const uint8_t *host_tips = nullptr) {
   if (!models || n_models < 1) return pgpu_set_err(ctx, PGPU_ERR_ARG, "prune: no model");
   if (n_models > 65535) return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "prune: at most 65,535 models per call");
   for (int v = 0; v < n_models; ++v) {
@@ -579,9 +620,11 @@ pgpu_status prune_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *mo
   a.R = R;
   a.NP = 0;
   a.depth = std::max(sch->max_depth, 1);
-  if (precision == 32) PGPU_TRY(launch_prune<Fp32>(ctx, a, RT, V));
-  else if (precision == 48) PGPU_TRY(launch_prune<Ff32>(ctx, a, RT, V));
-  else PGPU_TRY(launch_prune<Fp64>(ctx, a, RT, V));
+  HostTips ht{host_tips, const_cast<uint8_t *>(tips), (size_t)n};
+  const HostTips *htp = host_tips ? &ht : nullptr;
+  if (precision == 32) PGPU_TRY(launch_prune<Fp32>(ctx, a, RT, V, htp));
+  else if (precision == 48) PGPU_TRY(launch_prune<Ff32>(ctx, a, RT, V, htp));
+  else PGPU_TRY(launch_prune<Fp64>(ctx, a, RT, V, htp));
   prune_finalize_kernel<<<V, 1024, 0, ctx->stream>>>((const double2 *)dpart, (int)n_tiles, lnl_dev);
   return pgpu_after_launch(ctx, "prune_finalize_kernel");
 }
@@ -654,12 +697,16 @@ pgpu_status pgpu_prune_lnl(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_mode
   if (weights) PGPU_TRY(pgpu_buf(ctx, BUF_WEIGHTS, n_pat * 8, &dw));
   if (site_lnl) PGPU_TRY(pgpu_buf(ctx, BUF_SITECOST, n_pat * 8, &dsl));
   cudaStream_t s = ctx->stream;
-  if (n_pat) {
-    PGPU_CUDA(ctx, cudaMemcpy2DAsync(dt, ld, tip_codes, n_pat, n_pat, n, cudaMemcpyHostToDevice, s));
-    if (weights) PGPU_CUDA(ctx, cudaMemcpyAsync(dw, weights, n_pat * 8, cudaMemcpyHostToDevice, s));
-  }
+  // the tip codes go over in column chunks on the copy stream, after
+  // everything already queued on the context's stream (which may still read
+  // the device buffer), each chunk's scoring waiting for its own columns
+  PGPU_TRY(pgpu_copy_stream(ctx));
+  PGPU_CUDA(ctx, cudaEventRecord(ctx->copy_ev[PGPU_COPY_CHUNKS], s));
+  PGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev[PGPU_COPY_CHUNKS], 0));
+  if (n_pat && weights)
+    PGPU_CUDA(ctx, cudaMemcpyAsync(dw, weights, n_pat * 8, cudaMemcpyHostToDevice, s));
   PGPU_TRY(prune_dev(ctx, tree, model, 1, codes, (const uint8_t *)dt, ld, (const double *)dw, n_pat,
-                     precision, (double *)dl, (double *)dsl));
+                     precision, (double *)dl, (double *)dsl, tip_codes));
   double *hl = reinterpret_cast<double *>(ctx->h_pinned);
   PGPU_CUDA(ctx, cudaMemcpyAsync(hl, dl, 8, cudaMemcpyDeviceToHost, s));
   if (site_lnl && n_pat)
