@@ -152,7 +152,11 @@ pgpu_status pgpu_fitch_distance(pgpu_ctx *ctx, const uint32_t *a, const uint32_t
  *              site s took the union
  *   total      out: sum_s weights[s] * site_cost[s] (a per-site count is at
  *              most n_tips-1, so it always fits uint32; the total is exact
- *              while it stays below 2^64) */
+ *              while it stays below 2^64)
+ * Below 64-bit lanes the rows are copied in column chunks on two further
+ * streams of the context, so the copies in and out overlap each other and
+ * the kernels (pinned host memory lets them run asynchronously); the call
+ * returns once every output is written. */
 pgpu_status pgpu_fitch_tree(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
                             const uint32_t *weights, size_t n_sites, int lane_bits,
                             uint32_t *node_sets, uint32_t *site_cost, uint64_t *total);

@@ -69,7 +69,10 @@ pgpu_status pgpu_check_flag(pgpu_ctx *ctx, const char *what) {
 pgpu_status pgpu_copy_stream(pgpu_ctx *ctx) {
   if (ctx->copy_stream) return PGPU_OK;
   PGPU_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+  PGPU_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->d2h_stream, cudaStreamNonBlocking));
   for (cudaEvent_t &e : ctx->copy_ev)
+    PGPU_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  for (cudaEvent_t &e : ctx->done_ev)
     PGPU_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   return PGPU_OK;
 }
@@ -130,11 +133,14 @@ void pgpu_destroy(pgpu_ctx *ctx) {
     if (ctx->stage_ev[k]) cudaEventDestroy(ctx->stage_ev[k]);
   }
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
-  if (ctx->copy_stream) {
-    cudaStreamSynchronize(ctx->copy_stream);
-    cudaStreamDestroy(ctx->copy_stream);
-  }
+  for (cudaStream_t cs : {ctx->copy_stream, ctx->d2h_stream})
+    if (cs) {
+      cudaStreamSynchronize(cs);
+      cudaStreamDestroy(cs);
+    }
   for (cudaEvent_t &e : ctx->copy_ev)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t &e : ctx->done_ev)
     if (e) cudaEventDestroy(e);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   (void)cudaGetLastError();

@@ -556,6 +556,7 @@ struct FitchSplitArgs {
   int32_t n_tips;
   int n_top, rows;                       // rows: ring + stack rows per warp
   int tile_words;                        // words per CTA: 4 per active lane and part
+  size_t tile_base;                      // the launch's first tile (host-buffer calls launch by chunk)
   int count16;                           // per-site counts fit 16 bits (< 65,536 internal nodes)
   int tcm_period;                        // TcmOp<true>: steps between flushes of the packed sums
   const uint32_t *table;                 // cost-matrix pair table (TcmOp), else null
@@ -948,7 +949,7 @@ __global__ void __launch_bounds__(FS_W * 32, Op::MIN_BLOCKS) tree_split_kernel(c
   __syncthreads();
   // a tile of tile_words words: lanes past it idle (their loads are
   // zero-filled, nothing of theirs is counted or stored)
-  const size_t tile0 = (size_t)blockIdx.x * p.tile_words;
+  const size_t tile0 = ((size_t)blockIdx.x + p.tile_base) * p.tile_words;
   size_t word[NV];
   bool act[NV];
   uint4 valid[NV];
@@ -1376,9 +1377,17 @@ pgpu_status tree64_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tip
   return pgpu_after_launch(ctx, "fitch_tree64_kernel");
 }
 
+// Rows still in host memory: the tip rows are copied to `tips` and the node
+// rows back from `node_sets` column chunk by column chunk, on the context's
+// copy streams, so copies in both directions overlap the kernels.
+struct FitchHostIO {
+  const uint32_t *tips;   // [n_tips][n_words]
+  uint32_t *node_sets;    // [n_tips - 1][n_words]
+};
+
 pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips, size_t ld,
                      const uint32_t *weights, size_t n_sites, int lb, uint32_t *node_sets,
-                     uint32_t *site_cost, uint64_t *total) {
+                     uint32_t *site_cost, uint64_t *total, const FitchHostIO *io = nullptr) {
   if (!lane_bits_ok64(lb))
     return pgpu_set_err(ctx, PGPU_ERR_ARG, "lane_bits must be 4, 8, 16, 32 or 64");
   const size_t n_words = words_for(n_sites, lb);
@@ -1423,19 +1432,38 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
   a.flag = ctx->d_flag;
   const size_t tiles = (n_words + a.tile_words - 1) / a.tile_words;
   if (tiles > 0x7fffffffu) return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: too many tiles");
-  cudaError_t e;
-  switch (lb) {
-    case 4: e = launch_fitch_split<4>(s, a, tiles); break;
-    case 8: e = launch_fitch_split<8>(s, a, tiles); break;
-    case 16: e = launch_fitch_split<16>(s, a, tiles); break;
-    default: e = launch_fitch_split<32>(s, a, tiles); break;
+  const size_t n = (size_t)tree->n_tips, tw = (size_t)a.tile_words;
+  const int K = io ? (int)std::min<size_t>(PGPU_COPY_CHUNKS, tiles) : 1;
+  for (int k = 0; k < K; ++k) {
+    const size_t t0 = tiles * k / K, t1 = tiles * (k + 1) / K;
+    const size_t w0 = t0 * tw, w1 = std::min(t1 * tw, n_words);
+    if (io) {
+      PGPU_CUDA(ctx, cudaMemcpy2DAsync(const_cast<uint32_t *>(tips) + w0, ld * 4, io->tips + w0, n_words * 4,
+                                       (w1 - w0) * 4, n, cudaMemcpyHostToDevice, ctx->copy_stream));
+      PGPU_CUDA(ctx, cudaEventRecord(ctx->copy_ev[k], ctx->copy_stream));
+      PGPU_CUDA(ctx, cudaStreamWaitEvent(s, ctx->copy_ev[k], 0));
+    }
+    a.tile_base = t0;
+    cudaError_t e;
+    switch (lb) {
+      case 4: e = launch_fitch_split<4>(s, a, t1 - t0); break;
+      case 8: e = launch_fitch_split<8>(s, a, t1 - t0); break;
+      case 16: e = launch_fitch_split<16>(s, a, t1 - t0); break;
+      default: e = launch_fitch_split<32>(s, a, t1 - t0); break;
+    }
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      return pgpu_set_err(ctx, PGPU_ERR_CUDA, "launch of tree_split_kernel failed: %s",
+                          cudaGetErrorString(e));
+    }
+    ctx->launches++;
+    if (io) {
+      PGPU_CUDA(ctx, cudaEventRecord(ctx->done_ev[k], s));
+      PGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->d2h_stream, ctx->done_ev[k], 0));
+      PGPU_CUDA(ctx, cudaMemcpy2DAsync(io->node_sets + w0, n_words * 4, node_sets + w0, ld * 4,
+                                       (w1 - w0) * 4, n - 1, cudaMemcpyDeviceToHost, ctx->d2h_stream));
+    }
   }
-  if (e != cudaSuccess) {
-    (void)cudaGetLastError();
-    return pgpu_set_err(ctx, PGPU_ERR_CUDA, "launch of tree_split_kernel failed: %s",
-                        cudaGetErrorString(e));
-  }
-  ctx->launches++;
   return PGPU_OK;
 }
 
@@ -1471,6 +1499,7 @@ pgpu_status pgpu_tcm_tree_split(pgpu_ctx *ctx, const pgpu_tree *tree, const uint
   a.n_top = (int)sp.top.size();
   a.rows = sp.rows;
   a.tile_words = 128;
+  a.tile_base = 0;
   a.count16 = 0;
   a.tcm_period = flush_period;
   a.table = table_dev;
@@ -1638,23 +1667,34 @@ pgpu_status pgpu_fitch_tree(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t
   if (weights) PGPU_TRY(pgpu_buf(ctx, BUF_WEIGHTS, n_sites * 4, &dw));
   if (site_cost) PGPU_TRY(pgpu_buf(ctx, BUF_SITECOST, n_sites * 4, &dsc));
   cudaStream_t s = ctx->stream;
-  if (n_words) {
+  // below 64-bit lanes the rows go over in column chunks on the copy
+  // streams, after everything already queued on the context's stream
+  const bool chunked = lane_bits < 64 && n_words > 0;
+  if (chunked) {
+    PGPU_TRY(pgpu_copy_stream(ctx));
+    PGPU_CUDA(ctx, cudaEventRecord(ctx->copy_ev[PGPU_COPY_CHUNKS], s));
+    PGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev[PGPU_COPY_CHUNKS], 0));
+    PGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->d2h_stream, ctx->copy_ev[PGPU_COPY_CHUNKS], 0));
+  } else if (n_words) {
     PGPU_CUDA(ctx, cudaMemcpy2DAsync(dt, ld * 4, tips, n_words * 4, n_words * 4, n,
                                      cudaMemcpyHostToDevice, s));
-    if (weights)
-      PGPU_CUDA(ctx, cudaMemcpyAsync(dw, weights, n_sites * 4, cudaMemcpyHostToDevice, s));
   }
+  if (n_words && weights)
+    PGPU_CUDA(ctx, cudaMemcpyAsync(dw, weights, n_sites * 4, cudaMemcpyHostToDevice, s));
+  const FitchHostIO io{tips, node_sets};
   PGPU_TRY(tree_dev(ctx, tree, (const uint32_t *)dt, ld, (const uint32_t *)dw, n_sites, lane_bits,
-                    (uint32_t *)dn, (uint32_t *)dsc, (uint64_t *)dtot));
+                    (uint32_t *)dn, (uint32_t *)dsc, (uint64_t *)dtot, chunked ? &io : nullptr));
   if (n_words) {
-    PGPU_CUDA(ctx, cudaMemcpy2DAsync(node_sets, n_words * 4, dn, ld * 4, n_words * 4, n_int,
-                                     cudaMemcpyDeviceToHost, s));
+    if (!chunked)
+      PGPU_CUDA(ctx, cudaMemcpy2DAsync(node_sets, n_words * 4, dn, ld * 4, n_words * 4, n_int,
+                                       cudaMemcpyDeviceToHost, s));
     if (site_cost)
       PGPU_CUDA(ctx, cudaMemcpyAsync(site_cost, dsc, n_sites * 4, cudaMemcpyDeviceToHost, s));
   }
   uint64_t *ht = reinterpret_cast<uint64_t *>(ctx->h_pinned);
   PGPU_CUDA(ctx, cudaMemcpyAsync(ht, dtot, 8, cudaMemcpyDeviceToHost, s));
   PGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  if (chunked) PGPU_CUDA(ctx, cudaStreamSynchronize(ctx->d2h_stream));
   PGPU_TRY(pgpu_check_flag(ctx, "fitch_tree"));
   *total = *ht;
   return PGPU_OK;

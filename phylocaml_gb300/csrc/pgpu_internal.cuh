@@ -98,13 +98,15 @@ struct pgpu_ctx {
   // words of a state-set row per CTA of the Fitch tree kernel (0: picked
   // per launch)
   int fitch_tile_words = 0;
-  // a second stream for host-to-device copies that overlap the scoring,
-  // with one event per copied chunk and one for the start of a call
-  cudaStream_t copy_stream = nullptr;
+  // streams for host-to-device and device-to-host copies that overlap the
+  // kernels of host-buffer calls, with one event per copied chunk, one for
+  // the start of a call and one per finished chunk
+  cudaStream_t copy_stream = nullptr, d2h_stream = nullptr;
   cudaEvent_t copy_ev[PGPU_COPY_CHUNKS + 1] = {};
+  cudaEvent_t done_ev[PGPU_COPY_CHUNKS] = {};
 };
 
-// Creates the copy stream and its events on first use.
+// Creates the copy streams and their events on first use.
 pgpu_status pgpu_copy_stream(pgpu_ctx *ctx);
 
 pgpu_status pgpu_set_err(pgpu_ctx *ctx, pgpu_status st, const char *fmt, ...);
