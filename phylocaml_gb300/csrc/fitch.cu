@@ -1377,17 +1377,39 @@ pgpu_status tree64_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tip
   return pgpu_after_launch(ctx, "fitch_tree64_kernel");
 }
 
-// Rows still in host memory: the tip rows are copied to `tips` and the node
-// rows back from `node_sets` column chunk by column chunk, on the context's
-// copy streams, so copies in both directions overlap the kernels.
-struct FitchHostIO {
-  const uint32_t *tips;   // [n_tips][n_words]
-  uint32_t *node_sets;    // [n_tips - 1][n_words]
-};
+// The split kernel's launches over tiles [0, tiles), in up to
+// PGPU_COPY_CHUNKS column chunks when the rows are still in host memory
+// (io): chunk k's tip columns are copied in on the copy stream, its launch
+// waits for them, and its node columns go back on the device-to-host stream
+// once the launch is done.  launch(t0, t1) launches tiles [t0, t1).
+template <class Launch>
+pgpu_status split_chunks(pgpu_ctx *ctx, const FitchSplitArgs &a, size_t tiles, const HostRows *io,
+                         Launch launch) {
+  const size_t n = (size_t)a.n_tips, tw = (size_t)a.tile_words, ld = a.ld, nw = a.n_words;
+  const int K = io ? (int)std::min<size_t>(PGPU_COPY_CHUNKS, tiles) : 1;
+  for (int k = 0; k < K; ++k) {
+    const size_t t0 = tiles * k / K, t1 = tiles * (k + 1) / K;
+    const size_t w0 = t0 * tw, w1 = std::min(t1 * tw, nw);
+    if (io) {
+      PGPU_CUDA(ctx, cudaMemcpy2DAsync(const_cast<uint32_t *>(a.tips) + w0, ld * 4, io->tips + w0, nw * 4,
+                                       (w1 - w0) * 4, n, cudaMemcpyHostToDevice, ctx->copy_stream));
+      PGPU_CUDA(ctx, cudaEventRecord(ctx->copy_ev[k], ctx->copy_stream));
+      PGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[k], 0));
+    }
+    PGPU_TRY(launch(t0, t1));
+    if (io) {
+      PGPU_CUDA(ctx, cudaEventRecord(ctx->done_ev[k], ctx->stream));
+      PGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->d2h_stream, ctx->done_ev[k], 0));
+      PGPU_CUDA(ctx, cudaMemcpy2DAsync(io->node_sets + w0, nw * 4, a.node_sets + w0, ld * 4,
+                                       (w1 - w0) * 4, n - 1, cudaMemcpyDeviceToHost, ctx->d2h_stream));
+    }
+  }
+  return PGPU_OK;
+}
 
 pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips, size_t ld,
                      const uint32_t *weights, size_t n_sites, int lb, uint32_t *node_sets,
-                     uint32_t *site_cost, uint64_t *total, const FitchHostIO *io = nullptr) {
+                     uint32_t *site_cost, uint64_t *total, const HostRows *io = nullptr) {
   if (!lane_bits_ok64(lb))
     return pgpu_set_err(ctx, PGPU_ERR_ARG, "lane_bits must be 4, 8, 16, 32 or 64");
   const size_t n_words = words_for(n_sites, lb);
@@ -1432,17 +1454,7 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
   a.flag = ctx->d_flag;
   const size_t tiles = (n_words + a.tile_words - 1) / a.tile_words;
   if (tiles > 0x7fffffffu) return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "fitch_tree: too many tiles");
-  const size_t n = (size_t)tree->n_tips, tw = (size_t)a.tile_words;
-  const int K = io ? (int)std::min<size_t>(PGPU_COPY_CHUNKS, tiles) : 1;
-  for (int k = 0; k < K; ++k) {
-    const size_t t0 = tiles * k / K, t1 = tiles * (k + 1) / K;
-    const size_t w0 = t0 * tw, w1 = std::min(t1 * tw, n_words);
-    if (io) {
-      PGPU_CUDA(ctx, cudaMemcpy2DAsync(const_cast<uint32_t *>(tips) + w0, ld * 4, io->tips + w0, n_words * 4,
-                                       (w1 - w0) * 4, n, cudaMemcpyHostToDevice, ctx->copy_stream));
-      PGPU_CUDA(ctx, cudaEventRecord(ctx->copy_ev[k], ctx->copy_stream));
-      PGPU_CUDA(ctx, cudaStreamWaitEvent(s, ctx->copy_ev[k], 0));
-    }
+  return split_chunks(ctx, a, tiles, io, [&](size_t t0, size_t t1) -> pgpu_status {
     a.tile_base = t0;
     cudaError_t e;
     switch (lb) {
@@ -1457,14 +1469,8 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
                           cudaGetErrorString(e));
     }
     ctx->launches++;
-    if (io) {
-      PGPU_CUDA(ctx, cudaEventRecord(ctx->done_ev[k], s));
-      PGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->d2h_stream, ctx->done_ev[k], 0));
-      PGPU_CUDA(ctx, cudaMemcpy2DAsync(io->node_sets + w0, n_words * 4, node_sets + w0, ld * 4,
-                                       (w1 - w0) * 4, n - 1, cudaMemcpyDeviceToHost, ctx->d2h_stream));
-    }
-  }
-  return PGPU_OK;
+    return PGPU_OK;
+  });
 }
 
 }  // namespace
@@ -1478,7 +1484,8 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
 pgpu_status pgpu_tcm_tree_split(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
                                 size_t ld, const uint32_t *weights, size_t n_sites,
                                 const uint32_t *table_dev, int flush_period, uint32_t *node_sets,
-                                uint32_t *site_cost, unsigned long long *total, bool *launched) {
+                                uint32_t *site_cost, unsigned long long *total, bool *launched,
+                                const HostRows *io) {
   *launched = false;
   if (((uintptr_t)tips | (uintptr_t)node_sets) & 15) return PGPU_OK;
   if (ld % 4 != 0 || ld > 0xffffffffull) return PGPU_OK;
@@ -1505,14 +1512,18 @@ pgpu_status pgpu_tcm_tree_split(pgpu_ctx *ctx, const pgpu_tree *tree, const uint
   a.table = table_dev;
   a.flag = ctx->d_flag;
   const size_t tiles = (n_words + 127) / 128;
-  cudaError_t e = flush_period > 0 ? launch_split<TcmOp<true>>(ctx->stream, a, tiles)
-                                   : launch_split<TcmOp<false>>(ctx->stream, a, tiles);
-  if (e != cudaSuccess) {
-    (void)cudaGetLastError();
-    return pgpu_set_err(ctx, PGPU_ERR_CUDA, "launch of tree_split_kernel<TcmOp> failed: %s",
-                        cudaGetErrorString(e));
-  }
-  ctx->launches++;
+  PGPU_TRY(split_chunks(ctx, a, tiles, io, [&](size_t t0, size_t t1) -> pgpu_status {
+    a.tile_base = t0;
+    cudaError_t e = flush_period > 0 ? launch_split<TcmOp<true>>(ctx->stream, a, t1 - t0)
+                                     : launch_split<TcmOp<false>>(ctx->stream, a, t1 - t0);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      return pgpu_set_err(ctx, PGPU_ERR_CUDA, "launch of tree_split_kernel<TcmOp> failed: %s",
+                          cudaGetErrorString(e));
+    }
+    ctx->launches++;
+    return PGPU_OK;
+  }));
   *launched = true;
   return PGPU_OK;
 }
@@ -1681,7 +1692,7 @@ pgpu_status pgpu_fitch_tree(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t
   }
   if (n_words && weights)
     PGPU_CUDA(ctx, cudaMemcpyAsync(dw, weights, n_sites * 4, cudaMemcpyHostToDevice, s));
-  const FitchHostIO io{tips, node_sets};
+  const HostRows io{tips, node_sets};
   PGPU_TRY(tree_dev(ctx, tree, (const uint32_t *)dt, ld, (const uint32_t *)dw, n_sites, lane_bits,
                     (uint32_t *)dn, (uint32_t *)dsc, (uint64_t *)dtot, chunked ? &io : nullptr));
   if (n_words) {

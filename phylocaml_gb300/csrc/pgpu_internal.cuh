@@ -109,6 +109,14 @@ struct pgpu_ctx {
 // Creates the copy streams and their events on first use.
 pgpu_status pgpu_copy_stream(pgpu_ctx *ctx);
 
+// Rows of a host-buffer tree call still in host memory: the tip rows go to
+// the device buffer and the node rows come back column chunk by column
+// chunk on the copy streams, overlapping the kernels.
+struct HostRows {
+  const uint32_t *tips;   // [n_tips][n_words]
+  uint32_t *node_sets;    // [n_tips - 1][n_words]
+};
+
 pgpu_status pgpu_set_err(pgpu_ctx *ctx, pgpu_status st, const char *fmt, ...);
 
 #define PGPU_CUDA(ctx, call)                                                        \
@@ -157,7 +165,8 @@ pgpu_status pgpu_schedule_device(pgpu_ctx *ctx, const pgpu_tree *tree, const Tre
 pgpu_status pgpu_tcm_tree_split(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
                                 size_t ld, const uint32_t *weights, size_t n_sites,
                                 const uint32_t *table_dev, int flush_period, uint32_t *node_sets,
-                                uint32_t *site_cost, unsigned long long *total, bool *launched);
+                                uint32_t *site_cost, unsigned long long *total, bool *launched,
+                                const HostRows *io = nullptr);
 
 // ---------------------------------------------------------------------------
 // device helpers: mbarrier, bulk copies, bounded waits

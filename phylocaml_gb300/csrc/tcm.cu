@@ -351,9 +351,12 @@ void median(const int32_t *tcm, int S, int mode, uint32_t i, uint32_t j, int64_t
   *code = assign;
 }
 
+// io: the rows are still in host memory (see HostRows); the segmented
+// kernel copies them in chunks, the single-walk kernel whole.
 pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips, size_t ld,
                      const uint32_t *weights, size_t n_sites, const uint32_t *table,
-                     uint32_t *node_sets, uint32_t *site_cost, unsigned long long *total) {
+                     uint32_t *node_sets, uint32_t *site_cost, unsigned long long *total,
+                     const HostRows *io = nullptr) {
   if (!tree || tree->n_tips < 2) return pgpu_set_err(ctx, PGPU_ERR_ARG, "tcm_tree: need at least 2 tips");
   if (!tips || !node_sets || !total || !table) return pgpu_set_err(ctx, PGPU_ERR_ARG, "tcm_tree: null buffer");
   const size_t n_words = (n_sites + 7) / 8;
@@ -385,8 +388,12 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
   bool launched = false;
   PGPU_TRY(pgpu_tcm_tree_split(ctx, tree, tips, ld, weights, n_sites,
                                static_cast<const uint32_t *>(d), period, node_sets, site_cost, total,
-                               &launched));
+                               &launched, io));
   if (launched) return PGPU_OK;
+  const size_t n = (size_t)tree->n_tips;
+  if (io)
+    PGPU_CUDA(ctx, cudaMemcpy2DAsync(const_cast<uint32_t *>(tips), ld * 4, io->tips, n_words * 4, n_words * 4,
+                                     n, cudaMemcpyHostToDevice, ctx->stream));
   TcmArgs a;
   a.tips = tips;
   a.weights = weights;
@@ -409,7 +416,11 @@ pgpu_status tree_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
                                       (int)smem));
   const unsigned grid = (unsigned)((n_words + TC_THREADS - 1) / TC_THREADS);
   tcm_tree_kernel<<<grid, TC_THREADS, smem, ctx->stream>>>(a);
-  return pgpu_after_launch(ctx, "tcm_tree_kernel");
+  PGPU_TRY(pgpu_after_launch(ctx, "tcm_tree_kernel"));
+  if (io)
+    PGPU_CUDA(ctx, cudaMemcpy2DAsync(io->node_sets, n_words * 4, node_sets, ld * 4, n_words * 4, n - 1,
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+  return PGPU_OK;
 }
 
 pgpu_status tree_wide_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips, size_t ld,
@@ -648,21 +659,24 @@ pgpu_status pgpu_tcm_tree(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *
   if (weights) PGPU_TRY(pgpu_buf(ctx, BUF_WEIGHTS, n_sites * 4, &dw));
   if (site_cost) PGPU_TRY(pgpu_buf(ctx, BUF_SITECOST, n_sites * 4, &dsc));
   cudaStream_t s = ctx->stream;
-  if (n_words) {
-    PGPU_CUDA(ctx, cudaMemcpy2DAsync(dt, ld * 4, tips, n_words * 4, n_words * 4, n,
-                                     cudaMemcpyHostToDevice, s));
-    if (weights) PGPU_CUDA(ctx, cudaMemcpyAsync(dw, weights, n_sites * 4, cudaMemcpyHostToDevice, s));
-  }
+  // the rows go over in column chunks on the copy streams (or whole, where
+  // the single-walk kernel runs), after everything already queued on the
+  // context's stream
+  PGPU_TRY(pgpu_copy_stream(ctx));
+  PGPU_CUDA(ctx, cudaEventRecord(ctx->copy_ev[PGPU_COPY_CHUNKS], s));
+  PGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev[PGPU_COPY_CHUNKS], 0));
+  PGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->d2h_stream, ctx->copy_ev[PGPU_COPY_CHUNKS], 0));
+  if (n_words && weights)
+    PGPU_CUDA(ctx, cudaMemcpyAsync(dw, weights, n_sites * 4, cudaMemcpyHostToDevice, s));
+  const HostRows io{tips, node_sets};
   PGPU_TRY(tree_dev(ctx, tree, (const uint32_t *)dt, ld, (const uint32_t *)dw, n_sites, table,
-                    (uint32_t *)dn, (uint32_t *)dsc, (unsigned long long *)dtot));
-  if (n_words) {
-    PGPU_CUDA(ctx, cudaMemcpy2DAsync(node_sets, n_words * 4, dn, ld * 4, n_words * 4, n_int,
-                                     cudaMemcpyDeviceToHost, s));
-    if (site_cost) PGPU_CUDA(ctx, cudaMemcpyAsync(site_cost, dsc, n_sites * 4, cudaMemcpyDeviceToHost, s));
-  }
+                    (uint32_t *)dn, (uint32_t *)dsc, (unsigned long long *)dtot, n_words ? &io : nullptr));
+  if (n_words && site_cost)
+    PGPU_CUDA(ctx, cudaMemcpyAsync(site_cost, dsc, n_sites * 4, cudaMemcpyDeviceToHost, s));
   uint64_t *ht = reinterpret_cast<uint64_t *>(ctx->h_pinned);
   PGPU_CUDA(ctx, cudaMemcpyAsync(ht, dtot, 8, cudaMemcpyDeviceToHost, s));
   PGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  PGPU_CUDA(ctx, cudaStreamSynchronize(ctx->d2h_stream));
   PGPU_TRY(pgpu_check_flag(ctx, "tcm_tree"));
   *total = *ht;
   return PGPU_OK;
