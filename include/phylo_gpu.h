@@ -235,7 +235,8 @@ pgpu_status pgpu_tcm_tables(pgpu_ctx *ctx, const int32_t *tcm, int n_states, int
  * pgpu_fitch_tree with lane_bits 4; node_sets, site_cost and total as
  * there, site_cost[s] the sum of the costs over the internal nodes (the
  * call fails with PGPU_ERR_OVERFLOW if that could exceed 2^32 - 1).  A code
- * without a median in a site returns PGPU_ERR_ARG. */
+ * without a median in a site returns PGPU_ERR_ARG.  The rows are copied as
+ * for pgpu_fitch_tree (column chunks overlapping the kernels). */
 pgpu_status pgpu_tcm_tree(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
                           const uint32_t *weights, size_t n_sites, const uint32_t *table,
                           uint32_t *node_sets, uint32_t *site_cost, uint64_t *total);
