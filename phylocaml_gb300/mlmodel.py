@@ -443,29 +443,38 @@ def gen_prior_opt_func(model: Model, ctx: _native.Context | None = None):
 HOOKS = {"subst": gen_subst_opt_func, "rates": gen_rates_opt_func, "prior": gen_prior_opt_func}
 
 
-def lnl_and_gradient(x: np.ndarray, build, lnl_many, h: float = 1e-4):
-    """lnL at a hook's parameter vector x and its central-difference gradient,
-    from one batched evaluation of the 2k + 1 models build(x), build(x +- h e_i)
-    (lnl_many: list of models -> array of lnL, e.g. likelihood.tree_lnl_models,
-    which scores them all in one pruning launch)."""
+def lnl_and_gradient(x: np.ndarray, build, lnl_many, h: float = 1e-4, central: bool = True):
+    """lnL at a hook's parameter vector x and its finite-difference gradient,
+    from one batched evaluation (lnl_many: list of models -> array of lnL,
+    e.g. likelihood.tree_lnl_models, which scores them all in one pruning
+    launch): central differences from the 2k + 1 models build(x),
+    build(x +- h e_i), or forward differences from the k + 1 models build(x),
+    build(x + h e_i)."""
     x = np.asarray(x, np.float64)
     k = len(x)
-    pts = [x] + [x + h * e for e in np.eye(k)] + [x - h * e for e in np.eye(k)]
+    pts = [x] + [x + h * e for e in np.eye(k)]
+    if central:
+        pts += [x - h * e for e in np.eye(k)]
     vals = np.asarray(lnl_many([build(p) for p in pts]), np.float64)
-    grad = (vals[1:k + 1] - vals[k + 1:]) / (2.0 * h)
+    if central:
+        grad = (vals[1:k + 1] - vals[k + 1:]) / (2.0 * h)
+    else:
+        grad = (vals[1:k + 1] - vals[0]) / h
     return float(vals[0]), grad
 
 
 def optimize_model(model: Model, lnl_of=None, hooks=("subst", "rates", "prior"), rounds: int = 8,
-                   tol: float = 1e-4, ctx: _native.Context | None = None, lnl_many=None):
+                   tol: float = 1e-4, ctx: _native.Context | None = None, lnl_many=None,
+                   central: bool = True):
     """Maximise the tree's lnL over the hooks' parameters, one hook at a time,
     until a round gains less than tol.  Returns (model, lnl, evaluations).
 
     With ``lnl_many`` (list of models -> array of lnL) every L-BFGS step takes
-    the lnL and its central-difference gradient from one batched evaluation
-    of 2k + 1 models (``lnl_and_gradient``); otherwise ``lnl_of`` (model ->
-    lnL) is called once per point, L-BFGS forming forward differences itself.
-    ``evaluations`` counts models scored."""
+    the lnL and its gradient from one batched evaluation
+    (``lnl_and_gradient``: 2k + 1 models for central differences, k + 1 with
+    ``central=False``); otherwise ``lnl_of`` (model -> lnL) is called once
+    per point, L-BFGS forming forward differences itself.  ``evaluations``
+    counts models scored."""
     from scipy.optimize import minimize
     if lnl_of is None and lnl_many is None:
         raise ValueError("optimize_model needs lnl_of or lnl_many")
@@ -482,8 +491,8 @@ def optimize_model(model: Model, lnl_of=None, hooks=("subst", "rates", "prior"),
             if lnl_many is not None:
                 def fg(x):
                     nonlocal calls
-                    calls += 2 * len(x) + 1
-                    f, g = lnl_and_gradient(x, build, lnl_many)
+                    calls += (2 if central else 1) * len(x) + 1
+                    f, g = lnl_and_gradient(x, build, lnl_many, central=central)
                     return -f, -g
 
                 res = minimize(fg, x0, jac=True, method="L-BFGS-B", options={"maxiter": 60})

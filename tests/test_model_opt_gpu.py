@@ -110,6 +110,10 @@ def test_batched_gradient_matches_oracle_differences(ctx, orc):
         f_c, g_c = M.lnl_and_gradient(x0, build, many_cpu)
         assert abs(f_g - f_c) <= 1e-9 * abs(f_c)
         assert np.abs(g_g - g_c).max() <= 1e-4 * max(1.0, np.abs(g_c).max()), name
+        # forward differences: k + 1 models in the launch
+        _, gf_g = M.lnl_and_gradient(x0, build, many_gpu, central=False)
+        _, gf_c = M.lnl_and_gradient(x0, build, many_cpu, central=False)
+        assert np.abs(gf_g - gf_c).max() <= 2e-4 * max(1.0, np.abs(gf_c).max()), name
 
 
 def test_ml_fit_with_batched_gradients(ctx, orc):
@@ -128,5 +132,8 @@ def test_ml_fit_with_batched_gradients(ctx, orc):
     fit_cpu, best_cpu, _ = M.optimize_model(start, cpu_lnl, ctx=ctx)
     assert best >= float(many_gpu([start])[0]) + 10.0
     assert abs(best - best_cpu) <= 2e-2
+    # forward-difference gradients from k + 1 batched models reach the same fit
+    _, best_f, evals_f = M.optimize_model(start, lnl_many=many_gpu, ctx=ctx, central=False)
+    assert abs(best_f - best_cpu) <= 2e-2
     np.testing.assert_allclose(fit.spec.substitution[1], fit_cpu.spec.substitution[1], rtol=2e-2)
     np.testing.assert_allclose(fit.priors, fit_cpu.priors, atol=2e-3)
