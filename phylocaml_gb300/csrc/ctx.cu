@@ -66,6 +66,15 @@ pgpu_status pgpu_check_flag(pgpu_ctx *ctx, const char *what) {
   return PGPU_OK;
 }
 
+pgpu_status pgpu_settle_copies(pgpu_ctx *ctx, pgpu_status st) {
+  if (st != PGPU_OK) {
+    for (cudaStream_t cs : {ctx->stream, ctx->copy_stream, ctx->d2h_stream})
+      if (cs) cudaStreamSynchronize(cs);
+    (void)cudaGetLastError();
+  }
+  return st;
+}
+
 pgpu_status pgpu_copy_stream(pgpu_ctx *ctx) {
   if (ctx->copy_stream) return PGPU_OK;
   PGPU_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));

@@ -1693,8 +1693,9 @@ pgpu_status pgpu_fitch_tree(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t
   if (n_words && weights)
     PGPU_CUDA(ctx, cudaMemcpyAsync(dw, weights, n_sites * 4, cudaMemcpyHostToDevice, s));
   const HostRows io{tips, node_sets};
-  PGPU_TRY(tree_dev(ctx, tree, (const uint32_t *)dt, ld, (const uint32_t *)dw, n_sites, lane_bits,
-                    (uint32_t *)dn, (uint32_t *)dsc, (uint64_t *)dtot, chunked ? &io : nullptr));
+  PGPU_TRY(pgpu_settle_copies(ctx, tree_dev(ctx, tree, (const uint32_t *)dt, ld, (const uint32_t *)dw,
+                                             n_sites, lane_bits, (uint32_t *)dn, (uint32_t *)dsc,
+                                             (uint64_t *)dtot, chunked ? &io : nullptr)));
   if (n_words) {
     if (!chunked)
       PGPU_CUDA(ctx, cudaMemcpy2DAsync(node_sets, n_words * 4, dn, ld * 4, n_words * 4, n_int,

@@ -108,6 +108,9 @@ struct pgpu_ctx {
 
 // Creates the copy streams and their events on first use.
 pgpu_status pgpu_copy_stream(pgpu_ctx *ctx);
+// A host-buffer call that fails after queueing chunk copies waits for them
+// before returning, so no copy touches the caller's buffers afterwards.
+pgpu_status pgpu_settle_copies(pgpu_ctx *ctx, pgpu_status st);
 
 // Rows of a host-buffer tree call still in host memory: the tip rows go to
 // the device buffer and the node rows come back column chunk by column

@@ -705,8 +705,9 @@ pgpu_status pgpu_prune_lnl(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_mode
   PGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev[PGPU_COPY_CHUNKS], 0));
   if (n_pat && weights)
     PGPU_CUDA(ctx, cudaMemcpyAsync(dw, weights, n_pat * 8, cudaMemcpyHostToDevice, s));
-  PGPU_TRY(prune_dev(ctx, tree, model, 1, codes, (const uint8_t *)dt, ld, (const double *)dw, n_pat,
-                     precision, (double *)dl, (double *)dsl, tip_codes));
+  PGPU_TRY(pgpu_settle_copies(ctx, prune_dev(ctx, tree, model, 1, codes, (const uint8_t *)dt, ld,
+                                              (const double *)dw, n_pat, precision, (double *)dl,
+                                              (double *)dsl, tip_codes)));
   double *hl = reinterpret_cast<double *>(ctx->h_pinned);
   PGPU_CUDA(ctx, cudaMemcpyAsync(hl, dl, 8, cudaMemcpyDeviceToHost, s));
   if (site_lnl && n_pat)

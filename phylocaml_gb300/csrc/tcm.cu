@@ -669,8 +669,9 @@ pgpu_status pgpu_tcm_tree(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *
   if (n_words && weights)
     PGPU_CUDA(ctx, cudaMemcpyAsync(dw, weights, n_sites * 4, cudaMemcpyHostToDevice, s));
   const HostRows io{tips, node_sets};
-  PGPU_TRY(tree_dev(ctx, tree, (const uint32_t *)dt, ld, (const uint32_t *)dw, n_sites, table,
-                    (uint32_t *)dn, (uint32_t *)dsc, (unsigned long long *)dtot, n_words ? &io : nullptr));
+  PGPU_TRY(pgpu_settle_copies(ctx, tree_dev(ctx, tree, (const uint32_t *)dt, ld, (const uint32_t *)dw,
+                                             n_sites, table, (uint32_t *)dn, (uint32_t *)dsc,
+                                             (unsigned long long *)dtot, n_words ? &io : nullptr)));
   if (n_words && site_cost)
     PGPU_CUDA(ctx, cudaMemcpyAsync(site_cost, dsc, n_sites * 4, cudaMemcpyDeviceToHost, s));
   uint64_t *ht = reinterpret_cast<uint64_t *>(ctx->h_pinned);
