@@ -312,48 +312,56 @@ __global__ void __launch_bounds__(256) stationary_kernel(const double *Q, int S,
 }
 
 // P[b][r] = U diag(exp(lambda * rate_r * t_b)) Ui for every branch b and
-// rate r of one model.  One CTA per branch.  Writes FP64 and, if P32 is
-// given, an FP32 copy.  t == -1 (compose only) gives Q; t < 1e-10 gives I.
+// rate r of a model.  One CTA per branch and model (blockIdx.y).  Writes
+// FP64 and, if P32 is given, an FP32 copy.  t == -1 (compose only) gives Q;
+// t < 1e-10 gives I.
 struct ComposeArgs {
-  const double *U, *lam, *Ui;   // one model
+  const double *U, *lam, *Ui;   // model 0; model m at m*S*S, m*S, m*S*S
   const double *t;              // [n_br]
-  const double *rates;          // [R] or null (rate 1)
+  const double *rates;          // [R] or null (rate 1); model m at m*R
   double *P;                    // [n_br][R][S][S] or null
   float *P32;                   // [n_br][R][S][S] or null
   int S, R;
   int n_br;
   int allow_q;                  // t == -1 returns Q (the reference's compose)
-  const int *status;            // eigendecomposition status or null
+  const int *status;            // eigendecomposition status or null; model m at m
   int *flag;
   int p32_mode;                 // P32Mode
+  size_t model_bytes;           // byte stride of P and P32 between models
 };
 
 __global__ void __launch_bounds__(256) compose_kernel(const ComposeArgs p) {
   extern __shared__ __align__(16) double sm[];
   const int S = p.S, R = p.R, SS = S * S;
   double *U = sm, *Ui = U + SS, *e = Ui + SS;   // e: [R][S]
-  const int b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
-  if (p.status && *p.status) {
-    if (b == 0 && tid == 0) atomicOr(p.flag, pgpu_model_flag(*p.status));
+  const int b = blockIdx.x, m = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
+  const int *status = p.status ? p.status + m : nullptr;
+  if (status && *status) {
+    if (b == 0 && tid == 0) atomicOr(p.flag, pgpu_model_flag(*status));
     return;
   }
+  const double *gU = p.U + (size_t)m * SS, *gUi = p.Ui + (size_t)m * SS;
+  const double *lam = p.lam + (size_t)m * S;
+  const double *rates = p.rates ? p.rates + (size_t)m * R : nullptr;
+  double *P = p.P ? (double *)((char *)p.P + m * p.model_bytes) : nullptr;
+  float *P32 = p.P32 ? (float *)((char *)p.P32 + m * p.model_bytes) : nullptr;
   for (int i = tid; i < SS; i += nt) {
-    U[i] = p.U[i];
-    Ui[i] = p.Ui[i];
+    U[i] = gU[i];
+    Ui[i] = gUi[i];
   }
   const double t = p.t[b];
   const bool q_mode = p.allow_q && t == -1.0;
   for (int i = tid; i < R * S; i += nt) {
     const int r = i / S, k = i % S;
-    const double rate = p.rates ? p.rates[r] : 1.0;
-    e[i] = q_mode ? p.lam[k] * rate : exp(p.lam[k] * rate * t);
+    const double rate = rates ? rates[r] : 1.0;
+    e[i] = q_mode ? lam[k] * rate : exp(lam[k] * rate * t);
   }
   __syncthreads();
   for (int o = tid; o < R * SS; o += nt) {
     const int r = o / SS, i = (o % SS) / S, j = o % S;
     // the identity below an effective time of 1e-10 (rate times length):
     // a rate-0 class (invariant sites) gets I exactly, not U Ui to rounding
-    const bool ident = !q_mode && !(t * (p.rates ? p.rates[r] : 1.0) >= 1e-10);
+    const bool ident = !q_mode && !(t * (rates ? rates[r] : 1.0) >= 1e-10);
     double v;
     if (ident) {
       v = (i == j) ? 1.0 : 0.0;
@@ -362,16 +370,16 @@ __global__ void __launch_bounds__(256) compose_kernel(const ComposeArgs p) {
       for (int k = 0; k < S; ++k) v = fma(U[i * S + k] * e[r * S + k], Ui[k * S + j], v);
     }
     const size_t off = ((size_t)b * R + r) * SS + (size_t)i * S + j;
-    if (p.P) p.P[off] = v;
-    if (p.P32) {
+    if (P) P[off] = v;
+    if (P32) {
       const bool minus_i = p.p32_mode == P32_MINUS_I || p.p32_mode == P32_MINUS_I_PAIRS;
       const double d = (minus_i && i == j) ? v - 1.0 : v;
       if (p.p32_mode == P32_MINUS_I_PAIRS || p.p32_mode == P32_PAIRS) {
         const float hi = (float)d;
-        p.P32[2 * off] = hi;
-        p.P32[2 * off + 1] = (float)(d - (double)hi);
+        P32[2 * off] = hi;
+        P32[2 * off + 1] = (float)(d - (double)hi);
       } else {
-        p.P32[off] = (float)d;
+        P32[off] = (float)d;
       }
     }
   }
@@ -383,22 +391,27 @@ __global__ void __launch_bounds__(256) compose_kernel(const ComposeArgs p) {
 // child then costs the pruning kernel one table read instead of a
 // matrix-vector product.
 struct TipTabArgs {
-  const double *U, *lam, *Ui;
+  const double *U, *lam, *Ui;   // model 0; model m at m*S*S, m*S, m*S*S
   const double *t;          // [n_tips] branch lengths above the tips
-  const double *rates;      // [R]
+  const double *rates;      // [R]; model m at m*R
   const double *code_tab;   // [n_codes][S]
   void *out;
   int S, R, n_codes, form;  // form: 0 float, 1 float pair, 2 double
-  const int *status;
+  const int *status;        // model m at m
+  size_t model_bytes;       // byte stride of out between models
 };
 
+// One CTA per tip, rate (blockIdx.y) and model (blockIdx.z).
 __global__ void __launch_bounds__(128) tip_table_kernel(const TipTabArgs p) {
   extern __shared__ __align__(16) double sm[];
   const int S = p.S, SS = S * S;
   double *P = sm;   // [S][S]
-  const int tip = blockIdx.x, r = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
-  if (p.status && *p.status) return;
-  const double tt = p.t[tip], rate = p.rates ? p.rates[r] : 1.0;
+  const int tip = blockIdx.x, r = blockIdx.y, m = blockIdx.z, tid = threadIdx.x, nt = blockDim.x;
+  if (p.status && p.status[m]) return;
+  const double *U = p.U + (size_t)m * SS, *Ui = p.Ui + (size_t)m * SS;
+  const double *lam = p.lam + (size_t)m * S;
+  char *out = static_cast<char *>(p.out) + m * p.model_bytes;
+  const double tt = p.t[tip], rate = p.rates ? p.rates[(size_t)m * p.R + r] : 1.0;
   const bool ident = !(tt * rate >= 1e-10);   // effective time, as in compose_kernel
   for (int o = tid; o < SS; o += nt) {
     const int i = o / S, j = o % S;
@@ -406,7 +419,7 @@ __global__ void __launch_bounds__(128) tip_table_kernel(const TipTabArgs p) {
     if (ident) {
       v = i == j ? 1.0 : 0.0;
     } else {
-      for (int k = 0; k < S; ++k) v = fma(p.U[i * S + k] * exp(p.lam[k] * rate * tt), p.Ui[k * S + j], v);
+      for (int k = 0; k < S; ++k) v = fma(U[i * S + k] * exp(lam[k] * rate * tt), Ui[k * S + j], v);
     }
     P[o] = v;
   }
@@ -418,13 +431,13 @@ __global__ void __launch_bounds__(128) tip_table_kernel(const TipTabArgs p) {
     for (int j = 0; j < S; ++j) v = fma(P[i * S + j], p.code_tab[c * S + j], v);
     const size_t at = base + o;
     if (p.form == 0) {
-      static_cast<float *>(p.out)[at] = (float)v;
+      reinterpret_cast<float *>(out)[at] = (float)v;
     } else if (p.form == 1) {
       const float hi = (float)v;
-      static_cast<float *>(p.out)[2 * at] = hi;
-      static_cast<float *>(p.out)[2 * at + 1] = (float)(v - (double)hi);
+      reinterpret_cast<float *>(out)[2 * at] = hi;
+      reinterpret_cast<float *>(out)[2 * at + 1] = (float)(v - (double)hi);
     } else {
-      static_cast<double *>(p.out)[at] = v;
+      reinterpret_cast<double *>(out)[at] = v;
     }
   }
 }
@@ -452,30 +465,38 @@ pgpu_status pgpu_launch_eig(pgpu_ctx *ctx, const double *Q_dev, const double *pi
 pgpu_status pgpu_launch_compose(pgpu_ctx *ctx, const double *U_dev, const double *lam_dev,
                                 const double *Ui_dev, int S, const double *t_dev, int n_br,
                                 const double *rates_dev, int R, double *P_dev, float *P32_dev,
-                                bool allow_q, const int *status_dev, int p32_mode) {
-  if (n_br <= 0) return PGPU_OK;
+                                bool allow_q, const int *status_dev, int p32_mode, int n_models,
+                                size_t model_bytes) {
+  if (n_br <= 0 || n_models <= 0) return PGPU_OK;
+  if (n_models > 65535)
+    return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "compose: %d models in one launch; at most 65535",
+                        n_models);
   ComposeArgs a{U_dev, lam_dev, Ui_dev, t_dev,       rates_dev,  P_dev,       P32_dev,
                 S,     R,       n_br,   allow_q ? 1 : 0, status_dev, ctx->d_flag,
-                p32_mode};
+                p32_mode, model_bytes};
   const size_t smem = sizeof(double) * (2 * (size_t)S * S + (size_t)R * S);
   PGPU_CUDA(ctx, cudaFuncSetAttribute(compose_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)std::max<size_t>(smem, 1024)));
   const int threads = R * S * S <= 64 ? 64 : (R * S * S <= 128 ? 128 : 256);
-  compose_kernel<<<n_br, threads, smem, ctx->stream>>>(a);
+  compose_kernel<<<dim3(n_br, n_models), threads, smem, ctx->stream>>>(a);
   return pgpu_after_launch(ctx, "compose_kernel");
 }
 
 pgpu_status pgpu_launch_tip_table(pgpu_ctx *ctx, const double *U_dev, const double *lam_dev,
                                   const double *Ui_dev, int S, const double *t_dev, int n_tips,
                                   const double *rates_dev, int R, const double *code_tab_dev,
-                                  int n_codes, void *out_dev, int form, const int *status_dev) {
-  if (n_tips <= 0) return PGPU_OK;
+                                  int n_codes, void *out_dev, int form, const int *status_dev,
+                                  int n_models, size_t model_bytes) {
+  if (n_tips <= 0 || n_models <= 0) return PGPU_OK;
+  if (n_models > 65535)
+    return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "tip table: %d models in one launch; at most 65535",
+                        n_models);
   TipTabArgs a{U_dev, lam_dev, Ui_dev, t_dev, rates_dev, code_tab_dev, out_dev, S, R, n_codes, form,
-               status_dev};
+               status_dev, model_bytes};
   const size_t smem = sizeof(double) * (size_t)S * S;
   PGPU_CUDA(ctx, cudaFuncSetAttribute(tip_table_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)std::max<size_t>(smem, 1024)));
-  tip_table_kernel<<<dim3(n_tips, R), 128, smem, ctx->stream>>>(a);
+  tip_table_kernel<<<dim3(n_tips, R, n_models), 128, smem, ctx->stream>>>(a);
   return pgpu_after_launch(ctx, "tip_table_kernel");
 }
 

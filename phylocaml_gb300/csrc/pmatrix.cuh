@@ -15,7 +15,10 @@ pgpu_status pgpu_launch_eig(pgpu_ctx *ctx, const double *Q_dev, const double *pi
 // context's error word records the model failure.  p32_mode selects the FP32
 // copy: P, P - I (formed in FP64 before rounding, which keeps the small
 // entries of short branches at full relative precision), or P - I as
-// (hi, lo) float pairs.
+// (hi, lo) float pairs.  n_models > 1 composes that many models in one
+// launch: model m reads U, Ui at m*S*S, lam at m*S, rates at m*R and
+// status_dev[m], and writes its matrices model_bytes further on than model
+// m - 1's (the same byte stride for P_dev and P32_dev).
 enum P32Mode {
   P32_PLAIN = 0,          // fl32(P)
   P32_MINUS_I = 1,        // fl32(P - I)
@@ -26,12 +29,15 @@ pgpu_status pgpu_launch_compose(pgpu_ctx *ctx, const double *U_dev, const double
                                 const double *Ui_dev, int S, const double *t_dev, int n_br,
                                 const double *rates_dev, int R, double *P_dev, float *P32_dev,
                                 bool allow_q, const int *status_dev = nullptr,
-                                int p32_mode = P32_PLAIN);
+                                int p32_mode = P32_PLAIN, int n_models = 1,
+                                size_t model_bytes = 0);
 
 // Tip rows tab[t][r][c][i] = (P(t, r) code_tab[c])[i] for the n_tips branches
 // above the tips (t_dev holds their lengths), in FP64, stored as float
-// (form 0), (hi, lo) float pairs (form 1) or double (form 2).
+// (form 0), (hi, lo) float pairs (form 1) or double (form 2).  n_models
+// and model_bytes batch models as in pgpu_launch_compose.
 pgpu_status pgpu_launch_tip_table(pgpu_ctx *ctx, const double *U_dev, const double *lam_dev,
                                   const double *Ui_dev, int S, const double *t_dev, int n_tips,
                                   const double *rates_dev, int R, const double *code_tab_dev,
-                                  int n_codes, void *out_dev, int form, const int *status_dev);
+                                  int n_codes, void *out_dev, int form, const int *status_dev,
+                                  int n_models = 1, size_t model_bytes = 0);

@@ -578,21 +578,17 @@ pgpu_status prune_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *mo
   double *dU = (double *)deig, *dUi = dU + V * SS, *dlam = dUi + V * SS;
   int *dst = reinterpret_cast<int *>(dlam + (size_t)V * S);
   PGPU_TRY(pgpu_launch_eig(ctx, rebase(d, lay.Q), rebase(d, lay.pi), S, V, dU, dlam, dUi, dst));
-  for (int v = 0; v < V; ++v) {
-    char *Pv = static_cast<char *>(dP) + (size_t)v * p_bytes;
-    PGPU_TRY(pgpu_launch_compose(ctx, dU + v * SS, dlam + (size_t)v * S, dUi + v * SS, S,
-                                 rebase(d, lay.brlen), n_br, rebase(d, lay.rates) + (size_t)v * R, R,
-                                 precision == 64 ? (double *)Pv : nullptr,
-                                 precision == 64 ? nullptr : (float *)Pv, false, dst + v,
-                                 precision == 32 ? P32_MINUS_I : precision == 48 ? P32_PAIRS
-                                                                                 : P32_PLAIN));
-    // tip rows in FP64, stored in the form's value type
-    PGPU_TRY(pgpu_launch_tip_table(ctx, dU + v * SS, dlam + (size_t)v * S, dUi + v * SS, S,
-                                   rebase(d, lay.brlen), n, rebase(d, lay.rates) + (size_t)v * R, R,
-                                   rebase(d, lay.tab), codes->n_codes,
-                                   static_cast<char *>(dtt) + (size_t)v * tt_bytes,
-                                   precision == 32 ? 0 : precision == 48 ? 1 : 2, dst + v));
-  }
+  // every model's P matrices, then every model's tip rows in FP64, stored in
+  // the form's value type: one launch each for all V models
+  PGPU_TRY(pgpu_launch_compose(ctx, dU, dlam, dUi, S, rebase(d, lay.brlen), n_br,
+                               rebase(d, lay.rates), R, precision == 64 ? (double *)dP : nullptr,
+                               precision == 64 ? nullptr : (float *)dP, false, dst,
+                               precision == 32 ? P32_MINUS_I : precision == 48 ? P32_PAIRS
+                                                                               : P32_PLAIN,
+                               V, p_bytes));
+  PGPU_TRY(pgpu_launch_tip_table(ctx, dU, dlam, dUi, S, rebase(d, lay.brlen), n,
+                                 rebase(d, lay.rates), R, rebase(d, lay.tab), codes->n_codes, dtt,
+                                 precision == 32 ? 0 : precision == 48 ? 1 : 2, dst, V, tt_bytes));
   if (n_pat == 0) {
     PGPU_CUDA(ctx, cudaMemsetAsync(lnl_dev, 0, (size_t)V * sizeof(double), ctx->stream));
     return PGPU_OK;
