@@ -396,12 +396,34 @@ pgpu_status copy_chunk(pgpu_ctx *ctx, const HostTips &ht, const PruneArgs &a, si
   return PGPU_OK;
 }
 
+// Column chunks for tip codes in host memory: the first chunk is one wave
+// of CTAs (the one copy the scoring cannot hide), each next one twice the
+// last, so a chunk's copy ends while the chunk before it is scored; whole
+// waves keep every launch but the last free of a part-filled wave.
 template <typename Pol, int RT>
 pgpu_status launch_prune_chunks(pgpu_ctx *ctx, PruneArgs &a, size_t n_tiles, size_t smem, int n_models,
                                 const HostTips *ht) {
-  const int K = ht ? (int)std::min<size_t>(PGPU_COPY_CHUNKS, n_tiles) : 1;
+  size_t bounds[PGPU_COPY_CHUNKS + 1] = {0};
+  int K = 0;
+  if (ht) {
+    PGPU_CUDA(ctx, cudaFuncSetAttribute(prune_tree_kernel<Pol, RT>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)std::max<size_t>(smem, 48 * 1024)));
+    int per_sm = 0;
+    PGPU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, prune_tree_kernel<Pol, RT>,
+                                                                 32 + PR_THREADS, smem));
+    const size_t wave =
+        std::max<size_t>((size_t)std::max(per_sm, 1) * (size_t)ctx->num_sms / (size_t)std::max(n_models, 1), 1);
+    size_t t = 0, c = wave;
+    while (K < PGPU_COPY_CHUNKS - 1 && n_tiles - t >= c + wave) {
+      t += c;
+      bounds[++K] = t;
+      c *= 2;
+    }
+  }
+  bounds[++K] = n_tiles;
   for (int k = 0; k < K; ++k) {
-    const size_t t0 = n_tiles * k / K, t1 = n_tiles * (k + 1) / K;
+    const size_t t0 = bounds[k], t1 = bounds[k + 1];
     if (ht) PGPU_TRY(copy_chunk(ctx, *ht, a, t0 * a.NP, std::min(t1 * a.NP, a.n_pat), k));
     a.tile_base = t0;
     PGPU_TRY((launch_prune_rt<Pol, RT>(ctx, a, t1 - t0, smem, n_models)));
