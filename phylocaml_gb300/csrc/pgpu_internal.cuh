@@ -64,7 +64,8 @@ struct SplitSchedule {
   std::vector<int4> top;       // {k, ref_a, ref_b, 0} in postorder
 };
 
-// column chunks of the host-buffer pruning call's tip-code copy
+// column chunks (at most) of the host-buffer calls' copies: 2-D copies of
+// narrower columns overlap each other worse
 constexpr int PGPU_COPY_CHUNKS = 4;
 
 struct pgpu_ctx {

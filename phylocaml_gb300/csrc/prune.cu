@@ -387,66 +387,92 @@ struct HostTips {
   size_t n_tips;
 };
 
-pgpu_status copy_chunk(pgpu_ctx *ctx, const HostTips &ht, const PruneArgs &a, size_t c0, size_t c1, int k) {
-  if (c1 > c0)
-    PGPU_CUDA(ctx, cudaMemcpy2DAsync(ht.dev + c0, a.ld_pat, ht.host + c0, a.n_pat, c1 - c0, ht.n_tips,
-                                     cudaMemcpyHostToDevice, ctx->copy_stream));
-  PGPU_CUDA(ctx, cudaEventRecord(ctx->copy_ev[k], ctx->copy_stream));
-  PGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[k], 0));
-  return PGPU_OK;
-}
+// The launches of one scoring: tile ranges [bounds[k], bounds[k + 1]).
+struct ChunkPlan {
+  size_t bounds[PGPU_COPY_CHUNKS + 1];
+  int K;
+  size_t smem;
+};
 
 // Column chunks for tip codes in host memory: the first chunk is one wave
 // of CTAs (the one copy the scoring cannot hide), each next one twice the
 // last, so a chunk's copy ends while the chunk before it is scored; whole
-// waves keep every launch but the last free of a part-filled wave.
+// waves keep every launch but the last free of a part-filled wave.  Tip
+// codes already on the device: one launch.
 template <typename Pol, int RT>
-pgpu_status launch_prune_chunks(pgpu_ctx *ctx, PruneArgs &a, size_t n_tiles, size_t smem, int n_models,
-                                const HostTips *ht) {
-  size_t bounds[PGPU_COPY_CHUNKS + 1] = {0};
-  int K = 0;
-  if (ht) {
+pgpu_status plan_chunks_rt(pgpu_ctx *ctx, size_t n_tiles, int n_models, bool host, ChunkPlan &pl) {
+  pl.K = 0;
+  pl.bounds[0] = 0;
+  if (host) {
     PGPU_CUDA(ctx, cudaFuncSetAttribute(prune_tree_kernel<Pol, RT>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)std::max<size_t>(smem, 48 * 1024)));
+                                        (int)std::max<size_t>(pl.smem, 48 * 1024)));
     int per_sm = 0;
     PGPU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, prune_tree_kernel<Pol, RT>,
-                                                                 32 + PR_THREADS, smem));
+                                                                 32 + PR_THREADS, pl.smem));
     const size_t wave =
         std::max<size_t>((size_t)std::max(per_sm, 1) * (size_t)ctx->num_sms / (size_t)std::max(n_models, 1), 1);
     size_t t = 0, c = wave;
-    while (K < PGPU_COPY_CHUNKS - 1 && n_tiles - t >= c + wave) {
+    while (pl.K < PGPU_COPY_CHUNKS - 1 && n_tiles - t >= c + wave) {
       t += c;
-      bounds[++K] = t;
+      pl.bounds[++pl.K] = t;
       c *= 2;
     }
   }
-  bounds[++K] = n_tiles;
-  for (int k = 0; k < K; ++k) {
-    const size_t t0 = bounds[k], t1 = bounds[k + 1];
-    if (ht) PGPU_TRY(copy_chunk(ctx, *ht, a, t0 * a.NP, std::min(t1 * a.NP, a.n_pat), k));
-    a.tile_base = t0;
-    PGPU_TRY((launch_prune_rt<Pol, RT>(ctx, a, t1 - t0, smem, n_models)));
+  pl.bounds[++pl.K] = n_tiles;
+  return PGPU_OK;
+}
+
+// Sets a's tiling and plans its launches.  With the tip codes in host
+// memory it also queues every chunk's copy on the copy stream, chunk k's
+// end marked by copy_ev[k], so that the first copy runs beside the model
+// setup kernels queued after it.
+template <typename Pol>
+pgpu_status plan_prune(pgpu_ctx *ctx, PruneArgs &a, int RT, int n_models, const HostTips *ht, ChunkPlan &pl) {
+  a.NP = PR_THREADS / RT;
+  const size_t n_tiles = (a.n_pat + a.NP - 1) / a.NP;
+  a.n_tiles_total = n_tiles;
+  a.tile_base = 0;
+  pl.smem = PruneLayout<Pol>::bytes(a.NP, a.R, a.n_codes, a.depth);
+  if (pl.smem > ctx->smem_optin)
+    return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "prune: %zu bytes of shared memory needed (tree too deep)",
+                        pl.smem);
+  const bool host = ht != nullptr;
+  switch (RT) {
+    case 1: PGPU_TRY((plan_chunks_rt<Pol, 1>(ctx, n_tiles, n_models, host, pl))); break;
+    case 2: PGPU_TRY((plan_chunks_rt<Pol, 2>(ctx, n_tiles, n_models, host, pl))); break;
+    case 4: PGPU_TRY((plan_chunks_rt<Pol, 4>(ctx, n_tiles, n_models, host, pl))); break;
+    default: PGPU_TRY((plan_chunks_rt<Pol, 8>(ctx, n_tiles, n_models, host, pl))); break;
+  }
+  if (host)
+    for (int k = 0; k < pl.K; ++k) {
+      const size_t c0 = pl.bounds[k] * a.NP, c1 = std::min(pl.bounds[k + 1] * a.NP, a.n_pat);
+      if (c1 > c0)
+        PGPU_CUDA(ctx, cudaMemcpy2DAsync(ht->dev + c0, a.ld_pat, ht->host + c0, a.n_pat, c1 - c0, ht->n_tips,
+                                         cudaMemcpyHostToDevice, ctx->copy_stream));
+      PGPU_CUDA(ctx, cudaEventRecord(ctx->copy_ev[k], ctx->copy_stream));
+    }
+  return PGPU_OK;
+}
+
+template <typename Pol, int RT>
+pgpu_status launch_prune_chunks(pgpu_ctx *ctx, PruneArgs &a, const ChunkPlan &pl, int n_models, bool host) {
+  for (int k = 0; k < pl.K; ++k) {
+    if (host) PGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[k], 0));
+    a.tile_base = pl.bounds[k];
+    PGPU_TRY((launch_prune_rt<Pol, RT>(ctx, a, pl.bounds[k + 1] - pl.bounds[k], pl.smem, n_models)));
   }
   a.tile_base = 0;
   return PGPU_OK;
 }
 
 template <typename Pol>
-pgpu_status launch_prune(pgpu_ctx *ctx, PruneArgs &a, int RT, int n_models, const HostTips *ht) {
-  a.NP = PR_THREADS / RT;
-  const size_t n_tiles = (a.n_pat + a.NP - 1) / a.NP;
-  a.n_tiles_total = n_tiles;
-  a.tile_base = 0;
-  const size_t smem = PruneLayout<Pol>::bytes(a.NP, a.R, a.n_codes, a.depth);
-  if (smem > ctx->smem_optin)
-    return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "prune: %zu bytes of shared memory needed (tree too deep)",
-                        smem);
+pgpu_status launch_prune(pgpu_ctx *ctx, PruneArgs &a, int RT, int n_models, const ChunkPlan &pl, bool host) {
   switch (RT) {
-    case 1: return launch_prune_chunks<Pol, 1>(ctx, a, n_tiles, smem, n_models, ht);
-    case 2: return launch_prune_chunks<Pol, 2>(ctx, a, n_tiles, smem, n_models, ht);
-    case 4: return launch_prune_chunks<Pol, 4>(ctx, a, n_tiles, smem, n_models, ht);
-    default: return launch_prune_chunks<Pol, 8>(ctx, a, n_tiles, smem, n_models, ht);
+    case 1: return launch_prune_chunks<Pol, 1>(ctx, a, pl, n_models, host);
+    case 2: return launch_prune_chunks<Pol, 2>(ctx, a, pl, n_models, host);
+    case 4: return launch_prune_chunks<Pol, 4>(ctx, a, pl, n_models, host);
+    default: return launch_prune_chunks<Pol, 8>(ctx, a, pl, n_models, host);
   }
 }
 
@@ -599,22 +625,6 @@ pgpu_status prune_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *mo
   PGPU_TRY(pgpu_buf(ctx, BUF_J, (size_t)V * tt_bytes, &dtt));
   double *dU = (double *)deig, *dUi = dU + V * SS, *dlam = dUi + V * SS;
   int *dst = reinterpret_cast<int *>(dlam + (size_t)V * S);
-  PGPU_TRY(pgpu_launch_eig(ctx, rebase(d, lay.Q), rebase(d, lay.pi), S, V, dU, dlam, dUi, dst));
-  // every model's P matrices, then every model's tip rows in FP64, stored in
-  // the form's value type: one launch each for all V models
-  PGPU_TRY(pgpu_launch_compose(ctx, dU, dlam, dUi, S, rebase(d, lay.brlen), n_br,
-                               rebase(d, lay.rates), R, precision == 64 ? (double *)dP : nullptr,
-                               precision == 64 ? nullptr : (float *)dP, false, dst,
-                               precision == 32 ? P32_MINUS_I : precision == 48 ? P32_PAIRS
-                                                                               : P32_PLAIN,
-                               V, p_bytes));
-  PGPU_TRY(pgpu_launch_tip_table(ctx, dU, dlam, dUi, S, rebase(d, lay.brlen), n,
-                                 rebase(d, lay.rates), R, rebase(d, lay.tab), codes->n_codes, dtt,
-                                 precision == 32 ? 0 : precision == 48 ? 1 : 2, dst, V, tt_bytes));
-  if (n_pat == 0) {
-    PGPU_CUDA(ctx, cudaMemsetAsync(lnl_dev, 0, (size_t)V * sizeof(double), ctx->stream));
-    return PGPU_OK;
-  }
   PruneArgs a;
   a.tiptab = dtt;
   a.tip_codes = tips;
@@ -640,9 +650,31 @@ pgpu_status prune_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *mo
   a.depth = std::max(sch->max_depth, 1);
   HostTips ht{host_tips, const_cast<uint8_t *>(tips), (size_t)n};
   const HostTips *htp = host_tips ? &ht : nullptr;
-  if (precision == 32) PGPU_TRY(launch_prune<Fp32>(ctx, a, RT, V, htp));
-  else if (precision == 48) PGPU_TRY(launch_prune<Ff32>(ctx, a, RT, V, htp));
-  else PGPU_TRY(launch_prune<Fp64>(ctx, a, RT, V, htp));
+  ChunkPlan pl;
+  if (n_pat > 0) {
+    if (precision == 32) PGPU_TRY(plan_prune<Fp32>(ctx, a, RT, V, htp, pl));
+    else if (precision == 48) PGPU_TRY(plan_prune<Ff32>(ctx, a, RT, V, htp, pl));
+    else PGPU_TRY(plan_prune<Fp64>(ctx, a, RT, V, htp, pl));
+  }
+  PGPU_TRY(pgpu_launch_eig(ctx, rebase(d, lay.Q), rebase(d, lay.pi), S, V, dU, dlam, dUi, dst));
+  // every model's P matrices, then every model's tip rows in FP64, stored in
+  // the form's value type: one launch each for all V models
+  PGPU_TRY(pgpu_launch_compose(ctx, dU, dlam, dUi, S, rebase(d, lay.brlen), n_br,
+                               rebase(d, lay.rates), R, precision == 64 ? (double *)dP : nullptr,
+                               precision == 64 ? nullptr : (float *)dP, false, dst,
+                               precision == 32 ? P32_MINUS_I : precision == 48 ? P32_PAIRS
+                                                                               : P32_PLAIN,
+                               V, p_bytes));
+  PGPU_TRY(pgpu_launch_tip_table(ctx, dU, dlam, dUi, S, rebase(d, lay.brlen), n,
+                                 rebase(d, lay.rates), R, rebase(d, lay.tab), codes->n_codes, dtt,
+                                 precision == 32 ? 0 : precision == 48 ? 1 : 2, dst, V, tt_bytes));
+  if (n_pat == 0) {
+    PGPU_CUDA(ctx, cudaMemsetAsync(lnl_dev, 0, (size_t)V * sizeof(double), ctx->stream));
+    return PGPU_OK;
+  }
+  if (precision == 32) PGPU_TRY(launch_prune<Fp32>(ctx, a, RT, V, pl, htp != nullptr));
+  else if (precision == 48) PGPU_TRY(launch_prune<Ff32>(ctx, a, RT, V, pl, htp != nullptr));
+  else PGPU_TRY(launch_prune<Fp64>(ctx, a, RT, V, pl, htp != nullptr));
   prune_finalize_kernel<<<V, 1024, 0, ctx->stream>>>((const double2 *)dpart, (int)n_tiles, lnl_dev);
   return pgpu_after_launch(ctx, "prune_finalize_kernel");
 }
@@ -721,8 +753,9 @@ pgpu_status pgpu_prune_lnl(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_mode
   PGPU_TRY(pgpu_copy_stream(ctx));
   PGPU_CUDA(ctx, cudaEventRecord(ctx->copy_ev[PGPU_COPY_CHUNKS], s));
   PGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev[PGPU_COPY_CHUNKS], 0));
+  // the weights go first on the copy stream: the first chunk's event covers them
   if (n_pat && weights)
-    PGPU_CUDA(ctx, cudaMemcpyAsync(dw, weights, n_pat * 8, cudaMemcpyHostToDevice, s));
+    PGPU_CUDA(ctx, cudaMemcpyAsync(dw, weights, n_pat * 8, cudaMemcpyHostToDevice, ctx->copy_stream));
   PGPU_TRY(pgpu_settle_copies(ctx, prune_dev(ctx, tree, model, 1, codes, (const uint8_t *)dt, ld,
                                               (const double *)dw, n_pat, precision, (double *)dl,
                                               (double *)dsl, tip_codes)));
