@@ -153,10 +153,15 @@ pgpu_status pgpu_fitch_distance(pgpu_ctx *ctx, const uint32_t *a, const uint32_t
  *   total      out: sum_s weights[s] * site_cost[s] (a per-site count is at
  *              most n_tips-1, so it always fits uint32; the total is exact
  *              while it stays below 2^64)
- * Below 64-bit lanes the rows are copied in column chunks on two further
- * streams of the context, so the copies in and out overlap each other and
- * the kernels (pinned host memory lets them run asynchronously); the call
- * returns once every output is written. */
+ * Below 64-bit lanes, when tips and node_sets both lie in page-locked host
+ * memory the device can address (cudaMallocHost, cudaHostAlloc,
+ * cudaHostRegister), start on 16-byte boundaries and n_words is a multiple
+ * of 4, the kernel reads the tips and writes the node sets in host memory
+ * itself over the CPU-GPU link, both directions at once.  Otherwise the
+ * rows are copied in column chunks on two further streams of the context,
+ * so the copies in and out overlap each other and the kernels (pinned host
+ * memory lets them run asynchronously).  The call returns once every
+ * output is written. */
 pgpu_status pgpu_fitch_tree(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
                             const uint32_t *weights, size_t n_sites, int lane_bits,
                             uint32_t *node_sets, uint32_t *site_cost, uint64_t *total);
@@ -235,8 +240,8 @@ pgpu_status pgpu_tcm_tables(pgpu_ctx *ctx, const int32_t *tcm, int n_states, int
  * pgpu_fitch_tree with lane_bits 4; node_sets, site_cost and total as
  * there, site_cost[s] the sum of the costs over the internal nodes (the
  * call fails with PGPU_ERR_OVERFLOW if that could exceed 2^32 - 1).  A code
- * without a median in a site returns PGPU_ERR_ARG.  The rows are copied as
- * for pgpu_fitch_tree (column chunks overlapping the kernels). */
+ * without a median in a site returns PGPU_ERR_ARG.  The rows are read and
+ * written in page-locked host memory, or copied, as for pgpu_fitch_tree. */
 pgpu_status pgpu_tcm_tree(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *tips,
                           const uint32_t *weights, size_t n_sites, const uint32_t *table,
                           uint32_t *node_sets, uint32_t *site_cost, uint64_t *total);

@@ -75,6 +75,16 @@ pgpu_status pgpu_settle_copies(pgpu_ctx *ctx, pgpu_status st) {
   return st;
 }
 
+void *pgpu_host_view(const void *p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 pgpu_status pgpu_copy_stream(pgpu_ctx *ctx) {
   if (ctx->copy_stream) return PGPU_OK;
   PGPU_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));

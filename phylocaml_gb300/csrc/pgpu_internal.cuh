@@ -112,6 +112,11 @@ pgpu_status pgpu_copy_stream(pgpu_ctx *ctx);
 // A host-buffer call that fails after queueing chunk copies waits for them
 // before returning, so no copy touches the caller's buffers afterwards.
 pgpu_status pgpu_settle_copies(pgpu_ctx *ctx, pgpu_status st);
+// The device's address of p when p lies in page-locked host memory the
+// device can reach (cudaMallocHost, cudaHostAlloc, cudaHostRegister), else
+// null: kernels may then read and write the caller's buffer over the
+// CPU-GPU link directly.
+void *pgpu_host_view(const void *p);
 
 // Rows of a host-buffer tree call still in host memory: the tip rows go to
 // the device buffer and the node rows come back column chunk by column

@@ -652,13 +652,37 @@ pgpu_status pgpu_tcm_tree(pgpu_ctx *ctx, const pgpu_tree *tree, const uint32_t *
   const size_t n_words = (n_sites + 7) / 8;
   const size_t ld = (n_words + 3) / 4 * 4;
   const size_t n = (size_t)tree->n_tips, n_int = n - 1;
-  void *dt, *dn, *dw = nullptr, *dsc = nullptr, *dtot;
-  PGPU_TRY(pgpu_buf(ctx, BUF_TIPS, n * ld * 4, &dt));
-  PGPU_TRY(pgpu_buf(ctx, BUF_OUT, n_int * ld * 4, &dn));
+  void *dw = nullptr, *dsc = nullptr, *dtot;
   PGPU_TRY(pgpu_buf(ctx, BUF_SCALAR, 64, &dtot));
   if (weights) PGPU_TRY(pgpu_buf(ctx, BUF_WEIGHTS, n_sites * 4, &dw));
   if (site_cost) PGPU_TRY(pgpu_buf(ctx, BUF_SITECOST, n_sites * 4, &dsc));
   cudaStream_t s = ctx->stream;
+  // rows in page-locked host memory the device can address, 16-byte aligned
+  // and a multiple of 4 words long: read and written by the kernel over the
+  // CPU-GPU link, with no staging buffers
+  const uint32_t *tv = nullptr;
+  uint32_t *nv = nullptr;
+  if (n_words > 0 && n_words % 4 == 0) {
+    tv = static_cast<const uint32_t *>(pgpu_host_view(tips));
+    nv = static_cast<uint32_t *>(pgpu_host_view(node_sets));
+    if (((uintptr_t)tv | (uintptr_t)nv) & 15) tv = nullptr;
+  }
+  if (tv && nv) {
+    if (weights) PGPU_CUDA(ctx, cudaMemcpyAsync(dw, weights, n_sites * 4, cudaMemcpyHostToDevice, s));
+    PGPU_TRY(pgpu_settle_copies(ctx, tree_dev(ctx, tree, tv, n_words, (const uint32_t *)dw, n_sites, table,
+                                               nv, (uint32_t *)dsc, (unsigned long long *)dtot)));
+    if (site_cost)
+      PGPU_CUDA(ctx, cudaMemcpyAsync(site_cost, dsc, n_sites * 4, cudaMemcpyDeviceToHost, s));
+    uint64_t *ht = reinterpret_cast<uint64_t *>(ctx->h_pinned);
+    PGPU_CUDA(ctx, cudaMemcpyAsync(ht, dtot, 8, cudaMemcpyDeviceToHost, s));
+    PGPU_CUDA(ctx, cudaStreamSynchronize(s));
+    PGPU_TRY(pgpu_check_flag(ctx, "tcm_tree"));
+    *total = *ht;
+    return PGPU_OK;
+  }
+  void *dt, *dn;
+  PGPU_TRY(pgpu_buf(ctx, BUF_TIPS, n * ld * 4, &dt));
+  PGPU_TRY(pgpu_buf(ctx, BUF_OUT, n_int * ld * 4, &dn));
   // the rows go over in column chunks on the copy streams (or whole, where
   // the single-walk kernel runs), after everything already queued on the
   // context's stream

@@ -207,6 +207,46 @@ def test_tree_device_api_matches_host_api(ctx):
     assert int(tot.item()) == host.total
 
 
+def _pinned(a: np.ndarray) -> np.ndarray:
+    """A page-locked copy of a (uint32 or uint8) host array."""
+    import torch
+    t = torch.from_numpy(a.view(np.int32) if a.dtype == np.uint32 else a).pin_memory()
+    v = t.numpy()
+    return v.view(a.dtype)
+
+
+@pytest.mark.parametrize("lb,n_sites,pin_out", [(4, 64_000, True), (8, 40_000, True), (16, 20_000, True),
+                                                (32, 8_000, True), (4, 64_008, True), (4, 64_000, False)])
+def test_tree_pinned_host_buffers(ctx, lb, n_sites, pin_out):
+    """pgpu_fitch_tree on page-locked host rows: with rows a multiple of 4
+    words the kernel reads the tips and writes the node sets in host memory
+    itself; other row lengths, or a pageable output, take the staged copies.
+    Both equal the call on pageable buffers bit for bit."""
+    import ctypes as C
+    from phylocaml_gb300 import _native, fitch
+    rng = np.random.default_rng(lb * 1000 + n_sites)
+    tr = T.yule(300, rng, 0.1)
+    top = 1 << min(lb, 8)
+    tips = rng.integers(1, top, (tr.n_tips, n_sites)).astype(np.uint32)
+    w = rng.integers(1, 9, n_sites).astype(np.uint32)
+    words = synth.pack_lanes(tips, lb)
+    ref = fitch.fitch_tree(tr, words, n_sites, lb, w, ctx=ctx)
+    nw = words.shape[1]
+    p_tips, p_w = _pinned(words), _pinned(w)
+    out = _pinned(np.zeros((tr.n_internal, nw), np.uint32)) if pin_out else np.zeros((tr.n_internal, nw),
+                                                                                     np.uint32)
+    sc = _pinned(np.zeros(n_sites, np.uint32))
+    out[:] = 0xDEADBEEF
+    total = C.c_uint64(0)
+    t, keep = _native.make_tree(tr.left, tr.right)
+    ctx.call("pgpu_fitch_tree", C.byref(t), p_tips.ctypes.data, p_w.ctypes.data, n_sites, lb,
+             out.ctypes.data, sc.ctypes.data, C.byref(total))
+    del keep
+    assert np.array_equal(out, ref.node_sets)
+    assert np.array_equal(sc, ref.site_cost)
+    assert total.value == ref.total
+
+
 def test_tree_full_size_config(ctx, orc):
     """The large Fitch workload (1,024 taxa x 1e6 sites, 4-bit lanes, 3%
     ambiguity, weights 1..8) against the restated bv_fitch on one byte per

@@ -172,12 +172,17 @@ def test_edge_cases(ctx):
         Lk.tree_lnl(bad, m, codes, synth.dna_code_table(), None, 32, ctx)
 
 
-def test_device_api_matches_host_api(ctx):
+@pytest.mark.parametrize("n_taxa,n_sites,prec", [(40, 20000, 32), (24, 200_000, 32), (24, 200_000, 48),
+                                                  (24, 200_000, 64)])
+def test_device_api_matches_host_api(ctx, n_taxa, n_sites, prec):
+    """The host-buffer call (tip codes copied in column chunks, one launch
+    per chunk: several chunks at 200,000 sites) equals the device-pointer
+    call (one launch) bit for bit, per pattern and in total."""
     import torch
     from phylocaml_gb300 import likelihood as Lk
-    tr, spec, pats, w = synth.prune_workload(40, 20000, seed=3)
+    tr, spec, pats, w = synth.prune_workload(n_taxa, n_sites, seed=3)
     m = M.create(spec, ctx)
-    host = Lk.tree_lnl(tr, m, pats, synth.dna_code_table(), w, 32, ctx)
+    host, host_site = Lk.tree_lnl(tr, m, pats, synth.dna_code_table(), w, prec, ctx, site_lnl=True)
     n_pat = pats.shape[1]
     ld = (n_pat + 15) // 16 * 16
     dev = torch.device("cuda:0")
@@ -185,15 +190,18 @@ def test_device_api_matches_host_api(ctx):
     tips[:, :n_pat] = torch.from_numpy(pats).to(dev)
     wd = torch.from_numpy(w).to(dev)
     out = torch.zeros(1, dtype=torch.float64, device=dev)
+    site = torch.zeros(n_pat, dtype=torch.float64, device=dev)
     stream = torch.cuda.Stream(dev)
     torch.cuda.synchronize(dev)
     ctx.set_stream(stream.cuda_stream)
     try:
-        Lk.tree_lnl_dev(tr, m, tips, ld, n_pat, synth.dna_code_table(), wd, out, 32, ctx=ctx)
+        Lk.tree_lnl_dev(tr, m, tips, ld, n_pat, synth.dna_code_table(), wd, out, prec, site_lnl_dev=site,
+                        ctx=ctx)
         ctx.synchronize()
     finally:
         ctx.set_stream(None)
     assert float(out.item()) == host
+    assert np.array_equal(site.cpu().numpy(), host_site)
 
 
 def test_full_size_precision_config(ctx, orc):

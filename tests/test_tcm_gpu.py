@@ -181,6 +181,44 @@ def test_device_pointer_form(ctx):
     assert np.array_equal(sc.cpu().numpy().view(np.uint32), host.site_cost)
 
 
+@pytest.mark.parametrize("n_sites,pin_out", [(64_000, True), (64_008, True), (64_000, False)])
+def test_pinned_host_buffers(ctx, n_sites, pin_out):
+    """pgpu_tcm_tree on page-locked host rows: with rows a multiple of 4
+    words the kernel reads and writes them in host memory itself; other row
+    lengths, or a pageable output, take the staged copies.  Both equal the
+    restatement bit for bit."""
+    import ctypes as C
+    import torch
+    rng = np.random.default_rng(n_sites + int(pin_out))
+    tr = T.yule(200, rng, 0.1)
+    codes = _codes(rng, tr.n_tips, n_sites)
+    tcm = rng.integers(1, 40, (4, 4)).astype(np.int32)
+    tcm = np.minimum(tcm, tcm.T)
+    np.fill_diagonal(tcm, 0)
+    cm = CM.CostMatrix(tcm, mode="general")
+    w = rng.integers(1, 9, n_sites).astype(np.uint32)
+    cost, assign = TO.fill_tables(cm.tcm, CM.MODES[cm.mode], cm.symmetric)
+    node, site, total_exp = TO.tree_cost(tr.left, tr.right, codes, cost, assign, w)
+    words = synth.pack_lanes(codes.astype(np.uint32), 4)
+    nw = words.shape[1]
+
+    def pinned(a):
+        return torch.from_numpy(a.view(np.int32)).pin_memory().numpy().view(np.uint32)
+
+    p_tips, p_w = pinned(words), pinned(w)
+    out = pinned(np.zeros((tr.n_internal, nw), np.uint32)) if pin_out else np.zeros((tr.n_internal, nw),
+                                                                                    np.uint32)
+    sc = pinned(np.zeros(n_sites, np.uint32))
+    total = C.c_uint64(0)
+    t, keep = _native.make_tree(tr.left, tr.right)
+    ctx.call("pgpu_tcm_tree", C.byref(t), p_tips.ctypes.data, p_w.ctypes.data, n_sites,
+             cm.table.ctypes.data, out.ctypes.data, sc.ctypes.data, C.byref(total))
+    del keep
+    assert np.array_equal(synth.unpack_lanes(out, n_sites, 4), node)
+    assert np.array_equal(sc.astype(np.int64), site)
+    assert total.value == total_exp
+
+
 @pytest.mark.parametrize("sub", [("JC69",), ("GTR", [1.2, 0.6, 1.7, 0.8, 1.3])])
 def test_integerized_model(ctx, sub):
     """MlModel.integerized_model on the GPU's compose, then a tree under it."""
