@@ -294,7 +294,9 @@ def bench_fitch(args, rank, world, local):
         "e2e": {"value": units / e2e_s, "unit": "node-site updates/s",
                 "h2d_bytes_per_step": int(words.nbytes + w.nbytes),
                 "d2h_bytes_per_step": int(pin_out.nbytes + pin_sc.nbytes + 8),
-                "ms_per_step": e2e_s * 1e3},
+                "ms_per_step": e2e_s * 1e3,
+                "transfer": "page-locked host rows read and written by the kernel over the "
+                            "CPU-GPU link; weights and per-site costs copied"},
         "gpu_launches": int(launches),
         "clocks": clk,
     }
@@ -428,7 +430,9 @@ def bench_tcm(args, rank, world, local):
         "e2e": {"value": units / e2e_s, "unit": "node-site updates/s",
                 "h2d_bytes_per_step": int(words.nbytes + w.nbytes),
                 "d2h_bytes_per_step": int(pin_out.nbytes + pin_sc.nbytes + 8),
-                "ms_per_step": e2e_s * 1e3},
+                "ms_per_step": e2e_s * 1e3,
+                "transfer": "page-locked host rows read and written by the kernel over the "
+                            "CPU-GPU link; weights and per-site costs copied"},
         "gpu_launches": int(launches), "clocks": clk,
     }
     if rank == 0:   # the restatement (numpy, one core) on a bounded sample
