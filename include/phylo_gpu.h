@@ -378,7 +378,8 @@ pgpu_status pgpu_compose_sym(pgpu_ctx *ctx, const double *U, const double *D, in
  * are copied in column chunks on a second stream of the context, so the
  * copy overlaps the scoring (pinned host memory lets the copies run
  * asynchronously): the first chunk is one wave of the scoring kernel's
- * CTAs, each next twice the last.  The call returns once lnl is written. */
+ * CTAs, each next a fixed factor larger.  The call returns once lnl is
+ * written. */
 pgpu_status pgpu_prune_lnl(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *model,
                            const pgpu_tip_codes *codes, const uint8_t *tip_codes,
                            const double *weights, size_t n_pat, int precision, double *lnl,

@@ -69,15 +69,19 @@ constexpr int PR_THREADS = 256;   // consumer threads per CTA
 
 // Ring depth in postorder steps (a power of two) and the CTAs each SM should
 // hold.  The pair form's slots and stack are twice the FP32 form's, so its
-// ring is shorter to fit three CTAs (27 warps) per SM.
+// ring is shorter to fit three CTAs (27 warps) per SM.  growth: how much
+// larger each column chunk of host tip codes is than the one before; a
+// chunk's copy must end while the previous chunk is scored, and a wave of
+// scoring takes about 2.5 (FP32), 6 (pair) or 30 (FP64) times as long as
+// copying its tip codes.
 template <typename Pol> struct PruneTune {
-  static constexpr int stages = 8, min_ctas = 1;
+  static constexpr int stages = 8, min_ctas = 1, growth = 8;
 };
 template <> struct PruneTune<pgpu_forms::Ff32> {
-  static constexpr int stages = 4, min_ctas = 3;
+  static constexpr int stages = 4, min_ctas = 3, growth = 4;
 };
 template <> struct PruneTune<pgpu_forms::Fp32> {
-  static constexpr int stages = 8, min_ctas = 4;
+  static constexpr int stages = 8, min_ctas = 4, growth = 2;
 };
 // Steps per ring barrier: the producer stages PR_GROUP consecutive steps
 // under one mbarrier phase, so the consumers wait and release once per group.
@@ -395,10 +399,11 @@ struct ChunkPlan {
 };
 
 // Column chunks for tip codes in host memory: the first chunk is one wave
-// of CTAs (the one copy the scoring cannot hide), each next one twice the
-// last, so a chunk's copy ends while the chunk before it is scored; whole
-// waves keep every launch but the last free of a part-filled wave.  Tip
-// codes already on the device: one launch.
+// of CTAs (the one copy the scoring cannot hide), each next one
+// PruneTune::growth times the last, so a chunk's copy ends while the chunk
+// before it is scored and few launch boundaries drain the GPU; whole waves
+// keep every launch but the last free of a part-filled wave.  Tip codes
+// already on the device: one launch.
 template <typename Pol, int RT>
 pgpu_status plan_chunks_rt(pgpu_ctx *ctx, size_t n_tiles, int n_models, bool host, ChunkPlan &pl) {
   pl.K = 0;
@@ -416,7 +421,7 @@ pgpu_status plan_chunks_rt(pgpu_ctx *ctx, size_t n_tiles, int n_models, bool hos
     while (pl.K < PGPU_COPY_CHUNKS - 1 && n_tiles - t >= c + wave) {
       t += c;
       pl.bounds[++pl.K] = t;
-      c *= 2;
+      c *= PruneTune<Pol>::growth;
     }
   }
   pl.bounds[++pl.K] = n_tiles;
