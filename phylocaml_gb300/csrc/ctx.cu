@@ -68,7 +68,7 @@ pgpu_status pgpu_check_flag(pgpu_ctx *ctx, const char *what) {
 
 pgpu_status pgpu_settle_copies(pgpu_ctx *ctx, pgpu_status st) {
   if (st != PGPU_OK) {
-    for (cudaStream_t cs : {ctx->stream, ctx->copy_stream, ctx->d2h_stream})
+    for (cudaStream_t cs : {ctx->stream, ctx->copy_stream, ctx->d2h_stream, ctx->aux_stream})
       if (cs) cudaStreamSynchronize(cs);
     (void)cudaGetLastError();
   }
@@ -92,6 +92,9 @@ pgpu_status pgpu_copy_stream(pgpu_ctx *ctx) {
   for (cudaEvent_t &e : ctx->copy_ev)
     PGPU_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   for (cudaEvent_t &e : ctx->done_ev)
+    PGPU_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  PGPU_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
+  for (cudaEvent_t &e : ctx->aux_ev)
     PGPU_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   return PGPU_OK;
 }
@@ -152,7 +155,7 @@ void pgpu_destroy(pgpu_ctx *ctx) {
     if (ctx->stage_ev[k]) cudaEventDestroy(ctx->stage_ev[k]);
   }
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
-  for (cudaStream_t cs : {ctx->copy_stream, ctx->d2h_stream})
+  for (cudaStream_t cs : {ctx->copy_stream, ctx->d2h_stream, ctx->aux_stream})
     if (cs) {
       cudaStreamSynchronize(cs);
       cudaStreamDestroy(cs);
@@ -160,6 +163,8 @@ void pgpu_destroy(pgpu_ctx *ctx) {
   for (cudaEvent_t &e : ctx->copy_ev)
     if (e) cudaEventDestroy(e);
   for (cudaEvent_t &e : ctx->done_ev)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t &e : ctx->aux_ev)
     if (e) cudaEventDestroy(e);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   (void)cudaGetLastError();

@@ -105,9 +105,14 @@ struct pgpu_ctx {
   cudaStream_t copy_stream = nullptr, d2h_stream = nullptr;
   cudaEvent_t copy_ev[PGPU_COPY_CHUNKS + 1] = {};
   cudaEvent_t done_ev[PGPU_COPY_CHUNKS] = {};
+  // a second stream for launches that may run beside the context stream's
+  // (the next chunk's CTAs fill SMs as the previous chunk's drain), with
+  // the events that fork it from and join it to the context stream
+  cudaStream_t aux_stream = nullptr;
+  cudaEvent_t aux_ev[2] = {};
 };
 
-// Creates the copy streams and their events on first use.
+// Creates the copy streams, the auxiliary stream and their events on first use.
 pgpu_status pgpu_copy_stream(pgpu_ctx *ctx);
 // A host-buffer call that fails after queueing chunk copies waits for them
 // before returning, so no copy touches the caller's buffers afterwards.

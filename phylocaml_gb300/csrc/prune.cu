@@ -373,12 +373,13 @@ __global__ void __launch_bounds__(1024) prune_finalize_kernel(const double2 *par
 }
 
 template <typename Pol, int RT>
-pgpu_status launch_prune_rt(pgpu_ctx *ctx, PruneArgs &a, size_t n_tiles, size_t smem, int n_models) {
+pgpu_status launch_prune_rt(pgpu_ctx *ctx, PruneArgs &a, size_t n_tiles, size_t smem, int n_models,
+                            cudaStream_t stream) {
   PGPU_CUDA(ctx, cudaFuncSetAttribute(prune_tree_kernel<Pol, RT>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)std::max<size_t>(smem, 48 * 1024)));
   prune_tree_kernel<Pol, RT><<<dim3((unsigned)n_tiles, (unsigned)n_models), 32 + PR_THREADS, smem,
-                               ctx->stream>>>(a);
+                               stream>>>(a);
   return pgpu_after_launch(ctx, "prune_tree_kernel");
 }
 
@@ -460,12 +461,26 @@ pgpu_status plan_prune(pgpu_ctx *ctx, PruneArgs &a, int RT, int n_models, const 
   return PGPU_OK;
 }
 
+// With several chunks, consecutive launches alternate between the context
+// stream and the auxiliary one, so a chunk's CTAs take the SMs the previous
+// chunk's CTAs leave instead of waiting for the whole launch to drain (the
+// tiles are disjoint; each launch waits only for its own columns).
 template <typename Pol, int RT>
 pgpu_status launch_prune_chunks(pgpu_ctx *ctx, PruneArgs &a, const ChunkPlan &pl, int n_models, bool host) {
+  const bool fork = host && pl.K > 1;
+  if (fork) {
+    PGPU_CUDA(ctx, cudaEventRecord(ctx->aux_ev[0], ctx->stream));
+    PGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->aux_stream, ctx->aux_ev[0], 0));
+  }
   for (int k = 0; k < pl.K; ++k) {
-    if (host) PGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[k], 0));
+    const cudaStream_t ks = fork && (k & 1) ? ctx->aux_stream : ctx->stream;
+    if (host) PGPU_CUDA(ctx, cudaStreamWaitEvent(ks, ctx->copy_ev[k], 0));
     a.tile_base = pl.bounds[k];
-    PGPU_TRY((launch_prune_rt<Pol, RT>(ctx, a, pl.bounds[k + 1] - pl.bounds[k], pl.smem, n_models)));
+    PGPU_TRY((launch_prune_rt<Pol, RT>(ctx, a, pl.bounds[k + 1] - pl.bounds[k], pl.smem, n_models, ks)));
+  }
+  if (fork) {
+    PGPU_CUDA(ctx, cudaEventRecord(ctx->aux_ev[1], ctx->aux_stream));
+    PGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->aux_ev[1], 0));
   }
   a.tile_base = 0;
   return PGPU_OK;
