@@ -110,12 +110,13 @@ __host__ __device__ inline size_t cm_off(int n, int k, int Kp) {
   return (size_t)(n / 8) * (size_t)(Kp / 4) * 128 + (size_t)(k / 4) * 128 + (n % 8) * 16 + (k % 4) * 4;
 }
 
-// x rounded to the nearest TF32 value (10-bit mantissa), as bits: the MMA
-// then reads an unbiased operand instead of one whose low bits are dropped
+// x rounded to the nearest TF32 value (10-bit mantissa, ties away from
+// zero), as bits: the MMA then reads an unbiased operand instead of one
+// whose low bits are dropped.  For a finite x >= 0 adding half a TF32 unit
+// to the bit pattern and clearing the 13 dropped bits rounds it (a carry
+// out of the mantissa raises the exponent), with two integer instructions.
 __device__ __forceinline__ uint32_t tf32_bits(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return r;
+  return (__float_as_uint(x) + 0x1000u) & 0xffffe000u;
 }
 
 // W consecutive TMEM columns of this thread's lane (32x32b shape)
