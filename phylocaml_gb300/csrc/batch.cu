@@ -52,6 +52,8 @@
 #include "pgpu_internal.cuh"
 #include "pmatrix.cuh"
 
+using namespace pgpu_forms;
+
 namespace {
 
 constexpr int BT_M = 128;          // patterns per tile (TMEM lanes)
@@ -84,6 +86,7 @@ struct BVar {
   long long ctab_off;              // doubles into the code-table array ([n_codes][S])
   int group, group_idx;            // eigen system: model group_idx of the group of this S
   double probs[4];
+  float probsf[4];                 // probs rounded to float (the root's join)
 };
 
 // op.x = internal index k, op.y = first child, op.z = second child,
@@ -210,6 +213,8 @@ struct BatchArgs {
   const float *bmat;
   const float *tiptab;
   const double *pis;
+  const float2 *pis2;             // pis as (hi, lo) float pairs
+  const float4 *logtab;           // the float-pair logarithm's table (64 entries)
   double *site_lnl;               // [total patterns] or null
   double2 *partials;              // [n_work]
   int *flag;
@@ -235,7 +240,7 @@ struct EpiIn {
   int m;                     // pattern within the tile (TMEM lane)
   int lg;                    // TMEM lane group (its warps of one rate class share a named barrier)
   bool active, last;
-  const double *pi;
+  const float2 *pi2;         // the variant's stationary frequencies as float pairs
 };
 
 // The share of a row that epilogue warp w owns (PT = w / 4; the warps of a
@@ -266,7 +271,7 @@ struct Share {
 template <int KP, int RP, int PT>
 __device__ __forceinline__ void epi_step(const BatchArgs &p, const EpiIn &in, const int4 op, int lane,
                                          int slot, uint64_t *empty, float (*xch)[BT_M], int &escale,
-                                         bool &ok, double &Lp) {
+                                         bool &ok, ff &Lp) {
   using SH = Share<KP, RP, PT>;
   constexpr int B = SH::B, e0 = SH::e0, rate = SH::rate;
   constexpr int BA = B > 0 ? B : 1;
@@ -360,14 +365,25 @@ __device__ __forceinline__ void epi_step(const BatchArgs &p, const EpiIn &in, co
 #pragma unroll
     for (int c0 = 0; c0 < B; c0 += WS) tmem_st<WS>(col + (uint32_t)c0, &acc[c0]);
     if (in.last) {
-      double l = 0.0;
+      // sum_e pi_e x_e as a float pair: pi as (hi, lo), every product exact
+      // with its cross term, the high parts added by an ordered Fast2Sum
+      // (the terms are non-negative), all low parts in one float
+      float hs = 0.0f, lo = 0.0f;
 #pragma unroll
       for (int e = 0; e < B; ++e)
-        if (e0 + e < in.S) l += in.pi[e0 + e] * (double)acc[e];
-      Lp = l;
+        if (e0 + e < in.S) {
+          const float2 pv = in.pi2[e0 + e];
+          const float q = __fmul_rn(pv.x, acc[e]);
+          float err = __fmaf_rn(pv.x, acc[e], -q);
+          err = __fmaf_rn(pv.y, acc[e], err);
+          const ff t = fast_two_sum(fmaxf(hs, q), fminf(hs, q));
+          hs = t.h;
+          lo = __fadd_rn(lo, __fadd_rn(t.l, err));
+        }
+      Lp = fast_two_sum(hs, lo);
     }
   } else {
-    if (in.last) Lp = 0.0;
+    if (in.last) Lp = ff{0.0f, 0.0f};
   }
 }
 
@@ -379,8 +395,8 @@ struct EpiShared {
   const int4 *slot_op;       // each ring slot's postorder step, written by the producer
   unsigned char *smem;
   float (*xch)[BT_M];        // [2][BT_PARTS]: per step parity and share, lane: max entry
-  double (*xchd)[BT_M];      // per share, lane: root likelihood
-  double (*lnr)[BT_M];       // per rate class, lane: log root likelihood
+  ff (*xchd)[BT_M];          // per share, lane: root likelihood (float pair)
+  ff (*lnr)[BT_M];           // per rate class, lane: log root likelihood (float pair)
   double2 *red;
   uint32_t tmem;
 };
@@ -414,8 +430,8 @@ __device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh
   in.lg = lg;
   const long long pat = (long long)wk.y * BT_M + m;
   in.active = pat < vg.n_pat;
-  in.pi = p.pis + vg.pi_off;
-  double Lp = 0.0;
+  in.pi2 = p.pis2 + vg.pi_off;
+  ff Lp{0.0f, 0.0f};
   for (int r0 = 0; r0 < R && ok; r0 += RP) {
     int escale = 0;
     for (int i = 0; i < n_ops; ++i, ++seq) {
@@ -465,27 +481,45 @@ __device__ __forceinline__ void epi_item(const BatchArgs &p, const EpiShared &sh
     sh.xchd[pt][m] = Lp;
     asm volatile("bar.sync 1, %0;" ::"n"(BT_EPI) : "memory");
     if (lead) {
-      double L = 0.0;
+      ff L{0.0f, 0.0f};
 #pragma unroll
-      for (int pp = my_rate * PPR; pp < my_rate * PPR + PPR; ++pp) L += sh.xchd[pp][m];
-      sh.lnr[r0 + my_rate][m] = log(L) + (double)escale * 0.69314718055994530942;
+      for (int pp = my_rate * PPR; pp < my_rate * PPR + PPR; ++pp) L = ff_add(L, sh.xchd[pp][m]);
+      // log(L 2^escale) in float pairs (no FP64 instruction: the FP64 pipe
+      // of this GPU retires a warp's instruction in tens of cycles)
+      sh.lnr[r0 + my_rate][m] = L.h > 0.0f ? ff_log(L, escale, p.logtab) : ff{-INFINITY, 0.0f};
     }
     asm volatile("bar.sync 1, %0;" ::"n"(BT_EPI) : "memory");
   }
-  // join the rate classes: log sum_r probs[r] exp(lnr[r])
-  double s = 0.0, comp = 0.0;
+  // join the rate classes: log sum_r probs[r] exp(lnr[r]), the largest
+  // class's logarithm as a float pair plus the float logarithm of a sum in
+  // [probs_min, 1]
+  ff s{0.0f, 0.0f};
   if (ok && in.active && pt == 0) {
-    double mxl = -INFINITY;
-    for (int r = 0; r < R; ++r) mxl = fmax(mxl, sh.lnr[r][m]);
-    double sum = 0.0;
-    for (int r = 0; r < R; ++r) sum += vg.probs[r] * exp(sh.lnr[r][m] - mxl);
-    const double lnl = mxl + log(sum);
-    if (p.site_lnl) p.site_lnl[vg.pat_off + pat] = lnl;
-    s = vg.weights ? vg.weights[pat] * lnl : lnl;
+    ff mx = sh.lnr[0][m];
+    for (int r = 1; r < R; ++r)
+      if (sh.lnr[r][m].h > mx.h) mx = sh.lnr[r][m];
+    ff lnl = mx;
+    if (mx.h != -INFINITY) {
+      float sum = 0.0f;
+      for (int r = 0; r < R; ++r) {
+        const ff v = sh.lnr[r][m];
+        sum += vg.probsf[r] * expf((v.h - mx.h) + (v.l - mx.l));
+      }
+      lnl = ff_add(mx, ff{logf(sum), 0.0f});
+    }
+    if (p.site_lnl) p.site_lnl[vg.pat_off + pat] = (double)lnl.h + (double)lnl.l;
+    if (vg.weights) {
+      const double w = vg.weights[pat];
+      const float wh = (float)w;
+      s = ff_mul(lnl, ff{wh, (float)(w - (double)wh)});
+    } else {
+      s = lnl;
+    }
   }
   if (pt == 0) {
-    warp_csum_d(s, comp);
-    if (lane == 0) sh.red[lg] = make_double2(s, comp);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s = ff_add(s, ff_shfl_xor(s, o));
+    if (lane == 0) sh.red[lg] = make_double2((double)s.h, (double)s.l);
   }
   asm volatile("bar.sync 1, %0;" ::"n"(BT_EPI) : "memory");
   if (tid == 0) {
@@ -616,8 +650,8 @@ __global__ void __launch_bounds__(BT_THREADS, 1) batch_tc_kernel(const BatchArgs
   __shared__ int4 slot_op[BT_ST];
   __shared__ uint32_t tmem_base;
   __shared__ float xch[2 * BT_PARTS][BT_M];   // per step parity and share, lane: max entry
-  __shared__ double xchd[BT_PARTS][BT_M];   // per share, lane: root likelihood
-  __shared__ double lnr[4][BT_M];           // per rate class, lane: log root likelihood
+  __shared__ ff xchd[BT_PARTS][BT_M];   // per share, lane: root likelihood
+  __shared__ ff lnr[4][BT_M];           // per rate class, lane: log root likelihood
   __shared__ double2 red[4];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -951,6 +985,8 @@ struct pgpu_batch {
   int4 *ops = nullptr;
   float *bmat = nullptr, *tiptab = nullptr;
   double *pis = nullptr, *brlen = nullptr, *rates = nullptr, *ctab = nullptr;
+  float2 *pis2 = nullptr;
+  float4 *logtab = nullptr;
   double *Q = nullptr, *U = nullptr, *Ui = nullptr, *lam = nullptr;
   int *status = nullptr, *members = nullptr;
   long long *tile_base = nullptr;
@@ -974,7 +1010,7 @@ pgpu_status upload(pgpu_ctx *ctx, T **dst, const std::vector<T> &src) {
 void free_batch(pgpu_batch *b) {
   void *ptrs[] = {b->vars, b->work,   b->ops, b->bmat,   b->tiptab,  b->pis,      b->brlen,
                   b->rates, b->ctab,  b->Q,   b->U,      b->Ui,      b->lam,      b->status,
-                  b->members, b->tile_base, b->n_tiles, b->partials};
+                  b->members, b->tile_base, b->n_tiles, b->partials, b->pis2, b->logtab};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   delete b;
@@ -1054,7 +1090,10 @@ pgpu_status pgpu_batch_create_opts(pgpu_ctx *ctx, const pgpu_variant *vs, int n_
     v.brlen_off = (long long)brl.size();
     v.rates_off = (long long)rts.size();
     v.ctab_off = (long long)ctab.size();
-    for (int r = 0; r < 4; ++r) v.probs[r] = r < R ? m.probs[r] : 0.0;
+    for (int r = 0; r < 4; ++r) {
+      v.probs[r] = r < R ? m.probs[r] : 0.0;
+      v.probsf[r] = (float)v.probs[r];
+    }
     if (sch.max_depth > v.n_slots) return fail(PGPU_ERR_LIMIT, "tree too deep for the TMEM stack", vi);
     // two rate classes per pass when their D columns and stacks fit in TMEM
     v.RP = 1;
@@ -1154,6 +1193,15 @@ pgpu_status pgpu_batch_create_opts(pgpu_ctx *ctx, const pgpu_variant *vs, int n_
   if (st == PGPU_OK) st = upload(ctx, &b->work, work);
   if (st == PGPU_OK) st = upload(ctx, &b->ops, ops);
   if (st == PGPU_OK) st = upload(ctx, &b->pis, pis);
+  std::vector<float2> pis2(pis.size());
+  for (size_t i = 0; i < pis.size(); ++i) {
+    const float h = (float)pis[i];
+    pis2[i] = make_float2(h, (float)(pis[i] - (double)h));
+  }
+  std::vector<float4> lt(64);
+  ff_log_table(lt.data(), [](double c) { return std::log(c); });
+  if (st == PGPU_OK) st = upload(ctx, &b->pis2, pis2);
+  if (st == PGPU_OK) st = upload(ctx, &b->logtab, lt);
   if (st == PGPU_OK) st = upload(ctx, &b->brlen, brl);
   if (st == PGPU_OK) st = upload(ctx, &b->rates, rts);
   if (st == PGPU_OK) st = upload(ctx, &b->ctab, ctab);
@@ -1245,6 +1293,8 @@ pgpu_status pgpu_batch_run(pgpu_ctx *ctx, pgpu_batch *b, double *lnl_dev, double
   a.bmat = b->bmat;
   a.tiptab = b->tiptab;
   a.pis = b->pis;
+  a.pis2 = b->pis2;
+  a.logtab = b->logtab;
   a.site_lnl = site_lnl_dev;
   a.partials = b->partials;
   a.flag = ctx->d_flag;

@@ -141,6 +141,17 @@ __device__ __forceinline__ ff ff_exp2_log(int E) {
   return ff_from_d((double)E * 0.69314718055994530942);
 }
 
+// The table ff_log reads: tab[k] = {log c hi, log c lo, 1/c hi, 1/c lo},
+// c = 1 + (2k + 1) / 128, formed in FP64 (host code; std::log).
+template <class Log>
+inline void ff_log_table(float4 *tab, Log log_fn) {
+  for (int k = 0; k < 64; ++k) {
+    const double c = 1.0 + (2.0 * k + 1.0) / 128.0, l = log_fn(c), inv = 1.0 / c;
+    const float lh = (float)l, ih = (float)inv;
+    tab[k] = make_float4(lh, (float)(l - (double)lh), ih, (float)(inv - (double)ih));
+  }
+}
+
 // Natural logarithm of x = h + l (x > 0, h normal) times 2^e2, as a float
 // pair.  Table-driven reduction (Tang's method): m = h 2^-ex in [1, 2),
 // c = 1 + (2k + 1) / 128 the centre of m's 1/64-wide cell, r = (m - c) / c

@@ -1730,11 +1730,7 @@ pgpu_status pgpu_spr_create(pgpu_ctx *ctx, const pgpu_model *m, const pgpu_tip_c
   SPR_TRY(upload(s, reinterpret_cast<uint32_t *>(s->planes), planes.data(), planes.size()));
   // logarithm table of the pair form
   std::vector<float4> lt(64);
-  for (int k = 0; k < 64; ++k) {
-    const double c = 1.0 + (2.0 * k + 1.0) / 128.0, l = std::log(c), inv = 1.0 / c;
-    const float lh = (float)l, ih = (float)inv;
-    lt[k] = make_float4(lh, (float)(l - (double)lh), ih, (float)(inv - (double)ih));
-  }
+  ff_log_table(lt.data(), [](double c) { return std::log(c); });
   SPR_TRY(dalloc_t(s, 64, &s->logtab));
   SPR_TRY(upload(s, s->logtab, lt.data(), lt.size()));
   // pool and tables
