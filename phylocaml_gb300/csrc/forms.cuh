@@ -316,32 +316,43 @@ struct Ff32 {
     y[3] = {b.z, b.w};
   }
   // y_i = sum_j P_ij x_j with P as (hi, lo) pairs: every product exact
-  // (TwoProduct), the hi products summed exactly (the terms are
-  // non-negative, so max/min orders them for Fast2Sum), the small cross
+  // (TwoProduct), the hi products summed exactly (2Sum), the small cross
   // terms (P_hi x_lo, P_lo x_hi) and all rounding errors gathered in one
-  // float.  The pair keeps about 48 bits and is left unnormalised.
+  // float.  The pair keeps about 48 bits and is left unnormalised.  Rows go
+  // two at a time through packed float2 arithmetic (FFMA2, FADD2, FMUL2:
+  // two rows per instruction, each lane rounded as the scalar instruction
+  // would be), reading P in the P32_PAIRS_ROWS4 layout: float4 4 (i / 2) + j
+  // = {hi P[i][j], hi P[i+1][j], lo P[i][j], lo P[i+1][j]}.
   __device__ static void rows(const Coef *P, const V *x, V *y) {
+    const float4 *Q = reinterpret_cast<const float4 *>(P);
+    const float2 m1 = make_float2(-1.0f, -1.0f);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const float4 d01 = reinterpret_cast<const float4 *>(P)[2 * i];
-      const float4 d23 = reinterpret_cast<const float4 *>(P)[2 * i + 1];
-      const float ph[4] = {d01.x, d01.z, d23.x, d23.z};
-      const float pl[4] = {d01.y, d01.w, d23.y, d23.w};
-      float sh = __fmul_rn(ph[0], x[0].h);
-      float lo = __fmaf_rn(ph[0], x[0].h, -sh);
-      lo = __fmaf_rn(ph[0], x[0].l, lo);
-      lo = __fmaf_rn(pl[0], x[0].h, lo);
+    for (int ip = 0; ip < 2; ++ip) {
+      float2 sh = make_float2(0.0f, 0.0f), lo = make_float2(0.0f, 0.0f);
 #pragma unroll
-      for (int j = 1; j < 4; ++j) {
-        const float p = __fmul_rn(ph[j], x[j].h);
-        float e = __fmaf_rn(ph[j], x[j].h, -p);
-        e = __fmaf_rn(ph[j], x[j].l, e);
-        e = __fmaf_rn(pl[j], x[j].h, e);
-        const ff t = fast_two_sum(fmaxf(sh, p), fminf(sh, p));
-        sh = t.h;
-        lo = __fadd_rn(lo, __fadd_rn(t.l, e));
+      for (int j = 0; j < 4; ++j) {
+        const float4 q = Q[ip * 4 + j];
+        const float2 ph = make_float2(q.x, q.y), pl = make_float2(q.z, q.w);
+        const float2 xh = make_float2(x[j].h, x[j].h), xl = make_float2(x[j].l, x[j].l);
+        const float2 p = __fmul2_rn(ph, xh);
+        float2 e = __ffma2_rn(ph, xh, __fmul2_rn(p, m1));   // ph xh - p, exact
+        e = __ffma2_rn(ph, xl, e);
+        e = __ffma2_rn(pl, xh, e);
+        if (j == 0) {
+          sh = p;
+          lo = e;
+        } else {
+          // 2Sum: s = sh + p rounded, and its rounding error exactly
+          const float2 s = __fadd2_rn(sh, p);
+          const float2 bp = __ffma2_rn(sh, m1, s);           // s - sh
+          const float2 bs = __ffma2_rn(bp, m1, s);           // s - (s - sh)
+          const float2 err = __fadd2_rn(__ffma2_rn(bs, m1, sh), __ffma2_rn(bp, m1, p));
+          sh = s;
+          lo = __fadd2_rn(lo, __fadd2_rn(err, e));
+        }
       }
-      y[i] = {sh, lo};
+      y[2 * ip] = {sh.x, lo.x};
+      y[2 * ip + 1] = {sh.y, lo.y};
     }
   }
 };

@@ -374,7 +374,13 @@ __global__ void __launch_bounds__(256) compose_kernel(const ComposeArgs p) {
     if (P32) {
       const bool minus_i = p.p32_mode == P32_MINUS_I || p.p32_mode == P32_MINUS_I_PAIRS;
       const double d = (minus_i && i == j) ? v - 1.0 : v;
-      if (p.p32_mode == P32_MINUS_I_PAIRS || p.p32_mode == P32_PAIRS) {
+      if (p.p32_mode == P32_PAIRS_ROWS4) {
+        // S == 4 (checked by the launcher): 32 floats per (branch, rate)
+        const size_t at = ((size_t)b * R + r) * 32 + 4 * ((i >> 1) * 4 + j) + (i & 1);
+        const float hi = (float)d;
+        P32[at] = hi;
+        P32[at + 2] = (float)(d - (double)hi);
+      } else if (p.p32_mode == P32_MINUS_I_PAIRS || p.p32_mode == P32_PAIRS) {
         const float hi = (float)d;
         P32[2 * off] = hi;
         P32[2 * off + 1] = (float)(d - (double)hi);
@@ -468,6 +474,8 @@ pgpu_status pgpu_launch_compose(pgpu_ctx *ctx, const double *U_dev, const double
                                 bool allow_q, const int *status_dev, int p32_mode, int n_models,
                                 size_t model_bytes) {
   if (n_br <= 0 || n_models <= 0) return PGPU_OK;
+  if (p32_mode == P32_PAIRS_ROWS4 && S != 4)
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "compose: the row-pair layout is for 4 states (got %d)", S);
   if (n_models > 65535)
     return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "compose: %d models in one launch; at most 65535",
                         n_models);

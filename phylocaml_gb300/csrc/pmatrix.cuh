@@ -23,7 +23,11 @@ enum P32Mode {
   P32_PLAIN = 0,          // fl32(P)
   P32_MINUS_I = 1,        // fl32(P - I)
   P32_MINUS_I_PAIRS = 2,  // (hi, lo) float pairs of P - I, two floats per entry
-  P32_PAIRS = 3           // (hi, lo) float pairs of P
+  P32_PAIRS = 3,          // (hi, lo) float pairs of P
+  // (hi, lo) float pairs of a 4 x 4 P, rows taken two at a time for packed
+  // float2 arithmetic: float4 k = 4 (i / 2) + j of a block holds
+  // {hi P[i][j], hi P[i+1][j], lo P[i][j], lo P[i+1][j]} for even i
+  P32_PAIRS_ROWS4 = 4
 };
 pgpu_status pgpu_launch_compose(pgpu_ctx *ctx, const double *U_dev, const double *lam_dev,
                                 const double *Ui_dev, int S, const double *t_dev, int n_br,

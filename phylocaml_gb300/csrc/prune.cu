@@ -682,7 +682,7 @@ pgpu_status prune_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *mo
   PGPU_TRY(pgpu_launch_compose(ctx, dU, dlam, dUi, S, rebase(d, lay.brlen), n_br,
                                rebase(d, lay.rates), R, precision == 64 ? (double *)dP : nullptr,
                                precision == 64 ? nullptr : (float *)dP, false, dst,
-                               precision == 32 ? P32_MINUS_I : precision == 48 ? P32_PAIRS
+                               precision == 32 ? P32_MINUS_I : precision == 48 ? P32_PAIRS_ROWS4
                                                                                : P32_PLAIN,
                                V, p_bytes));
   PGPU_TRY(pgpu_launch_tip_table(ctx, dU, dlam, dUi, S, rebase(d, lay.brlen), n,

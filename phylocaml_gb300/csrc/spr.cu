@@ -1171,7 +1171,7 @@ pgpu_status upload(pgpu_spr *s, T *dst, const T *src, size_t n) {
   return PGPU_OK;
 }
 
-int p32_mode(int prec) { return prec == 32 ? P32_MINUS_I : prec == 64 ? P32_PLAIN : P32_PAIRS; }
+int p32_mode(int prec) { return prec == 32 ? P32_MINUS_I : prec == 64 ? P32_PLAIN : P32_PAIRS_ROWS4; }
 int tip_form(int prec) { return prec == 32 ? 0 : prec == 64 ? 2 : 1; }
 
 pgpu_status compose(pgpu_spr *s, const double *t_dev, int n_br, void *out) {
