@@ -500,11 +500,12 @@ def bench_fitch_reference(args):
 PRUNE_TAXA, PRUNE_SITES, PRUNE_BL = 512, 500_000, 0.05
 PRUNE_GATE = 1e-3
 FORMS = {32: "fp32", 48: "fp32x2", 64: "fp64"}
-# FP32 lane instructions of each form, counted from csrc/forms.cuh: per row of
-# a P x child product (internal children only; tip children are table rows),
-# and per node and rate class for the product of the two children and the
-# rescale test
-FP32_INSTR_PER_ROW = {32: 5, 48: 37}
+# FP32 thread instructions of each form, counted from csrc/forms.cuh: per row
+# of a P x child product (internal children only; tip children are table
+# rows; the pair form computes two rows per packed float2 instruction, 44 per
+# row pair), and per node and rate class for the product of the two children
+# and the rescale test
+FP32_INSTR_PER_ROW = {32: 5, 48: 22}
 FP32_INSTR_PER_NODE = {32: 4 + 6, 48: 4 * 4 + 6}
 
 

@@ -316,7 +316,7 @@ struct Ff32 {
     y[3] = {b.z, b.w};
   }
   // y_i = sum_j P_ij x_j with P as (hi, lo) pairs: every product exact
-  // (TwoProduct), the hi products summed exactly (2Sum), the small cross
+  // (TwoProduct), the hi products summed exactly (ordered Fast2Sum), the small cross
   // terms (P_hi x_lo, P_lo x_hi) and all rounding errors gathered in one
   // float.  The pair keeps about 48 bits and is left unnormalised.  Rows go
   // two at a time through packed float2 arithmetic (FFMA2, FADD2, FMUL2:
@@ -342,11 +342,13 @@ struct Ff32 {
           sh = p;
           lo = e;
         } else {
-          // 2Sum: s = sh + p rounded, and its rounding error exactly
-          const float2 s = __fadd2_rn(sh, p);
-          const float2 bp = __ffma2_rn(sh, m1, s);           // s - sh
-          const float2 bs = __ffma2_rn(bp, m1, s);           // s - (s - sh)
-          const float2 err = __fadd2_rn(__ffma2_rn(bs, m1, sh), __ffma2_rn(bp, m1, p));
+          // Fast2Sum of the larger and the smaller term (all terms are
+          // non-negative): the ordering on the ALU pipe, the three adds
+          // packed on the FMA pipe
+          const float2 a = make_float2(fmaxf(sh.x, p.x), fmaxf(sh.y, p.y));
+          const float2 b = make_float2(fminf(sh.x, p.x), fminf(sh.y, p.y));
+          const float2 s = __fadd2_rn(a, b);
+          const float2 err = __ffma2_rn(__ffma2_rn(a, m1, s), m1, b);   // b - (s - a)
           sh = s;
           lo = __fadd2_rn(lo, __fadd2_rn(err, e));
         }
