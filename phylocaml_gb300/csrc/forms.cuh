@@ -214,6 +214,10 @@ struct Fp32 {
   __device__ static float mag(V v) { return v; }
   __device__ static double to_d(V v) { return (double)v; }
   __device__ static V mul(V a, V b) { return a * b; }
+  __device__ static void mul4(const V *a, const V *b, V *y) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) y[e] = a[e] * b[e];
+  }
   __device__ static V scale(V v, int k) { return v * pow2f(k); }
   __device__ static void load_tip(const void *tab, size_t at, V *y) {
     const float4 v = reinterpret_cast<const float4 *>(tab)[at];
@@ -255,6 +259,10 @@ struct Fp64 {
   __device__ static double mag(V v) { return v; }
   __device__ static double to_d(V v) { return v; }
   __device__ static V mul(V a, V b) { return a * b; }
+  __device__ static void mul4(const V *a, const V *b, V *y) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) y[e] = a[e] * b[e];
+  }
   __device__ static V scale(V v, int k) { return v * __longlong_as_double((long long)(1023 + k) << 52); }
   __device__ static void load_tip(const void *tab, size_t at, V *y) {
     const double2 a = reinterpret_cast<const double2 *>(tab)[2 * at];
@@ -286,9 +294,11 @@ struct Ff32 {
   __device__ static V add(V a, V b) { return ff_add(a, b); }
   __device__ static V shfl_xor(V v, int o) { return ff_shfl_xor(v, o); }
   __device__ static bool positive(V v) { return v.h > 0.0f; }
+  // four pairs stored element pairs first: {h0, h1, l0, l1}, {h2, h3, l2, l3},
+  // so that a 16-byte load gives packed float2 operands
   __device__ static void store4(void *tab, size_t at, const V *y) {
-    reinterpret_cast<float4 *>(tab)[2 * at] = make_float4(y[0].h, y[0].l, y[1].h, y[1].l);
-    reinterpret_cast<float4 *>(tab)[2 * at + 1] = make_float4(y[2].h, y[2].l, y[3].h, y[3].l);
+    reinterpret_cast<float4 *>(tab)[2 * at] = make_float4(y[0].h, y[1].h, y[0].l, y[1].l);
+    reinterpret_cast<float4 *>(tab)[2 * at + 1] = make_float4(y[2].h, y[3].h, y[2].l, y[3].l);
   }
   __device__ static ff site_log(V v, int e2, const float4 *tab) { return ff_log(v, e2, tab); }
   __device__ static V zero() { return {0.0f, 0.0f}; }
@@ -310,10 +320,26 @@ struct Ff32 {
   __device__ static void load_tip(const void *tab, size_t at, V *y) {
     const float4 a = reinterpret_cast<const float4 *>(tab)[2 * at];
     const float4 b = reinterpret_cast<const float4 *>(tab)[2 * at + 1];
-    y[0] = {a.x, a.y};
-    y[1] = {a.z, a.w};
-    y[2] = {b.x, b.y};
-    y[3] = {b.z, b.w};
+    y[0] = {a.x, a.z};
+    y[1] = {a.y, a.w};
+    y[2] = {b.x, b.z};
+    y[3] = {b.y, b.w};
+  }
+  // y[e] = a[e] b[e] for four elements, two per packed float2 instruction:
+  // each product exact and left unnormalised, as mul
+  __device__ static void mul4(const V *a, const V *b, V *y) {
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const float2 ah = make_float2(a[2 * k].h, a[2 * k + 1].h), al = make_float2(a[2 * k].l, a[2 * k + 1].l);
+      const float2 bh = make_float2(b[2 * k].h, b[2 * k + 1].h), bl = make_float2(b[2 * k].l, b[2 * k + 1].l);
+      const float2 p = __fmul2_rn(ah, bh);
+      float2 e = __ffma2_rn(ah, bh, __fmul2_rn(p, m1));
+      e = __ffma2_rn(ah, bl, e);
+      e = __ffma2_rn(al, bh, e);
+      y[2 * k] = {p.x, e.x};
+      y[2 * k + 1] = {p.y, e.y};
+    }
   }
   // y_i = sum_j P_ij x_j with P as (hi, lo) pairs: every product exact
   // (TwoProduct), the hi products summed exactly (ordered Fast2Sum), the small cross

@@ -402,7 +402,7 @@ struct TipTabArgs {
   const double *rates;      // [R]; model m at m*R
   const double *code_tab;   // [n_codes][S]
   void *out;
-  int S, R, n_codes, form;  // form: 0 float, 1 float pair, 2 double
+  int S, R, n_codes, form;  // form: 0 float, 1 float pair, 2 double, 3 float pairs element pairs first (S = 4)
   const int *status;        // model m at m
   size_t model_bytes;       // byte stride of out between models
 };
@@ -436,7 +436,13 @@ __global__ void __launch_bounds__(128) tip_table_kernel(const TipTabArgs p) {
     double v = 0.0;
     for (int j = 0; j < S; ++j) v = fma(P[i * S + j], p.code_tab[c * S + j], v);
     const size_t at = base + o;
-    if (p.form == 0) {
+    if (p.form == 3) {
+      // float pairs of S = 4 entries, element pairs first: {h0, h1, l0, l1}, {h2, h3, l2, l3}
+      float *q = reinterpret_cast<float *>(out) + 2 * (base + (size_t)c * 4) + (i >> 1) * 4 + (i & 1);
+      const float hi = (float)v;
+      q[0] = hi;
+      q[2] = (float)(v - (double)hi);
+    } else if (p.form == 0) {
       reinterpret_cast<float *>(out)[at] = (float)v;
     } else if (p.form == 1) {
       const float hi = (float)v;
@@ -496,6 +502,8 @@ pgpu_status pgpu_launch_tip_table(pgpu_ctx *ctx, const double *U_dev, const doub
                                   int n_codes, void *out_dev, int form, const int *status_dev,
                                   int n_models, size_t model_bytes) {
   if (n_tips <= 0 || n_models <= 0) return PGPU_OK;
+  if (form == 3 && S != 4)
+    return pgpu_set_err(ctx, PGPU_ERR_ARG, "tip table: the element-pair layout is for 4 states (got %d)", S);
   if (n_models > 65535)
     return pgpu_set_err(ctx, PGPU_ERR_LIMIT, "tip table: %d models in one launch; at most 65535",
                         n_models);

@@ -38,8 +38,10 @@ pgpu_status pgpu_launch_compose(pgpu_ctx *ctx, const double *U_dev, const double
 
 // Tip rows tab[t][r][c][i] = (P(t, r) code_tab[c])[i] for the n_tips branches
 // above the tips (t_dev holds their lengths), in FP64, stored as float
-// (form 0), (hi, lo) float pairs (form 1) or double (form 2).  n_models
-// and model_bytes batch models as in pgpu_launch_compose.
+// (form 0), (hi, lo) float pairs (form 1), double (form 2), or for S = 4
+// float pairs with the elements two at a time, {h0, h1, l0, l1}, {h2, h3,
+// l2, l3} per code (form 3, the pair form's packed layout).  n_models and
+// model_bytes batch models as in pgpu_launch_compose.
 pgpu_status pgpu_launch_tip_table(pgpu_ctx *ctx, const double *U_dev, const double *lam_dev,
                                   const double *Ui_dev, int S, const double *t_dev, int n_tips,
                                   const double *rates_dev, int R, const double *code_tab_dev,

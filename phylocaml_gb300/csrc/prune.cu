@@ -293,8 +293,7 @@ __global__ void __launch_bounds__(32 + PR_THREADS, PruneTune<Pol>::min_ctas)
           Pol::rows(coef(1), top, y1);
         }
       }
-#pragma unroll
-      for (int e = 0; e < 4; ++e) acc[e] = Pol::mul(y0[e], y1[e]);
+      Pol::mul4(y0, y1, acc);
     }
     // exact power-of-two rescaling of this rate class's vector (each rate
     // class keeps its own scaler; the root aligns them); rare, so the warp
@@ -687,7 +686,7 @@ pgpu_status prune_dev(pgpu_ctx *ctx, const pgpu_tree *tree, const pgpu_model *mo
                                V, p_bytes));
   PGPU_TRY(pgpu_launch_tip_table(ctx, dU, dlam, dUi, S, rebase(d, lay.brlen), n,
                                  rebase(d, lay.rates), R, rebase(d, lay.tab), codes->n_codes, dtt,
-                                 precision == 32 ? 0 : precision == 48 ? 1 : 2, dst, V, tt_bytes));
+                                 precision == 32 ? 0 : precision == 48 ? 3 : 2, dst, V, tt_bytes));
   if (n_pat == 0) {
     PGPU_CUDA(ctx, cudaMemsetAsync(lnl_dev, 0, (size_t)V * sizeof(double), ctx->stream));
     return PGPU_OK;

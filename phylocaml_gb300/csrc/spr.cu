@@ -1172,7 +1172,7 @@ pgpu_status upload(pgpu_spr *s, T *dst, const T *src, size_t n) {
 }
 
 int p32_mode(int prec) { return prec == 32 ? P32_MINUS_I : prec == 64 ? P32_PLAIN : P32_PAIRS_ROWS4; }
-int tip_form(int prec) { return prec == 32 ? 0 : prec == 64 ? 2 : 1; }
+int tip_form(int prec) { return prec == 32 ? 0 : prec == 64 ? 2 : 3; }
 
 pgpu_status compose(pgpu_spr *s, const double *t_dev, int n_br, void *out) {
   return pgpu_launch_compose(s->ctx, s->U, s->lam, s->Ui, 4, t_dev, n_br, s->rates, s->R,
