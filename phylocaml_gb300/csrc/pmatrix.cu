@@ -372,18 +372,13 @@ __global__ void __launch_bounds__(256) compose_kernel(const ComposeArgs p) {
     const size_t off = ((size_t)b * R + r) * SS + (size_t)i * S + j;
     if (P) P[off] = v;
     if (P32) {
-      const bool minus_i = p.p32_mode == P32_MINUS_I || p.p32_mode == P32_MINUS_I_PAIRS;
-      const double d = (minus_i && i == j) ? v - 1.0 : v;
+      const double d = (p.p32_mode == P32_MINUS_I && i == j) ? v - 1.0 : v;
       if (p.p32_mode == P32_PAIRS_ROWS4) {
         // S == 4 (checked by the launcher): 32 floats per (branch, rate)
         const size_t at = ((size_t)b * R + r) * 32 + 4 * ((i >> 1) * 4 + j) + (i & 1);
         const float hi = (float)d;
         P32[at] = hi;
         P32[at + 2] = (float)(d - (double)hi);
-      } else if (p.p32_mode == P32_MINUS_I_PAIRS || p.p32_mode == P32_PAIRS) {
-        const float hi = (float)d;
-        P32[2 * off] = hi;
-        P32[2 * off + 1] = (float)(d - (double)hi);
       } else {
         P32[off] = (float)d;
       }

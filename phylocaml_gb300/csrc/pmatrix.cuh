@@ -14,16 +14,14 @@ pgpu_status pgpu_launch_eig(pgpu_ctx *ctx, const double *Q_dev, const double *pi
 // If status_dev is given and non-zero the matrices are not built and the
 // context's error word records the model failure.  p32_mode selects the FP32
 // copy: P, P - I (formed in FP64 before rounding, which keeps the small
-// entries of short branches at full relative precision), or P - I as
-// (hi, lo) float pairs.  n_models > 1 composes that many models in one
+// entries of short branches at full relative precision), or P as (hi, lo)
+// float pairs in the pair form's row-pair layout.  n_models > 1 composes that many models in one
 // launch: model m reads U, Ui at m*S*S, lam at m*S, rates at m*R and
 // status_dev[m], and writes its matrices model_bytes further on than model
 // m - 1's (the same byte stride for P_dev and P32_dev).
 enum P32Mode {
   P32_PLAIN = 0,          // fl32(P)
   P32_MINUS_I = 1,        // fl32(P - I)
-  P32_MINUS_I_PAIRS = 2,  // (hi, lo) float pairs of P - I, two floats per entry
-  P32_PAIRS = 3,          // (hi, lo) float pairs of P
   // (hi, lo) float pairs of a 4 x 4 P, rows taken two at a time for packed
   // float2 arithmetic: float4 k = 4 (i / 2) + j of a block holds
   // {hi P[i][j], hi P[i+1][j], lo P[i][j], lo P[i+1][j]} for even i
